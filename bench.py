@@ -1,0 +1,323 @@
+#!/usr/bin/env python3
+"""Benchmark: TDGL cell-steps/s including the depolarisation PCG.
+
+A step is one time step of the P-E loop on the film of the second benchmark
+configuration (256x256x32 cells, 200-grain columnar Voronoi from seed 1, 40 %
+AFE grains, triangle field +-4 MV/cm at 4000 steps/period): the TDGL update,
+the depolarisation solve to ||b - A phi|| <= 1e-8 ||b|| and the sweep-row
+averages.  Inputs are synthetic (seeded generator; the reference ships no
+grain maps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|fp64]
+  python bench.py --impl reference ...   # the oracle (CPU FP64 port) on host cores
+
+Under torchrun (N > 1) every rank advances its own film (replicas: the path
+has no exchange step); value is all ranks' cell-steps over the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TDGL cell-steps/s incl. PCG, FP32-refined vs FP64 on GB300 at equal P-E error"
+CONFIG_ID = 1
+
+# Algorithmic bytes per cell and launch (compulsory DRAM traffic of each kernel).
+#   tdgl:   read 6 P + phi(f64) + code, write 6 P
+#   setup:  FP64 rhs: read Pm(3) + phi + code + dinv, write r
+#           FP32 refine: read phi(f64) + delta + Pm(3) + code + dinv, write phi(f64) + r
+#   spmv:   read r, p_old, dinv, code, write p, q
+#   update: read x, p, r, q, dinv, write x, r
+BYTES = {
+    "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4, "setup": 8 + 4 + 12 + 4 + 4 + 8 + 4, "spmv": 4 * 3 + 4 + 8,
+             "update": 5 * 4 + 2 * 4},
+    "fp64": {"tdgl": 6 * 8 * 2 + 8 + 4, "setup": 24 + 8 + 4 + 8 + 8, "spmv": 8 * 3 + 4 + 16,
+             "update": 5 * 8 + 2 * 8},
+}
+KERNELS = ["tdgl", "setup", "spmv", "update"]
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-cell DRAM bytes per kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh)
+    return {}
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_oracle_film(w, orc, crit_relres=True):
+    import oracle
+    f = oracle.Film(nx=w.nx, ny=w.ny, nz=w.nz, del_h=w.del_h, del_t=w.del_t, omega=w.omega,
+                    grain_mat=w.grain_mat, TR=w.TR, mats=w.mats,
+                    is_interface=orc.interface_flags(w.nx, w.ny, w.nz, w.omega, w.grain_mat),
+                    dep_flag=1, eps_0_nd=w.eps_0_nd)
+    if crit_relres:
+        f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-8, 4000
+    return f
+
+
+def cpu_port_rate(w, steps: int, budget_s: float):
+    """Times the oracle (FP64 CPU port, all host threads) on the film for up to
+    `steps` steps or `budget_s` seconds; returns (cell-steps/s, steps, seconds)."""
+    import oracle
+    orc = oracle.load()
+    f = make_oracle_film(w, orc)
+    P = [p.copy() for p in w.P_init]
+    phi = np.zeros(w.N)
+    E = None
+    done, t_total = 0, 0.0
+    Ez = w.sched.Ez
+    while done < steps:
+        t0 = time.perf_counter()
+        P, E, phi, _, _, rc = orc.run(f, P, phi, Ez[done:done + 1], np.array([0], np.int32), E=E)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total > budget_s:
+            break
+    return w.N * done / t_total, done, t_total
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from cmsl_gb300 import workloads as wl
+    import oracle
+    oracle.build()
+    w = wl.config(CONFIG_ID)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    # each step is a bounded sample: the full film, one time step
+    cpu_port_rate(w, max(1, min(args.warmup, 1)), 60.0)
+    rate, done, secs = cpu_port_rate(w, args.steps, 150.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-steps/s", "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(done, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "cells": w.N, "precision": "fp64", "pcg": "relres 1e-8",
+                   "implementation": "oracle (CPU FP64 port of the reference kernels, OpenMP)"},
+        "cpu_baseline": {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+                         "sample": "%d full time steps of %s (%d cells) from its initial state" %
+                                   (done, w.name, w.N)},
+        "e2e": {"value": rate, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from cmsl_gb300 import build
+    if rank == 0:
+        build.build()
+    if dist:
+        dist.barrier()
+    import cmsl_gb300 as cg
+    from cmsl_gb300 import workloads as wl
+
+    fp64 = args.precision == "fp64"
+    w = wl.config(CONFIG_ID)
+    kw = dict(precision=cg.FP64 if fp64 else cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8,
+              max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000)
+    film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **kw)
+    film.set_state(w.P_init)
+    K, W = args.steps, args.warmup
+    Ez = w.sched.Ez[: W + K]
+    rows = np.arange(W + K, dtype=np.int32)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        film.run(Ez[:W], rows[:W], stream=sp)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        clocks = Clocks(local)
+        clocks.start()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        film.run(Ez[W:W + K], rows[:K], stream=sp, sync=False)
+        ev1.record(stream)
+        ev1.synchronize()
+        film.sync()
+        clk = clocks.stop()
+        ms = ev0.elapsed_time(ev1)
+        torch.cuda.synchronize()
+    it, rf = film.iters(K)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_max = float(t.item())
+    value = world * w.N * K / (ms_max * 1e-3)
+
+    # per-kernel device times (CUDA events on the launch stream)
+    kms = film.time_kernels(reps=20, stream=sp)
+    mode = "fp64" if fp64 else "fp32"
+    n_iter = float(np.mean(it))
+    n_ref = float(np.mean(rf))
+    per_step = {"tdgl": kms[0], "setup": kms[1] * n_ref, "spmv": kms[2] * n_iter, "update": kms[3] * n_iter}
+    top = max(per_step, key=per_step.get)
+    ki = KERNELS.index(top)
+    peak, peak_kind = measured_peaks()
+    achieved = BYTES[mode][top] * w.N / (kms[ki] * 1e-3) / 1e9
+    traffic = ncu_traffic().get(mode, {}).get(top)
+    roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "bytes_per_cell": BYTES[mode][top],
+            "traffic": (traffic * w.N) if traffic is not None else None,
+            "kernel_ms": {k: float(kms[i]) for i, k in enumerate(KERNELS)},
+            "share": {k: per_step[k] / sum(per_step.values()) for k in per_step}}
+    launches = int(K * 2 + rf.sum() + 2 * it.sum())
+
+    # end to end through the C ABI: host state in, K steps, host rows + state out
+    film.set_state(w.P_init)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    film.set_state(w.P_init)
+    film.run(Ez[W:W + K], rows[:K])
+    r = film.rows(0, K)
+    P_out, phi_out = film.get_state()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    esz = 8 if fp64 else 4
+    h2d = 6 * w.N * esz + K * 12
+    d2h = K * 88 + 6 * w.N * esz + w.N * 8
+    e2e = {"value": w.N * K / e2e_s * world, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d // K,
+           "d2h_bytes_per_step": d2h // K,
+           "note": "per call: host P upload, K steps with host field/row arrays, host rows, P and phi download"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        rate, done, secs = cpu_port_rate(w, 3, 20.0)
+        cpu = {"value": rate, "unit": "cell-steps/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+               "sample": "%d time steps of %s on the oracle (FP64, %.1f s)" % (done, w.name, secs)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if fp64 else "f32", "data": "synthetic",
+            "config": {"workload": w.name, "cells": w.N, "grid": [w.nx, w.ny, w.nz],
+                       "precision": "fp64" if fp64 else "fp32-refined (fp64 phi, refine to 1e-8)",
+                       "pcg": "||b-A phi|| <= 1e-8 ||b||", "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "no flush: per-step state %.0f MB > 129 MB L2" % (film.device_bytes() / 1e6)},
+            "pcg_iters_per_step": n_iter, "refine_passes_per_step": n_ref,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    film.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

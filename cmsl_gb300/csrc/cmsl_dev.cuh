@@ -1,0 +1,110 @@
+// cmsl_dev.cuh -- device-side data layout shared by the kernels and the engine.
+//
+// Layout in HBM (one "batch" = one or more films, concatenated):
+//   * every per-cell array holds all films back to back; film f's cells start
+//     at FilmDev::off and are in the reference's C order i + nx*(j + ny*k);
+//   * P fields: two ping-pong sets of six SoA arrays (Pmx..Psz) in the
+//     compute type T (double for CMSL_FP64, float for CMSL_FP32_REFINED);
+//   * code[c]: grain id (bits 0-23, film-local) | material (bits 24-25) |
+//     interface flag (bit 26) -- replaces the reference's seven per-voxel FP64
+//     parameter arrays, omega and is_interface (kernels_evol.cu:133-146);
+//   * phi: two FP64 ping-pong potentials; PCG vectors r, p[2], q, dinv, x in T;
+//   * per-grain rotations TR (9 per grain, row major) in T.
+// Work is cut into items (film, x0, y0, z0..z1): one thread block per item,
+// a TX x TY thread tile marching through z0..z1.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cmsl {
+
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NT = TX * TY;
+constexpr int SX = TX + 2;
+constexpr int SY = TY + 2;
+constexpr int SPL = SX * SY;        // smem cells of one staged plane
+constexpr int NPART = 8;            // doubles of partial sums per item
+
+constexpr uint32_t GID_MASK = 0x00ffffffu;
+__host__ __device__ inline int code_gid(uint32_t c) { return (int)(c & GID_MASK); }
+__host__ __device__ inline int code_mat(uint32_t c) { return (int)((c >> 24) & 3u); }
+__host__ __device__ inline int code_iface(uint32_t c) { return (int)((c >> 26) & 1u); }
+constexpr uint32_t CODE_INVALID = 0x80000000u;   // grain id out of range: cell frozen
+
+// Per (material, interface) TDGL coefficients, computed on the host in the
+// reference's operation order (kernels_evol.cu:139-153, :212, :223).
+template <class T> struct Coef {
+    T relax;   // 1 - 6 A
+    T A;       // kappa dt / h^2
+    T LdT;     // Lfac * dt
+    T ag, ags; // 2 (alpha +- g_loc)
+    T b4, b12, g6, a02;
+};
+
+struct FilmDev {
+    int nx, ny, nz, zbc;
+    long long off;              // first cell of the film
+    int g_off;                  // first grain of the film in TR
+    int item_begin, item_end;
+    int dep_flag;
+    int ref_id;                 // Neumann pinned cell (film-local)
+    int crit;
+    int max_iter, max_refine, inner_max;
+    double h, dt, eps0nd, inv_N, two_h, h2, inv_h2, inv_2h;
+    double tol_abs2, tol_rel2, refine_tol2, inner_tol2;
+    double n_mat[3];            // voxels per material (sum of the reference's masks)
+    Coef<double> coef[6];       // index mat*2 + iface
+    Coef<float> coef32[6];
+    double epsf[9];             // harmonic face eps for (mat_c, mat_nb), depol_varEPS.cu:10-15
+    float epsf32[9];
+};
+
+struct SolveDev {               // per film, lives in device memory
+    double rz, rz0, pq, alpha, beta, rr, bb, rr64;
+    int iters;                  // PCG iterations of the current (inner) solve
+    int active;                 // inner PCG still running
+    int status;                 // 0 ok, 1 breakdown, 2 bad initial residual, 3 refine cap
+    int outer_active;           // FP32_REFINED: refinement still running
+    int refine;                 // refinement passes this step
+    int total_iters;            // PCG iterations this step
+    int phi_cur;                // which phi buffer is current
+    int sticky;                 // first non-zero status seen since set_state
+};
+
+struct Ctl {
+    int step;                   // steps done since set_state
+    int cur;                    // which P set is "old"
+    int run_step;               // step index within the current run (waveform index)
+    int pad;
+};
+
+template <class T> struct Fields {
+    T *P[2][6];
+    T *r, *q, *dinv, *x;
+    T *p[2];
+    const T *TR;
+};
+
+struct Dev {
+    const FilmDev *films;
+    const int4 *items;
+    int n_films, n_items;
+    const uint32_t *code;
+    double *phi[2];
+    double *partial;            // [n_items * NPART]
+    unsigned int *counter;      // one ticket counter (reset by the last block)
+    SolveDev *solve;            // [n_films]
+    Ctl *ctl;
+    const double *wave;         // [n_films * wstride] applied field per run step
+    const int *rows;            // [n_films * wstride] output row per run step (-1 none)
+    double *rowbuf;             // [n_films * rstride * 11]
+    int *iters_log;             // [n_films * wstride]
+    int *refine_log;            // [n_films * wstride]
+    int wstride, rstride;
+    int use_cond;
+    int force;                  // run the PCG kernels whatever the flags (kernel timing)
+    cudaGraphConditionalHandle h_inner, h_outer;
+};
+
+}  // namespace cmsl

@@ -1,0 +1,176 @@
+"""Python handle over a libcmsl_gb film (numpy in, numpy out).
+
+Mirrors the reference's per-simulation objects: the grain map and material
+table a ``SetupAndRunSimulation`` call builds (HZO_Code_github/src/main.cu:
+261-359) and the ``Evolve`` loop (src/evolve.cu:73-440) that advances it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+MAT_COLS = ("alpha", "beta", "gamma", "g", "a0", "kappa", "L", "eps_r")
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class Film:
+    """One film on the GPU.
+
+    mats: [3, 8] array, rows AFE, FE, DE; columns alpha, beta, gamma, g, a0,
+    kappa, L, eps_r (non-dimensional, as make_nd_wrt_reference gives them).
+    """
+
+    def __init__(self, nx, ny, nz, omega, grain_mat, TR, mats, *, del_h, del_t, dep_flag=1,
+                 zbc=_lib.DIRICHLET, eps_0_nd=0.0, is_interface=None, precision=_lib.FP64,
+                 pcg_crit=_lib.CRIT_REF, tol_abs=1e-3, tol_rel=1e-2, max_iter=4000,
+                 refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000):
+        L = lib()
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.N = self.nx * self.ny * self.nz
+        self.precision = precision
+        self._omega = np.ascontiguousarray(omega, np.int32)
+        self._gm = np.ascontiguousarray(grain_mat, np.int32)
+        self._tr = np.ascontiguousarray(TR, np.float64)
+        self._fl = None if is_interface is None else np.ascontiguousarray(is_interface, np.int32)
+        if self._omega.size != self.N:
+            raise ValueError("omega has %d cells, grid has %d" % (self._omega.size, self.N))
+        d = _lib.FilmDesc()
+        d.nx, d.ny, d.nz = self.nx, self.ny, self.nz
+        d.del_h, d.del_t = float(del_h), float(del_t)
+        d.dep_flag, d.zbc, d.eps_0_nd = int(dep_flag), int(zbc), float(eps_0_nd)
+        d.n_grains = int(self._gm.size)
+        d.omega, d.grain_mat, d.TR = _i(self._omega), _i(self._gm), _d(self._tr)
+        d.is_interface = _i(self._fl) if self._fl is not None else None
+        m = np.asarray(mats, np.float64).reshape(3, 8)
+        for q in range(3):
+            for c, n in enumerate(MAT_COLS):
+                setattr(d.mats[q], n, float(m[q, c]))
+        d.precision, d.pcg_crit = int(precision), int(pcg_crit)
+        d.tol_abs, d.tol_rel, d.max_iter = float(tol_abs), float(tol_rel), int(max_iter)
+        d.refine_tol, d.max_refine = float(refine_tol), int(max_refine)
+        d.inner_tol, d.inner_max_iter = float(inner_tol), int(inner_max_iter)
+        h = C.c_void_p()
+        check(L.cmsl_film_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self._n_rows = 0
+        self._n_steps = 0
+
+    @classmethod
+    def from_oracle_film(cls, f, **kw):
+        """Builds the GPU film for an oracle.Film description (tests, bench)."""
+        return cls(f.nx, f.ny, f.nz, f.omega, f.grain_mat, f.TR, f.mats, del_h=f.del_h, del_t=f.del_t,
+                   dep_flag=f.dep_flag, zbc=f.zbc, eps_0_nd=f.eps_0_nd, is_interface=f.is_interface,
+                   tol_abs=f.tol_abs, tol_rel=f.tol_rel, max_iter=f.max_iter, pcg_crit=f.crit, **kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cmsl_film_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state -----------------------------------------------------------
+    def set_state(self, P, phi=None):
+        P = [np.ascontiguousarray(p, np.float64) for p in P]
+        arr = (_dp * 6)(*[_d(p) for p in P])
+        ph = None if phi is None else np.ascontiguousarray(phi, np.float64)
+        check(lib().cmsl_film_set_state(self._h, arr, _d(ph) if ph is not None else None))
+
+    def get_state(self):
+        P = [np.zeros(self.N) for _ in range(6)]
+        phi = np.zeros(self.N)
+        arr = (_dp * 6)(*[_d(p) for p in P])
+        check(lib().cmsl_film_get_state(self._h, arr, _d(phi)))
+        return P, phi
+
+    # -- the P-E loop driver ----------------------------------------------
+    def run(self, Ez, rows=None, stream=None, sync=True):
+        Ez = np.ascontiguousarray(Ez, np.float64)
+        n = int(Ez.size)
+        r = None if rows is None else np.ascontiguousarray(rows, np.int32)
+        check(lib().cmsl_film_run(self._h, n, _d(Ez), _i(r) if r is not None else None,
+                                  C.c_void_p(stream) if stream else None))
+        self._n_steps = n
+        self._n_rows = int(r.max()) + 1 if r is not None and n and r.max() >= 0 else 0
+        if sync:
+            self.sync()
+
+    def sync(self):
+        check(lib().cmsl_film_sync(self._h))
+
+    def rows(self, first=0, n=None):
+        n = self._n_rows - first if n is None else n
+        out = np.zeros((max(n, 0), 11))
+        if n > 0:
+            check(lib().cmsl_film_get_rows(self._h, first, n, _d(out)))
+        return out
+
+    def iters(self, n=None):
+        n = self._n_steps if n is None else n
+        it = np.zeros(max(n, 1), np.int32)
+        rf = np.zeros(max(n, 1), np.int32)
+        if n > 0:
+            check(lib().cmsl_film_get_iters(self._h, n, _i(it), _i(rf)))
+        return it[:n], rf[:n]
+
+    # -- single pieces (parity tests) --------------------------------------
+    def tdgl_step(self, Ez):
+        check(lib().cmsl_film_tdgl_step(self._h, float(Ez)))
+
+    def depol(self):
+        it = np.zeros(2, np.int32)
+        st = np.zeros(1, np.int32)
+        check(lib().cmsl_film_depol(self._h, _i(it), _i(st)))
+        return {"iters": int(it[0]), "refine": int(it[1]), "status": int(st[0])}
+
+    def apply_operator(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.N)
+        check(lib().cmsl_film_apply_operator(self._h, _d(x), _d(y)))
+        return y
+
+    def efield(self):
+        E = [np.zeros(self.N) for _ in range(3)]
+        check(lib().cmsl_film_efield(self._h, _d(E[0]), _d(E[1]), _d(E[2])))
+        return E
+
+    def diag_inv(self):
+        y = np.zeros(self.N)
+        check(lib().cmsl_film_diag_inv(self._h, _d(y)))
+        return y
+
+    def time_kernels(self, reps=20, stream=None):
+        """Average ms per launch of [tdgl, solve set-up, spmv, update]."""
+        ms = np.zeros(4)
+        check(lib().cmsl_film_time_kernels(self._h, int(reps), C.c_void_p(stream) if stream else None,
+                                           _d(ms)))
+        return ms
+
+    def device_bytes(self):
+        b = C.c_size_t()
+        check(lib().cmsl_film_device_bytes(self._h, C.byref(b)))
+        return int(b.value)

@@ -1,0 +1,148 @@
+/*
+ * cmsl.h -- C ABI of libcmsl_gb, the GB300 (sm_103a) implementation of the
+ * HZO phase-field hot path of jhb6617-arch/cmsl: the explicit TDGL step, the
+ * Jacobi-PCG depolarisation solve and the P-E loop driver that sequences them.
+ *
+ * Conventions: plain C types only; host pointers unless a name says _dev;
+ * every call returns cmsl_status and never exits the process (the reference
+ * prints and calls exit(1), HZO_Code_github/include/check.h:9-83);
+ * cmsl_last_error() gives the text of the last failure on the calling thread.
+ * A film handle is not thread-safe; distinct handles are independent.
+ *
+ * Cell order is the reference's C order id = i + nx*(j + ny*k)
+ * (HZO_Code_github/src/kernels_evol.cu:65).  Field arrays are the six
+ * polarisation components Pmx, Pmy, Pmz, Psx, Psy, Psz (non-dimensional).
+ */
+#ifndef CMSL_H
+#define CMSL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CMSL_OK = 0,
+    CMSL_ERR_ARG = 1,      /* bad argument or size */
+    CMSL_ERR_CUDA = 2,     /* CUDA runtime failure (no device, launch error) */
+    CMSL_ERR_IO = 3,       /* file missing, short or malformed */
+    CMSL_ERR_PCG = 4,      /* PCG breakdown or non-finite residual in some step */
+    CMSL_ERR_STATE = 5,    /* call out of order */
+    CMSL_ERR_NOMEM = 6
+} cmsl_status;
+
+typedef enum { CMSL_AFE = 0, CMSL_FE = 1, CMSL_DE = 2 } cmsl_material_id;
+typedef enum { CMSL_DIRICHLET = 0, CMSL_NEUMANN = 1 } cmsl_zbc;
+
+/* CMSL_FP64: FP64 storage and arithmetic, TDGL and operator bit-identical to
+ *   the reference kernels; one PCG solve per step.
+ * CMSL_FP32_REFINED: FP32 fields, stencils and PCG vectors; PCG dots summed in
+ *   FP32 within a warp and FP64 above it; the potential is kept in FP64 and an
+ *   outer FP64 residual-refinement loop drives ||b - A phi|| / ||b|| below
+ *   refine_tol. */
+typedef enum { CMSL_FP64 = 0, CMSL_FP32_REFINED = 1 } cmsl_precision;
+
+/* Stop test of the (inner) PCG.  CMSL_CRIT_REF is the reference's
+ * (depol_varEPS.cu:472-474): continue while r.z > tol_abs^2 and
+ * r.z/r0.z0 > tol_rel^2.  CMSL_CRIT_RELRES: continue while
+ * ||r||_2 > tol_rel * ||b||_2. */
+typedef enum { CMSL_CRIT_REF = 0, CMSL_CRIT_RELRES = 1 } cmsl_pcg_crit;
+
+/* Non-dimensional material parameters, as make_nd_wrt_reference produces them
+ * (HZO_Code_github/src/main.cu:232-256, include/types.h:22-28). */
+typedef struct {
+    double alpha, beta, gamma, g, a0, kappa, L, eps_r;
+} cmsl_material;
+
+typedef struct {
+    int nx, ny, nz;
+    double del_h, del_t;
+    int dep_flag;                 /* 0: no depolarisation solve (E_dep = 0) */
+    int zbc;                      /* cmsl_zbc for the potential */
+    double eps_0_nd;              /* main.cu:343-344 */
+    int n_grains;
+    const int32_t *omega;         /* [N] grain id per cell, 0 <= id < n_grains */
+    const int32_t *grain_mat;     /* [n_grains] cmsl_material_id */
+    const double *TR;             /* [9*n_grains] lab->crystal rotation, row major */
+    const int32_t *is_interface;  /* [N] 0/1, or NULL: built as main.cu:13-42 does */
+    cmsl_material mats[3];        /* indexed by cmsl_material_id */
+    int precision;                /* cmsl_precision */
+    int pcg_crit;                 /* cmsl_pcg_crit (FP64 solve; FP32 inner solve uses RELRES-free rz test) */
+    double tol_abs, tol_rel;      /* reference defaults 1e-3, 1e-2 (global.cu:140-144) */
+    int max_iter;                 /* reference default 4000 */
+    double refine_tol;            /* FP32_REFINED: outer ||r||/||b|| target, e.g. 1e-8 */
+    int max_refine;               /* FP32_REFINED: outer passes per step (>= 2) */
+    double inner_tol;             /* FP32_REFINED: inner sqrt(r.z/r0.z0) target, e.g. 1e-4 */
+    int inner_max_iter;           /* FP32_REFINED: inner iterations per pass */
+} cmsl_film_desc;
+
+typedef struct cmsl_film cmsl_film;
+
+/* One sweep row: the 11 averages the reference writes per output step
+ * (evolve.cu:256-357): <Pm_z>, <Ps_z>, <Pm_z^loc>, <Ps_z^loc>, <Pm_z>_FE, f_FE,
+ * <Pm_z>_AFE, f_AFE, <Pm_z>_DE, f_DE, N_steps_done.  Non-dimensional. */
+#define CMSL_ROW_WIDTH 11
+
+const char *cmsl_last_error(void);
+const char *cmsl_version(void);
+
+/* Replaces the film set-up of SetupAndRunSimulation/AllocateData/Init_Conf
+ * (main.cu:261-359, allocateVars.cu:4-112, init_conf.cu:68-106): uploads the
+ * grain map, builds the per-cell code, the coefficient tables and the Jacobi
+ * diagonal (depol_varEPS.cu:126-180, built once instead of every step), and
+ * zeroes P, phi and the work vectors. */
+cmsl_status cmsl_film_create(const cmsl_film_desc *desc, cmsl_film **out);
+cmsl_status cmsl_film_destroy(cmsl_film *film);
+
+/* Host <-> device state.  P: 6 arrays of N doubles; phi: N doubles or NULL
+ * (leaves phi unchanged / not read).  set_state also resets the step counter. */
+cmsl_status cmsl_film_set_state(cmsl_film *film, const double *const P[6], const double *phi);
+cmsl_status cmsl_film_get_state(cmsl_film *film, double *const P[6], double *phi);
+
+/* The P-E loop driver body (Evolve, evolve.cu:217-409): runs n_steps TDGL steps,
+ * each followed by the depolarisation solve when dep_flag.  Ez[s] is the
+ * applied non-dimensional field of step s (host array); row[s] >= 0 stores the
+ * sweep averages of step s as row row[s] (host array or NULL).  The whole loop
+ * is enqueued on `stream` (a cudaStream_t, NULL = legacy default) as CUDA
+ * graphs with device-side PCG loops; the call returns after enqueueing.
+ * cmsl_film_sync waits and reports a PCG failure seen by any step. */
+cmsl_status cmsl_film_run(cmsl_film *film, int n_steps, const double *Ez, const int32_t *row,
+                          void *stream);
+cmsl_status cmsl_film_sync(cmsl_film *film);
+
+/* Copies rows [first, first+n) (n*CMSL_ROW_WIDTH doubles) of the last run. */
+cmsl_status cmsl_film_get_rows(cmsl_film *film, int first, int n, double *out);
+
+/* Per-step solver counters of the last run: PCG iterations (summed over the
+ * refinement passes) and refinement passes (1 in FP64 mode). */
+cmsl_status cmsl_film_get_iters(cmsl_film *film, int n, int32_t *pcg_iters, int32_t *refine_passes);
+
+/* Single pieces of the path on the film's current state, for parity tests:
+ *  - tdgl_step: one TDGL step with applied field Ez (no solve), the E_dep of
+ *    kernelCalc_antiferro computed from the current phi (Calc_EfieldMag);
+ *  - depol: one Depol_field (RHS from the current Pm, warm-started PCG);
+ *  - apply_operator: y = A x with the film's operator (apply_A), FP64 or FP32;
+ *  - efield: E = -grad(phi) of the current phi (Calc_EfieldMag). */
+cmsl_status cmsl_film_tdgl_step(cmsl_film *film, double Ez);
+cmsl_status cmsl_film_depol(cmsl_film *film, int32_t *iters, int32_t *status);
+cmsl_status cmsl_film_apply_operator(cmsl_film *film, const double *x, double *y);
+cmsl_status cmsl_film_efield(cmsl_film *film, double *Ex, double *Ey, double *Ez);
+cmsl_status cmsl_film_diag_inv(cmsl_film *film, double *dinv);
+
+/* Average device time (ms, CUDA events on the launch stream) of each kernel
+ * of a step, each launched `reps` times back to back on the current state:
+ * ms[0] TDGL step, ms[1] solve set-up (FP64 RHS + r0, or FP32_REFINED FP64
+ * residual pass), ms[2] PCG p-update + SpMV + p.Ap, ms[3] PCG x/r update +
+ * r.z.  The PCG kernels run with the solve forced active, so the call
+ * changes the film's work vectors; run it after the steps being measured. */
+cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, double *ms);
+
+/* Bytes of device memory the film holds. */
+cmsl_status cmsl_film_device_bytes(cmsl_film *film, size_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

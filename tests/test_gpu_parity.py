@@ -1,0 +1,181 @@
+"""GPU parity: libcmsl_gb (through its C ABI) against the oracle.
+
+FP64 mode: the TDGL step, operator, Jacobi diagonal and E field are compared
+bit for bit (the kernels use explicitly rounded FP64 operations in the
+reference's order); PCG-dependent quantities agree to dot-product summation
+order (relative 1e-10 after tens of steps).
+FP32_REFINED mode: compared with an FP64 oracle run whose PCG is converged
+far below the refinement target; tolerances are stated per test.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.films import random_film
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(4, 4, 3), (5, 7, 4), (16, 12, 6), (33, 9, 5), (40, 17, 9), (64, 16, 8)]
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cmsl_gb300 import build
+    build.build()
+    import cmsl_gb300
+    return cmsl_gb300
+
+
+@pytest.fixture(scope="module")
+def orc():
+    return oracle.load()
+
+
+def _film(cg, f, **kw):
+    return cg.Film.from_oracle_film(f, **kw)
+
+
+def _same(a, b):
+    return all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+@pytest.mark.parametrize("shape", SIZES)
+@pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
+def test_tdgl_step_bitwise(gpu, orc, shape, zbc):
+    f, P = random_film(*shape, seed=sum(shape), zbc=zbc, layered=True)
+    phi = np.random.default_rng(3).normal(size=f.N) * 0.2
+    E = orc.efield(f, phi)
+    want, _ = orc.tdgl_step(f, P, 0.173, E)
+    with _film(gpu, f) as g:
+        g.set_state(P, phi)
+        g.tdgl_step(0.173)
+        got, phi_out = g.get_state()
+    assert _same(got, want)
+    assert np.array_equal(phi_out, phi)
+
+
+@pytest.mark.parametrize("shape", SIZES)
+def test_tdgl_step_no_depolarisation(gpu, orc, shape):
+    f, P = random_film(*shape, seed=2 + sum(shape), dep_flag=0)
+    want, _ = orc.tdgl_step(f, P, -0.31)
+    with _film(gpu, f) as g:
+        g.set_state(P)
+        g.tdgl_step(-0.31)
+        got, _ = g.get_state()
+    assert _same(got, want)
+
+
+@pytest.mark.parametrize("shape", SIZES)
+@pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
+def test_operator_diag_efield_bitwise(gpu, orc, shape, zbc):
+    f, P = random_film(*shape, seed=7, zbc=zbc)
+    x = np.random.default_rng(5).normal(size=f.N)
+    with _film(gpu, f) as g:
+        assert np.array_equal(g.apply_operator(x), orc.apply_A(f, x))
+        assert np.array_equal(g.diag_inv(), orc.diag_inv(f))
+        g.set_state(P, x)
+        assert _same(g.efield(), orc.efield(f, x))
+
+
+@pytest.mark.parametrize("shape", [(16, 12, 6), (33, 9, 5), (40, 17, 9)])
+@pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
+def test_depol_solve_fp64(gpu, orc, shape, zbc):
+    f, P = random_film(*shape, seed=11, zbc=zbc, eps_0_nd=3.0)
+    f.tol_abs, f.tol_rel = 1e-10, 1e-8
+    phi0 = np.zeros(f.N)
+    phi_w, E_w, _, info = orc.depol_field(f, P[:3], phi0)
+    with _film(gpu, f) as g:
+        g.set_state(P, phi0)
+        res = g.depol()
+        _, phi = g.get_state()
+    assert res["status"] == 0 and info["status"] == 0
+    assert abs(res["iters"] - info["iters"]) <= 1
+    assert np.abs(phi - phi_w).max() <= 1e-10 * np.abs(phi_w).max()
+
+
+@pytest.mark.parametrize("shape", [(16, 12, 6), (33, 9, 5)])
+@pytest.mark.parametrize("graph", [True, False])
+def test_run_fp64_matches_oracle(gpu, orc, shape, graph, monkeypatch):
+    """Twenty full steps (TDGL + depolarisation) with a staircase field and a
+    sweep row per step: P, phi and rows to 1e-10 relative."""
+    if not graph:
+        monkeypatch.setenv("CMSL_NO_GRAPH", "1")
+    f, P = random_film(*shape, seed=21, eps_0_nd=4.0, p_scale=0.2)
+    f.tol_abs, f.tol_rel = 1e-3, 1e-2           # the reference's defaults
+    n = 20
+    Ez = np.linspace(0.0, 0.5, n)
+    rows = np.arange(n, dtype=np.int32)
+    Pw, Ew, phiw, statw, itw, rc = orc.run(f, P, np.zeros(f.N), Ez, rows)
+    assert rc == 0
+    with _film(gpu, f) as g:
+        g.set_state(P)
+        g.run(Ez, rows)
+        Pg, phig = g.get_state()
+        rg = g.rows()
+        itg, _ = g.iters()
+    for a, b in zip(Pg, Pw):
+        assert np.abs(a - b).max() <= 1e-10 * max(1e-30, np.abs(b).max())
+    assert np.abs(phig - phiw).max() <= 1e-9 * np.abs(phiw).max()
+    assert np.abs(rg[:, :10] - statw[:, :10]).max() <= 1e-10
+    assert np.array_equal(rg[:, 10], np.arange(1, n + 1))
+    assert np.abs(itg - itw).max() <= 1
+
+
+def test_rows_material_fractions(gpu, orc):
+    f, P = random_film(24, 20, 6, seed=4, fracs=(0.3, 0.5, 0.2))
+    with _film(gpu, f) as g:
+        g.set_state(P)
+        g.run(np.array([0.1]), np.array([0], np.int32))
+        r = g.rows()[0]
+        Pg, _ = g.get_state()
+    Pn, loc = orc.tdgl_step(f, P, 0.1)
+    st = orc.sweep_stats(f, Pn[2], Pn[5], loc[2], loc[5])
+    assert np.allclose(r[:10], st, rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("shape", [(16, 12, 6), (40, 17, 9)])
+def test_run_fp32_refined_vs_fp64_oracle(gpu, orc, shape):
+    """FP32 fields + FP64-refined potential against the FP64 oracle solved to
+    ||r|| <= 1e-12 ||b||: fields within 2e-5 of max |P| after 30 steps,
+    potential within 1e-4 relative, rows within 1e-5."""
+    f, P = random_film(*shape, seed=31, eps_0_nd=4.0, p_scale=0.2)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    n = 30
+    Ez = np.linspace(0.0, -0.4, n)
+    rows = np.arange(n, dtype=np.int32)
+    Pw, _, phiw, statw, _, rc = orc.run(f, P, np.zeros(f.N), Ez, rows)
+    assert rc == 0
+    import cmsl_gb300 as cg
+    with _film(gpu, f, precision=cg.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-4) as g:
+        g.set_state(P)
+        g.run(Ez, rows)
+        Pg, phig = g.get_state()
+        rg = g.rows()
+        it, rf = g.iters()
+    for a, b in zip(Pg, Pw):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+    assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
+    assert np.abs(rg[:, :10] - statw[:, :10]).max() <= 1e-5
+    assert (rf >= 1).all() and (it >= 1).all()
+
+
+def test_fp32_refined_reaches_refine_tolerance(gpu, orc):
+    """After one refined solve ||b - A phi|| / ||b|| <= 1e-8 (checked in FP64 by the oracle)."""
+    f, P = random_film(40, 17, 9, seed=41, eps_0_nd=4.0)
+    import cmsl_gb300 as cg
+    with _film(gpu, f, precision=cg.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-4) as g:
+        g.set_state(P)
+        res = g.depol()
+        Pg, phi = g.get_state()
+    assert res["status"] == 0
+    div = orc.divergence(f, Pg[0], Pg[1], Pg[2])
+    b = -div
+    k = np.repeat(np.arange(f.nz), f.nx * f.ny)
+    b[(k == 0) | (k == f.nz - 1)] = 0.0
+    r = b - orc.apply_A(f, phi)
+    assert np.linalg.norm(r) <= 1.2e-8 * np.linalg.norm(b)
