@@ -135,7 +135,7 @@ def test_rows_material_fractions(gpu, orc):
         Pg, _ = g.get_state()
     Pn, loc = orc.tdgl_step(f, P, 0.1)
     st = orc.sweep_stats(f, Pn[2], Pn[5], loc[2], loc[5])
-    assert np.allclose(r[:10], st, rtol=1e-12, atol=1e-15)
+    assert np.allclose(r[:10], st[:10], rtol=1e-12, atol=1e-15)
 
 
 @pytest.mark.parametrize("shape", [(16, 12, 6), (40, 17, 9)])
