@@ -53,6 +53,7 @@ struct FilmDev {
     int max_iter, max_refine, inner_max;
     double h, dt, eps0nd, inv_N, two_h, h2, inv_h2, inv_2h;
     double tol_abs2, tol_rel2, refine_tol2, inner_tol2;
+    float inv_h2f, inv_2hf, eps0f, pad_f;
     double n_mat[3];            // voxels per material (sum of the reference's masks)
     Coef<double> coef[6];       // index mat*2 + iface
     Coef<float> coef32[6];
@@ -70,6 +71,18 @@ struct SolveDev {               // per film, lives in device memory
     int total_iters;            // PCG iterations this step
     int phi_cur;                // which phi buffer is current
     int sticky;                 // first non-zero status seen since set_state
+    double inner_tol2;          // inner target of the current refinement pass
+    int inner_max;              // inner iteration cap of the current pass
+    int pad2;
+};
+
+// Extra vectors of the single-reduction FP32 PCG (FP32_REFINED mode).
+struct CgBuf {
+    float *r[2], *w[2], *s[2];  // ping-pong by iteration parity
+    float *x, *p;
+    unsigned int *arrive;       // grid-barrier arrival counter (reset by k_refine)
+    double *part;               // [2][grid][2] per-block partial sums, by iteration parity
+    int *err;                   // barrier timeout flag
 };
 
 struct Ctl {
@@ -104,6 +117,7 @@ struct Dev {
     int wstride, rstride;
     int use_cond;
     int force;                  // run the PCG kernels whatever the flags (kernel timing)
+    unsigned int *arrive;       // grid-barrier counter of the persistent PCG (or null)
     cudaGraphConditionalHandle h_inner, h_outer;
 };
 

@@ -38,6 +38,9 @@ template <class T> __device__ __forceinline__ T dvd(Fast, T a, T b) { return a /
 template <class T> __device__ __forceinline__ const Coef<T> &coef_of(const FilmDev *f, int i);
 template <> __device__ __forceinline__ const Coef<double> &coef_of<double>(const FilmDev *f, int i) { return f->coef[i]; }
 template <> __device__ __forceinline__ const Coef<float> &coef_of<float>(const FilmDev *f, int i) { return f->coef32[i]; }
+template <class T> __device__ __forceinline__ T inv_h2_of(const FilmDev *f);
+template <> __device__ __forceinline__ double inv_h2_of<double>(const FilmDev *f) { return f->inv_h2; }
+template <> __device__ __forceinline__ float inv_h2_of<float>(const FilmDev *f) { return f->inv_h2f; }
 template <class T> __device__ __forceinline__ T epsf_of(const FilmDev *f, int i);
 template <> __device__ __forceinline__ double epsf_of<double>(const FilmDev *f, int i) { return f->epsf[i]; }
 template <> __device__ __forceinline__ float epsf_of<float>(const FilmDev *f, int i) { return f->epsf32[i]; }
@@ -149,7 +152,7 @@ __device__ __forceinline__ bool uniform_flag(const int *p)
 
 __device__ __forceinline__ void set_cond(const Dev &d, cudaGraphConditionalHandle h, int value)
 {
-    if (d.use_cond) cudaGraphSetConditional(h, value ? 1u : 0u);
+    if (d.use_cond && h) cudaGraphSetConditional(h, value ? 1u : 0u);
 }
 
 // ------------------------------------------------------------- operator
@@ -172,7 +175,7 @@ __device__ __forceinline__ T op_row(const FilmDev *f, int mc, int me, int mw, in
     if constexpr (sizeof(T) == 8 && std::is_same<M, Exact>::value)
         a = dvd(m, a, (T)f->h2);
     else
-        a = a * (T)f->inv_h2;
+        a = a * inv_h2_of<T>(f);
     return -a;
 }
 
@@ -365,7 +368,10 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
                 acc[1] += pn[5];
                 acc[2] += pMZl;
                 acc[3] += pSZl;
-                acc[mat == 1 ? 4 : (mat == 0 ? 5 : 6)] += pn[2];
+                const T pz = pn[2];
+                acc[4] += (mat == 1) ? pz : (T)0;
+                acc[5] += (mat == 0) ? pz : (T)0;
+                acc[6] += (mat == 2) ? pz : (T)0;
             }
         }
         if (g.valid) {
@@ -692,6 +698,13 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
             } else {
                 S->active = isfinite(S->rz) && S->rz > 0.0;
                 if (!S->active) { S->outer_active = 0; S->status = 2; }
+                // inner target: just enough reduction to reach the refinement
+                // tolerance in this pass (half-margin), between the FP32 floor
+                // inner_tol and 1e-2
+                double want = 0.25 * ff->refine_tol2 * sTot[1] / sTot[0];
+                want = fmax(want, ff->inner_tol2);
+                S->inner_tol2 = fmin(want, 1e-4);
+                S->inner_max = ff->inner_max;
             }
             any_outer |= S->outer_active;
             any_inner |= S->active;
@@ -700,6 +713,7 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
     if (threadIdx.x == 0) {
         set_cond(d, d.h_outer, any_outer);
         set_cond(d, d.h_inner, any_inner);
+        if (d.arrive) *d.arrive = 0u;
         *d.counter = 0u;
     }
 }

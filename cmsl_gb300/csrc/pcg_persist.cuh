@@ -1,0 +1,368 @@
+// pcg_persist.cuh -- persistent single-reduction Jacobi-PCG for the FP32 inner
+// solve of CMSL_FP32_REFINED.
+//
+// The reference runs textbook PCG with two blocking dot products per
+// iteration (depol_varEPS.cu:472-522).  Here the inner solve of each
+// refinement pass is one cooperative kernel that stays resident for all its
+// iterations.  It uses the Chronopoulos-Gear recurrences, which need a single
+// reduction (two dots) per iteration, so every iteration is one sweep over the
+// film and one grid barrier:
+//
+//   p_i = u_i + b_i p_{i-1}      s_i = w_i + b_i s_{i-1}
+//   x  += a_i p_i                r_{i+1} = r_i - a_i s_i
+//   u_{i+1} = D^-1 r_{i+1}       w_{i+1} = A u_{i+1}
+//   g_{i+1} = (r_{i+1}, u_{i+1}) d_{i+1} = (w_{i+1}, u_{i+1})
+//   b_{i+1} = g_{i+1}/g_i        a_{i+1} = g_{i+1} / (d_{i+1} - b_{i+1} g_{i+1} / a_i)
+//
+// w = A u needs u at the x/y/z neighbours; u there is recomputed from the
+// neighbour's r_i, w_i, s_{i-1} (r, w, s ping-pong by iteration parity so
+// that no block overwrites a value another block still reads).
+//
+// Grid barrier: arrival counter + bounded spin (about a second), after which
+// the block records a timeout and leaves; no wait is unbounded.  Every block
+// then sums all blocks' partials in block order, so all blocks hold the same
+// scalars and take the same loop decisions without a second barrier.
+#pragma once
+#include "kernels.cuh"
+
+namespace cmsl {
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+constexpr unsigned long long BARRIER_SPIN_LIMIT = 20000000ull;   // x ~100 ns sleeps
+
+// Brick geometry of the persistent solver: a block of PBX x PBY threads owns
+// the TX x TY column tile plus its one-cell x/y halo; it stages u = D^-1 r for
+// PZ planes (+1 above and below) in shared memory, then applies the stencil.
+constexpr int PBX = TX + 2;
+constexpr int PBY = TY + 2;
+constexpr int PNT = PBX * PBY;          // 340 threads
+constexpr int PNW = (PNT + 31) / 32;    // 11 warps
+constexpr int PZ = 8;
+constexpr int PBP = PZ + 2;
+
+// Block sum over PNT threads: FP32 within a warp, FP64 across warps.
+template <int NV, class T>
+__device__ __forceinline__ void block_sum_p(T (&v)[NV], double (*sm)[NV], double (&out)[NV])
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const T s = warp_sum(v[i]);
+        if (lane == 0) sm[w][i] = (double)s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        #pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = 0.0;
+            for (int q = 0; q < PNW; ++q) s += sm[q][i];
+            out[i] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// Writes this block's two partial sums, waits for all blocks, and returns the
+// grid totals (identical in every block).  False if the wait timed out.
+__device__ __forceinline__ bool grid_allreduce2(const CgBuf &B, int parity, unsigned int &target,
+                                                float v0, float v1, double (*sm)[2], double &t0,
+                                                double &t1)
+{
+    __shared__ int s_ok;
+    __shared__ double s_tot[2];
+    float a[2] = {v0, v1};
+    double blk[2];
+    block_sum_p<2, float>(a, sm, blk);
+    double *part = B.part + (size_t)parity * gridDim.x * 2;
+    target += gridDim.x;
+    if (threadIdx.x == 0) {
+        __stcg(part + 2 * blockIdx.x, blk[0]);
+        __stcg(part + 2 * blockIdx.x + 1, blk[1]);
+        __threadfence();
+        atomicAdd(B.arrive, 1u);
+        int ok = 1;
+        unsigned long long spins = 0;
+        while (ld_acquire(B.arrive) < target) {
+            if (++spins > BARRIER_SPIN_LIMIT) { ok = 0; atomicExch(B.err, 1); break; }
+            __nanosleep(64);
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) return false;
+    double q[2] = {0.0, 0.0};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += PNT) {
+        q[0] += __ldcg(part + 2 * b);
+        q[1] += __ldcg(part + 2 * b + 1);
+    }
+    double tot[2];
+    block_sum_p<2, double>(q, sm, tot);
+    if (threadIdx.x == 0) { s_tot[0] = tot[0]; s_tot[1] = tot[1]; }
+    __syncthreads();
+    t0 = s_tot[0];
+    t1 = s_tot[1];
+    return true;
+}
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Shared-memory carve-up of one brick (dynamic shared memory).
+constexpr int PNPL = PBP * PBY * PBX;   // staged cells, all planes
+constexpr int PNOWN = PZ * PBY * PBX;   // own planes
+struct BrickSmem {
+    float *r, *w, *s, *d, *u, *x, *p;
+    uint32_t *c;
+};
+constexpr size_t PSMEM_BYTES = sizeof(float) * (6 * PNPL + 2 * PNOWN);
+
+__device__ __forceinline__ BrickSmem brick_smem(float *base)
+{
+    BrickSmem m;
+    m.r = base; m.w = base + PNPL; m.s = base + 2 * PNPL; m.d = base + 3 * PNPL;
+    m.c = (uint32_t *)(base + 4 * PNPL); m.u = base + 5 * PNPL;
+    m.x = base + 6 * PNPL; m.p = base + 6 * PNPL + PNOWN;
+    return m;
+}
+
+// Film constants held in registers for the whole solve (the compiler would
+// otherwise reload them from global memory after every float store).
+struct FilmC {
+    int nx, ny, nz, zbc, ref_id, plane;
+    long long off;
+    float inv_h2;
+};
+
+__device__ __forceinline__ bool id_row(const FilmC &F, int k, int pl)
+{
+    if (F.zbc == 0) return k == 0 || k == F.nz - 1;
+    return pl + k * F.plane == F.ref_id;
+}
+
+// One brick (tile x0,y0; planes z0..z1-1, z1 - z0 <= PZ).  INIT: w_0 = A D^-1 r_0
+// and its dots.  Otherwise iteration i with parity c and (alpha, beta) = (a_i, b_i).
+// Stage (cp.async, every load of the brick in flight at once) -> pointwise
+// phase from shared memory -> stencil phase.  UNI: all materials share one
+// eps, so A is the constant-coefficient 7-point operator and no material codes
+// are read.
+template <bool INIT, bool UNI>
+__device__ __forceinline__ void cg_brick(const FilmC &F, const CgBuf &B, const uint32_t *__restrict__ code,
+                                         const float *__restrict__ dv, int x0, int y0, int z0, int z1, int c,
+                                         bool first, float alpha, float beta, float &gacc, float &dacc,
+                                         const BrickSmem &sm, const float *sEps)
+{
+    const int nx = F.nx, ny = F.ny, nz = F.nz, plane = F.plane;
+    const int bx = threadIdx.x % PBX, by = threadIdx.x / PBX;
+    const int wx = min(TX, nx - x0), wy = min(TY, ny - y0);
+    const bool own = bx >= 1 && bx <= wx && by >= 1 && by <= wy;
+    const bool ex = bx == 0 || bx == wx + 1, ey = by == 0 || by == wy + 1;
+    const bool need = bx <= wx + 1 && by <= wy + 1 && !(ex && ey);
+    const int gx = (x0 - 1 + bx + nx) % nx, gy = (y0 - 1 + by + ny) % ny;
+    const int pl = gx + nx * gy;
+    // parity selects by value: a dynamically indexed parameter array would be
+    // copied to local memory
+    const float *__restrict__ rA = (c ? B.r[1] : B.r[0]) + F.off;
+    const float *__restrict__ wA = (c ? B.w[1] : B.w[0]) + F.off;
+    const float *__restrict__ sA = (c ? B.s[1] : B.s[0]) + F.off;
+    float *__restrict__ rB = (c ? B.r[0] : B.r[1]) + F.off;
+    float *__restrict__ sB = (c ? B.s[0] : B.s[1]) + F.off;
+    float *__restrict__ wB = (INIT ? B.w[0] : (c ? B.w[0] : B.w[1])) + F.off;
+    float *__restrict__ x = B.x + F.off;
+    float *__restrict__ p = B.p + F.off;
+    constexpr int PP = PBY * PBX;
+    const int col = by * PBX + bx;
+    const int klo = own ? max(z0 - 1, 0) : z0;
+    const int khi = own ? min(z1, nz - 1) : z1 - 1;
+
+    if (need) {
+        for (int k = klo; k <= khi; ++k) {
+            const int o = pl + k * plane;
+            const int si = (k - z0 + 1) * PP + col;
+            cp_async4(sm.r + si, rA + o);
+            cp_async4(sm.d + si, dv + o);
+            if (!UNI) cp_async4(sm.c + si, code + o);
+            if (!INIT) {
+                cp_async4(sm.w + si, wA + o);
+                if (!first) cp_async4(sm.s + si, sA + o);
+                if (!first && own && k >= z0 && k < z1) {
+                    const int oi = (k - z0) * PP + col;
+                    cp_async4(sm.x + oi, x + o);
+                    cp_async4(sm.p + oi, p + o);
+                }
+            }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // u_{i+1} = D^-1 r_{i+1} for every staged cell; own cells do their pointwise updates
+    if (need) {
+        for (int k = klo; k <= khi; ++k) {
+            const int si = (k - z0 + 1) * PP + col;
+            const float dd = sm.d[si], ri = sm.r[si];
+            const bool mine = own && k >= z0 && k < z1;
+            float u, rn;
+            if (INIT) {
+                rn = ri;
+                u = dd * ri;
+            } else {
+                const float wi = sm.w[si];
+                const float sv = first ? wi : fmaf(beta, sm.s[si], wi);
+                rn = fmaf(-alpha, sv, ri);
+                u = dd * rn;
+                if (mine) {
+                    const int o = pl + k * plane;
+                    const int oi = (k - z0) * PP + col;
+                    const float ui = dd * ri;
+                    const float pi = first ? ui : fmaf(beta, sm.p[oi], ui);
+                    x[o] = first ? alpha * pi : fmaf(alpha, pi, sm.x[oi]);
+                    p[o] = pi;
+                    sB[o] = sv;
+                    rB[o] = rn;
+                }
+            }
+            if (mine) gacc = fmaf(rn, u, gacc);
+            sm.u[si] = u;
+        }
+    }
+    __syncthreads();
+    // w_{i+1} = A u_{i+1} on own cells (depol_varEPS.cu:101-123 operator order)
+    if (own) {
+        for (int k = z0; k < z1; ++k) {
+            const int zi = k - z0 + 1;
+            const int si = zi * PP + col;
+            const float uc = sm.u[si];
+            float wv;
+            if (id_row(F, k, pl)) {
+                wv = uc;
+            } else {
+                int zu = zi + 1, zd = zi - 1;
+                if (F.zbc != 0) {
+                    if (k == 0) zd = zu;
+                    else if (k == nz - 1) zu = zd;
+                }
+                const int su = zu * PP + col, sd = zd * PP + col;
+                const float ue = sm.u[si + 1], uw = sm.u[si - 1], un = sm.u[si + PBX], us = sm.u[si - PBX];
+                const float uu = sm.u[su], ud = sm.u[sd];
+                float a;
+                if (UNI) {
+                    const float e0 = sEps[0];
+                    a = e0 * ((((((ue - uc) - (uc - uw)) + (un - uc)) - (uc - us)) + (uu - uc)) - (uc - ud));
+                } else {
+                    const int mc = code_mat(sm.c[si]) * 3;
+                    a = sEps[mc + code_mat(sm.c[si + 1])] * (ue - uc) - sEps[mc + code_mat(sm.c[si - 1])] * (uc - uw);
+                    a += sEps[mc + code_mat(sm.c[si + PBX])] * (un - uc);
+                    a -= sEps[mc + code_mat(sm.c[si - PBX])] * (uc - us);
+                    a += sEps[mc + code_mat(sm.c[su])] * (uu - uc);
+                    a -= sEps[mc + code_mat(sm.c[sd])] * (uc - ud);
+                }
+                wv = -(a * F.inv_h2);
+            }
+            wB[pl + k * plane] = wv;
+            dacc = fmaf(wv, uc, dacc);
+        }
+    }
+    __syncthreads();
+}
+
+template <bool INIT, bool UNI>
+__device__ __forceinline__ void cg_sweep_all(const Dev &d, const FilmC &F, const CgBuf &B, const float *dinv,
+                                             int c, bool first, float alpha, float beta, float &ga, float &da,
+                                             const BrickSmem &sm, const float *sEps)
+{
+    const uint32_t *code = d.code + F.off;
+    const float *dv = dinv + F.off;
+    for (int i = blockIdx.x; i < d.n_items; i += gridDim.x) {
+        const int4 it = d.items[i];
+        const int z0 = it.w & 0xffff, z1 = it.w >> 16;
+        for (int zz = z0; zz < z1; zz += PZ)
+            cg_brick<INIT, UNI>(F, B, code, dv, it.y, it.z, zz, min(zz + PZ, z1), c, first, alpha, beta, ga, da,
+                                sm, sEps);
+    }
+}
+
+// The inner FP32 solve of one refinement pass on a single film: starts from
+// r_0 in B.r[0] (written by k_refine) and x = 0, runs until
+// (r,u) <= inner_tol2 (r_0,u_0) or inner_max iterations, leaves the
+// correction in B.x.  Cooperative launch of PNT-thread blocks; grid <=
+// co-resident blocks.  The scalar recurrences run in FP64 on thread 0 only
+// and are broadcast through shared memory.
+template <bool UNI>
+__global__ void __launch_bounds__(PNT, 2) k_pcg_cg1(Dev d, CgBuf B, const float *dinv)
+{
+    extern __shared__ float4 dsm4[];
+    const BrickSmem sm = brick_smem((float *)dsm4);
+    __shared__ double sRed[PNW][2];
+    __shared__ float sEps[9];
+    __shared__ float s_ab[2];
+    __shared__ int s_go;
+    const FilmDev *f = d.films;
+    SolveDev *S = d.solve;
+    const bool run = f->dep_flag != 0 && *(volatile int *)&S->active != 0;
+    if (!run) return;                       // uniform: k_refine decided for every block
+    FilmC F;
+    F.nx = f->nx; F.ny = f->ny; F.nz = f->nz; F.zbc = f->zbc; F.ref_id = f->ref_id;
+    F.plane = f->nx * f->ny; F.off = f->off; F.inv_h2 = f->inv_h2f;
+    if (threadIdx.x < 9) sEps[threadIdx.x] = f->epsf32[threadIdx.x];
+    __syncthreads();
+    const double tol2 = S->inner_tol2;
+    const int imax = S->inner_max;
+    unsigned int target = 0;
+    float ga = 0.f, da = 0.f;
+    cg_sweep_all<true, UNI>(d, F, B, dinv, 0, true, 0.f, 0.f, ga, da, sm, sEps);
+    double g0, dl;
+    if (!grid_allreduce2(B, 0, target, ga, da, sRed, g0, dl)) return;
+    // thread 0 owns the recurrences
+    double gam = g0, alpha = (dl > 0.0) ? g0 / dl : 0.0;
+    int it = 0, status = 0;
+    if (threadIdx.x == 0) {
+        s_go = isfinite(g0) && g0 > 0.0 && dl > 0.0 && gam > tol2 * g0 && imax > 0;
+        if (!(isfinite(g0) && g0 > 0.0 && dl > 0.0)) status = (g0 == 0.0) ? 0 : 1;
+        s_ab[0] = (float)alpha;
+        s_ab[1] = 0.f;
+    }
+    __syncthreads();
+    while (s_go) {
+        const float a = s_ab[0], b = s_ab[1];
+        ga = 0.f; da = 0.f;
+        cg_sweep_all<false, UNI>(d, F, B, dinv, it & 1, it == 0, a, b, ga, da, sm, sEps);
+        double gn, dn;
+        if (!grid_allreduce2(B, (it + 1) & 1, target, ga, da, sRed, gn, dn)) return;
+        ++it;
+        if (threadIdx.x == 0) {
+            const double bn = gn / gam;
+            const double den = dn - bn * gn / alpha;
+            int go = 1;
+            if (!isfinite(gn) || gn < 0.0 || !(den > 0.0)) {
+                status = (gn == 0.0) ? 0 : 1;
+                go = 0;
+            } else {
+                alpha = gn / den;
+                s_ab[0] = (float)alpha;
+                s_ab[1] = (float)bn;
+            }
+            gam = gn;
+            s_go = go && gam > tol2 * g0 && it < imax;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S->iters = it;
+        S->total_iters += it;
+        S->rz = gam;
+        S->rz0 = g0;
+        S->active = 0;
+        if (status) { S->status = 1; S->outer_active = 0; }
+    }
+}
+
+}  // namespace cmsl

@@ -179,3 +179,25 @@ def test_fp32_refined_reaches_refine_tolerance(gpu, orc):
     b[(k == 0) | (k == f.nz - 1)] = 0.0
     r = b - orc.apply_A(f, phi)
     assert np.linalg.norm(r) <= 1.2e-8 * np.linalg.norm(b)
+
+
+def test_fp32_refined_uniform_eps(gpu, orc):
+    """Every material with the same eps_r selects the constant-coefficient
+    operator specialisation of the persistent solver."""
+    from tests.films import MATS_DEFAULT
+    mats = MATS_DEFAULT.copy()
+    mats[:, 7] = 30.0
+    f, P = random_film(40, 17, 9, seed=43, eps_0_nd=4.0, mats=mats, p_scale=0.2)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    n = 12
+    Ez = np.linspace(0.0, 0.3, n)
+    Pw, _, phiw, _, _, rc = orc.run(f, P, np.zeros(f.N), Ez)
+    assert rc == 0
+    import cmsl_gb300 as cg
+    with _film(gpu, f, precision=cg.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-5) as g:
+        g.set_state(P)
+        g.run(Ez)
+        Pg, phig = g.get_state()
+    for a, b in zip(Pg, Pw):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+    assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
