@@ -97,7 +97,9 @@ struct cmsl_film {
     CgBuf cg{};                 // FP32_REFINED persistent PCG vectors
     int cg_grid = 0;
     bool uni_eps = false;       // every material has the same eps_r
-    void *cg_fn = nullptr;      // k_pcg_cg1<uni_eps>
+    bool cg_fused = false;      // single-sweep variant (CMSL_PCG_FUSED=1) instead of two-phase
+    void *cg_fn = nullptr;      // the persistent solver kernel in use
+    size_t cg_smem = 0;
 
     ~cmsl_film()
     {
@@ -302,7 +304,7 @@ cmsl_status build_graph(cmsl_film *f)
             a.d = f->dev(1, 0, h_outer);
             TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine<float>, nit, NT, args32));
             void *args_cg[] = {&a.d, &f->cg, &f->d_dinv};
-            TRY(add_kernel(outer, &n_cg, &n_ref, 1, f->cg_fn, f->cg_grid, PNT, args_cg, PSMEM_BYTES));
+            TRY(add_kernel(outer, &n_cg, &n_ref, 1, f->cg_fn, f->cg_grid, PNT, args_cg, f->cg_smem));
             cudaLaunchAttributeValue av{};
             av.cooperative = 1;
             CK(cudaGraphKernelNodeSetAttribute(n_cg, cudaLaunchAttributeCooperative, &av));
@@ -352,7 +354,7 @@ cmsl_status solve_direct(cmsl_film *f, cudaStream_t st, const Dev &d, const Fiel
                 CgBuf B = f->cg;
                 const float *dv = (const float *)f->d_dinv;
                 void *args[] = {&dd, &B, &dv};
-                CK(cudaLaunchCooperativeKernel(f->cg_fn, f->cg_grid, PNT, args, PSMEM_BYTES, st));
+                CK(cudaLaunchCooperativeKernel(f->cg_fn, f->cg_grid, PNT, args, f->cg_smem, st));
                 TRY(read_flags(f, st, &S));
             }
             if (!S.outer_active) break;
@@ -535,9 +537,20 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         CK(cudaFuncSetAttribute(k_pcg_cg1<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PSMEM_BYTES));
         CK(cudaFuncSetAttribute(k_pcg_cg1<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PSMEM_BYTES));
+        CK(cudaFuncSetAttribute(k_pcg_cg2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2SMEM_BYTES));
+        CK(cudaFuncSetAttribute(k_pcg_cg2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2SMEM_BYTES));
         f->uni_eps = dsc->mats[0].eps_r == dsc->mats[1].eps_r && dsc->mats[1].eps_r == dsc->mats[2].eps_r;
-        f->cg_fn = f->uni_eps ? (void *)k_pcg_cg1<true> : (void *)k_pcg_cg1<false>;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg1<false>, PNT, PSMEM_BYTES));
+        const char *solver = getenv("CMSL_PCG_FUSED");
+        f->cg_fused = solver && atoi(solver) != 0;
+        if (f->cg_fused) {
+            f->cg_fn = f->uni_eps ? (void *)k_pcg_cg1<true> : (void *)k_pcg_cg1<false>;
+            f->cg_smem = PSMEM_BYTES;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg1<false>, PNT, PSMEM_BYTES));
+        } else {
+            f->cg_fn = f->uni_eps ? (void *)k_pcg_cg2<true> : (void *)k_pcg_cg2<false>;
+            f->cg_smem = P2SMEM_BYTES;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg2<false>, PNT, P2SMEM_BYTES));
+        }
         if (per < 1) return fail(CMSL_ERR_CUDA, "persistent PCG kernel cannot be resident");
         f->cg_grid = std::min<int>((int)f->items.size(), per * nsm);
         TRY(f->alloc((void **)&B.part, sizeof(double) * 2 * 2 * f->cg_grid));
@@ -811,7 +824,7 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *f, int reps, void *stream, double 
                     const float *dv = (const float *)f->d_dinv;
                     void *args[] = {&dd, &B, &dv};
                     CK(cudaMemsetAsync(f->cg.arrive, 0, sizeof(unsigned int), st));
-                    CK(cudaLaunchCooperativeKernel(f->cg_fn, f->cg_grid, PNT, args, PSMEM_BYTES, st));
+                    CK(cudaLaunchCooperativeKernel(f->cg_fn, f->cg_grid, PNT, args, f->cg_smem, st));
                     CK(cudaMemcpyAsync(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice, st));
                 }
                 break;

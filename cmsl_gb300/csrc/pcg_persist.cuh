@@ -365,4 +365,277 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg1(Dev d, CgBuf B, const float 
     }
 }
 
+// ------------------------------------------------------------------------
+// Two-phase persistent solver.  Per iteration:
+//   P (pointwise, float4, every cell, no halo):
+//       s = w + b s,  p = D^-1 r + b p,  x += a p,  r -= a s,  u = D^-1 r,
+//       gamma += r.u
+//   grid sync
+//   S (stencil bricks staging only u): w = A u,  delta += w.u
+//   grid sync + all-reduce (gamma, delta)
+// All updates are in place (P touches only its own cells; S reads u, which P
+// does not write again before the next grid sync).
+// ------------------------------------------------------------------------
+
+// Plain grid barrier (no reduction), same bounded wait.
+__device__ __forceinline__ bool grid_sync(const CgBuf &B, unsigned int &target)
+{
+    __shared__ int s_ok2;
+    __syncthreads();
+    target += gridDim.x;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(B.arrive, 1u);
+        int ok = 1;
+        unsigned long long spins = 0;
+        while (ld_acquire(B.arrive) < target) {
+            if (++spins > BARRIER_SPIN_LIMIT) { ok = 0; atomicExch(B.err, 1); break; }
+            __nanosleep(32);
+        }
+        s_ok2 = ok;
+    }
+    __syncthreads();
+    return s_ok2 != 0;
+}
+
+// Phase P over all cells of the film.  INIT: u = D^-1 r, gamma = r.u.
+template <bool INIT>
+__device__ __forceinline__ void cg2_point(const FilmC &F, const CgBuf &B, const float *__restrict__ dv,
+                                          long long n, bool first, float a, float b, float &gacc)
+{
+    float *__restrict__ r = B.r[0] + F.off;
+    float *__restrict__ u = B.r[1] + F.off;
+    float *__restrict__ w = B.w[0] + F.off;
+    float *__restrict__ s = B.s[0] + F.off;
+    float *__restrict__ x = B.x + F.off;
+    float *__restrict__ p = B.p + F.off;
+    const float *__restrict__ d = dv + F.off;
+    const long long n4 = n >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
+        const float4 D4 = reinterpret_cast<const float4 *>(d)[q];
+        const float4 R4 = reinterpret_cast<const float4 *>(r)[q];
+        const float dd[4] = {D4.x, D4.y, D4.z, D4.w};
+        const float ri[4] = {R4.x, R4.y, R4.z, R4.w};
+        float uo[4], ro[4];
+        if (INIT) {
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                ro[j] = ri[j];
+                uo[j] = dd[j] * ri[j];
+                gacc = fmaf(ro[j], uo[j], gacc);
+            }
+        } else {
+            const float4 W4 = reinterpret_cast<const float4 *>(w)[q];
+            const float wi[4] = {W4.x, W4.y, W4.z, W4.w};
+            float si[4] = {0.f, 0.f, 0.f, 0.f}, pi[4] = {0.f, 0.f, 0.f, 0.f}, xi[4] = {0.f, 0.f, 0.f, 0.f};
+            if (!first) {
+                const float4 S4 = reinterpret_cast<const float4 *>(s)[q];
+                const float4 P4 = reinterpret_cast<const float4 *>(p)[q];
+                const float4 X4 = reinterpret_cast<const float4 *>(x)[q];
+                si[0] = S4.x; si[1] = S4.y; si[2] = S4.z; si[3] = S4.w;
+                pi[0] = P4.x; pi[1] = P4.y; pi[2] = P4.z; pi[3] = P4.w;
+                xi[0] = X4.x; xi[1] = X4.y; xi[2] = X4.z; xi[3] = X4.w;
+            }
+            float so[4], po[4], xo[4];
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                so[j] = first ? wi[j] : fmaf(b, si[j], wi[j]);
+                const float ui = dd[j] * ri[j];
+                po[j] = first ? ui : fmaf(b, pi[j], ui);
+                xo[j] = first ? a * po[j] : fmaf(a, po[j], xi[j]);
+                ro[j] = fmaf(-a, so[j], ri[j]);
+                uo[j] = dd[j] * ro[j];
+                gacc = fmaf(ro[j], uo[j], gacc);
+            }
+            reinterpret_cast<float4 *>(s)[q] = make_float4(so[0], so[1], so[2], so[3]);
+            reinterpret_cast<float4 *>(p)[q] = make_float4(po[0], po[1], po[2], po[3]);
+            reinterpret_cast<float4 *>(x)[q] = make_float4(xo[0], xo[1], xo[2], xo[3]);
+            reinterpret_cast<float4 *>(r)[q] = make_float4(ro[0], ro[1], ro[2], ro[3]);
+        }
+        reinterpret_cast<float4 *>(u)[q] = make_float4(uo[0], uo[1], uo[2], uo[3]);
+    }
+    // tail (n not a multiple of 4): block 0
+    if (blockIdx.x == 0) {
+        for (long long c = 4 * n4 + threadIdx.x; c < n; c += blockDim.x) {
+            const float dd = d[c], ri = r[c];
+            float ro, uo;
+            if (INIT) {
+                ro = ri;
+                uo = dd * ri;
+            } else {
+                const float wi = w[c];
+                const float so = first ? wi : fmaf(b, s[c], wi);
+                const float ui = dd * ri;
+                const float po = first ? ui : fmaf(b, p[c], ui);
+                x[c] = first ? a * po : fmaf(a, po, x[c]);
+                ro = fmaf(-a, so, ri);
+                uo = dd * ro;
+                s[c] = so;
+                p[c] = po;
+                r[c] = ro;
+            }
+            u[c] = uo;
+            gacc = fmaf(ro, uo, gacc);
+        }
+    }
+}
+
+// Phase S on one brick: stage u (and material codes) with a one-cell halo,
+// then w = A u and delta += w.u on own cells.
+template <bool UNI>
+__device__ __forceinline__ void cg2_brick(const FilmC &F, const CgBuf &B, const uint32_t *__restrict__ code,
+                                          int x0, int y0, int z0, int z1, float &dacc, float *sUb,
+                                          uint32_t *sCb, const float *sEps)
+{
+    const int nx = F.nx, ny = F.ny, nz = F.nz, plane = F.plane;
+    const int bx = threadIdx.x % PBX, by = threadIdx.x / PBX;
+    const int wx = min(TX, nx - x0), wy = min(TY, ny - y0);
+    const bool own = bx >= 1 && bx <= wx && by >= 1 && by <= wy;
+    const bool ex = bx == 0 || bx == wx + 1, ey = by == 0 || by == wy + 1;
+    const bool need = bx <= wx + 1 && by <= wy + 1 && !(ex && ey);
+    const int gx = (x0 - 1 + bx + nx) % nx, gy = (y0 - 1 + by + ny) % ny;
+    const int pl = gx + nx * gy;
+    const float *__restrict__ u = B.r[1] + F.off;
+    float *__restrict__ w = B.w[0] + F.off;
+    constexpr int PP = PBY * PBX;
+    const int col = by * PBX + bx;
+    if (need) {
+        const int klo = own ? max(z0 - 1, 0) : z0;
+        const int khi = own ? min(z1, nz - 1) : z1 - 1;
+        for (int k = klo; k <= khi; ++k) {
+            const int o = pl + k * plane;
+            const int si = (k - z0 + 1) * PP + col;
+            cp_async4(sUb + si, u + o);
+            if (!UNI) cp_async4(sCb + si, code + o);
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (own) {
+        for (int k = z0; k < z1; ++k) {
+            const int zi = k - z0 + 1;
+            const int si = zi * PP + col;
+            const float uc = sUb[si];
+            float wv;
+            if (id_row(F, k, pl)) {
+                wv = uc;
+            } else {
+                int zu = zi + 1, zd = zi - 1;
+                if (F.zbc != 0) {
+                    if (k == 0) zd = zu;
+                    else if (k == nz - 1) zu = zd;
+                }
+                const int su = zu * PP + col, sd = zd * PP + col;
+                const float ue = sUb[si + 1], uw = sUb[si - 1], un = sUb[si + PBX], us = sUb[si - PBX];
+                const float uu = sUb[su], ud = sUb[sd];
+                float a;
+                if (UNI) {
+                    a = sEps[0] * ((((((ue - uc) - (uc - uw)) + (un - uc)) - (uc - us)) + (uu - uc)) - (uc - ud));
+                } else {
+                    const int mc = code_mat(sCb[si]) * 3;
+                    a = sEps[mc + code_mat(sCb[si + 1])] * (ue - uc) - sEps[mc + code_mat(sCb[si - 1])] * (uc - uw);
+                    a += sEps[mc + code_mat(sCb[si + PBX])] * (un - uc);
+                    a -= sEps[mc + code_mat(sCb[si - PBX])] * (uc - us);
+                    a += sEps[mc + code_mat(sCb[su])] * (uu - uc);
+                    a -= sEps[mc + code_mat(sCb[sd])] * (uc - ud);
+                }
+                wv = -(a * F.inv_h2);
+            }
+            w[pl + k * plane] = wv;
+            dacc = fmaf(wv, uc, dacc);
+        }
+    }
+    __syncthreads();
+}
+
+template <bool UNI>
+__device__ __forceinline__ void cg2_stencil(const Dev &d, const FilmC &F, const CgBuf &B, float &dacc,
+                                            float *sUb, uint32_t *sCb, const float *sEps)
+{
+    const uint32_t *code = d.code + F.off;
+    for (int i = blockIdx.x; i < d.n_items; i += gridDim.x) {
+        const int4 it = d.items[i];
+        const int z0 = it.w & 0xffff, z1 = it.w >> 16;
+        for (int zz = z0; zz < z1; zz += PZ)
+            cg2_brick<UNI>(F, B, code, it.y, it.z, zz, min(zz + PZ, z1), dacc, sUb, sCb, sEps);
+    }
+}
+
+constexpr size_t P2SMEM_BYTES = sizeof(float) * 2 * PNPL;
+
+template <bool UNI>
+__global__ void __launch_bounds__(PNT, 2) k_pcg_cg2(Dev d, CgBuf B, const float *dinv)
+{
+    extern __shared__ float4 dsm4[];
+    float *sUb = (float *)dsm4;
+    uint32_t *sCb = (uint32_t *)(sUb + PNPL);
+    __shared__ double sRed[PNW][2];
+    __shared__ float sEps[9];
+    __shared__ float s_ab[2];
+    __shared__ int s_go;
+    const FilmDev *f = d.films;
+    SolveDev *S = d.solve;
+    const bool run = f->dep_flag != 0 && *(volatile int *)&S->active != 0;
+    if (!run) return;
+    FilmC F;
+    F.nx = f->nx; F.ny = f->ny; F.nz = f->nz; F.zbc = f->zbc; F.ref_id = f->ref_id;
+    F.plane = f->nx * f->ny; F.off = f->off; F.inv_h2 = f->inv_h2f;
+    const long long n = (long long)F.plane * F.nz;
+    if (threadIdx.x < 9) sEps[threadIdx.x] = f->epsf32[threadIdx.x];
+    __syncthreads();
+    const double tol2 = S->inner_tol2;
+    const int imax = S->inner_max;
+    unsigned int target = 0;
+    float ga = 0.f, da = 0.f;
+    cg2_point<true>(F, B, dinv, n, true, 0.f, 0.f, ga);
+    if (!grid_sync(B, target)) return;
+    cg2_stencil<UNI>(d, F, B, da, sUb, sCb, sEps);
+    double g0, dl;
+    if (!grid_allreduce2(B, 0, target, ga, da, sRed, g0, dl)) return;
+    double gam = g0, alpha = (dl > 0.0) ? g0 / dl : 0.0;
+    int it = 0, status = 0;
+    if (threadIdx.x == 0) {
+        s_go = isfinite(g0) && g0 > 0.0 && dl > 0.0 && gam > tol2 * g0 && imax > 0;
+        if (!(isfinite(g0) && g0 > 0.0 && dl > 0.0)) status = (g0 == 0.0) ? 0 : 1;
+        s_ab[0] = (float)alpha;
+        s_ab[1] = 0.f;
+    }
+    __syncthreads();
+    while (s_go) {
+        const float a = s_ab[0], b = s_ab[1];
+        ga = 0.f; da = 0.f;
+        cg2_point<false>(F, B, dinv, n, it == 0, a, b, ga);
+        if (!grid_sync(B, target)) return;
+        cg2_stencil<UNI>(d, F, B, da, sUb, sCb, sEps);
+        double gn, dn;
+        if (!grid_allreduce2(B, (it + 1) & 1, target, ga, da, sRed, gn, dn)) return;
+        ++it;
+        if (threadIdx.x == 0) {
+            const double bn = gn / gam;
+            const double den = dn - bn * gn / alpha;
+            int go = 1;
+            if (!isfinite(gn) || gn < 0.0 || !(den > 0.0)) {
+                status = (gn == 0.0) ? 0 : 1;
+                go = 0;
+            } else {
+                alpha = gn / den;
+                s_ab[0] = (float)alpha;
+                s_ab[1] = (float)bn;
+            }
+            gam = gn;
+            s_go = go && gam > tol2 * g0 && it < imax;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S->iters = it;
+        S->total_iters += it;
+        S->rz = gam;
+        S->rz0 = g0;
+        S->active = 0;
+        if (status) { S->status = 1; S->outer_active = 0; }
+    }
+}
+
 }  // namespace cmsl
