@@ -38,7 +38,7 @@ class FilmDesc(C.Structure):
         ("precision", C.c_int), ("pcg_crit", C.c_int),
         ("tol_abs", C.c_double), ("tol_rel", C.c_double), ("max_iter", C.c_int),
         ("refine_tol", C.c_double), ("max_refine", C.c_int),
-        ("inner_tol", C.c_double), ("inner_max_iter", C.c_int),
+        ("inner_tol", C.c_double), ("inner_max_iter", C.c_int), ("warm_start", C.c_int),
     ]
 
 

@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
     T *Pn[6];
     #pragma unroll
     for (int q = 0; q < 6; ++q) { Po[q] = F.P[cur][q] + off; Pn[q] = F.P[cur ^ 1][q] + off; }
-    const double *phi = d.phi[d.solve[it.x].phi_cur] + off;
+    const int pcur = d.solve[it.x].phi_cur;
+    const double *phi = (pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + off;
     const uint32_t *code = d.code + off;
     const double two_h = f->two_h, inv_2h = f->inv_2h;
 
@@ -455,7 +456,8 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
     const int cur = d.ctl->cur;
     const long long off = f->off;
     const T *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
-    const double *x = d.phi[d.solve[it.x].phi_cur] + off;
+    const int pcur = d.solve[it.x].phi_cur;
+    const double *x = (pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + off;
     const uint32_t *code = d.code + off;
     T *r = F.r + off;
     const T *dinv = F.dinv + off;
@@ -586,11 +588,14 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
     const int nz = g.nz;
     const bool run = f->dep_flag != 0 && (d.force || S0->outer_active);
     const bool apply = S0->refine > 0;   // a correction is pending after the first pass
-    const int cur = d.ctl->cur, pc = S0->phi_cur;
+    const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pf = 3 - pc - pp;
+    const bool extrap = !apply && f->warm != 0;   // first pass: phi0 = 2 phi_n - phi_{n-1}
     const long long off = f->off;
     const T *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
-    const double *phi = d.phi[pc] + off;
-    double *phin = d.phi[pc ^ 1] + off;
+    // phi buffers by value (no dynamic indexing of the parameter array)
+    const double *phi = (pc == 0 ? d.phi[0] : pc == 1 ? d.phi[1] : d.phi[2]) + off;
+    const double *phip = (pp == 0 ? d.phi[0] : pp == 1 ? d.phi[1] : d.phi[2]) + off;
+    double *phin = (pf == 0 ? d.phi[0] : pf == 1 ? d.phi[1] : d.phi[2]) + off;
     const T *dx = F.x + off;
     const uint32_t *code = d.code + off;
     T *r = F.r + off;
@@ -601,7 +606,9 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
         double xd = 0, xc = 0, xu = 0, hx = 0;
         T zd = 0, zc = 0, zu = 0, hPx = 0, hPy = 0;
         int md = 0, mc = 0, mu = 0, hm = 0;
-        auto eff = [&](long long o) { return apply ? phi[o] + (double)dx[o] : phi[o]; };
+        auto eff = [&](long long o) {
+            return apply ? phi[o] + (double)dx[o] : (extrap ? 2.0 * phi[o] - phip[o] : phi[o]);
+        };
         auto ld_own = [&](int k, double &xv, T &zv, int &mv) {
             const long long o = g.own_pl + (long long)k * g.plane;
             xv = eff(o); zv = Pmz[o]; mv = code_mat(code[o]);
@@ -680,7 +687,9 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
         if (was) film_total<3>(d, ff, sRed, sTot);
         if (threadIdx.x == 0 && was) {
-            S->phi_cur ^= 1;
+            const int c0 = S->phi_cur, p0 = S->phi_prev, fr = 3 - c0 - p0;
+            if (S->refine == 0) S->phi_prev = c0;   // keep phi_n for the next step's extrapolation
+            S->phi_cur = fr;
             S->refine += 1;
             S->rr64 = sTot[0];
             S->bb = sTot[1];
@@ -846,7 +855,10 @@ __global__ void __launch_bounds__(NT) k_update(Dev d, Fields<T> F)
     T *r = F.r + off;
     T *x;
     if constexpr (REFINE) x = F.x + off;
-    else x = (T *)(d.phi[S0->phi_cur] + off);
+    else {
+        const int pcur = S0->phi_cur;
+        x = (T *)((pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + off);
+    }
     T acc[2] = {(T)0, (T)0};
     if (run && g.valid) {
         for (int k = z0; k < z1; ++k) {
@@ -1002,7 +1014,8 @@ __global__ void k_efield(Dev d, double *Ex, double *Ey, double *Ez)
     if (!g.valid) return;
     const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
     const int i = g.x0 + lx, j = g.y0 + ly, nx = g.nx, ny = g.ny, nz = g.nz;
-    const double *phi = d.phi[d.solve[it.x].phi_cur] + f->off;
+    const int pcur = d.solve[it.x].phi_cur;
+    const double *phi = (pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + f->off;
     Ex += f->off; Ey += f->off; Ez += f->off;
     const double two_h = f->two_h;
     for (int k = z0; k < z1; ++k) {

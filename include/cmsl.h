@@ -76,6 +76,9 @@ typedef struct {
     int max_refine;               /* FP32_REFINED: outer passes per step (>= 2) */
     double inner_tol;             /* FP32_REFINED: inner sqrt(r.z/r0.z0) target, e.g. 1e-4 */
     int inner_max_iter;           /* FP32_REFINED: inner iterations per pass */
+    int warm_start;               /* FP32_REFINED: 0 = previous phi (the reference's warm
+                                     start, depol_varEPS.cu:429-430), 1 = linear
+                                     extrapolation 2 phi_n - phi_{n-1} */
 } cmsl_film_desc;
 
 typedef struct cmsl_film cmsl_film;
