@@ -45,6 +45,12 @@ template <class T> __device__ __forceinline__ T epsf_of(const FilmDev *f, int i)
 template <> __device__ __forceinline__ double epsf_of<double>(const FilmDev *f, int i) { return f->epsf[i]; }
 template <> __device__ __forceinline__ float epsf_of<float>(const FilmDev *f, int i) { return f->epsf32[i]; }
 
+// phi buffer by index without dynamically indexing the parameter array
+__device__ __forceinline__ double *phi_sel(const Dev &d, int i)
+{
+    return i == 0 ? d.phi[0] : i == 1 ? d.phi[1] : i == 2 ? d.phi[2] : d.phi[3];
+}
+
 // ------------------------------------------------------------------ tiles
 struct Geom {
     int nx, ny, nz, x0, y0, wx, wy;
@@ -226,7 +232,7 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
     #pragma unroll
     for (int q = 0; q < 6; ++q) { Po[q] = F.P[cur][q] + off; Pn[q] = F.P[cur ^ 1][q] + off; }
     const int pcur = d.solve[it.x].phi_cur;
-    const double *phi = (pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + off;
+    const double *phi = phi_sel(d, pcur) + off;
     const uint32_t *code = d.code + off;
     const double two_h = f->two_h, inv_2h = f->inv_2h;
 
@@ -457,7 +463,7 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
     const long long off = f->off;
     const T *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
     const int pcur = d.solve[it.x].phi_cur;
-    const double *x = (pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + off;
+    const double *x = phi_sel(d, pcur) + off;
     const uint32_t *code = d.code + off;
     T *r = F.r + off;
     const T *dinv = F.dinv + off;
@@ -588,14 +594,16 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
     const int nz = g.nz;
     const bool run = f->dep_flag != 0 && (d.force || S0->outer_active);
     const bool apply = S0->refine > 0;   // a correction is pending after the first pass
-    const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pf = 3 - pc - pp;
-    const bool extrap = !apply && f->warm != 0;   // first pass: phi0 = 2 phi_n - phi_{n-1}
+    const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pq = S0->phi_prev2;
+    const int pf = 6 - pc - pp - pq;              // the free buffer of the four
+    // first pass: phi0 = 2 phi_n - phi_{n-1}  or  3 phi_n - 3 phi_{n-1} + phi_{n-2}
+    const int extrap = apply ? 0 : f->warm;
     const long long off = f->off;
     const T *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
-    // phi buffers by value (no dynamic indexing of the parameter array)
-    const double *phi = (pc == 0 ? d.phi[0] : pc == 1 ? d.phi[1] : d.phi[2]) + off;
-    const double *phip = (pp == 0 ? d.phi[0] : pp == 1 ? d.phi[1] : d.phi[2]) + off;
-    double *phin = (pf == 0 ? d.phi[0] : pf == 1 ? d.phi[1] : d.phi[2]) + off;
+    const double *phi = phi_sel(d, pc) + off;
+    const double *phip = phi_sel(d, pp) + off;
+    const double *phiq = phi_sel(d, pq) + off;
+    double *phin = phi_sel(d, pf) + off;
     const T *dx = F.x + off;
     const uint32_t *code = d.code + off;
     T *r = F.r + off;
@@ -607,7 +615,10 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
         T zd = 0, zc = 0, zu = 0, hPx = 0, hPy = 0;
         int md = 0, mc = 0, mu = 0, hm = 0;
         auto eff = [&](long long o) {
-            return apply ? phi[o] + (double)dx[o] : (extrap ? 2.0 * phi[o] - phip[o] : phi[o]);
+            if (apply) return phi[o] + (double)dx[o];
+            if (extrap == 1) return 2.0 * phi[o] - phip[o];
+            if (extrap == 2) return 3.0 * (phi[o] - phip[o]) + phiq[o];
+            return phi[o];
         };
         auto ld_own = [&](int k, double &xv, T &zv, int &mv) {
             const long long o = g.own_pl + (long long)k * g.plane;
@@ -687,9 +698,13 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
         if (was) film_total<3>(d, ff, sRed, sTot);
         if (threadIdx.x == 0 && was) {
-            const int c0 = S->phi_cur, p0 = S->phi_prev, fr = 3 - c0 - p0;
-            if (S->refine == 0) S->phi_prev = c0;   // keep phi_n for the next step's extrapolation
-            S->phi_cur = fr;
+            const int c0 = S->phi_cur, p0 = S->phi_prev, q0 = S->phi_prev2, fr = 6 - c0 - p0 - q0;
+            if (S->refine == 0) {            // keep phi_n, phi_{n-1} for the next step's extrapolation
+                S->phi_prev2 = p0;
+                S->phi_prev = c0;
+                (void)q0;                    // phi_{n-2} is no longer needed: it becomes the free buffer
+            }
+            S->phi_cur = fr;                 // this pass wrote the free buffer
             S->refine += 1;
             S->rr64 = sTot[0];
             S->bb = sTot[1];
@@ -857,7 +872,7 @@ __global__ void __launch_bounds__(NT) k_update(Dev d, Fields<T> F)
     if constexpr (REFINE) x = F.x + off;
     else {
         const int pcur = S0->phi_cur;
-        x = (T *)((pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + off);
+        x = (T *)(phi_sel(d, pcur) + off);
     }
     T acc[2] = {(T)0, (T)0};
     if (run && g.valid) {
@@ -1015,7 +1030,7 @@ __global__ void k_efield(Dev d, double *Ex, double *Ey, double *Ez)
     const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
     const int i = g.x0 + lx, j = g.y0 + ly, nx = g.nx, ny = g.ny, nz = g.nz;
     const int pcur = d.solve[it.x].phi_cur;
-    const double *phi = (pcur == 0 ? d.phi[0] : pcur == 1 ? d.phi[1] : d.phi[2]) + f->off;
+    const double *phi = phi_sel(d, pcur) + f->off;
     Ex += f->off; Ey += f->off; Ez += f->off;
     const double two_h = f->two_h;
     for (int k = z0; k < z1; ++k) {

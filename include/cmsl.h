@@ -78,7 +78,8 @@ typedef struct {
     int inner_max_iter;           /* FP32_REFINED: inner iterations per pass */
     int warm_start;               /* FP32_REFINED: 0 = previous phi (the reference's warm
                                      start, depol_varEPS.cu:429-430), 1 = linear
-                                     extrapolation 2 phi_n - phi_{n-1} */
+                                     extrapolation 2 phi_n - phi_{n-1}, 2 = quadratic
+                                     3 phi_n - 3 phi_{n-1} + phi_{n-2} */
 } cmsl_film_desc;
 
 typedef struct cmsl_film cmsl_film;
