@@ -48,7 +48,7 @@ struct FilmDev {
     int g_off;                  // first grain of the film in TR
     int item_begin, item_end;
     int dep_flag;
-    int warm;                   // FP32_REFINED warm start: 0 previous phi, 1 linear, 2 quadratic extrapolation
+    int warm;                   // FP32_REFINED warm start: 0 previous phi, 1 linear, 2 quadratic, 3 cubic extrapolation
     int ref_id;                 // Neumann pinned cell (film-local)
     int crit;
     int max_iter, max_refine, inner_max;
@@ -73,6 +73,7 @@ struct SolveDev {               // per film, lives in device memory
     int phi_cur;                // which phi buffer is current
     int phi_prev;               // previous step's potential (extrapolated warm start)
     int phi_prev2;              // the one before (quadratic extrapolation)
+    int phi_prev3;              // and the one before that (cubic extrapolation)
     int sticky;                 // first non-zero status seen since set_state
     double inner_tol2;          // inner target of the current refinement pass
     int inner_max;              // inner iteration cap of the current pass
@@ -107,7 +108,7 @@ struct Dev {
     const int4 *items;
     int n_films, n_items;
     const uint32_t *code;
-    double *phi[4];
+    double *phi[5];
     double *partial;            // [n_items * NPART]
     unsigned int *counter;      // one ticket counter (reset by the last block)
     SolveDev *solve;            // [n_films]

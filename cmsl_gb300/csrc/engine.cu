@@ -74,7 +74,7 @@ struct cmsl_film {
     int4 *d_items = nullptr;
     uint32_t *d_code = nullptr;
     void *d_TR = nullptr;
-    double *d_phi[4] = {nullptr, nullptr, nullptr, nullptr};
+    double *d_phi[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     double *d_partial = nullptr;
     unsigned int *d_counter = nullptr;
     SolveDev *d_solve = nullptr;
@@ -128,7 +128,7 @@ struct cmsl_film {
     {
         Dev d{};
         d.films = d_films; d.items = d_items; d.n_films = 1; d.n_items = (int)items.size();
-        d.code = d_code; d.phi[0] = d_phi[0]; d.phi[1] = d_phi[1]; d.phi[2] = d_phi[2]; d.phi[3] = d_phi[3];
+        d.code = d_code; d.phi[0] = d_phi[0]; d.phi[1] = d_phi[1]; d.phi[2] = d_phi[2]; d.phi[3] = d_phi[3]; d.phi[4] = d_phi[4];
         d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
         d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
         d.iters_log = d_iters; d.refine_log = d_refine;
@@ -476,7 +476,7 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
     fd.nx = f->nx; fd.ny = f->ny; fd.nz = f->nz; fd.zbc = dsc->zbc;
     fd.off = 0; fd.g_off = 0; fd.item_begin = 0; fd.item_end = (int)f->items.size();
     fd.dep_flag = f->dep;
-    fd.warm = f->precision != CMSL_FP64 ? std::min(std::max(dsc->warm_start, 0), 2) : 0;
+    fd.warm = f->precision != CMSL_FP64 ? std::min(std::max(dsc->warm_start, 0), 3) : 0;
     fd.ref_id = f->nx / 2 + f->nx * (f->ny / 2 + (f->nz / 2) * f->ny);   // depol_varEPS.cu:339-346
     fd.crit = dsc->pcg_crit;
     fd.max_iter = dsc->max_iter;
@@ -563,6 +563,7 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
     if (f->precision != CMSL_FP64) {
         TRY(f->alloc((void **)&f->d_phi[2], sizeof(double) * cells));
         TRY(f->alloc((void **)&f->d_phi[3], sizeof(double) * cells));
+        TRY(f->alloc((void **)&f->d_phi[4], sizeof(double) * cells));
     }
     TRY(f->alloc((void **)&f->d_partial, sizeof(double) * NPART * f->items.size()));
     TRY(f->alloc((void **)&f->d_counter, sizeof(unsigned int) * 4));
@@ -600,11 +601,13 @@ cmsl_status cmsl_film_set_state(cmsl_film *f, const double *const P[6], const do
     else CK(cudaMemset(f->d_phi[0], 0, sizeof(double) * f->N));
     // the previous potential starts equal to the given one (no extrapolation on step 1)
     CK(cudaMemcpy(f->d_phi[1], f->d_phi[0], sizeof(double) * f->N, cudaMemcpyDeviceToDevice));
-    if (f->d_phi[2]) CK(cudaMemcpy(f->d_phi[2], f->d_phi[0], sizeof(double) * f->N, cudaMemcpyDeviceToDevice));
+    for (int q = 2; q < 4; ++q)
+        if (f->d_phi[q]) CK(cudaMemcpy(f->d_phi[q], f->d_phi[0], sizeof(double) * f->N, cudaMemcpyDeviceToDevice));
     SolveDev S0{};
     S0.phi_cur = 0;
     S0.phi_prev = f->precision == CMSL_FP64 ? 0 : 1;
     S0.phi_prev2 = f->precision == CMSL_FP64 ? 0 : 2;
+    S0.phi_prev3 = f->precision == CMSL_FP64 ? 0 : 3;
     CK(cudaMemcpy(f->d_solve, &S0, sizeof(SolveDev), cudaMemcpyHostToDevice));
     if (f->precision != CMSL_FP64) CK(cudaMemset(f->d_x, 0, f->esz * f->N));
     return CMSL_OK;

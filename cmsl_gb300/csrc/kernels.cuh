@@ -48,7 +48,7 @@ template <> __device__ __forceinline__ float epsf_of<float>(const FilmDev *f, in
 // phi buffer by index without dynamically indexing the parameter array
 __device__ __forceinline__ double *phi_sel(const Dev &d, int i)
 {
-    return i == 0 ? d.phi[0] : i == 1 ? d.phi[1] : i == 2 ? d.phi[2] : d.phi[3];
+    return i == 0 ? d.phi[0] : i == 1 ? d.phi[1] : i == 2 ? d.phi[2] : i == 3 ? d.phi[3] : d.phi[4];
 }
 
 // ------------------------------------------------------------------ tiles
@@ -594,8 +594,8 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
     const int nz = g.nz;
     const bool run = f->dep_flag != 0 && (d.force || S0->outer_active);
     const bool apply = S0->refine > 0;   // a correction is pending after the first pass
-    const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pq = S0->phi_prev2;
-    const int pf = 6 - pc - pp - pq;              // the free buffer of the four
+    const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pq = S0->phi_prev2, pr = S0->phi_prev3;
+    const int pf = 10 - pc - pp - pq - pr;        // the free buffer of the five
     // first pass: phi0 = 2 phi_n - phi_{n-1}  or  3 phi_n - 3 phi_{n-1} + phi_{n-2}
     const int extrap = apply ? 0 : f->warm;
     const long long off = f->off;
@@ -603,6 +603,7 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
     const double *phi = phi_sel(d, pc) + off;
     const double *phip = phi_sel(d, pp) + off;
     const double *phiq = phi_sel(d, pq) + off;
+    const double *phir = phi_sel(d, pr) + off;
     double *phin = phi_sel(d, pf) + off;
     const T *dx = F.x + off;
     const uint32_t *code = d.code + off;
@@ -618,6 +619,7 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
             if (apply) return phi[o] + (double)dx[o];
             if (extrap == 1) return 2.0 * phi[o] - phip[o];
             if (extrap == 2) return 3.0 * (phi[o] - phip[o]) + phiq[o];
+            if (extrap == 3) return 4.0 * (phi[o] + phiq[o]) - 6.0 * phip[o] - phir[o];
             return phi[o];
         };
         auto ld_own = [&](int k, double &xv, T &zv, int &mv) {
@@ -698,11 +700,13 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
         if (was) film_total<3>(d, ff, sRed, sTot);
         if (threadIdx.x == 0 && was) {
-            const int c0 = S->phi_cur, p0 = S->phi_prev, q0 = S->phi_prev2, fr = 6 - c0 - p0 - q0;
-            if (S->refine == 0) {            // keep phi_n, phi_{n-1} for the next step's extrapolation
+            const int c0 = S->phi_cur, p0 = S->phi_prev, q0 = S->phi_prev2, r0 = S->phi_prev3;
+            const int fr = 10 - c0 - p0 - q0 - r0;
+            if (S->refine == 0) {            // keep phi_n .. phi_{n-2} for the next step's extrapolation
+                S->phi_prev3 = q0;
                 S->phi_prev2 = p0;
                 S->phi_prev = c0;
-                (void)q0;                    // phi_{n-2} is no longer needed: it becomes the free buffer
+                (void)r0;                    // phi_{n-3} is no longer needed: it becomes the free buffer
             }
             S->phi_cur = fr;                 // this pass wrote the free buffer
             S->refine += 1;

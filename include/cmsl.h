@@ -79,7 +79,8 @@ typedef struct {
     int warm_start;               /* FP32_REFINED: 0 = previous phi (the reference's warm
                                      start, depol_varEPS.cu:429-430), 1 = linear
                                      extrapolation 2 phi_n - phi_{n-1}, 2 = quadratic
-                                     3 phi_n - 3 phi_{n-1} + phi_{n-2} */
+                                     3 phi_n - 3 phi_{n-1} + phi_{n-2}, 3 = cubic
+                                     4 phi_n - 6 phi_{n-1} + 4 phi_{n-2} - phi_{n-3} */
 } cmsl_film_desc;
 
 typedef struct cmsl_film cmsl_film;
