@@ -208,7 +208,8 @@ def run_ours(args):
     fp64 = args.precision == "fp64"
     w = wl.config(CONFIG_ID)
     kw = dict(precision=cg.FP64 if fp64 else cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8,
-              max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000)
+              max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000,
+              warm_start=3)
     film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **kw)
     film.set_state(w.P_init)
     K, W = args.steps, args.warmup

@@ -60,6 +60,8 @@ struct FilmDev {
     Coef<float> coef32[6];
     double epsf[9];             // harmonic face eps for (mat_c, mat_nb), depol_varEPS.cu:10-15
     float epsf32[9];
+    float cf_h[9], cf_l[9];     // epsf / h^2 as double-float pairs (FP32_REFINED residual)
+    float cb_h, cb_l;           // eps_0_nd / (2 h) as a double-float pair
 };
 
 struct SolveDev {               // per film, lives in device memory
@@ -108,6 +110,7 @@ struct Dev {
     const int4 *items;
     int n_films, n_items;
     const uint32_t *code;
+    long long ncells;           // cells of all films (double-float phi: lo half offset)
     double *phi[5];
     double *partial;            // [n_items * NPART]
     unsigned int *counter;      // one ticket counter (reset by the last block)

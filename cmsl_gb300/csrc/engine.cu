@@ -128,7 +128,7 @@ struct cmsl_film {
     {
         Dev d{};
         d.films = d_films; d.items = d_items; d.n_films = 1; d.n_items = (int)items.size();
-        d.code = d_code; d.phi[0] = d_phi[0]; d.phi[1] = d_phi[1]; d.phi[2] = d_phi[2]; d.phi[3] = d_phi[3]; d.phi[4] = d_phi[4];
+        d.code = d_code; d.ncells = N; d.phi[0] = d_phi[0]; d.phi[1] = d_phi[1]; d.phi[2] = d_phi[2]; d.phi[3] = d_phi[3]; d.phi[4] = d_phi[4];
         d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
         d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
         d.iters_log = d_iters; d.refine_log = d_refine;
@@ -302,7 +302,7 @@ cmsl_status build_graph(cmsl_film *f)
             cudaGraphNode_t n_ref, n_cg;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             a.d = f->dev(1, 0, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine<float>, nit, NT, args32));
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
             void *args_cg[] = {&a.d, &f->cg, &f->d_dinv};
             TRY(add_kernel(outer, &n_cg, &n_ref, 1, f->cg_fn, f->cg_grid, PNT, args_cg, f->cg_smem));
             cudaLaunchAttributeValue av{};
@@ -346,7 +346,7 @@ cmsl_status solve_direct(cmsl_film *f, cudaStream_t st, const Dev &d, const Fiel
     } else {
         for (int og = 0;; ++og) {
             if (og > f->fd.max_refine + 1) return fail(CMSL_ERR_STATE, "refinement loop did not stop");
-            k_refine<float><<<nit, NT, 0, st>>>(d, F32);
+            k_refine<<<nit, NT, 0, st>>>(d, F32);
             CK(cudaGetLastError());
             TRY(read_flags(f, st, &S));
             if (S.active) {
@@ -487,6 +487,10 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
     fd.inv_N = 1.0 / ((double)f->nx * f->ny * f->nz);              // main.cu:405
     fd.two_h = 2.0 * h; fd.h2 = h * h; fd.inv_h2 = 1.0 / (h * h); fd.inv_2h = 1.0 / (2.0 * h);
     fd.inv_h2f = (float)fd.inv_h2; fd.inv_2hf = (float)fd.inv_2h; fd.eps0f = (float)dsc->eps_0_nd;
+    {
+        const df cb = df_from_double(dsc->eps_0_nd * fd.inv_2h);
+        fd.cb_h = cb.h; fd.cb_l = cb.l;
+    }
     fd.tol_abs2 = dsc->tol_abs * dsc->tol_abs;
     fd.tol_rel2 = dsc->tol_rel * dsc->tol_rel;
     fd.refine_tol2 = dsc->refine_tol * dsc->refine_tol;
@@ -501,6 +505,8 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
         for (int b = 0; b < 3; ++b) {
             fd.epsf[a * 3 + b] = harm(dsc->mats[a].eps_r, dsc->mats[b].eps_r);
             fd.epsf32[a * 3 + b] = (float)fd.epsf[a * 3 + b];
+            const df c = df_from_double(fd.epsf[a * 3 + b] * fd.inv_h2);
+            fd.cf_h[a * 3 + b] = c.h; fd.cf_l[a * 3 + b] = c.l;
         }
 
     // device memory
@@ -597,8 +603,20 @@ cmsl_status cmsl_film_set_state(cmsl_film *f, const double *const P[6], const do
     CK(cudaMemset(f->d_solve, 0, sizeof(SolveDev)));
     if (f->precision == CMSL_FP64) TRY(put_fields<double>(f, 0, P));
     else TRY(put_fields<float>(f, 0, P));
-    if (phi) CK(cudaMemcpy(f->d_phi[0], phi, sizeof(double) * f->N, cudaMemcpyHostToDevice));
-    else CK(cudaMemset(f->d_phi[0], 0, sizeof(double) * f->N));
+    if (f->precision == CMSL_FP64) {
+        if (phi) CK(cudaMemcpy(f->d_phi[0], phi, sizeof(double) * f->N, cudaMemcpyHostToDevice));
+        else CK(cudaMemset(f->d_phi[0], 0, sizeof(double) * f->N));
+    } else {
+        // double-float: hi half then lo half
+        std::vector<float> t((size_t)2 * f->N, 0.f);
+        if (phi)
+            for (long long i = 0; i < f->N; ++i) {
+                const df v = df_from_double(phi[i]);
+                t[i] = v.h;
+                t[f->N + i] = v.l;
+            }
+        CK(cudaMemcpy(f->d_phi[0], t.data(), sizeof(float) * 2 * f->N, cudaMemcpyHostToDevice));
+    }
     // the previous potential starts equal to the given one (no extrapolation on step 1)
     CK(cudaMemcpy(f->d_phi[1], f->d_phi[0], sizeof(double) * f->N, cudaMemcpyDeviceToDevice));
     for (int q = 2; q < 4; ++q)
@@ -625,7 +643,15 @@ cmsl_status cmsl_film_get_state(cmsl_film *f, double *const P[6], double *phi)
         if (f->precision == CMSL_FP64) TRY(get_fields<double>(f, c.cur, P));
         else TRY(get_fields<float>(f, c.cur, P));
     }
-    if (phi) CK(cudaMemcpy(phi, f->d_phi[S.phi_cur], sizeof(double) * f->N, cudaMemcpyDeviceToHost));
+    if (phi) {
+        if (f->precision == CMSL_FP64) {
+            CK(cudaMemcpy(phi, f->d_phi[S.phi_cur], sizeof(double) * f->N, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> t((size_t)2 * f->N);
+            CK(cudaMemcpy(t.data(), f->d_phi[S.phi_cur], sizeof(float) * 2 * f->N, cudaMemcpyDeviceToHost));
+            for (long long i = 0; i < f->N; ++i) phi[i] = (double)t[i] + (double)t[f->N + i];
+        }
+    }
     return CMSL_OK;
 }
 
@@ -764,6 +790,7 @@ cmsl_status cmsl_film_apply_operator(cmsl_film *f, const double *x, double *y)
 cmsl_status cmsl_film_efield(cmsl_film *f, double *Ex, double *Ey, double *Ez)
 {
     if (!f || !Ex || !Ey || !Ez) return fail(CMSL_ERR_ARG, "NULL argument");
+    if (f->precision != CMSL_FP64) return fail(CMSL_ERR_STATE, "efield: FP64 films only");
     CK(cudaDeviceSynchronize());
     double *e = nullptr;
     CK(cudaMalloc(&e, sizeof(double) * 3 * f->N));
@@ -828,7 +855,7 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *f, int reps, void *stream, double 
                 break;
             case 1:
                 if (fp64) k_rhs<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-                else k_refine<float><<<nit, NT, 0, st>>>(d, F32);
+                else k_refine<<<nit, NT, 0, st>>>(d, F32);
                 break;
             case 2:
                 if (fp64) {

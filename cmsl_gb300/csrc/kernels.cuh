@@ -20,6 +20,7 @@
 #pragma once
 #include <type_traits>
 #include "cmsl_dev.cuh"
+#include "dfloat.cuh"
 
 namespace cmsl {
 
@@ -49,6 +50,30 @@ template <> __device__ __forceinline__ float epsf_of<float>(const FilmDev *f, in
 __device__ __forceinline__ double *phi_sel(const Dev &d, int i)
 {
     return i == 0 ? d.phi[0] : i == 1 ? d.phi[1] : i == 2 ? d.phi[2] : i == 3 ? d.phi[3] : d.phi[4];
+}
+
+// Potential storage: FP64 mode keeps doubles; FP32_REFINED keeps double-float
+// pairs (hi half at cell c, lo half at cell ncells + c of the same buffer).
+template <class T> struct PhiAcc;
+template <> struct PhiAcc<double> {
+    using V = double;
+    const double *p;
+    __device__ __forceinline__ PhiAcc(const Dev &d, int buf, long long off) : p(phi_sel(d, buf) + off) {}
+    __device__ __forceinline__ V ld(long long o) const { return p[o]; }
+    static __device__ __forceinline__ V zero() { return 0.0; }
+};
+template <> struct PhiAcc<float> {
+    using V = df;
+    const float *h, *l;
+    __device__ __forceinline__ PhiAcc(const Dev &d, int buf, long long off)
+        : h((const float *)phi_sel(d, buf) + off), l((const float *)phi_sel(d, buf) + d.ncells + off) {}
+    __device__ __forceinline__ V ld(long long o) const { return df{h[o], l[o]}; }
+    static __device__ __forceinline__ V zero() { return df{0.f, 0.f}; }
+};
+__device__ __forceinline__ float phi_diff(df a, df b)
+{
+    const df d = df_sub(a, b);
+    return d.h + d.l;
 }
 
 // ------------------------------------------------------------------ tiles
@@ -211,8 +236,9 @@ __device__ __forceinline__ void op_z(const FilmDev *f, int k, V up, V dn, V &u, 
 template <class T, class M>
 __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
 {
+    using PV = typename PhiAcc<T>::V;
     __shared__ T sP[6][SPL];
-    __shared__ double sF[SPL];
+    __shared__ PV sF[SPL];
     __shared__ Coef<T> sC[6];
     __shared__ double sRed[NT / 32][7];
     __shared__ double sTot[7];
@@ -231,29 +257,29 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
     T *Pn[6];
     #pragma unroll
     for (int q = 0; q < 6; ++q) { Po[q] = F.P[cur][q] + off; Pn[q] = F.P[cur ^ 1][q] + off; }
-    const int pcur = d.solve[it.x].phi_cur;
-    const double *phi = phi_sel(d, pcur) + off;
+    const PhiAcc<T> phi(d, d.solve[it.x].phi_cur, off);
     const uint32_t *code = d.code + off;
-    const double two_h = f->two_h, inv_2h = f->inv_2h;
+    const double two_h = f->two_h;
+    const float inv_2hf = f->inv_2hf;
 
     T cdn[6], ccu[6], cup[6], hv[6];
-    double fdn = 0, fcu = 0, fup = 0, hf = 0;
+    PV fdn = PhiAcc<T>::zero(), fcu = fdn, fup = fdn, hf = fdn;
     if (g.valid) {
         const long long o = g.own_pl + (long long)z0 * g.plane;
         #pragma unroll
         for (int q = 0; q < 6; ++q) ccu[q] = Po[q][o];
-        fcu = phi[o];
+        fcu = phi.ld(o);
         const long long od = g.own_pl + (long long)(z0 > 0 ? z0 - 1 : z0) * g.plane;
         const long long ou = g.own_pl + (long long)(z0 + 1 < nz ? z0 + 1 : z0) * g.plane;
         #pragma unroll
         for (int q = 0; q < 6; ++q) { cdn[q] = Po[q][od]; cup[q] = Po[q][ou]; }
-        fdn = phi[od]; fup = phi[ou];
+        fdn = phi.ld(od); fup = phi.ld(ou);
     }
     if (g.halo) {
         const long long o = g.halo_pl + (long long)z0 * g.plane;
         #pragma unroll
         for (int q = 0; q < 6; ++q) hv[q] = Po[q][o];
-        hf = phi[o];
+        hf = phi.ld(o);
     }
     T acc[7];
     #pragma unroll
@@ -273,19 +299,19 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
         }
         __syncthreads();
         T cnx[6];
-        double fnx = 0;
+        PV fnx = PhiAcc<T>::zero();
         const bool pre = g.valid && (k + 2 < nz) && (k + 1 < z1);
         if (pre) {
             const long long o = g.own_pl + (long long)(k + 2) * g.plane;
             #pragma unroll
             for (int q = 0; q < 6; ++q) cnx[q] = Po[q][o];
-            fnx = phi[o];
+            fnx = phi.ld(o);
         }
         if (g.halo && k + 1 < z1) {
             const long long o = g.halo_pl + (long long)(k + 1) * g.plane;
             #pragma unroll
             for (int q = 0; q < 6; ++q) hv[q] = Po[q][o];
-            hf = phi[o];
+            hf = phi.ld(o);
         }
         if (g.valid) {
             const int s0 = g.own_slot;
@@ -312,25 +338,26 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
             // E_dep from the previous potential (depol_varEPS.cu:246-273)
             T ex = (T)0, ey = (T)0, ez = (T)0;
             if (dep) {
-                double Ex, Ey, Ezd, pu, pd;
+                PV pu, pd;
                 if (f->zbc == 0) {
-                    pu = (k == nz - 1) ? 0.0 : fup;
-                    pd = (k == 0) ? 0.0 : fdn;
+                    pu = (k == nz - 1) ? PhiAcc<T>::zero() : fup;
+                    pd = (k == 0) ? PhiAcc<T>::zero() : fdn;
                 } else {
-                    op_z<double>(f, k, fup, fdn, pu, pd);
+                    op_z<PV>(f, k, fup, fdn, pu, pd);
                 }
                 if constexpr (std::is_same<M, Exact>::value) {
-                    Ex = __ddiv_rn(-__dsub_rn(sF[s0 + 1], sF[s0 - 1]), two_h);
-                    Ey = __ddiv_rn(-__dsub_rn(sF[s0 + SX], sF[s0 - SX]), two_h);
-                    Ezd = __ddiv_rn(-__dsub_rn(pu, pd), two_h);
+                    const double Ex = __ddiv_rn(-__dsub_rn(sF[s0 + 1], sF[s0 - 1]), two_h);
+                    const double Ey = __ddiv_rn(-__dsub_rn(sF[s0 + SX], sF[s0 - SX]), two_h);
+                    const double Ezd = __ddiv_rn(-__dsub_rn(pu, pd), two_h);
+                    ex = (T)(-1.0 * Ex);
+                    ey = (T)(-1.0 * Ey);
+                    ez = (T)(-1.0 * Ezd);
                 } else {
-                    Ex = -(sF[s0 + 1] - sF[s0 - 1]) * inv_2h;
-                    Ey = -(sF[s0 + SX] - sF[s0 - SX]) * inv_2h;
-                    Ezd = -(pu - pd) * inv_2h;
+                    // -1 * E with E = -(phi_+ - phi_-) / (2h)
+                    ex = (T)(phi_diff(sF[s0 + 1], sF[s0 - 1]) * inv_2hf);
+                    ey = (T)(phi_diff(sF[s0 + SX], sF[s0 - SX]) * inv_2hf);
+                    ez = (T)(phi_diff(pu, pd) * inv_2hf);
                 }
-                ex = (T)(-1.0 * Ex);
-                ey = (T)(-1.0 * Ey);
-                ez = (T)(-1.0 * Ezd);
             }
             // crystal frame (kernels_evol.cu:162-168)
             const T pMXl = add(m, add(m, mul(m, t[0], ccu[0]), mul(m, t[1], ccu[1])), mul(m, t[2], ccu[2]));
@@ -572,18 +599,21 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
     }
 }
 
-// -------------------------------------- FP32 refinement: FP64 residual pass
-// Applies the pending FP32 correction (phi += delta), forms b from the new Pm
-// and the FP64 residual r64 = b - A phi, tests ||r64|| <= refine_tol ||b||,
-// and seeds the next inner FP32 solve with r = (float) r64.
-template <class T>
-__global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
+// ----------------------------- FP32 refinement: double-float residual pass
+// The potential of CMSL_FP32_REFINED is stored as double-float (hi half at
+// cell c, lo half at cell ncells + c of the same buffer).  This pass applies
+// the pending FP32 correction (phi += delta) -- or, on the first pass of a
+// step, the extrapolated warm start -- forms b from the new Pm and the
+// residual r = b - A phi in double-float, tests ||r|| <= refine_tol ||b||, and
+// seeds the next inner FP32 solve with r.  No FP64 instruction is executed.
+__device__ __forceinline__ df phi_ld(const float *h, const float *l, long long o) { return df{h[o], l[o]}; }
+
+__global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<float> F)
 {
-    __shared__ T sX[SPL], sY[SPL];
-    __shared__ double sF[SPL];
+    __shared__ float sX[SPL], sY[SPL], sFh[SPL], sFl[SPL];
     __shared__ int sM[SPL];
-    __shared__ double sRedA[NT / 32][2];
-    __shared__ double sRedB[NT / 32][1];
+    __shared__ float sCh[9], sCl[9];
+    __shared__ double sRedA[NT / 32][3];
     __shared__ double sRed[NT / 32][3];
     __shared__ double sTot[3];
     const int4 it = d.items[blockIdx.x];
@@ -596,33 +626,38 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
     const bool apply = S0->refine > 0;   // a correction is pending after the first pass
     const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pq = S0->phi_prev2, pr = S0->phi_prev3;
     const int pf = 10 - pc - pp - pq - pr;        // the free buffer of the five
-    // first pass: phi0 = 2 phi_n - phi_{n-1}  or  3 phi_n - 3 phi_{n-1} + phi_{n-2}
+    // first pass: extrapolated warm start (linear, quadratic or cubic)
     const int extrap = apply ? 0 : f->warm;
-    const long long off = f->off;
-    const T *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
-    const double *phi = phi_sel(d, pc) + off;
-    const double *phip = phi_sel(d, pp) + off;
-    const double *phiq = phi_sel(d, pq) + off;
-    const double *phir = phi_sel(d, pr) + off;
-    double *phin = phi_sel(d, pf) + off;
-    const T *dx = F.x + off;
+    const long long off = f->off, lo = d.ncells;
+    if (threadIdx.x < 9) { sCh[threadIdx.x] = f->cf_h[threadIdx.x]; sCl[threadIdx.x] = f->cf_l[threadIdx.x]; }
+    const float *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
+    const float *ph = (const float *)phi_sel(d, pc) + off, *pl_ = ph + lo;
+    const float *qh = (const float *)phi_sel(d, pp) + off, *ql = qh + lo;
+    const float *uh = (const float *)phi_sel(d, pq) + off, *ul = uh + lo;
+    const float *vh = (const float *)phi_sel(d, pr) + off, *vl = vh + lo;
+    float *nh = (float *)phi_sel(d, pf) + off, *nl = nh + lo;
+    const float *dx = F.x + off;
     const uint32_t *code = d.code + off;
-    T *r = F.r + off;
-    const T *dinv = F.dinv + off;
-    double acc64[2] = {0.0, 0.0};
-    T acc32[1] = {(T)0};
+    float *r = F.r + off;
+    const float *dinv = F.dinv + off;
+    const df cb = df{f->cb_h, f->cb_l};
+    float acc[3] = {0.f, 0.f, 0.f};
+    __syncthreads();
     if (run) {
-        double xd = 0, xc = 0, xu = 0, hx = 0;
-        T zd = 0, zc = 0, zu = 0, hPx = 0, hPy = 0;
+        df xd{0, 0}, xc{0, 0}, xu{0, 0}, hx{0, 0};
+        float zd = 0, zc = 0, zu = 0, hPx = 0, hPy = 0;
         int md = 0, mc = 0, mu = 0, hm = 0;
-        auto eff = [&](long long o) {
-            if (apply) return phi[o] + (double)dx[o];
-            if (extrap == 1) return 2.0 * phi[o] - phip[o];
-            if (extrap == 2) return 3.0 * (phi[o] - phip[o]) + phiq[o];
-            if (extrap == 3) return 4.0 * (phi[o] + phiq[o]) - 6.0 * phip[o] - phir[o];
-            return phi[o];
+        auto eff = [&](long long o) -> df {
+            const df a = phi_ld(ph, pl_, o);
+            if (apply) return df_add_f(a, dx[o]);
+            if (extrap == 1) return df_sub(df{2.f * a.h, 2.f * a.l}, phi_ld(qh, ql, o));
+            if (extrap == 2) return df_add(df_mul_f(df_sub(a, phi_ld(qh, ql, o)), 3.f), phi_ld(uh, ul, o));
+            if (extrap == 3)
+                return df_sub(df_sub(df_mul_f(df_add(a, phi_ld(uh, ul, o)), 4.f), df_mul_f(phi_ld(qh, ql, o), 6.f)),
+                              phi_ld(vh, vl, o));
+            return a;
         };
-        auto ld_own = [&](int k, double &xv, T &zv, int &mv) {
+        auto ld_own = [&](int k, df &xv, float &zv, int &mv) {
             const long long o = g.own_pl + (long long)k * g.plane;
             xv = eff(o); zv = Pmz[o]; mv = code_mat(code[o]);
         };
@@ -640,41 +675,52 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
             __syncthreads();
             if (g.valid) {
                 const long long o = g.own_pl + (long long)k * g.plane;
-                sF[g.own_slot] = xc; sX[g.own_slot] = Pmx[o]; sY[g.own_slot] = Pmy[o]; sM[g.own_slot] = mc;
+                sFh[g.own_slot] = xc.h; sFl[g.own_slot] = xc.l;
+                sX[g.own_slot] = Pmx[o]; sY[g.own_slot] = Pmy[o]; sM[g.own_slot] = mc;
             }
-            if (g.halo) { sF[g.halo_slot] = hx; sX[g.halo_slot] = hPx; sY[g.halo_slot] = hPy; sM[g.halo_slot] = hm; }
+            if (g.halo) {
+                sFh[g.halo_slot] = hx.h; sFl[g.halo_slot] = hx.l;
+                sX[g.halo_slot] = hPx; sY[g.halo_slot] = hPy; sM[g.halo_slot] = hm;
+            }
             __syncthreads();
-            double xn2 = 0; T zn2 = 0; int mn2 = 0;
+            df xn2{0, 0}; float zn2 = 0; int mn2 = 0;
             const bool pre = g.valid && (k + 2 < nz) && (k + 1 < z1);
             if (pre) ld_own(k + 2, xn2, zn2, mn2);
             if (g.halo && k + 1 < z1) ld_halo(k + 1);
             if (g.valid) {
                 const int s0 = g.own_slot;
                 const long long o = g.own_pl + (long long)k * g.plane;
-                const double pzu = (k == nz - 1) ? (double)zc : (double)zu;
-                const double pzd = (k == 0) ? (double)zc : (double)zd;
-                const double dv = (((double)sX[s0 + 1] - (double)sX[s0 - 1]) +
-                                   ((double)sY[s0 + SX] - (double)sY[s0 - SX]) + (pzu - pzd)) *
-                                  (f->inv_2h * f->eps0nd);
-                double b = -dv, ax;
+                df b, ax;
                 if (identity_row(f, k, g.own_pl)) {
-                    b = 0.0;
-                    ax = xc;
+                    b = df{0.f, 0.f};
+                    ax = xc;                             // x - g, g = 0
                 } else {
-                    double u, dd; int mmu, mmd;
-                    op_z<double>(f, k, xu, xd, u, dd);
+                    // b = -eps_0_nd div(Pm), differences of FP32 values are exact in df
+                    const float pzu = (k == nz - 1) ? zc : zu, pzd = (k == 0) ? zc : zd;
+                    df dv = df_add(df_add(two_sum(sX[s0 + 1], -sX[s0 - 1]), two_sum(sY[s0 + SX], -sY[s0 - SX])),
+                                   two_sum(pzu, -pzd));
+                    b = df_neg(df_mul(dv, cb));
+                    df u, dd; int mmu, mmd;
+                    op_z<df>(f, k, xu, xd, u, dd);
                     op_z<int>(f, k, mu, md, mmu, mmd);
-                    ax = op_row<double, Fast>(f, mc, sM[s0 + 1], sM[s0 - 1], sM[s0 + SX], sM[s0 - SX],
-                                              mmu, mmd, xc, sF[s0 + 1], sF[s0 - 1], sF[s0 + SX],
-                                              sF[s0 - SX], u, dd);
+                    const df xe{sFh[s0 + 1], sFl[s0 + 1]}, xw{sFh[s0 - 1], sFl[s0 - 1]};
+                    const df xn{sFh[s0 + SX], sFl[s0 + SX]}, xs{sFh[s0 - SX], sFl[s0 - SX]};
+                    const int m3 = mc * 3;
+                    auto cf = [&](int mnb) { return df{sCh[m3 + mnb], sCl[m3 + mnb]}; };
+                    df a = df_sub(df_mul(cf(sM[s0 + 1]), df_sub(xe, xc)), df_mul(cf(sM[s0 - 1]), df_sub(xc, xw)));
+                    a = df_add(a, df_mul(cf(sM[s0 + SX]), df_sub(xn, xc)));
+                    a = df_sub(a, df_mul(cf(sM[s0 - SX]), df_sub(xc, xs)));
+                    a = df_add(a, df_mul(cf(mmu), df_sub(u, xc)));
+                    a = df_sub(a, df_mul(cf(mmd), df_sub(xc, dd)));
+                    ax = df_neg(a);
                 }
-                const double r64 = b - ax;
-                phin[o] = xc;
-                const T rv = (T)r64;
+                const df rr = df_sub(b, ax);
+                nh[o] = xc.h; nl[o] = xc.l;
+                const float rv = rr.h + rr.l;
                 r[o] = rv;
-                acc64[0] += r64 * r64;
-                acc64[1] += b * b;
-                acc32[0] += rv * (rv * dinv[o]);
+                acc[0] = fmaf(rv, rv, acc[0]);
+                acc[1] = fmaf(b.h, b.h, acc[1]);
+                acc[2] = fmaf(rv, rv * dinv[o], acc[2]);
             }
             if (g.valid) {
                 xd = xc; xc = xu; zd = zc; zc = zu; md = mc; mc = mu;
@@ -683,13 +729,12 @@ __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<T> F)
         }
     }
     {
-        double t64[2], t32[1];
-        block_sum<2, double>(acc64, sRedA, t64);
-        block_sum<1, T>(acc32, sRedB, t32);
+        double t[3];
+        block_sum<3, float>(acc, sRedA, t);
         if (threadIdx.x == 0) {
-            d.partial[(long long)blockIdx.x * NPART + 0] = t64[0];
-            d.partial[(long long)blockIdx.x * NPART + 1] = t64[1];
-            d.partial[(long long)blockIdx.x * NPART + 2] = t32[0];
+            d.partial[(long long)blockIdx.x * NPART + 0] = t[0];
+            d.partial[(long long)blockIdx.x * NPART + 1] = t[1];
+            d.partial[(long long)blockIdx.x * NPART + 2] = t[2];
         }
     }
     if (!ticket_last(d.counter)) return;

@@ -39,9 +39,10 @@ typedef enum { CMSL_DIRICHLET = 0, CMSL_NEUMANN = 1 } cmsl_zbc;
 /* CMSL_FP64: FP64 storage and arithmetic, TDGL and operator bit-identical to
  *   the reference kernels; one PCG solve per step.
  * CMSL_FP32_REFINED: FP32 fields, stencils and PCG vectors; PCG dots summed in
- *   FP32 within a warp and FP64 above it; the potential is kept in FP64 and an
- *   outer FP64 residual-refinement loop drives ||b - A phi|| / ||b|| below
- *   refine_tol. */
+ *   FP32 within a warp and FP64 above it; the potential is kept in
+ *   double-float (two FP32 halves, ~48 significand bits) and an outer
+ *   residual-refinement loop evaluated in double-float drives
+ *   ||b - A phi|| / ||b|| below refine_tol. */
 typedef enum { CMSL_FP64 = 0, CMSL_FP32_REFINED = 1 } cmsl_precision;
 
 /* Stop test of the (inner) PCG.  CMSL_CRIT_REF is the reference's
@@ -129,7 +130,7 @@ cmsl_status cmsl_film_get_iters(cmsl_film *film, int n, int32_t *pcg_iters, int3
  *    kernelCalc_antiferro computed from the current phi (Calc_EfieldMag);
  *  - depol: one Depol_field (RHS from the current Pm, warm-started PCG);
  *  - apply_operator: y = A x with the film's operator (apply_A), FP64 or FP32;
- *  - efield: E = -grad(phi) of the current phi (Calc_EfieldMag). */
+ *  - efield: E = -grad(phi) of the current phi (Calc_EfieldMag), FP64 films. */
 cmsl_status cmsl_film_tdgl_step(cmsl_film *film, double Ez);
 cmsl_status cmsl_film_depol(cmsl_film *film, int32_t *iters, int32_t *status);
 cmsl_status cmsl_film_apply_operator(cmsl_film *film, const double *x, double *y);
