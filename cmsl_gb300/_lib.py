@@ -76,6 +76,9 @@ def lib() -> C.CDLL:
     L.cmsl_film_diag_inv.argtypes = [fp, _dp]
     L.cmsl_film_time_kernels.argtypes = [fp, C.c_int, C.c_void_p, _dp]
     L.cmsl_film_device_bytes.argtypes = [fp, C.POINTER(C.c_size_t)]
+    L.cmsl_depol_solve_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double,
+                                           C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, _ip, _ip]
     _lib = L
     return L
 
@@ -90,5 +93,5 @@ EXPORTS = [
     "cmsl_last_error", "cmsl_version", "cmsl_film_create", "cmsl_film_destroy", "cmsl_film_set_state",
     "cmsl_film_get_state", "cmsl_film_run", "cmsl_film_sync", "cmsl_film_get_rows", "cmsl_film_get_iters",
     "cmsl_film_tdgl_step", "cmsl_film_depol", "cmsl_film_apply_operator", "cmsl_film_efield",
-    "cmsl_film_diag_inv", "cmsl_film_time_kernels", "cmsl_film_device_bytes",
+    "cmsl_film_diag_inv", "cmsl_film_time_kernels", "cmsl_film_device_bytes", "cmsl_depol_solve_noalloc",
 ]

@@ -60,6 +60,8 @@ double harm(double a, double b)   // depol_varEPS.cu:10-15
 
 }  // namespace
 
+void cmsl_internal_set_error(const char *msg) { g_err = msg; }
+
 struct cmsl_film {
     int precision = CMSL_FP64;
     int nx = 0, ny = 0, nz = 0, dep = 0, ng = 0;

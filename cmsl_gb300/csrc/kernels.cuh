@@ -608,7 +608,7 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
 // seeds the next inner FP32 solve with r.  No FP64 instruction is executed.
 __device__ __forceinline__ df phi_ld(const float *h, const float *l, long long o) { return df{h[o], l[o]}; }
 
-__global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<float> F)
+static __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<float> F)
 {
     __shared__ float sX[SPL], sY[SPL], sFh[SPL], sFl[SPL];
     __shared__ int sM[SPL];
@@ -981,7 +981,7 @@ __global__ void __launch_bounds__(NT) k_update(Dev d, Fields<T> F)
 }
 
 // ------------------------------------------------------------ step end
-__global__ void k_step_end(Dev d)
+static __global__ void k_step_end(Dev d)
 {
     for (int fi = threadIdx.x; fi < d.n_films; fi += blockDim.x) {
         SolveDev *S = d.solve + fi;
@@ -1069,7 +1069,7 @@ __global__ void k_apply_op(Dev d, const T *x, T *y)
 }
 
 // E = -grad(phi) of the current potential (Calc_EfieldMag), for the tests.
-__global__ void k_efield(Dev d, double *Ex, double *Ey, double *Ez)
+static __global__ void k_efield(Dev d, double *Ex, double *Ey, double *Ez)
 {
     const int4 it = d.items[blockIdx.x];
     const FilmDev *f = d.films + it.x;

@@ -148,6 +148,28 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, doub
 /* Bytes of device memory the film holds. */
 cmsl_status cmsl_film_device_bytes(cmsl_film *film, size_t *bytes);
 
+/* Depolarisation solve that allocates nothing.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc (an application
+ * that owns all device memory through its own pool, a plugin handed fixed
+ * buffers).  It runs the FP64 Jacobi-PCG of cmsl_film_depol -- the same
+ * kernels and stop test -- with every work buffer in one fixed device array
+ * of about 6.3 MB that stays resident on each GPU that loads the library.
+ *   - grids up to 131072 cells (nx*ny*nz; nz >= 3); larger grids return
+ *     CMSL_ERR_ARG and do nothing;
+ *   - inputs and outputs are device pointers: material id per cell (0 AFE,
+ *     1 FE, 2 DE), eps_r per material (host), the new Pm components, and phi
+ *     (warm start in, solution out, in place);
+ *   - the first call on a device looks up the array's device address with
+ *     that device current; make it before any stream capture;
+ *   - all calls share the array: calls whose GPU work overlaps race, so
+ *     serialise them; each call clears the state it reads;
+ *   - returns after the solve (it reads the loop flags on `stream`). */
+cmsl_status cmsl_depol_solve_noalloc(int nx, int ny, int nz, double del_h, int zbc, double eps_0_nd,
+                                     const int32_t *material_dev, const double eps_r[3],
+                                     const double *Pmx_dev, const double *Pmy_dev, const double *Pmz_dev,
+                                     double *phi_dev, double tol_abs, double tol_rel, int max_iter,
+                                     int pcg_crit, void *stream, int32_t *iters_out, int32_t *status_out);
+
 #ifdef __cplusplus
 }
 #endif
