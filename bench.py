@@ -168,7 +168,7 @@ def run_reference(args):
     from cmsl_gb300 import workloads as wl
     import oracle
     oracle.build()
-    w = wl.config(CONFIG_ID)
+    w = wl.config(args.config)
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     # each step is a bounded sample: the full film, one time step
@@ -206,7 +206,7 @@ def run_ours(args):
     from cmsl_gb300 import workloads as wl
 
     fp64 = args.precision == "fp64"
-    w = wl.config(CONFIG_ID)
+    w = wl.config(args.config)
     kw = dict(precision=cg.FP64 if fp64 else cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8,
               max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000,
               warm_start=3)
@@ -315,6 +315,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", type=int, default=CONFIG_ID, choices=[0, 1, 2, 4],
+                    help="benchmark configuration whose film is stepped (default 1)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

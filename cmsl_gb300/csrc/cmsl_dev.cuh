@@ -54,7 +54,9 @@ struct FilmDev {
     int max_iter, max_refine, inner_max;
     double h, dt, eps0nd, inv_N, two_h, h2, inv_h2, inv_2h;
     double tol_abs2, tol_rel2, refine_tol2, inner_tol2;
-    float inv_h2f, inv_2hf, eps0f, pad_f;
+    float inv_h2f, inv_2hf, eps0f;
+    float dinv_uni;             // Jacobi D^-1 of non-identity rows when every material has one eps
+    int uni_eps;                // all materials share eps_r
     double n_mat[3];            // voxels per material (sum of the reference's masks)
     Coef<double> coef[6];       // index mat*2 + iface
     Coef<float> coef32[6];
@@ -87,8 +89,10 @@ struct CgBuf {
     float *r[2], *w[2], *s[2];  // ping-pong by iteration parity
     float *x, *p;
     unsigned int *arrive;       // grid-barrier arrival counter (reset by k_refine)
-    double *part;               // [2][grid][2] per-block partial sums, by iteration parity
+    float4 *part;               // [2][grid] per-block partial sums (two double-float pairs), by parity
     int *err;                   // barrier timeout flag
+    const int4 *bricks;         // stencil work list: TX x TY x (<= PZ planes) bricks
+    int n_bricks;
 };
 
 struct Ctl {

@@ -498,6 +498,13 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
     fd.refine_tol2 = dsc->refine_tol * dsc->refine_tol;
     fd.inner_tol2 = dsc->inner_tol * dsc->inner_tol;
     for (int q = 0; q < 3; ++q) fd.n_mat[q] = nmat[q];
+    fd.uni_eps = dsc->mats[0].eps_r == dsc->mats[1].eps_r && dsc->mats[1].eps_r == dsc->mats[2].eps_r;
+    {
+        // depol_varEPS.cu:177-179 with six equal faces
+        const double e = harm(dsc->mats[0].eps_r, dsc->mats[0].eps_r);
+        const double D = (e + e + e + e + e + e) / (h * h);
+        fd.dinv_uni = (float)(D > 1e-30 ? 1.0 / D : 1.0);
+    }
     for (int mt = 0; mt < 3; ++mt)
         for (int fl = 0; fl < 2; ++fl) {
             fill_coef<double>(fd.coef[mt * 2 + fl], dsc->mats[mt], fl, h, dsc->del_t);
@@ -561,8 +568,20 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg2<false>, PNT, P2SMEM_BYTES));
         }
         if (per < 1) return fail(CMSL_ERR_CUDA, "persistent PCG kernel cannot be resident");
-        f->cg_grid = std::min<int>((int)f->items.size(), per * nsm);
-        TRY(f->alloc((void **)&B.part, sizeof(double) * 2 * 2 * f->cg_grid));
+        // stencil bricks of PZ planes; the grid is sized so that every block
+        // gets the same number of bricks
+        std::vector<int4> bricks;
+        for (int y0 = 0; y0 < f->ny; y0 += TY)
+            for (int x0 = 0; x0 < f->nx; x0 += TX)
+                for (int z0 = 0; z0 < f->nz; z0 += PZ)
+                    bricks.push_back(make_int4(0, x0, y0, z0 | (std::min(f->nz, z0 + PZ) << 16)));
+        const int nb = (int)bricks.size(), maxg = per * nsm;
+        const int per_block = (nb + maxg - 1) / maxg;
+        f->cg_grid = f->cg_fused ? std::min<int>((int)f->items.size(), maxg) : (nb + per_block - 1) / per_block;
+        TRY(f->alloc((void **)&B.bricks, sizeof(int4) * nb));
+        CK(cudaMemcpy((void *)B.bricks, bricks.data(), sizeof(int4) * nb, cudaMemcpyHostToDevice));
+        B.n_bricks = nb;
+        TRY(f->alloc((void **)&B.part, sizeof(float4) * 2 * f->cg_grid));
         TRY(f->alloc((void **)&B.arrive, sizeof(unsigned int) * 2));
         TRY(f->alloc((void **)&B.err, sizeof(int) * 2));
     }
@@ -875,7 +894,7 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *f, int reps, void *stream, double 
                 break;
             default:
                 if (fp64) k_update<double, Exact, false><<<nit, NT, 0, st>>>(d, F64);
-                else k_dinv<float><<<nit, NT, 0, st>>>(d, (float *)f->d_dinv);
+                else k_step_end<<<1, 32, 0, st>>>(d);   // FP32 mode has no fourth kernel
                 break;
             }
             CK(cudaGetLastError());

@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
     const Geom g = make_geom(f, it.y, it.z);
     const int cur = d.ctl->cur, rs = d.ctl->run_step;
     const double Ez_ext = d.wave[(long long)it.x * d.wstride + rs];
+    const T mEz = (T)(-Ez_ext);                   // dfdPmz_app, kernels_evol.cu:210
     const int row = d.rows[(long long)it.x * d.wstride + rs];
     const int dep = f->dep_flag, nz = g.nz;
     const long long off = f->off;
@@ -389,7 +390,7 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
             b[5] = add(m, add(m, mul(m, t[2], dsx), mul(m, t[5], dsy)), mul(m, t[8], dsz));
             b[0] = add(m, b[0], ex);
             b[1] = add(m, b[1], ey);
-            b[2] = add(m, b[2], add(m, (T)(-Ez_ext), ez));
+            b[2] = add(m, b[2], add(m, mEz, ez));
             // explicit Euler with the 6-neighbour Laplacian (kernels_evol.cu:223-229)
             T pn[6];
             #pragma unroll
@@ -720,7 +721,8 @@ static __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<float> F)
                 r[o] = rv;
                 acc[0] = fmaf(rv, rv, acc[0]);
                 acc[1] = fmaf(b.h, b.h, acc[1]);
-                acc[2] = fmaf(rv, rv * dinv[o], acc[2]);
+                const float dd = f->uni_eps ? (identity_row(f, k, g.own_pl) ? 1.f : f->dinv_uni) : dinv[o];
+                acc[2] = fmaf(rv, rv * dd, acc[2]);
             }
             if (g.valid) {
                 xd = xc; xc = xu; zd = zc; zc = zu; md = mc; mc = mu;

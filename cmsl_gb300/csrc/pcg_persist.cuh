@@ -70,6 +70,19 @@ __device__ __forceinline__ void block_sum_p(T (&v)[NV], double (*sm)[NV], double
 
 // Writes this block's two partial sums, waits for all blocks, and returns the
 // grid totals (identical in every block).  False if the wait timed out.
+// Block partials are stored as double-float pairs and summed across blocks by
+// one warp in double-float, so the all-reduce issues no FP64 instruction
+// beyond a handful of conversions.
+__device__ __forceinline__ df warp_sum_df(df v)
+{
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const df w{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)};
+        v = df_add(v, w);
+    }
+    return v;
+}
+
 __device__ __forceinline__ bool grid_allreduce2(const CgBuf &B, int parity, unsigned int &target,
                                                 float v0, float v1, double (*sm)[2], double &t0,
                                                 double &t1)
@@ -79,11 +92,11 @@ __device__ __forceinline__ bool grid_allreduce2(const CgBuf &B, int parity, unsi
     float a[2] = {v0, v1};
     double blk[2];
     block_sum_p<2, float>(a, sm, blk);
-    double *part = B.part + (size_t)parity * gridDim.x * 2;
+    float4 *part = B.part + (size_t)parity * gridDim.x;
     target += gridDim.x;
     if (threadIdx.x == 0) {
-        __stcg(part + 2 * blockIdx.x, blk[0]);
-        __stcg(part + 2 * blockIdx.x + 1, blk[1]);
+        const float h0 = (float)blk[0], h1 = (float)blk[1];
+        __stcg(part + blockIdx.x, make_float4(h0, (float)(blk[0] - (double)h0), h1, (float)(blk[1] - (double)h1)));
         __threadfence();
         atomicAdd(B.arrive, 1u);
         int ok = 1;
@@ -96,14 +109,20 @@ __device__ __forceinline__ bool grid_allreduce2(const CgBuf &B, int parity, unsi
     }
     __syncthreads();
     if (!s_ok) return false;
-    double q[2] = {0.0, 0.0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += PNT) {
-        q[0] += __ldcg(part + 2 * b);
-        q[1] += __ldcg(part + 2 * b + 1);
+    if (threadIdx.x < 32) {
+        df q0{0.f, 0.f}, q1{0.f, 0.f};
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
+            const float4 v = __ldcg(part + b);
+            q0 = df_add(q0, df{v.x, v.y});
+            q1 = df_add(q1, df{v.z, v.w});
+        }
+        q0 = warp_sum_df(q0);
+        q1 = warp_sum_df(q1);
+        if (threadIdx.x == 0) {
+            s_tot[0] = (double)q0.h + (double)q0.l;
+            s_tot[1] = (double)q1.h + (double)q1.l;
+        }
     }
-    double tot[2];
-    block_sum_p<2, double>(q, sm, tot);
-    if (threadIdx.x == 0) { s_tot[0] = tot[0]; s_tot[1] = tot[1]; }
     __syncthreads();
     t0 = s_tot[0];
     t1 = s_tot[1];
@@ -141,6 +160,7 @@ struct FilmC {
     int nx, ny, nz, zbc, ref_id, plane;
     long long off;
     float inv_h2;
+    float dinv_uni;
 };
 
 __device__ __forceinline__ bool id_row(const FilmC &F, int k, int pl)
@@ -311,7 +331,7 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg1(Dev d, CgBuf B, const float 
     if (!run) return;                       // uniform: k_refine decided for every block
     FilmC F;
     F.nx = f->nx; F.ny = f->ny; F.nz = f->nz; F.zbc = f->zbc; F.ref_id = f->ref_id;
-    F.plane = f->nx * f->ny; F.off = f->off; F.inv_h2 = f->inv_h2f;
+    F.plane = f->nx * f->ny; F.off = f->off; F.inv_h2 = f->inv_h2f; F.dinv_uni = f->dinv_uni;
     if (threadIdx.x < 9) sEps[threadIdx.x] = f->epsf32[threadIdx.x];
     __syncthreads();
     const double tol2 = S->inner_tol2;
@@ -399,10 +419,17 @@ __device__ __forceinline__ bool grid_sync(const CgBuf &B, unsigned int &target)
 }
 
 // Phase P over all cells of the film.  INIT: u = D^-1 r, gamma = r.u.
-template <bool INIT>
+template <bool INIT, bool UNI>
 __device__ __forceinline__ void cg2_point(const FilmC &F, const CgBuf &B, const float *__restrict__ dv,
                                           long long n, bool first, float a, float b, float &gacc)
 {
+    // UNI: D^-1 is 1 on the identity rows (Dirichlet planes / Neumann pin) and
+    // one constant elsewhere, so it is not read from memory
+    const long long id_lo = (long long)F.plane, id_hi = (long long)F.plane * (F.nz - 1);
+    auto dinv_of = [&](long long c) -> float {
+        const bool idr = F.zbc == 0 ? (c < id_lo || c >= id_hi) : (c == (long long)F.ref_id);
+        return idr ? 1.f : F.dinv_uni;
+    };
     float *__restrict__ r = B.r[0] + F.off;
     float *__restrict__ u = B.r[1] + F.off;
     float *__restrict__ w = B.w[0] + F.off;
@@ -413,9 +440,15 @@ __device__ __forceinline__ void cg2_point(const FilmC &F, const CgBuf &B, const 
     const long long n4 = n >> 2;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
-        const float4 D4 = reinterpret_cast<const float4 *>(d)[q];
+        float dd[4];
+        if (UNI) {
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) dd[j] = dinv_of(4 * q + j);
+        } else {
+            const float4 D4 = reinterpret_cast<const float4 *>(d)[q];
+            dd[0] = D4.x; dd[1] = D4.y; dd[2] = D4.z; dd[3] = D4.w;
+        }
         const float4 R4 = reinterpret_cast<const float4 *>(r)[q];
-        const float dd[4] = {D4.x, D4.y, D4.z, D4.w};
         const float ri[4] = {R4.x, R4.y, R4.z, R4.w};
         float uo[4], ro[4];
         if (INIT) {
@@ -458,7 +491,7 @@ __device__ __forceinline__ void cg2_point(const FilmC &F, const CgBuf &B, const 
     // tail (n not a multiple of 4): block 0
     if (blockIdx.x == 0) {
         for (long long c = 4 * n4 + threadIdx.x; c < n; c += blockDim.x) {
-            const float dd = d[c], ri = r[c];
+            const float dd = UNI ? dinv_of(c) : d[c], ri = r[c];
             float ro, uo;
             if (INIT) {
                 ro = ri;
@@ -554,11 +587,9 @@ __device__ __forceinline__ void cg2_stencil(const Dev &d, const FilmC &F, const 
                                             float *sUb, uint32_t *sCb, const float *sEps)
 {
     const uint32_t *code = d.code + F.off;
-    for (int i = blockIdx.x; i < d.n_items; i += gridDim.x) {
-        const int4 it = d.items[i];
-        const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-        for (int zz = z0; zz < z1; zz += PZ)
-            cg2_brick<UNI>(F, B, code, it.y, it.z, zz, min(zz + PZ, z1), dacc, sUb, sCb, sEps);
+    for (int i = blockIdx.x; i < B.n_bricks; i += gridDim.x) {
+        const int4 it = B.bricks[i];
+        cg2_brick<UNI>(F, B, code, it.y, it.z, it.w & 0xffff, it.w >> 16, dacc, sUb, sCb, sEps);
     }
 }
 
@@ -580,7 +611,7 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg2(Dev d, CgBuf B, const float 
     if (!run) return;
     FilmC F;
     F.nx = f->nx; F.ny = f->ny; F.nz = f->nz; F.zbc = f->zbc; F.ref_id = f->ref_id;
-    F.plane = f->nx * f->ny; F.off = f->off; F.inv_h2 = f->inv_h2f;
+    F.plane = f->nx * f->ny; F.off = f->off; F.inv_h2 = f->inv_h2f; F.dinv_uni = f->dinv_uni;
     const long long n = (long long)F.plane * F.nz;
     if (threadIdx.x < 9) sEps[threadIdx.x] = f->epsf32[threadIdx.x];
     __syncthreads();
@@ -588,7 +619,7 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg2(Dev d, CgBuf B, const float 
     const int imax = S->inner_max;
     unsigned int target = 0;
     float ga = 0.f, da = 0.f;
-    cg2_point<true>(F, B, dinv, n, true, 0.f, 0.f, ga);
+    cg2_point<true, UNI>(F, B, dinv, n, true, 0.f, 0.f, ga);
     if (!grid_sync(B, target)) return;
     cg2_stencil<UNI>(d, F, B, da, sUb, sCb, sEps);
     double g0, dl;
@@ -605,7 +636,7 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg2(Dev d, CgBuf B, const float 
     while (s_go) {
         const float a = s_ab[0], b = s_ab[1];
         ga = 0.f; da = 0.f;
-        cg2_point<false>(F, B, dinv, n, it == 0, a, b, ga);
+        cg2_point<false, UNI>(F, B, dinv, n, it == 0, a, b, ga);
         if (!grid_sync(B, target)) return;
         cg2_stencil<UNI>(d, F, B, da, sUb, sCb, sEps);
         double gn, dn;
