@@ -58,12 +58,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-cell DRAM bytes per kernel from the committed ncu summary, if any."""
+def ncu_traffic(workload: str):
+    """Per-cell DRAM bytes per kernel of this workload from the committed ncu
+    summary (profiles/traffic_per_cell.json), if measured."""
     p = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
     if os.path.exists(p):
         with open(p) as fh:
-            return json.load(fh)
+            return json.load(fh).get(workload, {})
     return {}
 
 
@@ -255,7 +256,7 @@ def run_ours(args):
     ki = names.index(top)
     peak, peak_kind = measured_peaks()
     achieved = BYTES[mode][top] * w.N / (kms[ki] * 1e-3) / 1e9
-    traffic = ncu_traffic().get(mode, {}).get(top)
+    traffic = ncu_traffic(w.name).get(mode, {}).get(top)
     roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "bytes_per_cell": BYTES[mode][top],
