@@ -8,10 +8,18 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _declared():
-    txt = open(os.path.join(ROOT, "include", "cmsl.h")).read()
+def _declared(header="cmsl.h"):
+    txt = open(os.path.join(ROOT, "include", header)).read()
     decl = r"^\s*(?:cmsl_status|const char \*|void)\s*(cmsl_[a-z_0-9]+)\s*\("
     return sorted(set(re.findall(decl, txt, flags=re.M)))
+
+
+def _all_declared():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if h.endswith(".h"):
+            names += _declared(h)
+    return sorted(set(names))
 
 
 def test_header_and_binding_agree():
@@ -19,11 +27,18 @@ def test_header_and_binding_agree():
     assert _declared() == sorted(_lib.EXPORTS)
 
 
+def test_io_header_functions_are_bound():
+    from cmsl_gb300 import formats
+    L = formats._bind()
+    for name in _declared("cmsl_io.h"):
+        assert getattr(L, name).argtypes is not None, name
+
+
 def test_library_exports_every_symbol():
     from cmsl_gb300 import build, _lib
     build.build()
     L = _lib.lib()
-    for name in _declared():
+    for name in _all_declared():
         assert hasattr(L, name), name
     assert b"sm_103a" in L.cmsl_version()
 
