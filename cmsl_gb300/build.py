@@ -33,6 +33,25 @@ def _stale(out: str, deps) -> bool:
     return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
 
 
+CLI = os.path.join(HERE, "cmsl_pe")
+
+
+def build_cli(verbose: bool = False, force: bool = False) -> str:
+    """The campaign driver executable (cmsl_pe), linked against libcmsl_gb.so."""
+    src = os.path.join(CSRC, "cmsl_pe.cpp")
+    deps = [src, OUT, os.path.join(ROOT, "include", "cmsl.h"), os.path.join(ROOT, "include", "cmsl_io.h")]
+    if not force and not _stale(CLI, deps):
+        return CLI
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off",
+           "-I" + os.path.join(ROOT, "include"), src, "-L" + HERE, "-lcmsl_gb", "-Wl,-rpath,$ORIGIN",
+           "-o", CLI + ".tmp"]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    subprocess.run(cmd, check=True)
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in CUDA_SOURCES + HOST_SOURCES if os.path.exists(os.path.join(CSRC, s))]
     deps = srcs + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "cmsl.h")]
@@ -49,5 +68,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return OUT
 
 
+def build_all(verbose: bool = False, force: bool = False) -> str:
+    out = build(verbose=verbose, force=force)
+    build_cli(verbose=verbose, force=force)
+    return out
+
+
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build_all(verbose=True, force="--force" in sys.argv))
