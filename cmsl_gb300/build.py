@@ -34,6 +34,23 @@ def _stale(out: str, deps) -> bool:
 
 
 CLI = os.path.join(HERE, "cmsl_pe")
+REFCOMPAT = os.path.join(HERE, "cmsl_refcompat.o")
+
+
+def build_refcompat(verbose: bool = False, force: bool = False) -> str:
+    """The object that defines the reference's Evolve/Depol_field entry points
+    over its globals; link it with the reference's own objects and -lcmsl_gb."""
+    src = os.path.join(CSRC, "refcompat.cu")
+    deps = [src, os.path.join(ROOT, "include", "cmsl.h"), os.path.join(ROOT, "include", "cmsl_io.h")]
+    if not force and not _stale(REFCOMPAT, deps):
+        return REFCOMPAT
+    cmd = [nvcc(), ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"),
+           "-c", src, "-o", REFCOMPAT + ".tmp"]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    subprocess.run(cmd, check=True)
+    os.replace(REFCOMPAT + ".tmp", REFCOMPAT)
+    return REFCOMPAT
 
 
 def build_cli(verbose: bool = False, force: bool = False) -> str:
@@ -71,6 +88,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
 def build_all(verbose: bool = False, force: bool = False) -> str:
     out = build(verbose=verbose, force=force)
     build_cli(verbose=verbose, force=force)
+    build_refcompat(verbose=verbose, force=force)
     return out
 
 
