@@ -3,11 +3,12 @@ phase-field hot path of jhb6617-arch/cmsl.
 
 The compute runs in libcmsl_gb.so (hand-written CUDA, C ABI in
 include/cmsl.h).  This package is its Python face: ``Film`` (one film on the
-GPU), the reference's input formats and set-up (``formats``), the P-E loop
-schedule of ``Evolve`` (``schedule``) and the synthetic workloads the
-benchmarks use (``workloads``).
+GPU), ``Batch`` (many films advancing together), the reference's input
+formats and set-up (``formats``), the P-E loop schedule of ``Evolve``
+(``schedule``) and the synthetic workloads the benchmarks use
+(``workloads``).
 """
 from ._lib import (  # noqa: F401
     FP64, FP32_REFINED, DIRICHLET, NEUMANN, CRIT_REF, CRIT_RELRES, CmslError, LIB_PATH,
 )
-from .film import Film  # noqa: F401
+from .film import Batch, Film  # noqa: F401

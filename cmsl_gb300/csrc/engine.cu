@@ -1,16 +1,22 @@
-// engine.cu -- film lifecycle, CUDA-graph construction and the run loop.
+// engine.cu -- film and batch lifecycle, CUDA-graph construction and the run loop.
 //
-// One time step is one CUDA graph:
+// A handle holds F >= 1 independent films (a cmsl_film is a batch of one).
+// Their cells, grains and work items are concatenated; every kernel launch
+// covers all films, each work item carrying its film index, and every
+// per-film quantity (solver scalars, convergence flags, waveform, sweep rows)
+// lives in per-film device slots.  One time step is one CUDA graph:
 //   CMSL_FP64:          k_tdgl -> k_rhs -> WHILE(inner){ k_spmv -> k_update } -> k_step_end
-//   CMSL_FP32_REFINED:  k_tdgl -> WHILE(outer){ k_refine -> WHILE(inner){ k_spmv -> k_update } }
-//                       -> k_step_end
-// The WHILE conditions are set on the device by the last block of k_rhs,
-// k_refine and k_update, so a step never returns to the host: the PCG loop of
-// the reference (depol_varEPS.cu:472-522, two blocking Ddot per iteration) and
-// its per-step cudaMalloc/cublasCreate churn (:373-393, :585-593) are gone.
-// The applied field and the output-row schedule of the P-E loop are device
-// arrays indexed by a device step counter, so the same graph is relaunched
-// for every step.
+//   CMSL_FP32_REFINED:  k_tdgl -> WHILE(outer){ k_refine -> inner solve } -> k_step_end
+// where the FP32 inner solve is the persistent cooperative PCG kernel for a
+// single film and WHILE(inner){ k_spmv -> k_update } for a batch (films that
+// have converged drop out of the masked kernels; the loop runs while any film
+// is active).  The WHILE conditions are set on the device by the last block of
+// k_rhs, k_refine and k_update, so a step never returns to the host: the PCG
+// loop of the reference (depol_varEPS.cu:472-522, two blocking Ddot per
+// iteration) and its per-step cudaMalloc/cublasCreate churn (:373-393,
+// :585-593) are gone.  The applied field and the output-row schedule of the
+// P-E loop are device arrays indexed by a device step counter, so the same
+// graph is relaunched for every step.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -50,6 +56,12 @@ cmsl_status fail(cmsl_status s, const char *fmt, ...)
                         __FILE__, __LINE__);                                                  \
     } while (0)
 
+#define TRY(x)                               \
+    do {                                     \
+        cmsl_status s_ = (x);                \
+        if (s_ != CMSL_OK) return s_;        \
+    } while (0)
+
 double harm(double a, double b)   // depol_varEPS.cu:10-15
 {
     const double eps = 1e-20;
@@ -58,17 +70,25 @@ double harm(double a, double b)   // depol_varEPS.cu:10-15
     return (2.0 * a * b) / denom;
 }
 
+// Host view of one film of a handle.
+struct FilmHost {
+    int nx, ny, nz, ng, dep;
+    long long N, off;   // cells, first cell
+};
+
 }  // namespace
 
 void cmsl_internal_set_error(const char *msg) { g_err = msg; }
 
-struct cmsl_film {
+struct Engine {
     int precision = CMSL_FP64;
-    int nx = 0, ny = 0, nz = 0, dep = 0, ng = 0;
-    long long N = 0;
+    int n_films = 0;
+    long long ncells = 0;
+    bool any_dep = false;
     size_t esz = 8;
+    int max_iter_cap = 0, max_refine_cap = 0, inner_max_cap = 0;
+    std::vector<FilmHost> fh;
     std::vector<int4> items;
-    FilmDev fd{};
     // device buffers
     std::vector<void *> allocs;
     size_t bytes = 0;
@@ -83,7 +103,7 @@ struct cmsl_film {
     Ctl *d_ctl = nullptr;
     void *d_P[2][6] = {};
     void *d_r = nullptr, *d_q = nullptr, *d_dinv = nullptr, *d_x = nullptr, *d_p[2] = {};
-    // schedule buffers (grown on demand)
+    // schedule buffers, [n_films][stride], grown on demand
     double *d_wave = nullptr;
     int *d_rows = nullptr;
     double *d_rowbuf = nullptr;
@@ -96,14 +116,16 @@ struct cmsl_film {
     bool graph_valid = false;
     bool use_graph = true;
     cudaStream_t stream = nullptr;
-    CgBuf cg{};                 // FP32_REFINED persistent PCG vectors
+    // FP32_REFINED inner solver: the persistent cooperative kernel (one film)
+    // or the masked two-kernel PCG (batches, or CMSL_PCG_TWO_KERNEL=1)
+    bool persistent = false;
+    CgBuf cg{};
     int cg_grid = 0;
-    bool uni_eps = false;       // every material has the same eps_r
     bool cg_fused = false;      // single-sweep variant (CMSL_PCG_FUSED=1) instead of two-phase
-    void *cg_fn = nullptr;      // the persistent solver kernel in use
+    void *cg_fn = nullptr;
     size_t cg_smem = 0;
 
-    ~cmsl_film()
+    ~Engine()
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -129,8 +151,9 @@ struct cmsl_film {
     Dev dev(int use_cond, cudaGraphConditionalHandle hi = 0, cudaGraphConditionalHandle ho = 0) const
     {
         Dev d{};
-        d.films = d_films; d.items = d_items; d.n_films = 1; d.n_items = (int)items.size();
-        d.code = d_code; d.ncells = N; d.phi[0] = d_phi[0]; d.phi[1] = d_phi[1]; d.phi[2] = d_phi[2]; d.phi[3] = d_phi[3]; d.phi[4] = d_phi[4];
+        d.films = d_films; d.items = d_items; d.n_films = n_films; d.n_items = (int)items.size();
+        d.code = d_code; d.ncells = ncells;
+        for (int q = 0; q < 5; ++q) d.phi[q] = d_phi[q];
         d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
         d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
         d.iters_log = d_iters; d.refine_log = d_refine;
@@ -156,22 +179,19 @@ struct cmsl_film {
     }
 };
 
+struct cmsl_film : Engine {};
+struct cmsl_batch : Engine {};
+
 namespace {
 
-#define TRY(x)                               \
-    do {                                     \
-        cmsl_status s_ = (x);                \
-        if (s_ != CMSL_OK) return s_;        \
-    } while (0)
-
-// z chunk: enough items to fill the 152 SMs a few times over, chunks >= 4 planes.
-int pick_zchunk(int nx, int ny, int nz)
+// z chunk: enough items to fill the 152 SMs a few times over (all films of
+// the handle together), chunks >= 4 planes.
+int pick_zchunk(long long xy_tiles, int nz)
 {
-    const long long xy = (long long)((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
     const char *env = getenv("CMSL_ZCHUNK");
     if (env && atoi(env) > 0) return std::min(nz, atoi(env));
     const long long target = 8LL * 152;
-    long long chunks = (target + xy - 1) / xy;
+    const long long chunks = (target + xy_tiles - 1) / xy_tiles;
     int zc = (int)std::max<long long>(1, (nz + chunks - 1) / chunks);
     zc = std::max(zc, std::min(nz, 4));
     return std::min(zc, nz);
@@ -197,36 +217,105 @@ template <class T> void fill_coef(Coef<T> &c, const cmsl_material &mt, int iface
     c.a02 = (T)(2.0 * mt.a0);
 }
 
-template <class T> cmsl_status upload_TR(cmsl_film *f, const double *TR)
+// The film-constant table of one film (set-up of main.cu:261-359 and
+// depol_varEPS.cu:126-180 reduced to per-material constants).
+void fill_film(FilmDev &fd, const cmsl_film_desc *dsc, int precision)
 {
-    std::vector<T> tr((size_t)9 * f->ng);
-    for (size_t i = 0; i < tr.size(); ++i) tr[i] = (T)TR[i];
-    TRY(f->alloc(&f->d_TR, tr.size() * sizeof(T)));
-    CK(cudaMemcpy(f->d_TR, tr.data(), tr.size() * sizeof(T), cudaMemcpyHostToDevice));
+    fd.nx = dsc->nx; fd.ny = dsc->ny; fd.nz = dsc->nz; fd.zbc = dsc->zbc;
+    fd.dep_flag = dsc->dep_flag != 0;
+    fd.warm = precision != CMSL_FP64 ? std::min(std::max(dsc->warm_start, 0), 3) : 0;
+    fd.ref_id = dsc->nx / 2 + dsc->nx * (dsc->ny / 2 + (dsc->nz / 2) * dsc->ny);   // depol_varEPS.cu:339-346
+    fd.crit = dsc->pcg_crit;
+    fd.max_iter = dsc->max_iter;
+    fd.max_refine = std::max(1, dsc->max_refine);
+    fd.inner_max = std::max(1, dsc->inner_max_iter);
+    const double h = dsc->del_h;
+    fd.h = h; fd.dt = dsc->del_t; fd.eps0nd = dsc->eps_0_nd;
+    fd.inv_N = 1.0 / ((double)dsc->nx * dsc->ny * dsc->nz);              // main.cu:405
+    fd.two_h = 2.0 * h; fd.h2 = h * h; fd.inv_h2 = 1.0 / (h * h); fd.inv_2h = 1.0 / (2.0 * h);
+    fd.inv_h2f = (float)fd.inv_h2; fd.inv_2hf = (float)fd.inv_2h; fd.eps0f = (float)dsc->eps_0_nd;
+    {
+        const df cb = df_from_double(dsc->eps_0_nd * fd.inv_2h);
+        fd.cb_h = cb.h; fd.cb_l = cb.l;
+    }
+    fd.tol_abs2 = dsc->tol_abs * dsc->tol_abs;
+    fd.tol_rel2 = dsc->tol_rel * dsc->tol_rel;
+    fd.refine_tol2 = dsc->refine_tol * dsc->refine_tol;
+    fd.inner_tol2 = dsc->inner_tol * dsc->inner_tol;
+    fd.uni_eps = dsc->mats[0].eps_r == dsc->mats[1].eps_r && dsc->mats[1].eps_r == dsc->mats[2].eps_r;
+    {
+        // depol_varEPS.cu:177-179 with six equal faces
+        const double e = harm(dsc->mats[0].eps_r, dsc->mats[0].eps_r);
+        const double D = (e + e + e + e + e + e) / (h * h);
+        fd.dinv_uni = (float)(D > 1e-30 ? 1.0 / D : 1.0);
+    }
+    for (int mt = 0; mt < 3; ++mt)
+        for (int fl = 0; fl < 2; ++fl) {
+            fill_coef<double>(fd.coef[mt * 2 + fl], dsc->mats[mt], fl, h, dsc->del_t);
+            fill_coef<float>(fd.coef32[mt * 2 + fl], dsc->mats[mt], fl, h, dsc->del_t);
+        }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            fd.epsf[a * 3 + b] = harm(dsc->mats[a].eps_r, dsc->mats[b].eps_r);
+            fd.epsf32[a * 3 + b] = (float)fd.epsf[a * 3 + b];
+            const df c = df_from_double(fd.epsf[a * 3 + b] * fd.inv_h2);
+            fd.cf_h[a * 3 + b] = c.h; fd.cf_l[a * 3 + b] = c.l;
+        }
+}
+
+cmsl_status check_desc(const cmsl_film_desc *dsc, int idx, int n)
+{
+    char who[32] = "";
+    if (n > 1) snprintf(who, sizeof who, "film %d: ", idx);
+    if (dsc->nx < 1 || dsc->ny < 1 || dsc->nz < 3)
+        return fail(CMSL_ERR_ARG, "%sgrid %dx%dx%d: need nx, ny >= 1 and nz >= 3", who, dsc->nx, dsc->ny, dsc->nz);
+    if (dsc->nx > 32767 || dsc->ny > 32767 || dsc->nz > 32767)
+        return fail(CMSL_ERR_ARG, "%sgrid dimension above 32767", who);
+    if (dsc->n_grains < 1 || dsc->n_grains > (int)GID_MASK)
+        return fail(CMSL_ERR_ARG, "%sn_grains %d out of range", who, dsc->n_grains);
+    if (!dsc->omega || !dsc->grain_mat || !dsc->TR) return fail(CMSL_ERR_ARG, "%somega/grain_mat/TR NULL", who);
+    if (dsc->precision != CMSL_FP64 && dsc->precision != CMSL_FP32_REFINED)
+        return fail(CMSL_ERR_ARG, "%sprecision %d unknown", who, dsc->precision);
+    if (dsc->zbc != CMSL_DIRICHLET && dsc->zbc != CMSL_NEUMANN) return fail(CMSL_ERR_ARG, "%szbc %d", who, dsc->zbc);
+    if (!(dsc->del_h > 0.0) || !(dsc->del_t > 0.0)) return fail(CMSL_ERR_ARG, "%sdel_h and del_t must be > 0", who);
+    for (int g = 0; g < dsc->n_grains; ++g)
+        if (dsc->grain_mat[g] < 0 || dsc->grain_mat[g] > 2)
+            return fail(CMSL_ERR_ARG, "%sgrain %d has material %d (need 0..2)", who, g, dsc->grain_mat[g]);
     return CMSL_OK;
 }
 
-cmsl_status ensure_schedule(cmsl_film *f, int n_steps, int n_rows)
+template <class T> cmsl_status upload_TR(Engine *e, const cmsl_film_desc *descs, int n)
 {
-    if (n_steps > f->wstride) {
+    std::vector<T> tr;
+    for (int i = 0; i < n; ++i)
+        for (int q = 0; q < 9 * descs[i].n_grains; ++q) tr.push_back((T)descs[i].TR[q]);
+    TRY(e->alloc(&e->d_TR, tr.size() * sizeof(T)));
+    CK(cudaMemcpy(e->d_TR, tr.data(), tr.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return CMSL_OK;
+}
+
+cmsl_status ensure_schedule(Engine *e, int n_steps, int n_rows)
+{
+    const size_t F = (size_t)e->n_films;
+    if (n_steps > e->wstride) {
         const int w = std::max(n_steps, 16);
-        if (f->d_wave) { cudaFree(f->d_wave); cudaFree(f->d_rows); cudaFree(f->d_iters); cudaFree(f->d_refine); }
-        f->d_wave = nullptr; f->d_rows = nullptr; f->d_iters = nullptr; f->d_refine = nullptr;
-        CK(cudaMalloc(&f->d_wave, sizeof(double) * w));
-        CK(cudaMalloc(&f->d_rows, sizeof(int) * w));
-        CK(cudaMalloc(&f->d_iters, sizeof(int) * w));
-        CK(cudaMalloc(&f->d_refine, sizeof(int) * w));
-        f->wstride = w;
-        f->graph_valid = false;
+        if (e->d_wave) { cudaFree(e->d_wave); cudaFree(e->d_rows); cudaFree(e->d_iters); cudaFree(e->d_refine); }
+        e->d_wave = nullptr; e->d_rows = nullptr; e->d_iters = nullptr; e->d_refine = nullptr;
+        CK(cudaMalloc(&e->d_wave, sizeof(double) * w * F));
+        CK(cudaMalloc(&e->d_rows, sizeof(int) * w * F));
+        CK(cudaMalloc(&e->d_iters, sizeof(int) * w * F));
+        CK(cudaMalloc(&e->d_refine, sizeof(int) * w * F));
+        e->wstride = w;
+        e->graph_valid = false;
     }
-    if (n_rows > f->rstride || !f->d_rowbuf) {
+    if (n_rows > e->rstride || !e->d_rowbuf) {
         const int r = std::max(n_rows, 16);
-        if (f->d_rowbuf) cudaFree(f->d_rowbuf);
-        f->d_rowbuf = nullptr;
-        CK(cudaMalloc(&f->d_rowbuf, sizeof(double) * 11 * r));
-        CK(cudaMemset(f->d_rowbuf, 0, sizeof(double) * 11 * r));
-        f->rstride = r;
-        f->graph_valid = false;
+        if (e->d_rowbuf) cudaFree(e->d_rowbuf);
+        e->d_rowbuf = nullptr;
+        CK(cudaMalloc(&e->d_rowbuf, sizeof(double) * 11 * r * F));
+        CK(cudaMemset(e->d_rowbuf, 0, sizeof(double) * 11 * r * F));
+        e->rstride = r;
+        e->graph_valid = false;
     }
     return CMSL_OK;
 }
@@ -267,30 +356,30 @@ cmsl_status add_while(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_
 }
 
 // Arguments must outlive graph instantiation only (node params are copied).
-cmsl_status build_graph(cmsl_film *f)
+cmsl_status build_graph(Engine *e)
 {
-    if (f->exec) { cudaGraphExecDestroy(f->exec); f->exec = nullptr; }
-    if (f->graph) { cudaGraphDestroy(f->graph); f->graph = nullptr; }
+    if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+    if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
     cudaGraph_t g;
     CK(cudaGraphCreate(&g, 0));
-    f->graph = g;
-    const int nit = (int)f->items.size();
+    e->graph = g;
+    const int nit = (int)e->items.size();
     KArgs a;
-    a.F64 = f->fields<double>();
-    a.F32 = f->fields<float>();
+    a.F64 = e->fields<double>();
+    a.F32 = e->fields<float>();
     cudaGraphConditionalHandle h_outer = 0, h_inner = 0;
-    const bool fp64 = f->precision == CMSL_FP64;
+    const bool fp64 = e->precision == CMSL_FP64;
     cudaGraphNode_t n_tdgl, n_solve, n_end;
-    if (!fp64 && f->dep) CK(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
-    if (fp64 && f->dep) CK(cudaGraphConditionalHandleCreate(&h_inner, g, 0, cudaGraphCondAssignDefault));
-    a.d = f->dev(1, h_inner, h_outer);
+    if (!fp64 && e->any_dep) CK(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
+    if (fp64 && e->any_dep) CK(cudaGraphConditionalHandleCreate(&h_inner, g, 0, cudaGraphCondAssignDefault));
+    a.d = e->dev(1, h_inner, h_outer);
     void *args64[] = {&a.d, &a.F64};
     void *args32[] = {&a.d, &a.F32};
     void *args_d[] = {&a.d};
     if (fp64) TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl<double, Exact>, nit, NT, args64));
     else TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl<float, Fast>, nit, NT, args32));
     cudaGraphNode_t last = n_tdgl;
-    if (f->dep) {
+    if (e->any_dep) {
         if (fp64) {
             cudaGraphNode_t n_rhs, n_sp, n_up;
             cudaGraph_t body;
@@ -299,255 +388,254 @@ cmsl_status build_graph(cmsl_film *f)
             TRY(add_kernel(body, &n_sp, nullptr, 0, (void *)k_spmv<double, Exact>, nit, NT, args64));
             TRY(add_kernel(body, &n_up, &n_sp, 1, (void *)k_update<double, Exact, false>, nit, NT, args64));
             last = n_solve;
-        } else {
+        } else if (e->persistent) {
             cudaGraph_t outer;
             cudaGraphNode_t n_ref, n_cg;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
-            a.d = f->dev(1, 0, h_outer);
+            a.d = e->dev(1, 0, h_outer);
             TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
-            void *args_cg[] = {&a.d, &f->cg, &f->d_dinv};
-            TRY(add_kernel(outer, &n_cg, &n_ref, 1, f->cg_fn, f->cg_grid, PNT, args_cg, f->cg_smem));
+            void *args_cg[] = {&a.d, &e->cg, &e->d_dinv};
+            TRY(add_kernel(outer, &n_cg, &n_ref, 1, e->cg_fn, e->cg_grid, PNT, args_cg, e->cg_smem));
             cudaLaunchAttributeValue av{};
             av.cooperative = 1;
             CK(cudaGraphKernelNodeSetAttribute(n_cg, cudaLaunchAttributeCooperative, &av));
             last = n_solve;
+        } else {
+            // the inner loop's handle belongs to the outer body graph it lives in
+            cudaGraph_t outer, inner;
+            cudaGraphNode_t n_ref, n_in, n_sp, n_up;
+            TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
+            CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
+            a.d = e->dev(1, h_inner, h_outer);
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
+            TRY(add_while(outer, &n_in, &n_ref, 1, h_inner, &inner));
+            TRY(add_kernel(inner, &n_sp, nullptr, 0, (void *)k_spmv<float, Fast>, nit, NT, args32));
+            TRY(add_kernel(inner, &n_up, &n_sp, 1, (void *)k_update<float, Fast, true>, nit, NT, args32));
+            last = n_solve;
         }
     }
     TRY(add_kernel(g, &n_end, &last, 1, (void *)k_step_end, 1, 32, args_d));
-    CK(cudaGraphInstantiate(&f->exec, g, 0));
-    f->graph_valid = true;
+    CK(cudaGraphInstantiate(&e->exec, g, 0));
+    e->graph_valid = true;
     return CMSL_OK;
 }
 
-cmsl_status read_flags(cmsl_film *f, cudaStream_t st, SolveDev *S)
+// Reads every film's solver slot; *active / *outer: any film still running.
+cmsl_status read_flags(Engine *e, cudaStream_t st, bool *active, bool *outer)
 {
-    CK(cudaMemcpyAsync(S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost, st));
+    std::vector<SolveDev> S((size_t)e->n_films);
+    CK(cudaMemcpyAsync(S.data(), e->d_solve, sizeof(SolveDev) * S.size(), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    *active = false;
+    if (outer) *outer = false;
+    for (const SolveDev &s : S) {
+        *active |= s.active != 0;
+        if (outer) *outer |= s.outer_active != 0;
+    }
     return CMSL_OK;
 }
 
 // The depolarisation solve launched from the host, one kernel at a time,
 // reading the loop flags back after each iteration.  Used by the
 // single-piece test hooks and when graphs are disabled (CMSL_NO_GRAPH=1).
-cmsl_status solve_direct(cmsl_film *f, cudaStream_t st, const Dev &d, const Fields<double> &F64,
+cmsl_status solve_direct(Engine *e, cudaStream_t st, const Dev &d, const Fields<double> &F64,
                          const Fields<float> &F32)
 {
-    const int nit = (int)f->items.size();
-    SolveDev S;
-    if (f->precision == CMSL_FP64) {
+    const int nit = (int)e->items.size();
+    bool act = false, out = false;
+    if (e->precision == CMSL_FP64) {
         k_rhs<double, Exact><<<nit, NT, 0, st>>>(d, F64);
         CK(cudaGetLastError());
         for (int guard = 0;; ++guard) {
-            TRY(read_flags(f, st, &S));
-            if (!S.active) break;
-            if (guard > f->fd.max_iter + 1) return fail(CMSL_ERR_STATE, "PCG loop did not stop");
+            TRY(read_flags(e, st, &act, nullptr));
+            if (!act) break;
+            if (guard > e->max_iter_cap + 1) return fail(CMSL_ERR_STATE, "PCG loop did not stop");
             k_spmv<double, Exact><<<nit, NT, 0, st>>>(d, F64);
             k_update<double, Exact, false><<<nit, NT, 0, st>>>(d, F64);
             CK(cudaGetLastError());
         }
     } else {
         for (int og = 0;; ++og) {
-            if (og > f->fd.max_refine + 1) return fail(CMSL_ERR_STATE, "refinement loop did not stop");
+            if (og > e->max_refine_cap + 1) return fail(CMSL_ERR_STATE, "refinement loop did not stop");
             k_refine<<<nit, NT, 0, st>>>(d, F32);
             CK(cudaGetLastError());
-            TRY(read_flags(f, st, &S));
-            if (S.active) {
+            TRY(read_flags(e, st, &act, &out));
+            if (act && e->persistent) {
                 Dev dd = d;
-                CgBuf B = f->cg;
-                const float *dv = (const float *)f->d_dinv;
+                CgBuf B = e->cg;
+                const float *dv = (const float *)e->d_dinv;
                 void *args[] = {&dd, &B, &dv};
-                CK(cudaLaunchCooperativeKernel(f->cg_fn, f->cg_grid, PNT, args, f->cg_smem, st));
-                TRY(read_flags(f, st, &S));
+                CK(cudaLaunchCooperativeKernel(e->cg_fn, e->cg_grid, PNT, args, e->cg_smem, st));
+                TRY(read_flags(e, st, &act, &out));
             }
-            if (!S.outer_active) break;
+            for (int guard = 0; act && !e->persistent; ++guard) {
+                if (guard > e->inner_max_cap + 1) return fail(CMSL_ERR_STATE, "inner PCG loop did not stop");
+                k_spmv<float, Fast><<<nit, NT, 0, st>>>(d, F32);
+                k_update<float, Fast, true><<<nit, NT, 0, st>>>(d, F32);
+                CK(cudaGetLastError());
+                TRY(read_flags(e, st, &act, &out));
+            }
+            if (!out) break;
         }
     }
     return CMSL_OK;
 }
 
-cmsl_status step_direct(cmsl_film *f, cudaStream_t st)
+cmsl_status step_direct(Engine *e, cudaStream_t st)
 {
-    const int nit = (int)f->items.size();
-    const Dev d = f->dev(0);
-    const Fields<double> F64 = f->fields<double>();
-    const Fields<float> F32 = f->fields<float>();
-    if (f->precision == CMSL_FP64) k_tdgl<double, Exact><<<nit, NT, 0, st>>>(d, F64);
+    const int nit = (int)e->items.size();
+    const Dev d = e->dev(0);
+    const Fields<double> F64 = e->fields<double>();
+    const Fields<float> F32 = e->fields<float>();
+    if (e->precision == CMSL_FP64) k_tdgl<double, Exact><<<nit, NT, 0, st>>>(d, F64);
     else k_tdgl<float, Fast><<<nit, NT, 0, st>>>(d, F32);
     CK(cudaGetLastError());
-    if (f->dep) TRY(solve_direct(f, st, d, F64, F32));
+    if (e->any_dep) TRY(solve_direct(e, st, d, F64, F32));
     k_step_end<<<1, 32, 0, st>>>(d);
     CK(cudaGetLastError());
     return CMSL_OK;
 }
 
 template <class T>
-cmsl_status put_fields(cmsl_film *f, int set, const double *const P[6])
+cmsl_status put_fields(Engine *e, int film, int set, const double *const P[6])
 {
-    std::vector<T> tmp((size_t)f->N);
+    const FilmHost &h = e->fh[film];
+    std::vector<T> tmp((size_t)h.N);
     for (int q = 0; q < 6; ++q) {
         if (!P[q]) return fail(CMSL_ERR_ARG, "P[%d] is NULL", q);
-        for (long long i = 0; i < f->N; ++i) tmp[i] = (T)P[q][i];
-        CK(cudaMemcpy(f->d_P[set][q], tmp.data(), f->N * sizeof(T), cudaMemcpyHostToDevice));
+        for (long long i = 0; i < h.N; ++i) tmp[i] = (T)P[q][i];
+        CK(cudaMemcpy((T *)e->d_P[set][q] + h.off, tmp.data(), h.N * sizeof(T), cudaMemcpyHostToDevice));
     }
     return CMSL_OK;
 }
 
 template <class T>
-cmsl_status get_fields(cmsl_film *f, int set, double *const P[6])
+cmsl_status get_fields(Engine *e, int film, int set, double *const P[6])
 {
-    std::vector<T> tmp((size_t)f->N);
+    const FilmHost &h = e->fh[film];
+    std::vector<T> tmp((size_t)h.N);
     for (int q = 0; q < 6; ++q) {
         if (!P[q]) continue;
-        CK(cudaMemcpy(tmp.data(), f->d_P[set][q], f->N * sizeof(T), cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < f->N; ++i) P[q][i] = (double)tmp[i];
+        CK(cudaMemcpy(tmp.data(), (const T *)e->d_P[set][q] + h.off, h.N * sizeof(T), cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < h.N; ++i) P[q][i] = (double)tmp[i];
     }
     return CMSL_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-const char *cmsl_last_error(void) { return g_err.c_str(); }
-const char *cmsl_version(void) { return "cmsl_gb300 0.1 (sm_103a)"; }
-
-cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
+cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
 {
-    if (!dsc || !out) return fail(CMSL_ERR_ARG, "NULL argument");
-    *out = nullptr;
-    if (dsc->nx < 1 || dsc->ny < 1 || dsc->nz < 3)
-        return fail(CMSL_ERR_ARG, "grid %dx%dx%d: need nx, ny >= 1 and nz >= 3", dsc->nx, dsc->ny, dsc->nz);
-    if (dsc->nx > 32767 || dsc->ny > 32767 || dsc->nz > 32767)
-        return fail(CMSL_ERR_ARG, "grid dimension above 32767");
-    if (dsc->n_grains < 1 || dsc->n_grains > (int)GID_MASK)
-        return fail(CMSL_ERR_ARG, "n_grains %d out of range", dsc->n_grains);
-    if (!dsc->omega || !dsc->grain_mat || !dsc->TR) return fail(CMSL_ERR_ARG, "omega/grain_mat/TR NULL");
-    if (dsc->precision != CMSL_FP64 && dsc->precision != CMSL_FP32_REFINED)
-        return fail(CMSL_ERR_ARG, "precision %d unknown", dsc->precision);
-    if (dsc->zbc != CMSL_DIRICHLET && dsc->zbc != CMSL_NEUMANN) return fail(CMSL_ERR_ARG, "zbc %d", dsc->zbc);
-    if (!(dsc->del_h > 0.0) || !(dsc->del_t > 0.0)) return fail(CMSL_ERR_ARG, "del_h and del_t must be > 0");
-
-    cmsl_film *f = new cmsl_film();
-    std::unique_ptr<cmsl_film> guard(f);
-    f->precision = dsc->precision;
-    f->nx = dsc->nx; f->ny = dsc->ny; f->nz = dsc->nz;
-    f->N = (long long)f->nx * f->ny * f->nz;
-    f->dep = dsc->dep_flag != 0;
-    f->ng = dsc->n_grains;
-    f->esz = f->precision == CMSL_FP64 ? 8 : 4;
+    for (int i = 0; i < n; ++i) TRY(check_desc(descs + i, i, n));
+    for (int i = 1; i < n; ++i)
+        if (descs[i].precision != descs[0].precision)
+            return fail(CMSL_ERR_ARG, "film %d: precision %d differs from film 0 (%d)", i, descs[i].precision,
+                        descs[0].precision);
+    e->precision = descs[0].precision;
+    e->n_films = n;
+    e->esz = e->precision == CMSL_FP64 ? 8 : 4;
     const char *ng = getenv("CMSL_NO_GRAPH");
-    f->use_graph = !(ng && atoi(ng) != 0);
+    e->use_graph = !(ng && atoi(ng) != 0);
+    long long xy_tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        const cmsl_film_desc &d = descs[i];
+        FilmHost h;
+        h.nx = d.nx; h.ny = d.ny; h.nz = d.nz; h.ng = d.n_grains; h.dep = d.dep_flag != 0;
+        h.N = (long long)d.nx * d.ny * d.nz;
+        h.off = e->ncells;
+        e->ncells += h.N;
+        e->fh.push_back(h);
+        e->any_dep |= h.dep != 0;
+        xy_tiles += (long long)((d.nx + TX - 1) / TX) * ((d.ny + TY - 1) / TY);
+        e->max_iter_cap = std::max(e->max_iter_cap, d.max_iter);
+        e->max_refine_cap = std::max(e->max_refine_cap, std::max(1, d.max_refine));
+        e->inner_max_cap = std::max(e->inner_max_cap, std::max(1, d.inner_max_iter));
+    }
+    // The persistent solver's single-reduction recurrence assumes a symmetric
+    // operator.  With the Neumann z boundary the mirrored rows of the first
+    // and last planes (depol_varEPS.cu:93-98) make A non-symmetric, so those
+    // films take the two-kernel PCG, the reference's own algorithm.
+    const char *tk = getenv("CMSL_PCG_TWO_KERNEL");
+    e->persistent = e->precision != CMSL_FP64 && n == 1 && descs[0].zbc == CMSL_DIRICHLET && !(tk && atoi(tk) != 0);
 
-    // per-cell code, interface flags (main.cu:13-42), material voxel counts
-    const long long N = f->N, plane = (long long)f->nx * f->ny;
-    std::vector<uint32_t> code((size_t)N);
-    double nmat[3] = {0, 0, 0};
-    for (int g = 0; g < f->ng; ++g)
-        if (dsc->grain_mat[g] < 0 || dsc->grain_mat[g] > 2)
-            return fail(CMSL_ERR_ARG, "grain %d has material %d (need 0..2)", g, dsc->grain_mat[g]);
-    for (long long i = 0; i < N; ++i) {
-        const int gid = dsc->omega[i];
-        if (gid < 0 || gid >= f->ng) return fail(CMSL_ERR_ARG, "cell %lld has grain id %d outside [0,%d)", i, gid, f->ng);
-        const int mat = dsc->grain_mat[gid];
-        int iface;
-        if (dsc->is_interface) {
-            iface = dsc->is_interface[i] != 0;
-        } else {
-            const long long k = i / plane;
-            iface = 0;
-            if (mat == CMSL_FE && k > 0 && k < f->nz - 1) {
-                const int mu = dsc->grain_mat[dsc->omega[i + plane]];
-                const int md = dsc->grain_mat[dsc->omega[i - plane]];
-                iface = (mu != CMSL_FE || md != CMSL_FE);
+    // per-cell code (grain id local to the film), interface flags
+    // (main.cu:13-42), material voxel counts, work items, film tables
+    std::vector<uint32_t> code((size_t)e->ncells);
+    std::vector<FilmDev> fds((size_t)n);
+    int g_off = 0;
+    for (int fi = 0; fi < n; ++fi) {
+        const cmsl_film_desc *dsc = descs + fi;
+        const FilmHost &h = e->fh[fi];
+        const long long plane = (long long)h.nx * h.ny;
+        const std::string who = n > 1 ? "film " + std::to_string(fi) + ": " : "";
+        double nmat[3] = {0, 0, 0};
+        for (long long i = 0; i < h.N; ++i) {
+            const int gid = dsc->omega[i];
+            if (gid < 0 || gid >= h.ng)
+                return fail(CMSL_ERR_ARG, "%scell %lld has grain id %d outside [0,%d)", who.c_str(), i, gid, h.ng);
+            const int mat = dsc->grain_mat[gid];
+            int iface;
+            if (dsc->is_interface) {
+                iface = dsc->is_interface[i] != 0;
+            } else {
+                const long long k = i / plane;
+                iface = 0;
+                if (mat == CMSL_FE && k > 0 && k < h.nz - 1) {
+                    const int mu = dsc->grain_mat[dsc->omega[i + plane]];
+                    const int md = dsc->grain_mat[dsc->omega[i - plane]];
+                    iface = (mu != CMSL_FE || md != CMSL_FE);
+                }
             }
+            code[h.off + i] = (uint32_t)gid | ((uint32_t)mat << 24) | ((uint32_t)iface << 26);
+            nmat[mat] += 1.0;
         }
-        code[i] = (uint32_t)gid | ((uint32_t)mat << 24) | ((uint32_t)iface << 26);
-        nmat[mat] += 1.0;
+        FilmDev &fd = fds[fi];
+        fill_film(fd, dsc, e->precision);
+        fd.off = h.off;
+        fd.g_off = g_off;
+        g_off += h.ng;
+        for (int q = 0; q < 3; ++q) fd.n_mat[q] = nmat[q];
+        // items: TX x TY x zchunk tiles
+        const int zc = pick_zchunk(xy_tiles, h.nz);
+        fd.item_begin = (int)e->items.size();
+        for (int y0 = 0; y0 < h.ny; y0 += TY)
+            for (int x0 = 0; x0 < h.nx; x0 += TX)
+                for (int z0 = 0; z0 < h.nz; z0 += zc) {
+                    const int z1 = std::min(h.nz, z0 + zc);
+                    e->items.push_back(make_int4(fi, x0, y0, z0 | (z1 << 16)));
+                }
+        fd.item_end = (int)e->items.size();
     }
-
-    // items: TX x TY x zchunk tiles
-    const int zc = pick_zchunk(f->nx, f->ny, f->nz);
-    for (int y0 = 0; y0 < f->ny; y0 += TY)
-        for (int x0 = 0; x0 < f->nx; x0 += TX)
-            for (int z0 = 0; z0 < f->nz; z0 += zc) {
-                const int z1 = std::min(f->nz, z0 + zc);
-                f->items.push_back(make_int4(0, x0, y0, z0 | (z1 << 16)));
-            }
-
-    FilmDev &fd = f->fd;
-    fd.nx = f->nx; fd.ny = f->ny; fd.nz = f->nz; fd.zbc = dsc->zbc;
-    fd.off = 0; fd.g_off = 0; fd.item_begin = 0; fd.item_end = (int)f->items.size();
-    fd.dep_flag = f->dep;
-    fd.warm = f->precision != CMSL_FP64 ? std::min(std::max(dsc->warm_start, 0), 3) : 0;
-    fd.ref_id = f->nx / 2 + f->nx * (f->ny / 2 + (f->nz / 2) * f->ny);   // depol_varEPS.cu:339-346
-    fd.crit = dsc->pcg_crit;
-    fd.max_iter = dsc->max_iter;
-    fd.max_refine = std::max(1, dsc->max_refine);
-    fd.inner_max = std::max(1, dsc->inner_max_iter);
-    const double h = dsc->del_h;
-    fd.h = h; fd.dt = dsc->del_t; fd.eps0nd = dsc->eps_0_nd;
-    fd.inv_N = 1.0 / ((double)f->nx * f->ny * f->nz);              // main.cu:405
-    fd.two_h = 2.0 * h; fd.h2 = h * h; fd.inv_h2 = 1.0 / (h * h); fd.inv_2h = 1.0 / (2.0 * h);
-    fd.inv_h2f = (float)fd.inv_h2; fd.inv_2hf = (float)fd.inv_2h; fd.eps0f = (float)dsc->eps_0_nd;
-    {
-        const df cb = df_from_double(dsc->eps_0_nd * fd.inv_2h);
-        fd.cb_h = cb.h; fd.cb_l = cb.l;
-    }
-    fd.tol_abs2 = dsc->tol_abs * dsc->tol_abs;
-    fd.tol_rel2 = dsc->tol_rel * dsc->tol_rel;
-    fd.refine_tol2 = dsc->refine_tol * dsc->refine_tol;
-    fd.inner_tol2 = dsc->inner_tol * dsc->inner_tol;
-    for (int q = 0; q < 3; ++q) fd.n_mat[q] = nmat[q];
-    fd.uni_eps = dsc->mats[0].eps_r == dsc->mats[1].eps_r && dsc->mats[1].eps_r == dsc->mats[2].eps_r;
-    {
-        // depol_varEPS.cu:177-179 with six equal faces
-        const double e = harm(dsc->mats[0].eps_r, dsc->mats[0].eps_r);
-        const double D = (e + e + e + e + e + e) / (h * h);
-        fd.dinv_uni = (float)(D > 1e-30 ? 1.0 / D : 1.0);
-    }
-    for (int mt = 0; mt < 3; ++mt)
-        for (int fl = 0; fl < 2; ++fl) {
-            fill_coef<double>(fd.coef[mt * 2 + fl], dsc->mats[mt], fl, h, dsc->del_t);
-            fill_coef<float>(fd.coef32[mt * 2 + fl], dsc->mats[mt], fl, h, dsc->del_t);
-        }
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b) {
-            fd.epsf[a * 3 + b] = harm(dsc->mats[a].eps_r, dsc->mats[b].eps_r);
-            fd.epsf32[a * 3 + b] = (float)fd.epsf[a * 3 + b];
-            const df c = df_from_double(fd.epsf[a * 3 + b] * fd.inv_h2);
-            fd.cf_h[a * 3 + b] = c.h; fd.cf_l[a * 3 + b] = c.l;
-        }
 
     // device memory
-    const size_t cells = (size_t)N;
-    TRY(f->alloc((void **)&f->d_films, sizeof(FilmDev)));
-    CK(cudaMemcpy(f->d_films, &fd, sizeof(FilmDev), cudaMemcpyHostToDevice));
-    TRY(f->alloc((void **)&f->d_items, sizeof(int4) * f->items.size()));
-    CK(cudaMemcpy(f->d_items, f->items.data(), sizeof(int4) * f->items.size(), cudaMemcpyHostToDevice));
-    TRY(f->alloc((void **)&f->d_code, sizeof(uint32_t) * cells));
-    CK(cudaMemcpy(f->d_code, code.data(), sizeof(uint32_t) * cells, cudaMemcpyHostToDevice));
-    if (f->precision == CMSL_FP64) TRY(upload_TR<double>(f, dsc->TR));
-    else TRY(upload_TR<float>(f, dsc->TR));
+    const size_t cells = (size_t)e->ncells;
+    TRY(e->alloc((void **)&e->d_films, sizeof(FilmDev) * n));
+    CK(cudaMemcpy(e->d_films, fds.data(), sizeof(FilmDev) * n, cudaMemcpyHostToDevice));
+    TRY(e->alloc((void **)&e->d_items, sizeof(int4) * e->items.size()));
+    CK(cudaMemcpy(e->d_items, e->items.data(), sizeof(int4) * e->items.size(), cudaMemcpyHostToDevice));
+    TRY(e->alloc((void **)&e->d_code, sizeof(uint32_t) * cells));
+    CK(cudaMemcpy(e->d_code, code.data(), sizeof(uint32_t) * cells, cudaMemcpyHostToDevice));
+    if (e->precision == CMSL_FP64) TRY(upload_TR<double>(e, descs, n));
+    else TRY(upload_TR<float>(e, descs, n));
     for (int s = 0; s < 2; ++s)
-        for (int q = 0; q < 6; ++q) TRY(f->alloc(&f->d_P[s][q], f->esz * cells));
-    TRY(f->alloc(&f->d_r, f->esz * cells));
-    TRY(f->alloc(&f->d_q, f->esz * cells));
-    TRY(f->alloc(&f->d_dinv, f->esz * cells));
-    TRY(f->alloc(&f->d_p[0], f->esz * cells));
-    TRY(f->alloc(&f->d_p[1], f->esz * cells));
-    if (f->precision != CMSL_FP64) {
-        TRY(f->alloc(&f->d_x, f->esz * cells));
+        for (int q = 0; q < 6; ++q) TRY(e->alloc(&e->d_P[s][q], e->esz * cells));
+    TRY(e->alloc(&e->d_r, e->esz * cells));
+    TRY(e->alloc(&e->d_q, e->esz * cells));
+    TRY(e->alloc(&e->d_dinv, e->esz * cells));
+    TRY(e->alloc(&e->d_p[0], e->esz * cells));
+    TRY(e->alloc(&e->d_p[1], e->esz * cells));
+    if (e->precision != CMSL_FP64) TRY(e->alloc(&e->d_x, e->esz * cells));
+    if (e->persistent) {
         // persistent single-reduction PCG: r ping-pong (r[0] is the shared r),
         // w and s ping-pong, x = correction, p in place
-        CgBuf &B = f->cg;
-        B.r[0] = (float *)f->d_r;
-        TRY(f->alloc((void **)&B.r[1], 4 * cells));
-        TRY(f->alloc((void **)&B.w[0], 4 * cells));
-        TRY(f->alloc((void **)&B.w[1], 4 * cells));
-        TRY(f->alloc((void **)&B.s[0], 4 * cells));
-        TRY(f->alloc((void **)&B.s[1], 4 * cells));
-        B.x = (float *)f->d_x;
-        B.p = (float *)f->d_p[0];
+        const FilmHost &h = e->fh[0];
+        CgBuf &B = e->cg;
+        B.r[0] = (float *)e->d_r;
+        TRY(e->alloc((void **)&B.r[1], 4 * cells));
+        TRY(e->alloc((void **)&B.w[0], 4 * cells));
+        TRY(e->alloc((void **)&B.w[1], 4 * cells));
+        TRY(e->alloc((void **)&B.s[0], 4 * cells));
+        TRY(e->alloc((void **)&B.s[1], 4 * cells));
+        B.x = (float *)e->d_x;
+        B.p = (float *)e->d_p[0];
         int dev = 0, nsm = 0, per = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -555,55 +643,311 @@ cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
         CK(cudaFuncSetAttribute(k_pcg_cg1<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PSMEM_BYTES));
         CK(cudaFuncSetAttribute(k_pcg_cg2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2SMEM_BYTES));
         CK(cudaFuncSetAttribute(k_pcg_cg2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2SMEM_BYTES));
-        f->uni_eps = dsc->mats[0].eps_r == dsc->mats[1].eps_r && dsc->mats[1].eps_r == dsc->mats[2].eps_r;
+        const bool uni = fds[0].uni_eps != 0;
         const char *solver = getenv("CMSL_PCG_FUSED");
-        f->cg_fused = solver && atoi(solver) != 0;
-        if (f->cg_fused) {
-            f->cg_fn = f->uni_eps ? (void *)k_pcg_cg1<true> : (void *)k_pcg_cg1<false>;
-            f->cg_smem = PSMEM_BYTES;
+        e->cg_fused = solver && atoi(solver) != 0;
+        if (e->cg_fused) {
+            e->cg_fn = uni ? (void *)k_pcg_cg1<true> : (void *)k_pcg_cg1<false>;
+            e->cg_smem = PSMEM_BYTES;
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg1<false>, PNT, PSMEM_BYTES));
         } else {
-            f->cg_fn = f->uni_eps ? (void *)k_pcg_cg2<true> : (void *)k_pcg_cg2<false>;
-            f->cg_smem = P2SMEM_BYTES;
+            e->cg_fn = uni ? (void *)k_pcg_cg2<true> : (void *)k_pcg_cg2<false>;
+            e->cg_smem = P2SMEM_BYTES;
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg2<false>, PNT, P2SMEM_BYTES));
         }
         if (per < 1) return fail(CMSL_ERR_CUDA, "persistent PCG kernel cannot be resident");
         // stencil bricks of PZ planes; the grid is sized so that every block
         // gets the same number of bricks
         std::vector<int4> bricks;
-        for (int y0 = 0; y0 < f->ny; y0 += TY)
-            for (int x0 = 0; x0 < f->nx; x0 += TX)
-                for (int z0 = 0; z0 < f->nz; z0 += PZ)
-                    bricks.push_back(make_int4(0, x0, y0, z0 | (std::min(f->nz, z0 + PZ) << 16)));
+        for (int y0 = 0; y0 < h.ny; y0 += TY)
+            for (int x0 = 0; x0 < h.nx; x0 += TX)
+                for (int z0 = 0; z0 < h.nz; z0 += PZ)
+                    bricks.push_back(make_int4(0, x0, y0, z0 | (std::min(h.nz, z0 + PZ) << 16)));
         const int nb = (int)bricks.size(), maxg = per * nsm;
         const int per_block = (nb + maxg - 1) / maxg;
-        f->cg_grid = f->cg_fused ? std::min<int>((int)f->items.size(), maxg) : (nb + per_block - 1) / per_block;
-        TRY(f->alloc((void **)&B.bricks, sizeof(int4) * nb));
+        e->cg_grid = e->cg_fused ? std::min<int>((int)e->items.size(), maxg) : (nb + per_block - 1) / per_block;
+        TRY(e->alloc((void **)&B.bricks, sizeof(int4) * nb));
         CK(cudaMemcpy((void *)B.bricks, bricks.data(), sizeof(int4) * nb, cudaMemcpyHostToDevice));
         B.n_bricks = nb;
-        TRY(f->alloc((void **)&B.part, sizeof(float4) * 2 * f->cg_grid));
-        TRY(f->alloc((void **)&B.arrive, sizeof(unsigned int) * 2));
-        TRY(f->alloc((void **)&B.err, sizeof(int) * 2));
+        TRY(e->alloc((void **)&B.part, sizeof(float4) * 2 * e->cg_grid));
+        TRY(e->alloc((void **)&B.arrive, sizeof(unsigned int) * 2));
+        TRY(e->alloc((void **)&B.err, sizeof(int) * 2));
     }
-    TRY(f->alloc((void **)&f->d_phi[0], sizeof(double) * cells));
-    TRY(f->alloc((void **)&f->d_phi[1], sizeof(double) * cells));
-    if (f->precision != CMSL_FP64) {
-        TRY(f->alloc((void **)&f->d_phi[2], sizeof(double) * cells));
-        TRY(f->alloc((void **)&f->d_phi[3], sizeof(double) * cells));
-        TRY(f->alloc((void **)&f->d_phi[4], sizeof(double) * cells));
+    TRY(e->alloc((void **)&e->d_phi[0], sizeof(double) * cells));
+    TRY(e->alloc((void **)&e->d_phi[1], sizeof(double) * cells));
+    if (e->precision != CMSL_FP64) {
+        TRY(e->alloc((void **)&e->d_phi[2], sizeof(double) * cells));
+        TRY(e->alloc((void **)&e->d_phi[3], sizeof(double) * cells));
+        TRY(e->alloc((void **)&e->d_phi[4], sizeof(double) * cells));
     }
-    TRY(f->alloc((void **)&f->d_partial, sizeof(double) * NPART * f->items.size()));
-    TRY(f->alloc((void **)&f->d_counter, sizeof(unsigned int) * 4));
-    TRY(f->alloc((void **)&f->d_solve, sizeof(SolveDev)));
-    TRY(f->alloc((void **)&f->d_ctl, sizeof(Ctl)));
-    TRY(ensure_schedule(f, 16, 16));
+    TRY(e->alloc((void **)&e->d_partial, sizeof(double) * NPART * e->items.size()));
+    TRY(e->alloc((void **)&e->d_counter, sizeof(unsigned int) * 4));
+    TRY(e->alloc((void **)&e->d_solve, sizeof(SolveDev) * n));
+    TRY(e->alloc((void **)&e->d_ctl, sizeof(Ctl)));
+    TRY(ensure_schedule(e, 16, 16));
 
-    const Dev d = f->dev(0);
-    if (f->precision == CMSL_FP64) k_dinv<double><<<(int)f->items.size(), NT>>>(d, (double *)f->d_dinv);
-    else k_dinv<float><<<(int)f->items.size(), NT>>>(d, (float *)f->d_dinv);
+    const Dev d = e->dev(0);
+    if (e->precision == CMSL_FP64) k_dinv<double><<<(int)e->items.size(), NT>>>(d, (double *)e->d_dinv);
+    else k_dinv<float><<<(int)e->items.size(), NT>>>(d, (float *)e->d_dinv);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
-    *out = guard.release();
+    return CMSL_OK;
+}
+
+// State of one film.  P goes into the set the next step reads (Ctl::cur);
+// phi into the film's slice of every potential buffer; the film's solver
+// slot restarts.  reset_clock also zeroes the shared step counters.
+cmsl_status set_state(Engine *e, int film, const double *const P[6], const double *phi, bool reset_clock)
+{
+    if (!P) return fail(CMSL_ERR_ARG, "NULL argument");
+    if (film < 0 || film >= e->n_films) return fail(CMSL_ERR_ARG, "film %d outside [0,%d)", film, e->n_films);
+    CK(cudaDeviceSynchronize());
+    if (reset_clock) CK(cudaMemset(e->d_ctl, 0, sizeof(Ctl)));
+    Ctl c;
+    CK(cudaMemcpy(&c, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    if (e->precision == CMSL_FP64) TRY(put_fields<double>(e, film, c.cur, P));
+    else TRY(put_fields<float>(e, film, c.cur, P));
+    const FilmHost &h = e->fh[film];
+    if (e->precision == CMSL_FP64) {
+        double *dst = e->d_phi[0] + h.off;
+        if (phi) CK(cudaMemcpy(dst, phi, sizeof(double) * h.N, cudaMemcpyHostToDevice));
+        else CK(cudaMemset(dst, 0, sizeof(double) * h.N));
+        CK(cudaMemcpy(e->d_phi[1] + h.off, dst, sizeof(double) * h.N, cudaMemcpyDeviceToDevice));
+    } else {
+        // double-float: hi half at the cell, lo half ncells further on
+        std::vector<float> hi((size_t)h.N, 0.f), lo((size_t)h.N, 0.f);
+        if (phi)
+            for (long long i = 0; i < h.N; ++i) {
+                const df v = df_from_double(phi[i]);
+                hi[i] = v.h;
+                lo[i] = v.l;
+            }
+        // the previous potentials start equal to the given one (no extrapolation on step 1)
+        for (int q = 0; q < 4; ++q) {
+            float *b = (float *)e->d_phi[q];
+            CK(cudaMemcpy(b + h.off, hi.data(), sizeof(float) * h.N, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(b + e->ncells + h.off, lo.data(), sizeof(float) * h.N, cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemset((float *)e->d_x + h.off, 0, sizeof(float) * h.N));
+    }
+    SolveDev S0{};
+    S0.phi_cur = 0;
+    S0.phi_prev = e->precision == CMSL_FP64 ? 0 : 1;
+    S0.phi_prev2 = e->precision == CMSL_FP64 ? 0 : 2;
+    S0.phi_prev3 = e->precision == CMSL_FP64 ? 0 : 3;
+    CK(cudaMemcpy(e->d_solve + film, &S0, sizeof(SolveDev), cudaMemcpyHostToDevice));
+    return CMSL_OK;
+}
+
+cmsl_status get_state(Engine *e, int film, double *const P[6], double *phi)
+{
+    if (film < 0 || film >= e->n_films) return fail(CMSL_ERR_ARG, "film %d outside [0,%d)", film, e->n_films);
+    CK(cudaDeviceSynchronize());
+    Ctl c;
+    SolveDev S;
+    CK(cudaMemcpy(&c, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&S, e->d_solve + film, sizeof(SolveDev), cudaMemcpyDeviceToHost));
+    if (P) {
+        if (e->precision == CMSL_FP64) TRY(get_fields<double>(e, film, c.cur, P));
+        else TRY(get_fields<float>(e, film, c.cur, P));
+    }
+    const FilmHost &h = e->fh[film];
+    if (phi) {
+        if (e->precision == CMSL_FP64) {
+            CK(cudaMemcpy(phi, e->d_phi[S.phi_cur] + h.off, sizeof(double) * h.N, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> hi((size_t)h.N), lo((size_t)h.N);
+            const float *b = (const float *)e->d_phi[S.phi_cur];
+            CK(cudaMemcpy(hi.data(), b + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(lo.data(), b + e->ncells + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
+            for (long long i = 0; i < h.N; ++i) phi[i] = (double)hi[i] + (double)lo[i];
+        }
+    }
+    return CMSL_OK;
+}
+
+// Ez and row are [n_films][n_steps] host arrays (row may be NULL).
+cmsl_status run(Engine *e, int n_steps, const double *Ez, const int32_t *row, void *stream)
+{
+    if (n_steps < 0 || (n_steps > 0 && !Ez)) return fail(CMSL_ERR_ARG, "bad run arguments");
+    if (n_steps == 0) return CMSL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t F = (size_t)e->n_films, ns = (size_t)n_steps;
+    int nrows = 0;
+    std::vector<int> rows(F * ns, -1);
+    if (row)
+        for (size_t s = 0; s < F * ns; ++s) {
+            rows[s] = row[s] < 0 ? -1 : row[s];
+            nrows = std::max(nrows, rows[s] + 1);
+        }
+    TRY(ensure_schedule(e, n_steps, nrows));
+    CK(cudaMemcpy2DAsync(e->d_wave, sizeof(double) * e->wstride, Ez, sizeof(double) * ns, sizeof(double) * ns, F,
+                         cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpy2DAsync(e->d_rows, sizeof(int) * e->wstride, rows.data(), sizeof(int) * ns, sizeof(int) * ns, F,
+                         cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(&e->d_ctl->run_step, 0, sizeof(int), st));
+    for (int fi = 0; fi < e->n_films; ++fi) CK(cudaMemsetAsync(&e->d_solve[fi].sticky, 0, sizeof(int), st));
+    e->stream = st;
+    e->last_steps = n_steps;
+    if (e->use_graph) {
+        if (!e->graph_valid) TRY(build_graph(e));
+        for (int s = 0; s < n_steps; ++s) CK(cudaGraphLaunch(e->exec, st));
+    } else {
+        for (int s = 0; s < n_steps; ++s) TRY(step_direct(e, st));
+    }
+    // the host rows vector must stay alive until the copy above has run
+    CK(cudaStreamSynchronize(st));
+    return CMSL_OK;
+}
+
+cmsl_status sync(Engine *e, int32_t *film_status)
+{
+    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaGetLastError());
+    std::vector<SolveDev> S((size_t)e->n_films);
+    CK(cudaMemcpy(S.data(), e->d_solve, sizeof(SolveDev) * S.size(), cudaMemcpyDeviceToHost));
+    if (e->cg.err) {
+        int err = 0;
+        CK(cudaMemcpy(&err, e->cg.err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return fail(CMSL_ERR_CUDA, "persistent PCG grid barrier timed out");
+    }
+    int first = -1;
+    for (int fi = 0; fi < e->n_films; ++fi) {
+        if (film_status) film_status[fi] = S[fi].sticky;
+        if (S[fi].sticky != 0 && first < 0) first = fi;
+    }
+    if (first >= 0) {
+        const int s = S[first].sticky;
+        const char *what = s == 1 ? "breakdown" : "invalid initial residual";
+        if (e->n_films > 1)
+            return fail(CMSL_ERR_PCG, "PCG failure (status %d: %s) in at least one step of film %d", s, what, first);
+        return fail(CMSL_ERR_PCG, "PCG failure (status %d: %s) in at least one step", s, what);
+    }
+    return CMSL_OK;
+}
+
+cmsl_status get_rows(Engine *e, int film, int first, int n, double *out)
+{
+    if (!out || film < 0 || film >= e->n_films || first < 0 || n < 0 || first + n > e->rstride)
+        return fail(CMSL_ERR_ARG, "bad row range");
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemcpy(out, e->d_rowbuf + ((size_t)film * e->rstride + first) * 11, sizeof(double) * 11 * n,
+                  cudaMemcpyDeviceToHost));
+    return CMSL_OK;
+}
+
+cmsl_status get_iters(Engine *e, int film, int n, int32_t *iters, int32_t *refine)
+{
+    if (film < 0 || film >= e->n_films || n < 0 || n > e->wstride) return fail(CMSL_ERR_ARG, "bad count");
+    CK(cudaDeviceSynchronize());
+    const size_t o = (size_t)film * e->wstride;
+    if (iters) CK(cudaMemcpy(iters, e->d_iters + o, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    if (refine) CK(cudaMemcpy(refine, e->d_refine + o, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    return CMSL_OK;
+}
+
+// ms[0] TDGL, ms[1] solve set-up / refinement pass, ms[2] and ms[3] the PCG
+// kernels (persistent FP32 solver: ms[2] per iteration, ms[3] the step end).
+cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
+{
+    if (!ms || reps < 1) return fail(CMSL_ERR_ARG, "bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaDeviceSynchronize());
+    const int nit = (int)e->items.size();
+    const size_t F = (size_t)e->n_films;
+    Dev d = e->dev(0);
+    d.force = 1;
+    const Fields<double> F64 = e->fields<double>();
+    const Fields<float> F32 = e->fields<float>();
+    std::vector<double> e0(F, 0.0);
+    std::vector<int> rowm1(F, -1);
+    CK(cudaMemcpy2D(e->d_wave, sizeof(double) * e->wstride, e0.data(), sizeof(double), sizeof(double), F,
+                    cudaMemcpyHostToDevice));
+    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, rowm1.data(), sizeof(int), sizeof(int), F,
+                    cudaMemcpyHostToDevice));
+    CK(cudaMemset(&e->d_ctl->run_step, 0, sizeof(int)));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    const bool fp64 = e->precision == CMSL_FP64;
+    std::vector<SolveDev> S(F);
+    for (int kind = 0; kind < 4; ++kind) {
+        CK(cudaMemcpy(S.data(), e->d_solve, sizeof(SolveDev) * F, cudaMemcpyDeviceToHost));
+        for (SolveDev &s : S) {
+            s.outer_active = 1; s.active = 1; s.iters = 1; s.refine = 1; s.status = 0;
+            s.alpha = 1e-3; s.beta = 0.5; s.rz = s.rz0 = 1.0;
+            s.inner_tol2 = 0.0; s.inner_max = CG_TIMING_ITERS;
+        }
+        CK(cudaMemcpy(e->d_solve, S.data(), sizeof(SolveDev) * F, cudaMemcpyHostToDevice));
+        // one untimed launch, then `reps` timed ones
+        for (int r = -1; r < reps; ++r) {
+            if (r == 0) CK(cudaEventRecord(a, st));
+            switch (kind) {
+            case 0:
+                if (fp64) k_tdgl<double, Exact><<<nit, NT, 0, st>>>(d, F64);
+                else k_tdgl<float, Fast><<<nit, NT, 0, st>>>(d, F32);
+                break;
+            case 1:
+                if (fp64) k_rhs<double, Exact><<<nit, NT, 0, st>>>(d, F64);
+                else k_refine<<<nit, NT, 0, st>>>(d, F32);
+                break;
+            case 2:
+                if (fp64) {
+                    k_spmv<double, Exact><<<nit, NT, 0, st>>>(d, F64);
+                } else if (e->persistent) {
+                    // one persistent solve of CG_TIMING_ITERS iterations
+                    Dev dd = d;
+                    CgBuf B = e->cg;
+                    const float *dv = (const float *)e->d_dinv;
+                    void *args[] = {&dd, &B, &dv};
+                    CK(cudaMemsetAsync(e->cg.arrive, 0, sizeof(unsigned int), st));
+                    CK(cudaLaunchCooperativeKernel(e->cg_fn, e->cg_grid, PNT, args, e->cg_smem, st));
+                    CK(cudaMemcpyAsync(e->d_solve, S.data(), sizeof(SolveDev) * F, cudaMemcpyHostToDevice, st));
+                } else {
+                    k_spmv<float, Fast><<<nit, NT, 0, st>>>(d, F32);
+                }
+                break;
+            default:
+                if (fp64) k_update<double, Exact, false><<<nit, NT, 0, st>>>(d, F64);
+                else if (e->persistent) k_step_end<<<1, 32, 0, st>>>(d);   // no fourth kernel
+                else k_update<float, Fast, true><<<nit, NT, 0, st>>>(d, F32);
+                break;
+            }
+            CK(cudaGetLastError());
+        }
+        CK(cudaEventRecord(b, st));
+        CK(cudaEventSynchronize(b));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, a, b));
+        ms[kind] = (double)t / reps;
+        if (kind == 2 && !fp64 && e->persistent) ms[kind] /= CG_TIMING_ITERS;
+        CK(cudaMemcpy(e->d_solve, S.data(), sizeof(SolveDev) * F, cudaMemcpyHostToDevice));
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return CMSL_OK;
+}
+
+size_t device_bytes(const Engine *e)
+{
+    return e->bytes + (size_t)e->n_films * ((size_t)e->wstride * (sizeof(double) + 3 * sizeof(int)) +
+                                            (size_t)e->rstride * 11 * sizeof(double));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cmsl_last_error(void) { return g_err.c_str(); }
+const char *cmsl_version(void) { return "cmsl_gb300 0.2 (sm_103a)"; }
+
+cmsl_status cmsl_film_create(const cmsl_film_desc *dsc, cmsl_film **out)
+{
+    if (!dsc || !out) return fail(CMSL_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    std::unique_ptr<cmsl_film> f(new cmsl_film());
+    TRY(engine_create(f.get(), dsc, 1));
+    *out = f.release();
     return CMSL_OK;
 }
 
@@ -618,127 +962,38 @@ cmsl_status cmsl_film_destroy(cmsl_film *f)
 
 cmsl_status cmsl_film_set_state(cmsl_film *f, const double *const P[6], const double *phi)
 {
-    if (!f || !P) return fail(CMSL_ERR_ARG, "NULL argument");
-    CK(cudaDeviceSynchronize());
-    CK(cudaMemset(f->d_ctl, 0, sizeof(Ctl)));
-    CK(cudaMemset(f->d_solve, 0, sizeof(SolveDev)));
-    if (f->precision == CMSL_FP64) TRY(put_fields<double>(f, 0, P));
-    else TRY(put_fields<float>(f, 0, P));
-    if (f->precision == CMSL_FP64) {
-        if (phi) CK(cudaMemcpy(f->d_phi[0], phi, sizeof(double) * f->N, cudaMemcpyHostToDevice));
-        else CK(cudaMemset(f->d_phi[0], 0, sizeof(double) * f->N));
-    } else {
-        // double-float: hi half then lo half
-        std::vector<float> t((size_t)2 * f->N, 0.f);
-        if (phi)
-            for (long long i = 0; i < f->N; ++i) {
-                const df v = df_from_double(phi[i]);
-                t[i] = v.h;
-                t[f->N + i] = v.l;
-            }
-        CK(cudaMemcpy(f->d_phi[0], t.data(), sizeof(float) * 2 * f->N, cudaMemcpyHostToDevice));
-    }
-    // the previous potential starts equal to the given one (no extrapolation on step 1)
-    CK(cudaMemcpy(f->d_phi[1], f->d_phi[0], sizeof(double) * f->N, cudaMemcpyDeviceToDevice));
-    for (int q = 2; q < 4; ++q)
-        if (f->d_phi[q]) CK(cudaMemcpy(f->d_phi[q], f->d_phi[0], sizeof(double) * f->N, cudaMemcpyDeviceToDevice));
-    SolveDev S0{};
-    S0.phi_cur = 0;
-    S0.phi_prev = f->precision == CMSL_FP64 ? 0 : 1;
-    S0.phi_prev2 = f->precision == CMSL_FP64 ? 0 : 2;
-    S0.phi_prev3 = f->precision == CMSL_FP64 ? 0 : 3;
-    CK(cudaMemcpy(f->d_solve, &S0, sizeof(SolveDev), cudaMemcpyHostToDevice));
-    if (f->precision != CMSL_FP64) CK(cudaMemset(f->d_x, 0, f->esz * f->N));
-    return CMSL_OK;
+    if (!f) return fail(CMSL_ERR_ARG, "NULL argument");
+    return set_state(f, 0, P, phi, true);
 }
 
 cmsl_status cmsl_film_get_state(cmsl_film *f, double *const P[6], double *phi)
 {
     if (!f) return fail(CMSL_ERR_ARG, "NULL film");
-    CK(cudaDeviceSynchronize());
-    Ctl c;
-    SolveDev S;
-    CK(cudaMemcpy(&c, f->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost));
-    if (P) {
-        if (f->precision == CMSL_FP64) TRY(get_fields<double>(f, c.cur, P));
-        else TRY(get_fields<float>(f, c.cur, P));
-    }
-    if (phi) {
-        if (f->precision == CMSL_FP64) {
-            CK(cudaMemcpy(phi, f->d_phi[S.phi_cur], sizeof(double) * f->N, cudaMemcpyDeviceToHost));
-        } else {
-            std::vector<float> t((size_t)2 * f->N);
-            CK(cudaMemcpy(t.data(), f->d_phi[S.phi_cur], sizeof(float) * 2 * f->N, cudaMemcpyDeviceToHost));
-            for (long long i = 0; i < f->N; ++i) phi[i] = (double)t[i] + (double)t[f->N + i];
-        }
-    }
-    return CMSL_OK;
+    return get_state(f, 0, P, phi);
 }
 
 cmsl_status cmsl_film_run(cmsl_film *f, int n_steps, const double *Ez, const int32_t *row, void *stream)
 {
-    if (!f || n_steps < 0 || (n_steps > 0 && !Ez)) return fail(CMSL_ERR_ARG, "bad run arguments");
-    if (n_steps == 0) return CMSL_OK;
-    cudaStream_t st = (cudaStream_t)stream;
-    int nrows = 0;
-    std::vector<int> rows((size_t)n_steps, -1);
-    if (row)
-        for (int s = 0; s < n_steps; ++s) {
-            rows[s] = row[s] < 0 ? -1 : row[s];
-            nrows = std::max(nrows, rows[s] + 1);
-        }
-    TRY(ensure_schedule(f, n_steps, nrows));
-    CK(cudaMemcpyAsync(f->d_wave, Ez, sizeof(double) * n_steps, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(f->d_rows, rows.data(), sizeof(int) * n_steps, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(&f->d_ctl->run_step, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(&f->d_solve->sticky, 0, sizeof(int), st));
-    f->stream = st;
-    f->last_steps = n_steps;
-    if (f->use_graph) {
-        if (!f->graph_valid) TRY(build_graph(f));
-        for (int s = 0; s < n_steps; ++s) CK(cudaGraphLaunch(f->exec, st));
-    } else {
-        for (int s = 0; s < n_steps; ++s) TRY(step_direct(f, st));
-    }
-    // the host rows vector must stay alive until the copy above has run
-    CK(cudaStreamSynchronize(st));
-    return CMSL_OK;
+    if (!f) return fail(CMSL_ERR_ARG, "bad run arguments");
+    return run(f, n_steps, Ez, row, stream);
 }
 
 cmsl_status cmsl_film_sync(cmsl_film *f)
 {
     if (!f) return fail(CMSL_ERR_ARG, "NULL film");
-    CK(cudaStreamSynchronize(f->stream));
-    CK(cudaGetLastError());
-    SolveDev S;
-    CK(cudaMemcpy(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost));
-    if (f->cg.err) {
-        int e = 0;
-        CK(cudaMemcpy(&e, f->cg.err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (e) return fail(CMSL_ERR_CUDA, "persistent PCG grid barrier timed out");
-    }
-    if (S.sticky != 0)
-        return fail(CMSL_ERR_PCG, "PCG failure (status %d: %s) in at least one step", S.sticky,
-                    S.sticky == 1 ? "breakdown" : "invalid initial residual");
-    return CMSL_OK;
+    return sync(f, nullptr);
 }
 
 cmsl_status cmsl_film_get_rows(cmsl_film *f, int first, int n, double *out)
 {
-    if (!f || !out || first < 0 || n < 0 || first + n > f->rstride) return fail(CMSL_ERR_ARG, "bad row range");
-    CK(cudaDeviceSynchronize());
-    CK(cudaMemcpy(out, f->d_rowbuf + (size_t)first * 11, sizeof(double) * 11 * n, cudaMemcpyDeviceToHost));
-    return CMSL_OK;
+    if (!f) return fail(CMSL_ERR_ARG, "bad row range");
+    return get_rows(f, 0, first, n, out);
 }
 
 cmsl_status cmsl_film_get_iters(cmsl_film *f, int n, int32_t *iters, int32_t *refine)
 {
-    if (!f || n < 0 || n > f->wstride) return fail(CMSL_ERR_ARG, "bad count");
-    CK(cudaDeviceSynchronize());
-    if (iters) CK(cudaMemcpy(iters, f->d_iters, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    if (refine) CK(cudaMemcpy(refine, f->d_refine, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    return CMSL_OK;
+    if (!f) return fail(CMSL_ERR_ARG, "bad count");
+    return get_iters(f, 0, n, iters, refine);
 }
 
 cmsl_status cmsl_film_tdgl_step(cmsl_film *f, double Ez)
@@ -790,20 +1045,21 @@ cmsl_status cmsl_film_apply_operator(cmsl_film *f, const double *x, double *y)
     if (!f || !x || !y) return fail(CMSL_ERR_ARG, "NULL argument");
     CK(cudaDeviceSynchronize());
     const int nit = (int)f->items.size();
+    const long long N = f->ncells;
     const Dev d = f->dev(0);
     if (f->precision == CMSL_FP64) {
-        CK(cudaMemcpy(f->d_q, x, sizeof(double) * f->N, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(f->d_q, x, sizeof(double) * N, cudaMemcpyHostToDevice));
         k_apply_op<double, Exact><<<nit, NT>>>(d, (const double *)f->d_q, (double *)f->d_r);
         CK(cudaGetLastError());
-        CK(cudaMemcpy(y, f->d_r, sizeof(double) * f->N, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(y, f->d_r, sizeof(double) * N, cudaMemcpyDeviceToHost));
     } else {
-        std::vector<float> t((size_t)f->N);
-        for (long long i = 0; i < f->N; ++i) t[i] = (float)x[i];
-        CK(cudaMemcpy(f->d_q, t.data(), sizeof(float) * f->N, cudaMemcpyHostToDevice));
+        std::vector<float> t((size_t)N);
+        for (long long i = 0; i < N; ++i) t[i] = (float)x[i];
+        CK(cudaMemcpy(f->d_q, t.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
         k_apply_op<float, Fast><<<nit, NT>>>(d, (const float *)f->d_q, (float *)f->d_r);
         CK(cudaGetLastError());
-        CK(cudaMemcpy(t.data(), f->d_r, sizeof(float) * f->N, cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < f->N; ++i) y[i] = t[i];
+        CK(cudaMemcpy(t.data(), f->d_r, sizeof(float) * N, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < N; ++i) y[i] = t[i];
     }
     return CMSL_OK;
 }
@@ -813,14 +1069,15 @@ cmsl_status cmsl_film_efield(cmsl_film *f, double *Ex, double *Ey, double *Ez)
     if (!f || !Ex || !Ey || !Ez) return fail(CMSL_ERR_ARG, "NULL argument");
     if (f->precision != CMSL_FP64) return fail(CMSL_ERR_STATE, "efield: FP64 films only");
     CK(cudaDeviceSynchronize());
+    const long long N = f->ncells;
     double *e = nullptr;
-    CK(cudaMalloc(&e, sizeof(double) * 3 * f->N));
+    CK(cudaMalloc(&e, sizeof(double) * 3 * N));
     const Dev d = f->dev(0);
-    k_efield<<<(int)f->items.size(), NT>>>(d, e, e + f->N, e + 2 * f->N);
+    k_efield<<<(int)f->items.size(), NT>>>(d, e, e + N, e + 2 * N);
     cudaError_t err = cudaGetLastError();
-    if (err == cudaSuccess) err = cudaMemcpy(Ex, e, sizeof(double) * f->N, cudaMemcpyDeviceToHost);
-    if (err == cudaSuccess) err = cudaMemcpy(Ey, e + f->N, sizeof(double) * f->N, cudaMemcpyDeviceToHost);
-    if (err == cudaSuccess) err = cudaMemcpy(Ez, e + 2 * f->N, sizeof(double) * f->N, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(Ex, e, sizeof(double) * N, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(Ey, e + N, sizeof(double) * N, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(Ez, e + 2 * N, sizeof(double) * N, cudaMemcpyDeviceToHost);
     cudaFree(e);
     if (err != cudaSuccess) return fail(CMSL_ERR_CUDA, "efield: %s", cudaGetErrorString(err));
     return CMSL_OK;
@@ -830,94 +1087,98 @@ cmsl_status cmsl_film_diag_inv(cmsl_film *f, double *dinv)
 {
     if (!f || !dinv) return fail(CMSL_ERR_ARG, "NULL argument");
     CK(cudaDeviceSynchronize());
+    const long long N = f->ncells;
     if (f->precision == CMSL_FP64) {
-        CK(cudaMemcpy(dinv, f->d_dinv, sizeof(double) * f->N, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(dinv, f->d_dinv, sizeof(double) * N, cudaMemcpyDeviceToHost));
     } else {
-        std::vector<float> t((size_t)f->N);
-        CK(cudaMemcpy(t.data(), f->d_dinv, sizeof(float) * f->N, cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < f->N; ++i) dinv[i] = t[i];
+        std::vector<float> t((size_t)N);
+        CK(cudaMemcpy(t.data(), f->d_dinv, sizeof(float) * N, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < N; ++i) dinv[i] = t[i];
     }
     return CMSL_OK;
 }
 
 cmsl_status cmsl_film_time_kernels(cmsl_film *f, int reps, void *stream, double *ms)
 {
-    if (!f || !ms || reps < 1) return fail(CMSL_ERR_ARG, "bad arguments");
-    cudaStream_t st = (cudaStream_t)stream;
-    CK(cudaDeviceSynchronize());
-    const int nit = (int)f->items.size();
-    Dev d = f->dev(0);
-    d.force = 1;
-    const Fields<double> F64 = f->fields<double>();
-    const Fields<float> F32 = f->fields<float>();
-    const int rowm1 = -1;
-    const double e0 = 0.0;
-    CK(cudaMemcpy(f->d_wave, &e0, sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(f->d_rows, &rowm1, sizeof(int), cudaMemcpyHostToDevice));
-    CK(cudaMemset(&f->d_ctl->run_step, 0, sizeof(int)));
-    cudaEvent_t a, b;
-    CK(cudaEventCreate(&a));
-    CK(cudaEventCreate(&b));
-    const bool fp64 = f->precision == CMSL_FP64;
-    SolveDev S;
-    for (int kind = 0; kind < 4; ++kind) {
-        CK(cudaMemcpy(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost));
-        S.outer_active = 1; S.active = 1; S.iters = 1; S.refine = 1; S.status = 0;
-        S.alpha = 1e-3; S.beta = 0.5; S.rz = S.rz0 = 1.0;
-        S.inner_tol2 = 0.0; S.inner_max = CG_TIMING_ITERS;
-        CK(cudaMemcpy(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice));
-        // one untimed launch, then `reps` timed ones
-        for (int r = -1; r < reps; ++r) {
-            if (r == 0) CK(cudaEventRecord(a, st));
-            switch (kind) {
-            case 0:
-                if (fp64) k_tdgl<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-                else k_tdgl<float, Fast><<<nit, NT, 0, st>>>(d, F32);
-                break;
-            case 1:
-                if (fp64) k_rhs<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-                else k_refine<<<nit, NT, 0, st>>>(d, F32);
-                break;
-            case 2:
-                if (fp64) {
-                    k_spmv<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-                } else {
-                    // one persistent solve of CG_TIMING_ITERS iterations
-                    Dev dd = d;
-                    CgBuf B = f->cg;
-                    const float *dv = (const float *)f->d_dinv;
-                    void *args[] = {&dd, &B, &dv};
-                    CK(cudaMemsetAsync(f->cg.arrive, 0, sizeof(unsigned int), st));
-                    CK(cudaLaunchCooperativeKernel(f->cg_fn, f->cg_grid, PNT, args, f->cg_smem, st));
-                    CK(cudaMemcpyAsync(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice, st));
-                }
-                break;
-            default:
-                if (fp64) k_update<double, Exact, false><<<nit, NT, 0, st>>>(d, F64);
-                else k_step_end<<<1, 32, 0, st>>>(d);   // FP32 mode has no fourth kernel
-                break;
-            }
-            CK(cudaGetLastError());
-        }
-        CK(cudaEventRecord(b, st));
-        CK(cudaEventSynchronize(b));
-        float t = 0.f;
-        CK(cudaEventElapsedTime(&t, a, b));
-        ms[kind] = (double)t / reps;
-        if (kind == 2 && !fp64) ms[kind] /= CG_TIMING_ITERS;
-        // the TDGL kernel flips nothing by itself; keep the state consistent
-        CK(cudaMemcpy(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice));
-    }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    return CMSL_OK;
+    if (!f) return fail(CMSL_ERR_ARG, "bad arguments");
+    return time_kernels(f, reps, stream, ms);
 }
 
 cmsl_status cmsl_film_device_bytes(cmsl_film *f, size_t *bytes)
 {
     if (!f || !bytes) return fail(CMSL_ERR_ARG, "NULL argument");
-    *bytes = f->bytes + (size_t)f->wstride * (sizeof(double) + 3 * sizeof(int)) +
-             (size_t)f->rstride * 11 * sizeof(double);
+    *bytes = device_bytes(f);
+    return CMSL_OK;
+}
+
+// ----------------------------------------------------------------- batches
+
+cmsl_status cmsl_batch_create(const cmsl_film_desc *descs, int n_films, cmsl_batch **out)
+{
+    if (!descs || !out) return fail(CMSL_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    if (n_films < 1 || n_films > (1 << 20)) return fail(CMSL_ERR_ARG, "n_films %d out of range", n_films);
+    std::unique_ptr<cmsl_batch> b(new cmsl_batch());
+    TRY(engine_create(b.get(), descs, n_films));
+    *out = b.release();
+    return CMSL_OK;
+}
+
+cmsl_status cmsl_batch_destroy(cmsl_batch *b)
+{
+    if (b) {
+        cudaDeviceSynchronize();
+        delete b;
+    }
+    return CMSL_OK;
+}
+
+cmsl_status cmsl_batch_set_state(cmsl_batch *b, int film, const double *const P[6], const double *phi)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return set_state(b, film, P, phi, false);
+}
+
+cmsl_status cmsl_batch_get_state(cmsl_batch *b, int film, double *const P[6], double *phi)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return get_state(b, film, P, phi);
+}
+
+cmsl_status cmsl_batch_run(cmsl_batch *b, int n_steps, const double *Ez, const int32_t *row, void *stream)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return run(b, n_steps, Ez, row, stream);
+}
+
+cmsl_status cmsl_batch_sync(cmsl_batch *b, int32_t *film_status)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return sync(b, film_status);
+}
+
+cmsl_status cmsl_batch_get_rows(cmsl_batch *b, int film, int first, int n, double *out)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return get_rows(b, film, first, n, out);
+}
+
+cmsl_status cmsl_batch_get_iters(cmsl_batch *b, int film, int n, int32_t *iters, int32_t *refine)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return get_iters(b, film, n, iters, refine);
+}
+
+cmsl_status cmsl_batch_time_kernels(cmsl_batch *b, int reps, void *stream, double *ms)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return time_kernels(b, reps, stream, ms);
+}
+
+cmsl_status cmsl_batch_device_bytes(cmsl_batch *b, size_t *bytes)
+{
+    if (!b || !bytes) return fail(CMSL_ERR_ARG, "NULL argument");
+    *bytes = device_bytes(b);
     return CMSL_OK;
 }
 

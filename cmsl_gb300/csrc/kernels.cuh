@@ -804,6 +804,7 @@ __global__ void __launch_bounds__(NT) k_spmv(Dev d, Fields<T> F)
     __shared__ int sM[SPL];
     __shared__ double sRed[NT / 32][1];
     __shared__ double sTot[1];
+    constexpr bool REFINE_T = sizeof(T) == 4;   // FP32 PCG runs only as the inner solve of a refinement
     const M m{};
     const int4 it = d.items[blockIdx.x];
     const FilmDev *f = d.films + it.x;
@@ -885,10 +886,14 @@ __global__ void __launch_bounds__(NT) k_spmv(Dev d, Fields<T> F)
         if (threadIdx.x == 0 && was) {
             const double den = sTot[0];
             S->pq = den;
-            if (!isfinite(den) || !(den > 0.0)) {   // depol_varEPS.cu:486-490
+            if (!isfinite(den) || (!REFINE_T && !(den > 0.0))) {   // depol_varEPS.cu:486-490
                 S->status = 1;
                 S->active = 0;
                 S->outer_active = 0;
+            } else if (!(den > 0.0)) {
+                // FP32 inner solve: p.Ap lost positivity to rounding; end this
+                // pass, the outer refinement recomputes the true residual
+                S->active = 0;
             } else {
                 S->alpha = S->rz / den;
             }
@@ -965,7 +970,7 @@ __global__ void __launch_bounds__(NT) k_update(Dev d, Fields<T> F)
                 S->beta = rzn / S->rz;
                 S->rz = rzn;
                 if (REFINE) {
-                    S->active = S->iters < ff->inner_max && rzn > ff->inner_tol2 * S->rz0 && rzn > 0.0;
+                    S->active = S->iters < S->inner_max && rzn > S->inner_tol2 * S->rz0 && rzn > 0.0;
                 } else if (ff->crit == 0) {
                     S->active = S->iters < ff->max_iter && rzn > ff->tol_abs2 &&
                                 (S->rz0 <= 0.0 || (rzn / S->rz0) > ff->tol_rel2);
@@ -1015,6 +1020,7 @@ __global__ void k_dinv(Dev d, T *dinv)
     const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
     const int i = g.x0 + lx, j = g.y0 + ly, nx = g.nx, ny = g.ny, nz = g.nz;
     const uint32_t *code = d.code + f->off;
+    dinv += f->off;
     for (int k = z0; k < z1; ++k) {
         const long long o = g.own_pl + (long long)k * g.plane;
         double v = 1.0;

@@ -310,6 +310,42 @@ __device__ __forceinline__ void cg_sweep_all(const Dev &d, const FilmC &F, const
     }
 }
 
+// Thread 0's scalar step of the single-reduction (Chronopoulos-Gear)
+// recurrence after an iteration produced gn = (r,u) and dn = (w,u), w = A u.
+// Returns 1 to go on (s_ab = {alpha, beta} of the next iteration), 0 to end
+// this inner pass; status = 1 only for a non-finite residual.  Rounding can
+// make the recurrence's estimate of (p, A p) non-positive on ill-conditioned
+// operators (a Neumann film pinned at one cell); the iteration then restarts
+// from p = u (beta = 0, alpha = gn / dn), which needs only (u, A u) > 0.  With
+// no positive direction left the pass ends and the outer refinement, which
+// recomputes the true residual, decides what follows.
+__device__ __forceinline__ int cg_scalars(double gn, double dn, double &gam, double &alpha, float *s_ab,
+                                          int &status)
+{
+    if (!isfinite(gn) || !isfinite(dn) || gn < 0.0) {
+        status = 1;
+        gam = gn;
+        return 0;
+    }
+    const double bn = gn / gam;
+    const double den = dn - bn * gn / alpha;
+    gam = gn;
+    if (gn == 0.0) return 0;
+    if (den > 0.0) {
+        alpha = gn / den;
+        s_ab[0] = (float)alpha;
+        s_ab[1] = (float)bn;
+        return 1;
+    }
+    if (dn > 0.0) {
+        alpha = gn / dn;
+        s_ab[0] = (float)alpha;
+        s_ab[1] = 0.f;
+        return 1;
+    }
+    return 0;
+}
+
 // The inner FP32 solve of one refinement pass on a single film: starts from
 // r_0 in B.r[0] (written by k_refine) and x = 0, runs until
 // (r,u) <= inner_tol2 (r_0,u_0) or inner_max iterations, leaves the
@@ -359,18 +395,7 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg1(Dev d, CgBuf B, const float 
         if (!grid_allreduce2(B, (it + 1) & 1, target, ga, da, sRed, gn, dn)) return;
         ++it;
         if (threadIdx.x == 0) {
-            const double bn = gn / gam;
-            const double den = dn - bn * gn / alpha;
-            int go = 1;
-            if (!isfinite(gn) || gn < 0.0 || !(den > 0.0)) {
-                status = (gn == 0.0) ? 0 : 1;
-                go = 0;
-            } else {
-                alpha = gn / den;
-                s_ab[0] = (float)alpha;
-                s_ab[1] = (float)bn;
-            }
-            gam = gn;
+            const int go = cg_scalars(gn, dn, gam, alpha, s_ab, status);
             s_go = go && gam > tol2 * g0 && it < imax;
         }
         __syncthreads();
@@ -643,18 +668,7 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg2(Dev d, CgBuf B, const float 
         if (!grid_allreduce2(B, (it + 1) & 1, target, ga, da, sRed, gn, dn)) return;
         ++it;
         if (threadIdx.x == 0) {
-            const double bn = gn / gam;
-            const double den = dn - bn * gn / alpha;
-            int go = 1;
-            if (!isfinite(gn) || gn < 0.0 || !(den > 0.0)) {
-                status = (gn == 0.0) ? 0 : 1;
-                go = 0;
-            } else {
-                alpha = gn / den;
-                s_ab[0] = (float)alpha;
-                s_ab[1] = (float)bn;
-            }
-            gam = gn;
+            const int go = cg_scalars(gn, dn, gam, alpha, s_ab, status);
             s_go = go && gam > tol2 * g0 && it < imax;
         }
         __syncthreads();

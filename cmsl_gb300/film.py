@@ -27,18 +27,13 @@ def _i(a):
     return a.ctypes.data_as(_ip)
 
 
-class Film:
-    """One film on the GPU.
-
-    mats: [3, 8] array, rows AFE, FE, DE; columns alpha, beta, gamma, g, a0,
-    kappa, L, eps_r (non-dimensional, as make_nd_wrt_reference gives them).
-    """
+class _Desc:
+    """A cmsl_film_desc with the arrays it points to kept alive."""
 
     def __init__(self, nx, ny, nz, omega, grain_mat, TR, mats, *, del_h, del_t, dep_flag=1,
                  zbc=_lib.DIRICHLET, eps_0_nd=0.0, is_interface=None, precision=_lib.FP64,
                  pcg_crit=_lib.CRIT_REF, tol_abs=1e-3, tol_rel=1e-2, max_iter=4000,
                  refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000, warm_start=3):
-        L = lib()
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
         self.N = self.nx * self.ny * self.nz
         self.precision = precision
@@ -64,8 +59,30 @@ class Film:
         d.refine_tol, d.max_refine = float(refine_tol), int(max_refine)
         d.inner_tol, d.inner_max_iter = float(inner_tol), int(inner_max_iter)
         d.warm_start = int(warm_start)
+        self.d = d
+
+
+def _oracle_kw(f):
+    return dict(nx=f.nx, ny=f.ny, nz=f.nz, omega=f.omega, grain_mat=f.grain_mat, TR=f.TR, mats=f.mats,
+                del_h=f.del_h, del_t=f.del_t, dep_flag=f.dep_flag, zbc=f.zbc, eps_0_nd=f.eps_0_nd,
+                is_interface=f.is_interface, tol_abs=f.tol_abs, tol_rel=f.tol_rel, max_iter=f.max_iter,
+                pcg_crit=f.crit)
+
+
+class Film:
+    """One film on the GPU.
+
+    mats: [3, 8] array, rows AFE, FE, DE; columns alpha, beta, gamma, g, a0,
+    kappa, L, eps_r (non-dimensional, as make_nd_wrt_reference gives them).
+    """
+
+    def __init__(self, nx, ny, nz, omega, grain_mat, TR, mats, **kw):
+        L = lib()
+        self._desc = _Desc(nx, ny, nz, omega, grain_mat, TR, mats, **kw)
+        self.nx, self.ny, self.nz, self.N = self._desc.nx, self._desc.ny, self._desc.nz, self._desc.N
+        self.precision = self._desc.precision
         h = C.c_void_p()
-        check(L.cmsl_film_create(C.byref(d), C.byref(h)))
+        check(L.cmsl_film_create(C.byref(self._desc.d), C.byref(h)))
         self._h = h
         self._n_rows = 0
         self._n_steps = 0
@@ -73,9 +90,7 @@ class Film:
     @classmethod
     def from_oracle_film(cls, f, **kw):
         """Builds the GPU film for an oracle.Film description (tests, bench)."""
-        return cls(f.nx, f.ny, f.nz, f.omega, f.grain_mat, f.TR, f.mats, del_h=f.del_h, del_t=f.del_t,
-                   dep_flag=f.dep_flag, zbc=f.zbc, eps_0_nd=f.eps_0_nd, is_interface=f.is_interface,
-                   tol_abs=f.tol_abs, tol_rel=f.tol_rel, max_iter=f.max_iter, pcg_crit=f.crit, **kw)
+        return cls(**{**_oracle_kw(f), **kw})
 
     def close(self):
         if getattr(self, "_h", None):
@@ -174,4 +189,116 @@ class Film:
     def device_bytes(self):
         b = C.c_size_t()
         check(lib().cmsl_film_device_bytes(self._h, C.byref(b)))
+        return int(b.value)
+
+
+class Batch:
+    """Many independent films on the GPU advancing together (cmsl_batch_*).
+
+    films: a list of dicts of Film's constructor arguments (nx, ny, nz, omega,
+    grain_mat, TR, mats, del_h, del_t, ...), one per film; all with the same
+    precision.  The campaign loop of the reference (HZO_Code_github/src/
+    main.cu:455-498) runs such films one after another.
+    """
+
+    def __init__(self, films):
+        L = lib()
+        self._descs = [_Desc(**f) for f in films]
+        if not self._descs:
+            raise ValueError("empty batch")
+        self.n_films = len(self._descs)
+        self.N = [d.N for d in self._descs]
+        self.precision = self._descs[0].precision
+        arr = (_lib.FilmDesc * self.n_films)(*[d.d for d in self._descs])
+        self._arr = arr
+        h = C.c_void_p()
+        check(L.cmsl_batch_create(arr, self.n_films, C.byref(h)))
+        self._h = h
+        self._n_rows = 0
+        self._n_steps = 0
+
+    @classmethod
+    def from_oracle_films(cls, films, **kw):
+        return cls([{**_oracle_kw(f), **kw} for f in films])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cmsl_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, film, P, phi=None):
+        P = [np.ascontiguousarray(p, np.float64) for p in P]
+        if any(p.size != self.N[film] for p in P):
+            raise ValueError("P of film %d needs %d cells" % (film, self.N[film]))
+        arr = (_dp * 6)(*[_d(p) for p in P])
+        ph = None if phi is None else np.ascontiguousarray(phi, np.float64)
+        check(lib().cmsl_batch_set_state(self._h, int(film), arr, _d(ph) if ph is not None else None))
+
+    def get_state(self, film):
+        n = self.N[film]
+        P = [np.zeros(n) for _ in range(6)]
+        phi = np.zeros(n)
+        arr = (_dp * 6)(*[_d(p) for p in P])
+        check(lib().cmsl_batch_get_state(self._h, int(film), arr, _d(phi)))
+        return P, phi
+
+    def run(self, Ez, rows=None, stream=None, sync=True):
+        """Ez, rows: [n_films, n_steps].  Returns the per-film PCG status when
+        sync (raises CmslError only for errors other than a film's PCG failure)."""
+        Ez = np.ascontiguousarray(Ez, np.float64)
+        if Ez.ndim != 2 or Ez.shape[0] != self.n_films:
+            raise ValueError("Ez must be [n_films, n_steps]")
+        n = int(Ez.shape[1])
+        r = None if rows is None else np.ascontiguousarray(rows, np.int32)
+        if r is not None and r.shape != Ez.shape:
+            raise ValueError("rows must have Ez's shape")
+        check(lib().cmsl_batch_run(self._h, n, _d(Ez), _i(r) if r is not None else None,
+                                   C.c_void_p(stream) if stream else None))
+        self._n_steps = n
+        self._n_rows = int(r.max()) + 1 if r is not None and n and r.max() >= 0 else 0
+        if sync:
+            return self.sync()
+
+    def sync(self):
+        st = np.zeros(self.n_films, np.int32)
+        s = lib().cmsl_batch_sync(self._h, _i(st))
+        if s not in (_lib.CMSL_OK, 4):
+            check(s)
+        return st
+
+    def rows(self, film, first=0, n=None):
+        n = self._n_rows - first if n is None else n
+        out = np.zeros((max(n, 0), 11))
+        if n > 0:
+            check(lib().cmsl_batch_get_rows(self._h, int(film), first, n, _d(out)))
+        return out
+
+    def iters(self, film, n=None):
+        n = self._n_steps if n is None else n
+        it = np.zeros(max(n, 1), np.int32)
+        rf = np.zeros(max(n, 1), np.int32)
+        if n > 0:
+            check(lib().cmsl_batch_get_iters(self._h, int(film), n, _i(it), _i(rf)))
+        return it[:n], rf[:n]
+
+    def time_kernels(self, reps=20, stream=None):
+        ms = np.zeros(4)
+        check(lib().cmsl_batch_time_kernels(self._h, int(reps), C.c_void_p(stream) if stream else None, _d(ms)))
+        return ms
+
+    def device_bytes(self):
+        b = C.c_size_t()
+        check(lib().cmsl_batch_device_bytes(self._h, C.byref(b)))
         return int(b.value)

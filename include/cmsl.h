@@ -148,6 +148,49 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, doub
 /* Bytes of device memory the film holds. */
 cmsl_status cmsl_film_device_bytes(cmsl_film *film, size_t *bytes);
 
+/* ---- Batches: many independent films advancing together.
+ * The reference runs its simulations one after another, each with its own
+ * allocation and P-E loop (the campaign loop main.cu:455-498 calling
+ * SetupAndRunSimulation -> Evolve, main.cu:261-359 / evolve.cu:73-440).  A
+ * batch holds films of any sizes, grain maps, materials and tolerances (one
+ * precision for all) and advances them in lockstep: every step is one graph
+ * whose kernels cover all films, with per-film PCG convergence masks -- a
+ * film that has converged drops out of the PCG kernels while the others
+ * iterate, and a PCG failure marks that film only.  Per-film results equal
+ * those of the same film run alone through cmsl_film_* (same kernels, same
+ * per-film reductions), except that the FP32_REFINED inner solve of a batch
+ * is the two-kernel masked PCG instead of the single-film persistent one. */
+typedef struct cmsl_batch cmsl_batch;
+
+/* descs: n_films film descriptions (as cmsl_film_create; equal precision). */
+cmsl_status cmsl_batch_create(const cmsl_film_desc *descs, int n_films, cmsl_batch **out);
+cmsl_status cmsl_batch_destroy(cmsl_batch *batch);
+
+/* State of film `film` (0-based), as cmsl_film_set_state/get_state.  Setting
+ * one film restarts its solver state and leaves the other films and the
+ * batch's step counter alone. */
+cmsl_status cmsl_batch_set_state(cmsl_batch *batch, int film, const double *const P[6], const double *phi);
+cmsl_status cmsl_batch_get_state(cmsl_batch *batch, int film, double *const P[6], double *phi);
+
+/* n_steps steps of every film.  Ez: [n_films][n_steps] applied fields (film
+ * major); row: [n_films][n_steps] output rows (-1 none) or NULL.  Returns once
+ * the loop is enqueued and the host arrays have been consumed. */
+cmsl_status cmsl_batch_run(cmsl_batch *batch, int n_steps, const double *Ez, const int32_t *row, void *stream);
+
+/* Waits for the run.  film_status (n_films entries, or NULL) receives each
+ * film's first PCG failure of the run (0 none, 1 breakdown, 2 invalid
+ * initial residual); returns CMSL_ERR_PCG if any film failed. */
+cmsl_status cmsl_batch_sync(cmsl_batch *batch, int32_t *film_status);
+
+/* Rows and solver counters of one film, as cmsl_film_get_rows/get_iters. */
+cmsl_status cmsl_batch_get_rows(cmsl_batch *batch, int film, int first, int n, double *out);
+cmsl_status cmsl_batch_get_iters(cmsl_batch *batch, int film, int n, int32_t *pcg_iters, int32_t *refine_passes);
+
+/* As cmsl_film_time_kernels over the whole batch (ms[2], ms[3] are the
+ * masked PCG's SpMV and update kernels in FP32_REFINED mode). */
+cmsl_status cmsl_batch_time_kernels(cmsl_batch *batch, int reps, void *stream, double *ms);
+cmsl_status cmsl_batch_device_bytes(cmsl_batch *batch, size_t *bytes);
+
 /* Depolarisation solve that allocates nothing.  No counterpart in the
  * reference: it is for callers that cannot call cudaMalloc (an application
  * that owns all device memory through its own pool, a plugin handed fixed

@@ -54,3 +54,30 @@ def test_create_rejects_bad_descriptors_without_gpu():
     with pytest.raises(cg.CmslError):
         cg.Film(4, 4, 4, np.full(64, 3, np.int32), np.zeros(1, np.int32), np.eye(3).ravel(),
                 np.zeros((3, 8)), del_h=0.5, del_t=1e-3)
+
+
+def test_batch_rejects_bad_descriptors_without_gpu():
+    """Batch argument checks (film index in the message, one precision for
+    all films) run before any CUDA call."""
+    import numpy as np
+    import cmsl_gb300 as cg
+    from cmsl_gb300 import _lib
+
+    def film(**kw):
+        d = dict(nx=4, ny=4, nz=4, omega=np.zeros(64, np.int32), grain_mat=np.ones(1, np.int32),
+                 TR=np.eye(3).ravel(), mats=np.ones((3, 8)), del_h=0.5, del_t=1e-3)
+        d.update(kw)
+        return d
+    with pytest.raises(cg.CmslError) as e:
+        cg.Batch([film(), film(precision=cg.FP32_REFINED)])
+    assert e.value.status == 1 and "film 1" in str(e.value)
+    with pytest.raises(cg.CmslError) as e:
+        cg.Batch([film(), film(), film(omega=np.full(64, 2, np.int32))])
+    assert e.value.status == 1 and "film 2" in str(e.value)
+    with pytest.raises(cg.CmslError) as e:
+        cg.Batch([film(), film(nz=2, omega=np.zeros(32, np.int32))])
+    assert "film 1" in str(e.value)
+    h = _lib.C.c_void_p()
+    assert _lib.lib().cmsl_batch_create(None, 1, _lib.C.byref(h)) == 1
+    with pytest.raises(ValueError):
+        cg.Batch([])

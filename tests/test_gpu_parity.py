@@ -201,3 +201,30 @@ def test_fp32_refined_uniform_eps(gpu, orc):
     for a, b in zip(Pg, Pw):
         assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
     assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
+
+
+@pytest.mark.parametrize("two_kernel", [False, True])
+def test_fp32_refined_neumann(gpu, orc, two_kernel, monkeypatch):
+    """Neumann film (one pinned cell, ill-conditioned operator) in
+    FP32_REFINED mode with the persistent single-reduction inner solver and
+    with the two-kernel one: no PCG failure, fields within 2e-5 of max |P|
+    and potential within 1e-4 of the FP64 oracle after 20 steps."""
+    if two_kernel:
+        monkeypatch.setenv("CMSL_PCG_TWO_KERNEL", "1")
+    f, P = random_film(33, 9, 5, seed=52, zbc=oracle.NEUMANN, eps_0_nd=3.0, del_t=5e-4, p_scale=0.2,
+                       layered=True)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    n = 20
+    Ez = 0.3 * np.sin(np.linspace(0.0, 3.0, n))
+    Pw, _, phiw, _, _, rc = orc.run(f, P, np.zeros(f.N), Ez)
+    assert rc == 0
+    import cmsl_gb300 as cg
+    with _film(gpu, f, precision=cg.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-4) as g:
+        g.set_state(P)
+        g.run(Ez)
+        Pg, phig = g.get_state()
+        it, rf = g.iters()
+    for a, b in zip(Pg, Pw):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+    assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
+    assert (rf >= 1).all()
