@@ -2,13 +2,17 @@
 //
 // Layout in HBM (one "batch" = one or more films, concatenated):
 //   * every per-cell array holds all films back to back; film f's cells start
-//     at FilmDev::off and are in the reference's C order i + nx*(j + ny*k);
+//     at FilmDev::off (a multiple of 32 cells: 128-byte aligned FP32 rows for
+//     the vectorised passes) and are in the reference's C order
+//     i + nx*(j + ny*k);
 //   * P fields: two ping-pong sets of six SoA arrays (Pmx..Psz) in the
 //     compute type T (double for CMSL_FP64, float for CMSL_FP32_REFINED);
 //   * code[c]: grain id (bits 0-23, film-local) | material (bits 24-25) |
 //     interface flag (bit 26) -- replaces the reference's seven per-voxel FP64
 //     parameter arrays, omega and is_interface (kernels_evol.cu:133-146);
-//   * phi: two FP64 ping-pong potentials; PCG vectors r, p[2], q, dinv, x in T;
+//   * phi: FP64 potentials (two buffers), or five double-float buffers in
+//     FP32_REFINED mode (hi half at the cell, lo half ncells further on) for
+//     the extrapolated warm start; PCG vectors r, p[2], q, dinv, x in T;
 //   * per-grain rotations TR (9 per grain, row major) in T.
 // Work is cut into items (film, x0, y0, z0..z1): one thread block per item,
 // a TX x TY thread tile marching through z0..z1.
@@ -47,6 +51,8 @@ struct FilmDev {
     long long off;              // first cell of the film
     int g_off;                  // first grain of the film in TR
     int item_begin, item_end;
+    int pb_begin, pb_end;       // persistent PCG: the film's block range of the cooperative grid
+    int brick_begin, brick_end; // persistent PCG: the film's stencil bricks
     int dep_flag;
     int warm;                   // FP32_REFINED warm start: 0 previous phi, 1 linear, 2 quadratic, 3 cubic extrapolation
     int ref_id;                 // Neumann pinned cell (film-local)
@@ -91,7 +97,8 @@ struct CgBuf {
     unsigned int *arrive;       // grid-barrier arrival counter (reset by k_refine)
     float4 *part;               // [2][grid] per-block partial sums (two double-float pairs), by parity
     int *err;                   // barrier timeout flag
-    const int4 *bricks;         // stencil work list: TX x TY x (<= PZ planes) bricks
+    const int4 *bricks;         // stencil work list: TX x TY x (<= PZ planes) bricks, film by film
+    const int *blk_film;        // film of each block of the cooperative grid
     int n_bricks;
 };
 

@@ -7,10 +7,11 @@
 // lives in per-film device slots.  One time step is one CUDA graph:
 //   CMSL_FP64:          k_tdgl -> k_rhs -> WHILE(inner){ k_spmv -> k_update } -> k_step_end
 //   CMSL_FP32_REFINED:  k_tdgl -> WHILE(outer){ k_refine -> inner solve } -> k_step_end
-// where the FP32 inner solve is the persistent cooperative PCG kernel for a
-// single film and WHILE(inner){ k_spmv -> k_update } for a batch (films that
-// have converged drop out of the masked kernels; the loop runs while any film
-// is active).  The WHILE conditions are set on the device by the last block of
+// where the FP32 inner solve is one persistent cooperative PCG launch over
+// all films (each film on its own block range with its own convergence flag),
+// or, for films with the Neumann z boundary, WHILE(inner){ k_spmv -> k_update }
+// (films that have converged drop out of the masked kernels; the loop runs
+// while any film is active).  The WHILE conditions are set on the device by the last block of
 // k_rhs, k_refine and k_update, so a step never returns to the host: the PCG
 // loop of the reference (depol_varEPS.cu:472-522, two blocking Ddot per
 // iteration) and its per-step cudaMalloc/cublasCreate churn (:373-393,
@@ -116,12 +117,11 @@ struct Engine {
     bool graph_valid = false;
     bool use_graph = true;
     cudaStream_t stream = nullptr;
-    // FP32_REFINED inner solver: the persistent cooperative kernel (one film)
-    // or the masked two-kernel PCG (batches, or CMSL_PCG_TWO_KERNEL=1)
+    // FP32_REFINED inner solver: the persistent cooperative kernel, or the
+    // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
     bool persistent = false;
     CgBuf cg{};
     int cg_grid = 0;
-    bool cg_fused = false;      // single-sweep variant (CMSL_PCG_FUSED=1) instead of two-phase
     void *cg_fn = nullptr;
     size_t cg_smem = 0;
 
@@ -540,8 +540,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         FilmHost h;
         h.nx = d.nx; h.ny = d.ny; h.nz = d.nz; h.ng = d.n_grains; h.dep = d.dep_flag != 0;
         h.N = (long long)d.nx * d.ny * d.nz;
-        h.off = e->ncells;
-        e->ncells += h.N;
+        h.off = (e->ncells + 31) / 32 * 32;   // 128-byte aligned FP32 film start
+        e->ncells = h.off + h.N;
         e->fh.push_back(h);
         e->any_dep |= h.dep != 0;
         xy_tiles += (long long)((d.nx + TX - 1) / TX) * ((d.ny + TY - 1) / TY);
@@ -549,12 +549,33 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         e->max_refine_cap = std::max(e->max_refine_cap, std::max(1, d.max_refine));
         e->inner_max_cap = std::max(e->inner_max_cap, std::max(1, d.inner_max_iter));
     }
-    // The persistent solver's single-reduction recurrence assumes a symmetric
-    // operator.  With the Neumann z boundary the mirrored rows of the first
-    // and last planes (depol_varEPS.cu:93-98) make A non-symmetric, so those
-    // films take the two-kernel PCG, the reference's own algorithm.
+    e->ncells = (e->ncells + 31) / 32 * 32;
+    // FP32_REFINED inner solver.  The persistent solver's single-reduction
+    // recurrence assumes a symmetric operator; with the Neumann z boundary
+    // the mirrored rows of the first and last planes (depol_varEPS.cu:93-98)
+    // make A non-symmetric, so a batch holding such a film takes the
+    // two-kernel PCG, the reference's own algorithm.  So does a batch with
+    // more films than one cooperative launch carries.
     const char *tk = getenv("CMSL_PCG_TWO_KERNEL");
-    e->persistent = e->precision != CMSL_FP64 && n == 1 && descs[0].zbc == CMSL_DIRICHLET && !(tk && atoi(tk) != 0);
+    bool all_dirichlet = true, all_uni = true;
+    for (int i = 0; i < n; ++i) {
+        all_dirichlet &= descs[i].zbc == CMSL_DIRICHLET;
+        all_uni &= descs[i].mats[0].eps_r == descs[i].mats[1].eps_r && descs[i].mats[1].eps_r == descs[i].mats[2].eps_r;
+    }
+    int cg_per = 0, cg_nsm = 0;
+    e->persistent = e->precision != CMSL_FP64 && all_dirichlet && n <= CG_MAX_FILMS && !(tk && atoi(tk) != 0);
+    if (e->persistent) {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&cg_nsm, cudaDevAttrMultiProcessorCount, dev));
+        if (n == 1) e->cg_fn = all_uni ? (void *)k_pcg_cg2<true, false> : (void *)k_pcg_cg2<false, false>;
+        else e->cg_fn = all_uni ? (void *)k_pcg_cg2<true, true> : (void *)k_pcg_cg2<false, true>;
+        e->cg_smem = P2SMEM_BYTES + sizeof(FilmState) * n;
+        CK(cudaFuncSetAttribute(e->cg_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->cg_smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cg_per, e->cg_fn, PNT, e->cg_smem));
+        if (cg_per < 1) return fail(CMSL_ERR_CUDA, "persistent PCG kernel cannot be resident");
+        if (n > cg_per * cg_nsm) e->persistent = false;
+    }
 
     // per-cell code (grain id local to the film), interface flags
     // (main.cu:13-42), material voxel counts, work items, film tables
@@ -605,6 +626,61 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         fd.item_end = (int)e->items.size();
     }
 
+    // persistent PCG partition: stencil bricks of PZ planes film by film;
+    // each film gets a contiguous block range in proportion to its cells
+    // (one film: as many blocks as give every block the same brick count)
+    std::vector<int4> bricks;
+    std::vector<int> blk_film;
+    if (e->persistent) {
+        for (int fi = 0; fi < n; ++fi) {
+            const FilmHost &h = e->fh[fi];
+            fds[fi].brick_begin = (int)bricks.size();
+            for (int y0 = 0; y0 < h.ny; y0 += TY)
+                for (int x0 = 0; x0 < h.nx; x0 += TX)
+                    for (int z0 = 0; z0 < h.nz; z0 += PZ)
+                        bricks.push_back(make_int4(fi, x0, y0, z0 | (std::min(h.nz, z0 + PZ) << 16)));
+            fds[fi].brick_end = (int)bricks.size();
+        }
+        const int maxg = cg_per * cg_nsm;
+        std::vector<int> nb((size_t)n, 1);
+        if (n == 1) {
+            const int nbk = (int)bricks.size(), per_block = (nbk + maxg - 1) / maxg;
+            nb[0] = (nbk + per_block - 1) / per_block;
+        } else {
+            long long tot = 0;
+            for (const FilmHost &h : e->fh) tot += h.N;
+            int sum = 0;
+            auto cap = [&](int fi) { return std::max(1, fds[fi].brick_end - fds[fi].brick_begin); };
+            for (int fi = 0; fi < n; ++fi) {
+                nb[fi] = std::min(cap(fi), std::max(1, (int)((double)maxg * e->fh[fi].N / tot)));
+                sum += nb[fi];
+            }
+            while (sum > maxg) {             // cannot happen with n <= maxg unless rounding up
+                int big = 0;
+                for (int fi = 1; fi < n; ++fi) if (nb[fi] > nb[big]) big = fi;
+                if (nb[big] <= 1) break;
+                --nb[big]; --sum;
+            }
+            while (sum < maxg) {             // hand out the rest to the most loaded films
+                int best = -1;
+                double load = 0.0;
+                for (int fi = 0; fi < n; ++fi) {
+                    if (nb[fi] >= cap(fi)) continue;
+                    const double l = (double)e->fh[fi].N / nb[fi];
+                    if (l > load) { load = l; best = fi; }
+                }
+                if (best < 0) break;
+                ++nb[best]; ++sum;
+            }
+        }
+        for (int fi = 0; fi < n; ++fi) {
+            fds[fi].pb_begin = (int)blk_film.size();
+            for (int j = 0; j < nb[fi]; ++j) blk_film.push_back(fi);
+            fds[fi].pb_end = (int)blk_film.size();
+        }
+        e->cg_grid = (int)blk_film.size();
+    }
+
     // device memory
     const size_t cells = (size_t)e->ncells;
     TRY(e->alloc((void **)&e->d_films, sizeof(FilmDev) * n));
@@ -624,51 +700,22 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     TRY(e->alloc(&e->d_p[1], e->esz * cells));
     if (e->precision != CMSL_FP64) TRY(e->alloc(&e->d_x, e->esz * cells));
     if (e->persistent) {
-        // persistent single-reduction PCG: r ping-pong (r[0] is the shared r),
-        // w and s ping-pong, x = correction, p in place
-        const FilmHost &h = e->fh[0];
+        // persistent single-reduction PCG: r (the shared r), u, w, s; x =
+        // correction, p in place
         CgBuf &B = e->cg;
         B.r[0] = (float *)e->d_r;
         TRY(e->alloc((void **)&B.r[1], 4 * cells));
         TRY(e->alloc((void **)&B.w[0], 4 * cells));
-        TRY(e->alloc((void **)&B.w[1], 4 * cells));
         TRY(e->alloc((void **)&B.s[0], 4 * cells));
-        TRY(e->alloc((void **)&B.s[1], 4 * cells));
+        B.w[1] = B.w[0];
+        B.s[1] = B.s[0];
         B.x = (float *)e->d_x;
         B.p = (float *)e->d_p[0];
-        int dev = 0, nsm = 0, per = 0;
-        CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        CK(cudaFuncSetAttribute(k_pcg_cg1<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PSMEM_BYTES));
-        CK(cudaFuncSetAttribute(k_pcg_cg1<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PSMEM_BYTES));
-        CK(cudaFuncSetAttribute(k_pcg_cg2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2SMEM_BYTES));
-        CK(cudaFuncSetAttribute(k_pcg_cg2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P2SMEM_BYTES));
-        const bool uni = fds[0].uni_eps != 0;
-        const char *solver = getenv("CMSL_PCG_FUSED");
-        e->cg_fused = solver && atoi(solver) != 0;
-        if (e->cg_fused) {
-            e->cg_fn = uni ? (void *)k_pcg_cg1<true> : (void *)k_pcg_cg1<false>;
-            e->cg_smem = PSMEM_BYTES;
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg1<false>, PNT, PSMEM_BYTES));
-        } else {
-            e->cg_fn = uni ? (void *)k_pcg_cg2<true> : (void *)k_pcg_cg2<false>;
-            e->cg_smem = P2SMEM_BYTES;
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pcg_cg2<false>, PNT, P2SMEM_BYTES));
-        }
-        if (per < 1) return fail(CMSL_ERR_CUDA, "persistent PCG kernel cannot be resident");
-        // stencil bricks of PZ planes; the grid is sized so that every block
-        // gets the same number of bricks
-        std::vector<int4> bricks;
-        for (int y0 = 0; y0 < h.ny; y0 += TY)
-            for (int x0 = 0; x0 < h.nx; x0 += TX)
-                for (int z0 = 0; z0 < h.nz; z0 += PZ)
-                    bricks.push_back(make_int4(0, x0, y0, z0 | (std::min(h.nz, z0 + PZ) << 16)));
-        const int nb = (int)bricks.size(), maxg = per * nsm;
-        const int per_block = (nb + maxg - 1) / maxg;
-        e->cg_grid = e->cg_fused ? std::min<int>((int)e->items.size(), maxg) : (nb + per_block - 1) / per_block;
-        TRY(e->alloc((void **)&B.bricks, sizeof(int4) * nb));
-        CK(cudaMemcpy((void *)B.bricks, bricks.data(), sizeof(int4) * nb, cudaMemcpyHostToDevice));
-        B.n_bricks = nb;
+        TRY(e->alloc((void **)&B.bricks, sizeof(int4) * bricks.size()));
+        CK(cudaMemcpy((void *)B.bricks, bricks.data(), sizeof(int4) * bricks.size(), cudaMemcpyHostToDevice));
+        B.n_bricks = (int)bricks.size();
+        TRY(e->alloc((void **)&B.blk_film, sizeof(int) * blk_film.size()));
+        CK(cudaMemcpy((void *)B.blk_film, blk_film.data(), sizeof(int) * blk_film.size(), cudaMemcpyHostToDevice));
         TRY(e->alloc((void **)&B.part, sizeof(float4) * 2 * e->cg_grid));
         TRY(e->alloc((void **)&B.arrive, sizeof(unsigned int) * 2));
         TRY(e->alloc((void **)&B.err, sizeof(int) * 2));
@@ -1045,7 +1092,7 @@ cmsl_status cmsl_film_apply_operator(cmsl_film *f, const double *x, double *y)
     if (!f || !x || !y) return fail(CMSL_ERR_ARG, "NULL argument");
     CK(cudaDeviceSynchronize());
     const int nit = (int)f->items.size();
-    const long long N = f->ncells;
+    const long long N = f->fh[0].N;   // the film's cells (the buffers are padded beyond)
     const Dev d = f->dev(0);
     if (f->precision == CMSL_FP64) {
         CK(cudaMemcpy(f->d_q, x, sizeof(double) * N, cudaMemcpyHostToDevice));
@@ -1069,7 +1116,7 @@ cmsl_status cmsl_film_efield(cmsl_film *f, double *Ex, double *Ey, double *Ez)
     if (!f || !Ex || !Ey || !Ez) return fail(CMSL_ERR_ARG, "NULL argument");
     if (f->precision != CMSL_FP64) return fail(CMSL_ERR_STATE, "efield: FP64 films only");
     CK(cudaDeviceSynchronize());
-    const long long N = f->ncells;
+    const long long N = f->fh[0].N;   // the film's cells (the buffers are padded beyond)
     double *e = nullptr;
     CK(cudaMalloc(&e, sizeof(double) * 3 * N));
     const Dev d = f->dev(0);
@@ -1087,7 +1134,7 @@ cmsl_status cmsl_film_diag_inv(cmsl_film *f, double *dinv)
 {
     if (!f || !dinv) return fail(CMSL_ERR_ARG, "NULL argument");
     CK(cudaDeviceSynchronize());
-    const long long N = f->ncells;
+    const long long N = f->fh[0].N;   // the film's cells (the buffers are padded beyond)
     if (f->precision == CMSL_FP64) {
         CK(cudaMemcpy(dinv, f->d_dinv, sizeof(double) * N, cudaMemcpyDeviceToHost));
     } else {

@@ -31,10 +31,12 @@ def orc():
     return oracle.load()
 
 
-def _films(fp32=False):
-    """Four uneven films; the third has no depolarisation solve."""
+def _films(fp32=False, neumann=True):
+    """Four uneven films; the third has no depolarisation solve, the second
+    has the Neumann z boundary unless neumann=False."""
     specs = [dict(shape=(16, 12, 6), seed=51, zbc=oracle.DIRICHLET, eps_0_nd=4.0),
-             dict(shape=(33, 9, 5), seed=52, zbc=oracle.NEUMANN, eps_0_nd=3.0, del_t=5e-4),
+             dict(shape=(33, 9, 5), seed=52, zbc=oracle.NEUMANN if neumann else oracle.DIRICHLET, eps_0_nd=3.0,
+                  del_t=5e-4),
              dict(shape=(40, 17, 9), seed=53, zbc=oracle.DIRICHLET, dep_flag=0),
              dict(shape=(24, 20, 7), seed=54, zbc=oracle.DIRICHLET, eps_0_nd=5.0, fracs=(0.2, 0.6, 0.2))]
     out = []
@@ -103,10 +105,16 @@ def test_batch_fp64_matches_oracle_per_film(gpu, orc, graph, monkeypatch):
 
 
 @pytest.mark.parametrize("graph", [True, False])
-def test_batch_fp32_refined_vs_fp64_oracle(gpu, orc, graph, monkeypatch):
+@pytest.mark.parametrize("variant", ["persistent", "two_kernel", "neumann_mix"])
+def test_batch_fp32_refined_vs_fp64_oracle(gpu, orc, graph, variant, monkeypatch):
+    """Dirichlet films share one persistent PCG launch per refinement pass
+    (each on its own block range with its own convergence); a batch holding a
+    Neumann film, or CMSL_PCG_TWO_KERNEL=1, takes the masked two-kernel PCG."""
     if not graph:
         monkeypatch.setenv("CMSL_NO_GRAPH", "1")
-    films = _films(fp32=True)
+    if variant == "two_kernel":
+        monkeypatch.setenv("CMSL_PCG_TWO_KERNEL", "1")
+    films = _films(fp32=True, neumann=variant == "neumann_mix")
     n = 20
     Ez, rows = _schedule(len(films), n)
     kw = dict(precision=gpu.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-4)
@@ -138,12 +146,12 @@ def test_batch_fp32_refined_vs_fp64_oracle(gpu, orc, graph, monkeypatch):
                 assert np.abs(a - w).max() <= 2e-5 * max(np.abs(w).max(), 1e-30), i
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp32_persistent"])
 def test_batch_pcg_failure_marks_one_film(gpu, orc, precision):
     """A film whose state is not finite fails its solve (status 2, invalid
     initial residual) without stopping or changing the other films."""
-    fp32 = precision == "fp32"
-    films = _films(fp32=fp32)[:3]
+    fp32 = precision != "fp64"
+    films = _films(fp32=fp32, neumann=precision != "fp32_persistent")[:3]
     bad = 1
     n = 6
     Ez, rows = _schedule(len(films), n)
