@@ -178,7 +178,15 @@ def hzo_film(name, nx, ny, nz, n_grains, seed, afe_frac, *, a1=-2.0e9, a11=1.0e1
         sched = sch.constant_schedule(Emax, fixed_steps, row_every=10)
     else:
         sched = sch.triangle_schedule(Emax, steps_per_period, n_periods)
-    return Workload(name, nx, ny, nz, omega, gm, TR, mats, dx, dt, eps_0_nd, E0_ref, P0_ref, P, sched)
+    return Workload(name, nx, ny, nz, omega, gm, TR, mats, dx, dt, eps_0_nd, E0_ref, P0_ref, P, sched,
+                    extra={"Emax": Emax})
+
+
+def with_loop(w: Workload, steps_per_period: int, n_periods: int = 1) -> Workload:
+    """The same film on a triangle loop of another length (same amplitude)."""
+    return Workload(w.name + "_loop%dx%d" % (steps_per_period, n_periods), w.nx, w.ny, w.nz, w.omega, w.grain_mat,
+                    w.TR, w.mats, w.del_h, w.del_t, w.eps_0_nd, w.E0_ref, w.P0_ref, w.P_init,
+                    sch.triangle_schedule(w.extra["Emax"], steps_per_period, n_periods), dict(w.extra))
 
 
 def config(i: int) -> Workload:

@@ -216,3 +216,19 @@ def test_voronoi_deterministic():
     assert (om == om[0]).all() and om.min() >= 0 and om.max() < 13
     ct = np.abs(np.cos(a[2][:, 1]))
     assert (ct >= 0.3 - 1e-12).all() and (ct <= 1.0).all()
+
+
+def test_loop_metrics_known_loop():
+    """Pr and Ec of an analytic loop P = tanh((E +- Ec)/w) on a triangle wave."""
+    from cmsl_gb300 import pe
+    Ec, wd, n = 0.3, 0.1, 4000
+    t = np.arange(n)
+    E = 1.0 - np.abs(2.0 * t / (n - 1) - 1.0) * 2.0          # +1 -> -1 -> +1
+    down = np.r_[True, np.diff(E) < 0]
+    P = np.where(down, np.tanh((E + Ec) / wd), np.tanh((E - Ec) / wd))
+    m = pe.loop_metrics(E, P)
+    assert abs(m["Ec"] - Ec) < 1e-3 and abs(m["Ec_plus"] - Ec) < 1e-3 and abs(m["Ec_minus"] + Ec) < 1e-3
+    want = np.tanh(Ec / wd)
+    assert abs(m["Pr"] - want) < 1e-3
+    r = pe.relative_errors(m, m)
+    assert r["Pr"] == 0.0 and r["Ec"] == 0.0
