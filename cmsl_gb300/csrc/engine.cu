@@ -28,15 +28,15 @@
 #include <string>
 #include <vector>
 
-#include "cmsl.h"
-#include "kernels.cuh"
-#include "pcg_persist.cuh"
+#include "engine.h"
 
 using namespace cmsl;
 
-namespace {
+namespace cmsl_eng {
 
+namespace {
 thread_local std::string g_err;
+}
 
 cmsl_status fail(cmsl_status s, const char *fmt, ...)
 {
@@ -49,19 +49,13 @@ cmsl_status fail(cmsl_status s, const char *fmt, ...)
     return s;
 }
 
-#define CK(call)                                                                              \
-    do {                                                                                      \
-        cudaError_t e_ = (call);                                                              \
-        if (e_ != cudaSuccess)                                                                \
-            return fail(CMSL_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                        __FILE__, __LINE__);                                                  \
-    } while (0)
+}  // namespace cmsl_eng
 
-#define TRY(x)                               \
-    do {                                     \
-        cmsl_status s_ = (x);                \
-        if (s_ != CMSL_OK) return s_;        \
-    } while (0)
+using namespace cmsl_eng;
+
+void cmsl_internal_set_error(const char *msg) { g_err = msg; }
+
+namespace {
 
 double harm(double a, double b)   // depol_varEPS.cu:10-15
 {
@@ -71,116 +65,7 @@ double harm(double a, double b)   // depol_varEPS.cu:10-15
     return (2.0 * a * b) / denom;
 }
 
-// Host view of one film of a handle.
-struct FilmHost {
-    int nx, ny, nz, ng, dep;
-    long long N, off;   // cells, first cell
-};
-
 }  // namespace
-
-void cmsl_internal_set_error(const char *msg) { g_err = msg; }
-
-struct Engine {
-    int precision = CMSL_FP64;
-    int n_films = 0;
-    long long ncells = 0;
-    bool any_dep = false;
-    size_t esz = 8;
-    int max_iter_cap = 0, max_refine_cap = 0, inner_max_cap = 0;
-    std::vector<FilmHost> fh;
-    std::vector<int4> items;
-    // device buffers
-    std::vector<void *> allocs;
-    size_t bytes = 0;
-    FilmDev *d_films = nullptr;
-    int4 *d_items = nullptr;
-    uint32_t *d_code = nullptr;
-    void *d_TR = nullptr;
-    double *d_phi[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    double *d_partial = nullptr;
-    unsigned int *d_counter = nullptr;
-    SolveDev *d_solve = nullptr;
-    Ctl *d_ctl = nullptr;
-    void *d_P[2][6] = {};
-    void *d_r = nullptr, *d_q = nullptr, *d_dinv = nullptr, *d_x = nullptr, *d_p[2] = {};
-    // schedule buffers, [n_films][stride], grown on demand
-    double *d_wave = nullptr;
-    int *d_rows = nullptr;
-    double *d_rowbuf = nullptr;
-    int *d_iters = nullptr, *d_refine = nullptr;
-    int wstride = 0, rstride = 0;
-    int last_steps = 0;
-    // graph
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    bool graph_valid = false;
-    bool use_graph = true;
-    cudaStream_t stream = nullptr;
-    // FP32_REFINED inner solver: the persistent cooperative kernel, or the
-    // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
-    bool persistent = false;
-    CgBuf cg{};
-    int cg_grid = 0;
-    void *cg_fn = nullptr;
-    size_t cg_smem = 0;
-
-    ~Engine()
-    {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        for (void *p : allocs) cudaFree(p);
-        if (d_wave) cudaFree(d_wave);
-        if (d_rows) cudaFree(d_rows);
-        if (d_rowbuf) cudaFree(d_rowbuf);
-        if (d_iters) cudaFree(d_iters);
-        if (d_refine) cudaFree(d_refine);
-    }
-
-    template <class T> Fields<T> fields() const
-    {
-        Fields<T> F{};
-        for (int s = 0; s < 2; ++s)
-            for (int q = 0; q < 6; ++q) F.P[s][q] = (T *)d_P[s][q];
-        F.r = (T *)d_r; F.q = (T *)d_q; F.dinv = (T *)d_dinv; F.x = (T *)d_x;
-        F.p[0] = (T *)d_p[0]; F.p[1] = (T *)d_p[1];
-        F.TR = (const T *)d_TR;
-        return F;
-    }
-
-    Dev dev(int use_cond, cudaGraphConditionalHandle hi = 0, cudaGraphConditionalHandle ho = 0) const
-    {
-        Dev d{};
-        d.films = d_films; d.items = d_items; d.n_films = n_films; d.n_items = (int)items.size();
-        d.code = d_code; d.ncells = ncells;
-        for (int q = 0; q < 5; ++q) d.phi[q] = d_phi[q];
-        d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
-        d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
-        d.iters_log = d_iters; d.refine_log = d_refine;
-        d.wstride = wstride; d.rstride = rstride;
-        d.use_cond = use_cond; d.h_inner = hi; d.h_outer = ho;
-        d.arrive = cg.arrive;
-        return d;
-    }
-
-    cmsl_status alloc(void **p, size_t n)
-    {
-        cudaError_t e = cudaMalloc(p, n ? n : 16);
-        if (e != cudaSuccess) {
-            *p = nullptr;
-            return fail(e == cudaErrorMemoryAllocation ? CMSL_ERR_NOMEM : CMSL_ERR_CUDA,
-                        "cudaMalloc(%zu) failed: %s", n, cudaGetErrorString(e));
-        }
-        allocs.push_back(*p);
-        bytes += n;
-        e = cudaMemset(*p, 0, n ? n : 16);
-        if (e != cudaSuccess) return fail(CMSL_ERR_CUDA, "cudaMemset failed: %s", cudaGetErrorString(e));
-        return CMSL_OK;
-    }
-};
-
-struct cmsl_film : Engine {};
-struct cmsl_batch : Engine {};
 
 namespace {
 
@@ -294,6 +179,10 @@ template <class T> cmsl_status upload_TR(Engine *e, const cmsl_film_desc *descs,
     return CMSL_OK;
 }
 
+}  // namespace
+
+namespace cmsl_eng {
+
 cmsl_status ensure_schedule(Engine *e, int n_steps, int n_rows)
 {
     const size_t F = (size_t)e->n_films;
@@ -329,7 +218,7 @@ struct KArgs {
 };
 
 cmsl_status add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *dep, int ndep,
-                       void *fn, int grid, int block, void **args, size_t smem = 0)
+                       void *fn, int grid, int block, void **args, size_t smem)
 {
     cudaKernelNodeParams kp{};
     kp.func = fn;
@@ -419,6 +308,10 @@ cmsl_status build_graph(Engine *e)
     e->graph_valid = true;
     return CMSL_OK;
 }
+
+}  // namespace cmsl_eng
+
+namespace {
 
 // Reads every film's solver slot; *active / *outer: any film still running.
 cmsl_status read_flags(Engine *e, cudaStream_t st, bool *active, bool *outer)
@@ -538,7 +431,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     for (int i = 0; i < n; ++i) {
         const cmsl_film_desc &d = descs[i];
         FilmHost h;
-        h.nx = d.nx; h.ny = d.ny; h.nz = d.nz; h.ng = d.n_grains; h.dep = d.dep_flag != 0;
+        h.nx = d.nx; h.ny = d.ny; h.nz = d.nz; h.ng = d.n_grains; h.dep = d.dep_flag != 0; h.zbc = d.zbc;
         h.N = (long long)d.nx * d.ny * d.nz;
         h.off = (e->ncells + 31) / 32 * 32;   // 128-byte aligned FP32 film start
         e->ncells = h.off + h.N;

@@ -1,0 +1,149 @@
+// engine.h -- the film/batch engine shared by the C-ABI translation units
+// (engine.cu: lifecycle, graphs, run loop; adjoint.cu: loop gradients).
+#pragma once
+#include <cstdarg>
+#include <string>
+#include <vector>
+
+#include "cmsl.h"
+#include "kernels.cuh"
+#include "pcg_persist.cuh"
+
+namespace cmsl_eng {
+
+using namespace cmsl;
+
+// Records the message returned by cmsl_last_error() and returns s.
+cmsl_status fail(cmsl_status s, const char *fmt, ...);
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return ::cmsl_eng::fail(CMSL_ERR_CUDA, "%s failed: %s (%s:%d)", #call,            \
+                                    cudaGetErrorString(e_), __FILE__, __LINE__);              \
+    } while (0)
+
+#define TRY(x)                               \
+    do {                                     \
+        cmsl_status s_ = (x);                \
+        if (s_ != CMSL_OK) return s_;        \
+    } while (0)
+
+// Host view of one film of a handle.
+struct FilmHost {
+    int nx, ny, nz, ng, dep, zbc;
+    long long N, off;   // cells, first cell
+};
+
+struct Engine {
+    int precision = CMSL_FP64;
+    int n_films = 0;
+    long long ncells = 0;
+    bool any_dep = false;
+    size_t esz = 8;
+    int max_iter_cap = 0, max_refine_cap = 0, inner_max_cap = 0;
+    std::vector<FilmHost> fh;
+    std::vector<int4> items;
+    // device buffers
+    std::vector<void *> allocs;
+    size_t bytes = 0;
+    FilmDev *d_films = nullptr;
+    int4 *d_items = nullptr;
+    uint32_t *d_code = nullptr;
+    void *d_TR = nullptr;
+    double *d_phi[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    double *d_partial = nullptr;
+    unsigned int *d_counter = nullptr;
+    SolveDev *d_solve = nullptr;
+    Ctl *d_ctl = nullptr;
+    void *d_P[2][6] = {};
+    void *d_r = nullptr, *d_q = nullptr, *d_dinv = nullptr, *d_x = nullptr, *d_p[2] = {};
+    // schedule buffers, [n_films][stride], grown on demand
+    double *d_wave = nullptr;
+    int *d_rows = nullptr;
+    double *d_rowbuf = nullptr;
+    int *d_iters = nullptr, *d_refine = nullptr;
+    int wstride = 0, rstride = 0;
+    int last_steps = 0;
+    // graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_valid = false;
+    bool use_graph = true;
+    cudaStream_t stream = nullptr;
+    // FP32_REFINED inner solver: the persistent cooperative kernel, or the
+    // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
+    bool persistent = false;
+    CgBuf cg{};
+    int cg_grid = 0;
+    void *cg_fn = nullptr;
+    size_t cg_smem = 0;
+
+    ~Engine()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (void *p : allocs) cudaFree(p);
+        if (d_wave) cudaFree(d_wave);
+        if (d_rows) cudaFree(d_rows);
+        if (d_rowbuf) cudaFree(d_rowbuf);
+        if (d_iters) cudaFree(d_iters);
+        if (d_refine) cudaFree(d_refine);
+    }
+
+    template <class T> Fields<T> fields() const
+    {
+        Fields<T> F{};
+        for (int s = 0; s < 2; ++s)
+            for (int q = 0; q < 6; ++q) F.P[s][q] = (T *)d_P[s][q];
+        F.r = (T *)d_r; F.q = (T *)d_q; F.dinv = (T *)d_dinv; F.x = (T *)d_x;
+        F.p[0] = (T *)d_p[0]; F.p[1] = (T *)d_p[1];
+        F.TR = (const T *)d_TR;
+        return F;
+    }
+
+    Dev dev(int use_cond, cudaGraphConditionalHandle hi = 0, cudaGraphConditionalHandle ho = 0) const
+    {
+        Dev d{};
+        d.films = d_films; d.items = d_items; d.n_films = n_films; d.n_items = (int)items.size();
+        d.code = d_code; d.ncells = ncells;
+        for (int q = 0; q < 5; ++q) d.phi[q] = d_phi[q];
+        d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
+        d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
+        d.iters_log = d_iters; d.refine_log = d_refine;
+        d.wstride = wstride; d.rstride = rstride;
+        d.use_cond = use_cond; d.h_inner = hi; d.h_outer = ho;
+        d.arrive = cg.arrive;
+        return d;
+    }
+
+    cmsl_status alloc(void **p, size_t n)
+    {
+        cudaError_t e = cudaMalloc(p, n ? n : 16);
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? CMSL_ERR_NOMEM : CMSL_ERR_CUDA,
+                        "cudaMalloc(%zu) failed: %s", n, cudaGetErrorString(e));
+        }
+        allocs.push_back(*p);
+        bytes += n;
+        e = cudaMemset(*p, 0, n ? n : 16);
+        if (e != cudaSuccess) return fail(CMSL_ERR_CUDA, "cudaMemset failed: %s", cudaGetErrorString(e));
+        return CMSL_OK;
+    }
+};
+
+
+// Shared pieces of the engine.
+cmsl_status ensure_schedule(Engine *e, int n_steps, int n_rows);
+cmsl_status add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *dep, int ndep, void *fn,
+                       int grid, int block, void **args, size_t smem = 0);
+cmsl_status add_while(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *dep, int ndep,
+                      cudaGraphConditionalHandle h, cudaGraph_t *body);
+cmsl_status build_graph(Engine *e);
+
+}  // namespace cmsl_eng
+
+struct cmsl_film : cmsl_eng::Engine {};
+struct cmsl_batch : cmsl_eng::Engine {};

@@ -467,6 +467,44 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
     if (threadIdx.x == 0) *d.counter = 0u;
 }
 
+// In the last block of a solve's set-up kernel (partials r.z, r.r, b.b per
+// item): every film's starting scalars and the stop test of
+// depol_varEPS.cu:447-474 (or the relative-residual test); drives the inner
+// WHILE node.
+__device__ __forceinline__ void start_solves(const Dev &d, double (*sRed)[3], double (&sTot)[3])
+{
+    int any = 0;
+    for (int fi = 0; fi < d.n_films; ++fi) {
+        const FilmDev *ff = d.films + fi;
+        film_total<3>(d, ff, sRed, sTot);
+        if (threadIdx.x == 0) {
+            SolveDev *S = d.solve + fi;
+            S->iters = 0;
+            S->active = 0;
+            S->status = 0;
+            if (ff->dep_flag) {
+                S->rz = S->rz0 = sTot[0];
+                S->rr = sTot[1];
+                S->bb = sTot[2];
+                S->refine = 1;
+                if (!isfinite(S->rz) || S->rz < 0.0) {
+                    S->status = 2;
+                } else if (ff->crit == 0) {
+                    S->active = ff->max_iter > 0 && S->rz > ff->tol_abs2 &&
+                                (S->rz0 <= 0.0 || (S->rz / S->rz0) > ff->tol_rel2);
+                } else {
+                    S->active = ff->max_iter > 0 && S->rr > ff->tol_rel2 * S->bb;
+                }
+                any |= S->active;
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        set_cond(d, d.h_inner, any);
+        *d.counter = 0u;
+    }
+}
+
 // ------------------------------------------------- FP64 solve: RHS + r0
 // divergence (depol_varEPS.cu:279-329), b = -divP with zero rows on the
 // Dirichlet planes / Neumann pin (:401-424), r = b - A x0 with the warm start
@@ -568,36 +606,7 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
         for (int q = 0; q < 3; ++q) d.partial[(long long)blockIdx.x * NPART + q] = tot[q];
     }
     if (!ticket_last(d.counter)) return;
-    int any = 0;
-    for (int fi = 0; fi < d.n_films; ++fi) {
-        const FilmDev *ff = d.films + fi;
-        film_total<3>(d, ff, sRed, sTot);
-        if (threadIdx.x == 0) {
-            SolveDev *S = d.solve + fi;
-            S->iters = 0;
-            S->active = 0;
-            S->status = 0;
-            if (ff->dep_flag) {
-                S->rz = S->rz0 = sTot[0];
-                S->rr = sTot[1];
-                S->bb = sTot[2];
-                S->refine = 1;
-                if (!isfinite(S->rz) || S->rz < 0.0) {
-                    S->status = 2;
-                } else if (ff->crit == 0) {
-                    S->active = ff->max_iter > 0 && S->rz > ff->tol_abs2 &&
-                                (S->rz0 <= 0.0 || (S->rz / S->rz0) > ff->tol_rel2);
-                } else {
-                    S->active = ff->max_iter > 0 && S->rr > ff->tol_rel2 * S->bb;
-                }
-                any |= S->active;
-            }
-        }
-    }
-    if (threadIdx.x == 0) {
-        set_cond(d, d.h_inner, any);
-        *d.counter = 0u;
-    }
+    start_solves(d, sRed, sTot);
 }
 
 // ----------------------------- FP32 refinement: double-float residual pass

@@ -179,6 +179,20 @@ class Film:
         check(lib().cmsl_film_diag_inv(self._h, _d(y)))
         return y
 
+    def loop_gradient(self, Ez, rows, target, checkpoint_every=200):
+        """Loss (1/R) sum_r (<Pm_z>_r - target_r)^2 of the loop run from the
+        current state, and its gradient [3, 5]: per material (AFE, FE, DE),
+        d loss / d (alpha, beta, gamma, g, kappa) non-dimensional (adjoint of
+        TDGL + PCG, cmsl_film_loop_gradient)."""
+        Ez = np.ascontiguousarray(Ez, np.float64)
+        r = np.ascontiguousarray(rows, np.int32)
+        t = np.ascontiguousarray(target, np.float64)
+        loss = np.zeros(1)
+        grad = np.zeros(15)
+        check(lib().cmsl_film_loop_gradient(self._h, int(Ez.size), _d(Ez), _i(r), _d(t), int(t.size),
+                                            int(checkpoint_every), _d(loss), _d(grad)))
+        return float(loss[0]), grad.reshape(3, 5)
+
     def time_kernels(self, reps=20, stream=None):
         """Average ms per launch of [tdgl, solve set-up, spmv, update]."""
         ms = np.zeros(4)

@@ -191,6 +191,27 @@ cmsl_status cmsl_batch_get_iters(cmsl_batch *batch, int film, int n, int32_t *pc
 cmsl_status cmsl_batch_time_kernels(cmsl_batch *batch, int reps, void *stream, double *ms);
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *batch, size_t *bytes);
 
+/* Gradient of a P-E loop misfit by a hand-written adjoint of the TDGL step and
+ * the depolarisation solve (no counterpart in the reference, which has no
+ * derivatives; for fitting Landau coefficients to measured loops).  From the
+ * film's current state it runs n_steps steps (Ez, row as cmsl_film_run; every
+ * row index < n_rows) and
+ *   loss = (1/n_rows) sum_r (<Pm_z>_r - target[r])^2,
+ * <Pm_z>_r the first column of sweep row r; then the adjoint backwards in
+ * time, recomputing each segment of checkpoint_every steps from a checkpoint
+ * of P and phi taken by the forward pass.  grad[5*m + p] = d loss / d of the
+ * non-dimensional parameter p in (alpha, beta, gamma, g, kappa) of material m
+ * (cmsl_material_id), through every voxel of that material (interfaces
+ * included).  FP64 films; with dep_flag, the Dirichlet z boundary.  The
+ * forward solves are taken as exact: converge them tightly (e.g.
+ * CMSL_CRIT_RELRES, tol_rel 1e-12) for a gradient that matches finite
+ * differences.  Work memory (about 8 * N * (7 * segments + 6 *
+ * checkpoint_every + 14) bytes) is allocated for the call.  Leaves the film
+ * in an unspecified state: set it again before the next run. */
+cmsl_status cmsl_film_loop_gradient(cmsl_film *film, int n_steps, const double *Ez, const int32_t *row,
+                                    const double *target, int n_rows, int checkpoint_every, double *loss,
+                                    double *grad);
+
 /* Depolarisation solve that allocates nothing.  No counterpart in the
  * reference: it is for callers that cannot call cudaMalloc (an application
  * that owns all device memory through its own pool, a plugin handed fixed
