@@ -334,14 +334,15 @@ extern "C" cmsl_status cmsl_film_loop_gradient(cmsl_film *f, int n_steps, const 
     // rows of the whole loop stay in the row buffer
     TRY(ensure_schedule(e, K, n_rows));
 
-    // ---- forward with checkpoints (P^{jK}, phi^{jK})
+    // ---- forward with checkpoints (P^{jK}, phi^{jK}); the last segment, the
+    // first one traversed backwards, keeps its P^n and is not recomputed
     for (int j = 0; j < nseg; ++j) {
         const int s0 = j * K, len = std::min(K, n_steps - s0);
         double *ck = ckpt + (size_t)j * 7 * N;
         for (int q = 0; q < 6; ++q)
             CK(cudaMemcpyAsync(ck + q * N, e->d_P[cur][q], sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(ck + 6 * N, e->d_phi[0] + off, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-        TRY(forward_segment(e, st, Ez + s0, row + s0, len, nullptr, cur));
+        TRY(forward_segment(e, st, Ez + s0, row + s0, len, j == nseg - 1 ? store : nullptr, cur));
         CK(cudaStreamSynchronize(st));
     }
     {
@@ -399,11 +400,13 @@ extern "C" cmsl_status cmsl_film_loop_gradient(cmsl_film *f, int n_steps, const 
     for (int q = 0; q < 6; ++q) { la.q[q] = lam + q * e->ncells; lb.q[q] = lam + (6 + q) * e->ncells; }
     for (int j = nseg - 1; j >= 0; --j) {
         const int s0 = j * K, len = std::min(K, n_steps - s0);
-        const double *ck = ckpt + (size_t)j * 7 * N;
-        for (int q = 0; q < 6; ++q)
-            CK(cudaMemcpyAsync(e->d_P[cur][q], ck + q * N, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-        CK(cudaMemcpyAsync(e->d_phi[0] + off, ck + 6 * N, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-        TRY(forward_segment(e, st, Ez + s0, nullptr, len, store, cur));
+        if (j < nseg - 1) {
+            const double *ck = ckpt + (size_t)j * 7 * N;
+            for (int q = 0; q < 6; ++q)
+                CK(cudaMemcpyAsync(e->d_P[cur][q], ck + q * N, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(e->d_phi[0] + off, ck + 6 * N, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            TRY(forward_segment(e, st, Ez + s0, nullptr, len, store, cur));
+        }
         for (int s = len - 1; s >= 0; --s) {
             const int n = s0 + s;
             if (dep) CK(cudaGraphLaunch(gx, st));

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "cmsl_io.h"
 
 using namespace cmsl;
 
@@ -431,7 +432,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     for (int i = 0; i < n; ++i) {
         const cmsl_film_desc &d = descs[i];
         FilmHost h;
-        h.nx = d.nx; h.ny = d.ny; h.nz = d.nz; h.ng = d.n_grains; h.dep = d.dep_flag != 0; h.zbc = d.zbc;
+        h.nx = d.nx; h.ny = d.ny; h.nz = d.nz; h.ng = d.n_grains; h.dep = d.dep_flag != 0; h.zbc = d.zbc; h.h = d.del_h;
         h.N = (long long)d.nx * d.ny * d.nz;
         h.off = (e->ncells + 31) / 32 * 32;   // 128-byte aligned FP32 film start
         e->ncells = h.off + h.N;
@@ -1034,6 +1035,43 @@ cmsl_status cmsl_film_diag_inv(cmsl_film *f, double *dinv)
         std::vector<float> t((size_t)N);
         CK(cudaMemcpy(t.data(), f->d_dinv, sizeof(float) * N, cudaMemcpyDeviceToHost));
         for (long long i = 0; i < N; ++i) dinv[i] = t[i];
+    }
+    return CMSL_OK;
+}
+
+cmsl_status cmsl_film_checkpoint_write(cmsl_film *f, const char *path, int peloop, int count, double Ez_ext,
+                                       double incEz)
+{
+    if (!f || !path) return fail(CMSL_ERR_ARG, "NULL argument");
+    const FilmHost &h = f->fh[0];
+    const size_t N = (size_t)h.N;
+    std::vector<double> P[6], E[3], phi(N);
+    double *Pp[6], *Ep[3];
+    for (int q = 0; q < 6; ++q) { P[q].resize(N); Pp[q] = P[q].data(); }
+    for (int q = 0; q < 3; ++q) { E[q].resize(N); Ep[q] = E[q].data(); }
+    TRY(get_state(f, 0, Pp, phi.data()));
+    TRY(cmsl_efield_host(h.nx, h.ny, h.nz, h.h, h.zbc, phi.data(), Ep[0], Ep[1], Ep[2]));
+    return cmsl_checkpoint_write(path, h.nx, h.ny, h.nz, peloop, count, Ez_ext, incEz, Pp, Ep);
+}
+
+cmsl_status cmsl_film_checkpoint_read(cmsl_film *f, const char *path, int *peloop, int *count, double *Ez_ext,
+                                      double *incEz)
+{
+    if (!f || !path) return fail(CMSL_ERR_ARG, "NULL argument");
+    const FilmHost &h = f->fh[0];
+    const size_t N = (size_t)h.N;
+    std::vector<double> P[6];
+    double *Pp[6];
+    for (int q = 0; q < 6; ++q) { P[q].resize(N); Pp[q] = P[q].data(); }
+    TRY(cmsl_checkpoint_read(path, h.nx, h.ny, h.nz, peloop, count, Ez_ext, incEz, Pp, nullptr));
+    const double *Pc[6] = {Pp[0], Pp[1], Pp[2], Pp[3], Pp[4], Pp[5]};
+    TRY(set_state(f, 0, Pc, nullptr, true));
+    if (h.dep) {
+        // the file holds E of the potential solved from these P (the last
+        // step's solve): solve for it again
+        int32_t it[2] = {0, 0}, st = 0;
+        TRY(cmsl_film_depol(f, it, &st));
+        if (st != 0 && st != 3) return fail(CMSL_ERR_PCG, "checkpoint restart: PCG failure (status %d)", st);
     }
     return CMSL_OK;
 }

@@ -34,6 +34,7 @@ cmsl_status fail(cmsl_status s, const char *fmt, ...);
 struct FilmHost {
     int nx, ny, nz, ng, dep, zbc;
     long long N, off;   // cells, first cell
+    double h;           // grid spacing (non-dimensional)
 };
 
 struct Engine {

@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -21,6 +23,15 @@ cmsl_status io_fail(cmsl_status s, const std::string &m)
     cmsl_internal_set_error(m.c_str());
     return s;
 }
+
+// FILE* closed on scope exit
+struct FileCloser {
+    void operator()(FILE *f) const
+    {
+        if (f) std::fclose(f);
+    }
+};
+using File = std::unique_ptr<FILE, FileCloser>;
 
 bool starts(const char *line, const char *key) { return std::strncmp(line, key, std::strlen(key)) == 0; }
 
@@ -304,6 +315,114 @@ cmsl_status cmsl_landau_pool_read(const char *path, cmsl_landau_set *out, int ma
 }
 
 // main.cu:81-98
+// generate.cu:90-163 (write_checkpoint) layout: int nx, ny, nz, peloop, count;
+// double Ez_ext, incEz; then Pmx, Pmy, Pmz, Psx, Psy, Psz, Ex, Ey, Ez, N
+// doubles each, host byte order.
+cmsl_status cmsl_checkpoint_write(const char *path, int nx, int ny, int nz, int peloop, int count, double Ez_ext,
+                                  double incEz, const double *const P[6], const double *const E[3])
+{
+    if (!path || !P || !E || nx < 1 || ny < 1 || nz < 1) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    for (int q = 0; q < 6; ++q)
+        if (!P[q]) return io_fail(CMSL_ERR_ARG, "P[" + std::to_string(q) + "] is NULL");
+    for (int q = 0; q < 3; ++q)
+        if (!E[q]) return io_fail(CMSL_ERR_ARG, "E[" + std::to_string(q) + "] is NULL");
+    const size_t N = (size_t)nx * ny * nz;
+    File f(std::fopen(path, "wb"));
+    if (!f) return io_fail(CMSL_ERR_IO, std::string("cannot write ") + path);
+    const int hdr[5] = {nx, ny, nz, peloop, count};
+    const double hd[2] = {Ez_ext, incEz};
+    bool ok = std::fwrite(hdr, sizeof(int), 5, f.get()) == 5 && std::fwrite(hd, sizeof(double), 2, f.get()) == 2;
+    for (int q = 0; ok && q < 6; ++q) ok = std::fwrite(P[q], sizeof(double), N, f.get()) == N;
+    for (int q = 0; ok && q < 3; ++q) ok = std::fwrite(E[q], sizeof(double), N, f.get()) == N;
+    if (!ok) return io_fail(CMSL_ERR_IO, std::string("short write ") + path);
+    return CMSL_OK;
+}
+
+// generate.cu:165-264 (read_checkpoint): the grid in the file must match.
+cmsl_status cmsl_checkpoint_read(const char *path, int nx, int ny, int nz, int *peloop, int *count, double *Ez_ext,
+                                 double *incEz, double *const P[6], double *const E[3])
+{
+    if (!path || nx < 1 || ny < 1 || nz < 1) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    const size_t N = (size_t)nx * ny * nz;
+    File f(std::fopen(path, "rb"));
+    if (!f) return io_fail(CMSL_ERR_IO, std::string("cannot open checkpoint ") + path);
+    int hdr[5];
+    double hd[2];
+    if (std::fread(hdr, sizeof(int), 5, f.get()) != 5 || std::fread(hd, sizeof(double), 2, f.get()) != 2)
+        return io_fail(CMSL_ERR_IO, std::string("checkpoint header read failed: ") + path);
+    if (hdr[0] != nx || hdr[1] != ny || hdr[2] != nz)
+        return io_fail(CMSL_ERR_IO, "checkpoint grid mismatch: file (" + std::to_string(hdr[0]) + "," +
+                                        std::to_string(hdr[1]) + "," + std::to_string(hdr[2]) + "), expected (" +
+                                        std::to_string(nx) + "," + std::to_string(ny) + "," + std::to_string(nz) + ")");
+    std::vector<double> skip;
+    for (int q = 0; q < 9; ++q) {
+        double *dst = q < 6 ? (P ? P[q] : nullptr) : (E ? E[q - 6] : nullptr);
+        if (!dst) {
+            skip.resize(N);
+            dst = skip.data();
+        }
+        if (std::fread(dst, sizeof(double), N, f.get()) != N)
+            return io_fail(CMSL_ERR_IO, std::string("checkpoint data read failed: ") + path);
+    }
+    if (peloop) *peloop = hdr[3];
+    if (count) *count = hdr[4];
+    if (Ez_ext) *Ez_ext = hd[0];
+    if (incEz) *incEz = hd[1];
+    return CMSL_OK;
+}
+
+// generate.cu:11-30 (write_vector_field_binary): (x, y, z) * scale per cell.
+cmsl_status cmsl_vector_field_write(const char *path, const double *Px, const double *Py, const double *Pz,
+                                    long long n, double scale)
+{
+    if (!path || !Px || !Py || !Pz || n < 0) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    File f(std::fopen(path, "wb"));
+    if (!f) return io_fail(CMSL_ERR_IO, std::string("cannot write ") + path);
+    std::vector<double> buf;
+    buf.reserve(3 * 4096);
+    for (long long i = 0; i < n;) {
+        buf.clear();
+        const long long e = std::min(n, i + 4096);
+        for (; i < e; ++i) {
+            buf.push_back(Px[i] * scale);
+            buf.push_back(Py[i] * scale);
+            buf.push_back(Pz[i] * scale);
+        }
+        if (std::fwrite(buf.data(), sizeof(double), buf.size(), f.get()) != buf.size())
+            return io_fail(CMSL_ERR_IO, std::string("short write ") + path);
+    }
+    return CMSL_OK;
+}
+
+// Calc_EfieldMag (depol_varEPS.cu:223-276) on the host: E = -grad(phi), x/y
+// periodic; Dirichlet z with phi = 0 beyond the planes, or the mirrored
+// Neumann neighbours.
+cmsl_status cmsl_efield_host(int nx, int ny, int nz, double del_h, int zbc, const double *phi, double *Ex,
+                             double *Ey, double *Ez)
+{
+    if (nx < 1 || ny < 1 || nz < 3 || !phi || !Ex || !Ey || !Ez) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    auto id = [&](int i, int j, int k) { return (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k); };
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t c = id(i, j, k);
+                Ex[c] = -(phi[id((i + 1) % nx, j, k)] - phi[id((i - 1 + nx) % nx, j, k)]) / (2.0 * del_h);
+                Ey[c] = -(phi[id(i, (j + 1) % ny, k)] - phi[id(i, (j - 1 + ny) % ny, k)]) / (2.0 * del_h);
+                double pu, pd;
+                if (zbc == CMSL_DIRICHLET) {
+                    pu = k == nz - 1 ? 0.0 : phi[id(i, j, k + 1)];
+                    pd = k == 0 ? 0.0 : phi[id(i, j, k - 1)];
+                } else {
+                    const int up = k == 0 ? 1 : (k == nz - 1 ? nz - 2 : k + 1);
+                    const int dn = k == 0 ? 1 : (k == nz - 1 ? nz - 2 : k - 1);
+                    pu = phi[id(i, j, up)];
+                    pd = phi[id(i, j, dn)];
+                }
+                Ez[c] = -(pu - pd) / (2.0 * del_h);
+            }
+    return CMSL_OK;
+}
+
 cmsl_status cmsl_phase_pool_read(const char *path, double *afe, double *fe, double *de, int max_entries, int *n)
 {
     if (!path || !n || max_entries < 0) return io_fail(CMSL_ERR_ARG, "bad arguments");

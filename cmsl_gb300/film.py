@@ -179,6 +179,19 @@ class Film:
         check(lib().cmsl_film_diag_inv(self._h, _d(y)))
         return y
 
+    def write_checkpoint(self, path, peloop=0, count=0, Ez_ext=0.0, incEz=0.0):
+        """The reference's checkpoint file of the current state (P, E)."""
+        check(lib().cmsl_film_checkpoint_write(self._h, str(path).encode(), int(peloop), int(count), float(Ez_ext),
+                                               float(incEz)))
+
+    def read_checkpoint(self, path):
+        """Restart from a reference checkpoint file; returns its loop counters."""
+        pe, cnt = C.c_int(), C.c_int()
+        ez, inc = np.zeros(1), np.zeros(1)
+        check(lib().cmsl_film_checkpoint_read(self._h, str(path).encode(), C.byref(pe), C.byref(cnt), _d(ez),
+                                              _d(inc)))
+        return {"peloop": pe.value, "count": cnt.value, "Ez_ext": float(ez[0]), "incEz": float(inc[0])}
+
     def loop_gradient(self, Ez, rows, target, checkpoint_every=200):
         """Loss (1/R) sum_r (<Pm_z>_r - target_r)^2 of the loop run from the
         current state, and its gradient [3, 5]: per material (AFE, FE, DE),

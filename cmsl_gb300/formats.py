@@ -73,6 +73,12 @@ def _bind():
     L.cmsl_evolve_schedule.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
                                        _dp, _ip, C.POINTER(C.c_int), _dp, _ip, C.POINTER(C.c_int)]
     L.cmsl_voronoi_columnar.argtypes = [C.c_int] * 4 + [C.c_uint64, _ip, _dp, _dp]
+    L.cmsl_checkpoint_write.argtypes = [C.c_char_p] + [C.c_int] * 5 + [C.c_double, C.c_double, C.POINTER(_dp),
+                                                                       C.POINTER(_dp)]
+    L.cmsl_checkpoint_read.argtypes = [C.c_char_p] + [C.c_int] * 3 + [C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                                      _dp, _dp, C.POINTER(_dp), C.POINTER(_dp)]
+    L.cmsl_vector_field_write.argtypes = [C.c_char_p, _dp, _dp, _dp, C.c_longlong, C.c_double]
+    L.cmsl_efield_host.argtypes = [C.c_int] * 3 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp]
     _bound = True
     return L
 
@@ -216,3 +222,45 @@ def voronoi_columnar(nx, ny, nz, n_grains, seed):
     cent, eul = np.zeros(3 * n_grains), np.zeros(3 * n_grains)
     check(L.cmsl_voronoi_columnar(nx, ny, nz, n_grains, int(seed), _i(om), _d(cent), _d(eul)))
     return om, cent.reshape(n_grains, 3), eul.reshape(n_grains, 3)
+
+
+def _parr(arrs):
+    return (_dp * len(arrs))(*[_d(a) for a in arrs])
+
+
+def write_checkpoint(path: str, nx, ny, nz, P, E, peloop=0, count=0, Ez_ext=0.0, incEz=0.0) -> None:
+    """The reference's checkpoint file (generate.cu:90-163)."""
+    L = _bind()
+    P = [np.ascontiguousarray(x, np.float64) for x in P]
+    E = [np.ascontiguousarray(x, np.float64) for x in E]
+    check(L.cmsl_checkpoint_write(path.encode(), nx, ny, nz, int(peloop), int(count), float(Ez_ext), float(incEz),
+                                  _parr(P), _parr(E)))
+
+
+def read_checkpoint(path: str, nx, ny, nz):
+    """-> (P[6], E[3], peloop, count, Ez_ext, incEz) (generate.cu:165-264)."""
+    L = _bind()
+    N = nx * ny * nz
+    P = [np.zeros(N) for _ in range(6)]
+    E = [np.zeros(N) for _ in range(3)]
+    pe, cnt = C.c_int(), C.c_int()
+    ez, inc = np.zeros(1), np.zeros(1)
+    check(L.cmsl_checkpoint_read(path.encode(), nx, ny, nz, C.byref(pe), C.byref(cnt), _d(ez), _d(inc), _parr(P),
+                                 _parr(E)))
+    return P, E, pe.value, cnt.value, float(ez[0]), float(inc[0])
+
+
+def write_vector_field(path: str, Px, Py, Pz, scale=1.0) -> None:
+    """write_vector_field_binary (generate.cu:11-30)."""
+    L = _bind()
+    a = [np.ascontiguousarray(x, np.float64) for x in (Px, Py, Pz)]
+    check(L.cmsl_vector_field_write(path.encode(), _d(a[0]), _d(a[1]), _d(a[2]), a[0].size, float(scale)))
+
+
+def efield(nx, ny, nz, del_h, zbc, phi):
+    """E = -grad(phi) on the host (Calc_EfieldMag)."""
+    L = _bind()
+    phi = np.ascontiguousarray(phi, np.float64)
+    E = [np.zeros(phi.size) for _ in range(3)]
+    check(L.cmsl_efield_host(nx, ny, nz, float(del_h), int(zbc), _d(phi), _d(E[0]), _d(E[1]), _d(E[2])))
+    return E

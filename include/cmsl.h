@@ -191,6 +191,17 @@ cmsl_status cmsl_batch_get_iters(cmsl_batch *batch, int film, int n, int32_t *pc
 cmsl_status cmsl_batch_time_kernels(cmsl_batch *batch, int reps, void *stream, double *ms);
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *batch, size_t *bytes);
 
+/* Restart files in the reference's checkpoint layout (generate.cu:90-264;
+ * cmsl_io.h cmsl_checkpoint_write/read).  write: P and E = -grad(phi) of the
+ * film's current state with the loop counters given.  read: sets P from the
+ * file (its grid must match the film's), resets the step counter, and, with
+ * dep_flag, solves for the potential of that P (the file's E is the field of
+ * that same solve); returns the loop counters. */
+cmsl_status cmsl_film_checkpoint_write(cmsl_film *film, const char *path, int peloop, int count, double Ez_ext,
+                                       double incEz);
+cmsl_status cmsl_film_checkpoint_read(cmsl_film *film, const char *path, int *peloop, int *count, double *Ez_ext,
+                                      double *incEz);
+
 /* Gradient of a P-E loop misfit by a hand-written adjoint of the TDGL step and
  * the depolarisation solve (no counterpart in the reference, which has no
  * derivatives; for fitting Landau coefficients to measured loops).  From the
@@ -199,7 +210,9 @@ cmsl_status cmsl_batch_device_bytes(cmsl_batch *batch, size_t *bytes);
  *   loss = (1/n_rows) sum_r (<Pm_z>_r - target[r])^2,
  * <Pm_z>_r the first column of sweep row r; then the adjoint backwards in
  * time, recomputing each segment of checkpoint_every steps from a checkpoint
- * of P and phi taken by the forward pass.  grad[5*m + p] = d loss / d of the
+ * of P and phi taken by the forward pass (the last segment keeps the states
+ * of the forward pass; checkpoint_every >= n_steps recomputes nothing).
+ * grad[5*m + p] = d loss / d of the
  * non-dimensional parameter p in (alpha, beta, gamma, g, kappa) of material m
  * (cmsl_material_id), through every voxel of that material (interfaces
  * included).  FP64 films; with dep_flag, the Dirichlet z boundary.  The

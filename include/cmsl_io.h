@@ -118,6 +118,25 @@ cmsl_status cmsl_evolve_schedule(double maxEz, double delEz, int num_steps, int 
 cmsl_status cmsl_voronoi_columnar(int nx, int ny, int nz, int n_grains, uint64_t seed, int32_t *omega,
                                   double *cent, double *euler);
 
+/* Checkpoint file of the reference (generate.cu:90-264, write_checkpoint /
+ * read_checkpoint): header int nx, ny, nz, peloop, count; double Ez_ext,
+ * incEz; then Pmx, Pmy, Pmz, Psx, Psy, Psz, Ex, Ey, Ez (N doubles each), host
+ * byte order.  read: the file's grid must equal (nx, ny, nz) (CMSL_ERR_IO
+ * otherwise); P or E may be NULL to skip them. */
+cmsl_status cmsl_checkpoint_write(const char *path, int nx, int ny, int nz, int peloop, int count, double Ez_ext,
+                                  double incEz, const double *const P[6], const double *const E[3]);
+cmsl_status cmsl_checkpoint_read(const char *path, int nx, int ny, int nz, int *peloop, int *count, double *Ez_ext,
+                                 double *incEz, double *const P[6], double *const E[3]);
+
+/* write_vector_field_binary (generate.cu:11-30): the interleaved
+ * (x, y, z) * scale of n cells as doubles. */
+cmsl_status cmsl_vector_field_write(const char *path, const double *Px, const double *Py, const double *Pz,
+                                    long long n, double scale);
+
+/* Calc_EfieldMag (depol_varEPS.cu:223-276) on the host: E = -grad(phi). */
+cmsl_status cmsl_efield_host(int nx, int ny, int nz, double del_h, int zbc, const double *phi, double *Ex,
+                             double *Ey, double *Ez);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,7 +5,8 @@
 # only; the output stays in oracle/_ref/ (git-ignored).
 #
 # The reference is compiled from the sources where they lie.  Three files are
-# used whole (kernels_evol.cu, global.cu, get_InputParams.cu, grain_io.cu);
+# used whole (kernels_evol.cu, global.cu, get_InputParams.cu, grain_io.cu,
+# generate.cu);
 # the kernel section of depol_varEPS.cu (lines 5-329), the kernel and the
 # non-dimensionalisation functions of main.cu (lines 13-42, 200-256) and the
 # host part of Init_Conf (init_conf.cu:108-279) are cut out with sed into
@@ -48,6 +49,7 @@ $CXX $FLAGS -shared -o "$OUT/libcmsl_ref.so" \
     -x c++ "$SRC/global.cu" \
     -x c++ "$SRC/get_InputParams.cu" \
     -x c++ "$SRC/grain_io.cu" \
+    -x c++ "$SRC/generate.cu" \
     "$OUT/depol_kernels.cpp" "$OUT/main_parts.cpp" "$OUT/init_conf_host.cpp" \
     "$HERE/ref_harness.cpp" -lm
 echo "built $OUT/libcmsl_ref.so"

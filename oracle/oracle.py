@@ -311,6 +311,11 @@ class RefLib:
         L.ref_depol_field.argtypes = [C.c_int] * 4 + [_dp] * 4 + [C.c_double, C.c_double, _dp, _dp,
                                                                   _dp, _dp, C.c_double, C.c_double,
                                                                   C.c_int, _ip]
+        L.ref_write_checkpoint.argtypes = [C.c_char_p, C.POINTER(_dp), C.POINTER(_dp)] + [C.c_int] * 3 + [
+            C.c_double, C.c_int, C.c_int, C.c_double]
+        L.ref_read_checkpoint.argtypes = [C.c_char_p, C.POINTER(_dp), C.POINTER(_dp)] + [C.c_int] * 3 + [
+            _ip, _ip, _dp, _dp]
+        L.ref_write_vector_field.argtypes = [C.c_char_p, _dp, _dp, _dp] + [C.c_int] * 3 + [C.c_double]
 
     @staticmethod
     def per_voxel(film: Film):
@@ -427,6 +432,29 @@ class RefLib:
         self.lib.ref_assign_materials(nx, ny, nz, cz.size, _i(om), _d(cz), lc.size, _i(lc), _d(a), _d(f),
                                       _d(d), _i(out))
         return out
+
+    def write_checkpoint(self, path: str, P, E, nx, ny, nz, Ez_ext, peloop, count, incEz):
+        """generate.cu write_checkpoint on host arrays."""
+        P = [np.ascontiguousarray(x, np.float64) for x in P]
+        E = [np.ascontiguousarray(x, np.float64) for x in E]
+        self.lib.ref_write_checkpoint(path.encode(), _arr_d(P), _arr_d(E), nx, ny, nz, float(Ez_ext), int(peloop),
+                                      int(count), float(incEz))
+
+    def read_checkpoint(self, path: str, nx, ny, nz):
+        """generate.cu read_checkpoint -> (P[6], E[3], peloop, count, Ez_ext, incEz)."""
+        N = nx * ny * nz
+        P = [np.zeros(N) for _ in range(6)]
+        E = [np.zeros(N) for _ in range(3)]
+        pe, cnt = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        ez, inc = np.zeros(1), np.zeros(1)
+        self.lib.ref_read_checkpoint(path.encode(), _arr_d(P), _arr_d(E), nx, ny, nz, _i(pe), _i(cnt), _d(ez),
+                                     _d(inc))
+        return P, E, int(pe[0]), int(cnt[0]), float(ez[0]), float(inc[0])
+
+    def write_vector_field(self, path: str, Px, Py, Pz, nx, ny, nz, p0):
+        """generate.cu write_vector_field_binary."""
+        a = [np.ascontiguousarray(x, np.float64) for x in (Px, Py, Pz)]
+        self.lib.ref_write_vector_field(path.encode(), _d(a[0]), _d(a[1]), _d(a[2]), nx, ny, nz, float(p0))
 
     def depol_field(self, film: Film, Pm, phi, tol_abs=1e-3, tol_rel=1e-2, max_iter=4000):
         eps = self.per_voxel(film)[7]

@@ -15,6 +15,7 @@
 #include <omp.h>
 #include "header.h"
 #include "kernels_evol.h"
+#include "io_utils.h"
 
 thread_local uint3 threadIdx;
 thread_local uint3 blockIdx;
@@ -282,6 +283,28 @@ void ref_depol_field(int nx_, int ny_, int nz_, int zbc, const double *eps, doub
     launch(g, kBlock, [&]() { Calc_EfieldMag(Ex, Ey, Ez, x, h, nx_, ny_, nz_, g_bot, g_top, 0, b); });
     *iters_out = k;
     std::free(b); std::free(x); std::free(r); std::free(z); std::free(p); std::free(Ap); std::free(dinv);
+}
+
+// generate.cu: the reference's checkpoint and field writers/readers (host
+// copies through the shim's cudaMemcpy).
+void ref_write_checkpoint(const char *fname, double *const P[6], double *const E[3], int nx_, int ny_, int nz_,
+                          double Ez_ext_, int peloop_, int count_, double incEz_)
+{
+    write_checkpoint(fname, P[0], P[1], P[2], P[3], P[4], P[5], E[0], E[1], E[2], nx_, ny_, nz_, Ez_ext_, peloop_,
+                     count_, incEz_);
+}
+
+void ref_read_checkpoint(const char *fname, double *const P[6], double *const E[3], int nx_, int ny_, int nz_,
+                         int *peloop_, int *count_, double *Ez_ext_, double *incEz_)
+{
+    read_checkpoint(fname, P[0], P[1], P[2], P[3], P[4], P[5], E[0], E[1], E[2], nx_, ny_, nz_, peloop_, count_,
+                    Ez_ext_, incEz_);
+}
+
+void ref_write_vector_field(const char *fname, double *Px, double *Py, double *Pz, int nx_, int ny_, int nz_,
+                            double p0)
+{
+    write_vector_field_binary(fname, Px, Py, Pz, nx_, ny_, nz_, p0);
 }
 
 }  // extern "C"

@@ -232,3 +232,60 @@ def test_loop_metrics_known_loop():
     assert abs(m["Pr"] - want) < 1e-3
     r = pe.relative_errors(m, m)
     assert r["Pr"] == 0.0 and r["Ec"] == 0.0
+
+
+def _fields(n, seed):
+    rng = np.random.default_rng(seed)
+    return [rng.normal(size=n) for _ in range(6)], [rng.normal(size=n) for _ in range(3)]
+
+
+def test_checkpoint_bytes_equal_reference_writer(ref, tmp_path):
+    nx, ny, nz = 7, 5, 4
+    P, E = _fields(nx * ny * nz, 1)
+    mine, theirs = tmp_path / "mine.bin", tmp_path / "theirs.bin"
+    fm.write_checkpoint(str(mine), nx, ny, nz, P, E, peloop=2, count=1234, Ez_ext=0.125, incEz=-3.5e-4)
+    ref.write_checkpoint(str(theirs), P, E, nx, ny, nz, 0.125, 2, 1234, -3.5e-4)
+    assert mine.read_bytes() == theirs.read_bytes()
+
+
+def test_checkpoint_read_of_reference_file(ref, tmp_path):
+    nx, ny, nz = 6, 4, 5
+    P, E = _fields(nx * ny * nz, 2)
+    p = tmp_path / "ck.bin"
+    ref.write_checkpoint(str(p), P, E, nx, ny, nz, -0.25, 1, 77, 1e-3)
+    P2, E2, pe, cnt, ez, inc = fm.read_checkpoint(str(p), nx, ny, nz)
+    assert (pe, cnt, ez, inc) == (1, 77, -0.25, 1e-3)
+    assert all(np.array_equal(a, b) for a, b in zip(P2 + E2, P + E))
+    P3, E3, pe3, cnt3, ez3, inc3 = ref.read_checkpoint(str(p), nx, ny, nz)
+    assert all(np.array_equal(a, b) for a, b in zip(P3 + E3, P + E)) and (pe3, cnt3) == (1, 77)
+
+
+def test_checkpoint_errors(tmp_path):
+    import cmsl_gb300 as cg
+    P, E = _fields(24, 3)
+    p = tmp_path / "ck.bin"
+    fm.write_checkpoint(str(p), 2, 3, 4, P, E)
+    with pytest.raises(cg.CmslError) as e:
+        fm.read_checkpoint(str(p), 3, 2, 4)
+    assert e.value.status == 3 and "mismatch" in str(e.value)
+    p.write_bytes(p.read_bytes()[:100])
+    with pytest.raises(cg.CmslError):
+        fm.read_checkpoint(str(p), 2, 3, 4)
+
+
+def test_vector_field_bytes_equal_reference(ref, tmp_path):
+    nx, ny, nz = 5, 4, 3
+    P, _ = _fields(nx * ny * nz, 4)
+    mine, theirs = tmp_path / "m.bin", tmp_path / "t.bin"
+    fm.write_vector_field(str(mine), P[0], P[1], P[2], 0.37)
+    ref.write_vector_field(str(theirs), P[0], P[1], P[2], nx, ny, nz, 0.37)
+    assert mine.read_bytes() == theirs.read_bytes()
+
+
+@pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
+def test_host_efield_matches_reference_kernel(ref, zbc):
+    f, _ = random_film(9, 7, 5, seed=8, zbc=zbc)
+    phi = np.random.default_rng(9).normal(size=f.N)
+    mine = fm.efield(9, 7, 5, f.del_h, zbc, phi)
+    theirs = ref.efield(f, phi)
+    assert all(np.array_equal(a, b) for a, b in zip(mine, theirs))

@@ -228,3 +228,36 @@ def test_fp32_refined_neumann(gpu, orc, two_kernel, monkeypatch):
         assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
     assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
     assert (rf >= 1).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_checkpoint_restart_continues_the_run(gpu, orc, precision, tmp_path):
+    """A film written to the reference's checkpoint file and restarted in a
+    new film continues the same trajectory: P after 10 more steps within
+    1e-9 (FP64) / 2e-5 (FP32_REFINED) of the uninterrupted run; the file's E
+    is the field of the written potential."""
+    import cmsl_gb300 as cg
+    from cmsl_gb300 import formats as fm
+    f, P = random_film(24, 20, 7, seed=71, eps_0_nd=4.0, p_scale=0.2, layered=True)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    kw = {} if precision == "fp64" else dict(precision=cg.FP32_REFINED, refine_tol=1e-10, inner_tol=1e-5)
+    Ez = np.linspace(0.0, 0.3, 20)
+    ck = tmp_path / "ck.bin"
+    with _film(gpu, f, **kw) as a:
+        a.set_state(P)
+        a.run(Ez[:10])
+        a.write_checkpoint(ck, peloop=1, count=10, Ez_ext=Ez[9], incEz=Ez[1] - Ez[0])
+        _, phi_a = a.get_state()
+        a.run(Ez[10:])
+        Pa, _ = a.get_state()
+    Pf, Ef, pe, cnt, ez, inc = fm.read_checkpoint(str(ck), f.nx, f.ny, f.nz)
+    assert (pe, cnt, ez) == (1, 10, Ez[9])
+    assert all(np.array_equal(x, y) for x, y in zip(Ef, orc.efield(f, phi_a)))
+    with _film(gpu, f, **kw) as b:
+        info = b.read_checkpoint(ck)
+        assert info["count"] == 10
+        b.run(Ez[10:])
+        Pb, _ = b.get_state()
+    tol = 1e-9 if precision == "fp64" else 2e-5
+    for x, y in zip(Pb, Pa):
+        assert np.abs(x - y).max() <= tol * np.abs(y).max()
