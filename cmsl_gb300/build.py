@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libcmsl_gb.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["engine.cu", "noalloc.cu", "adjoint.cu"]
+CUDA_SOURCES = ["engine.cu", "noalloc.cu", "adjoint.cu", "grains.cu"]
 HOST_SOURCES = ["formats.cpp"]
 HEADERS = ["cmsl_dev.cuh", "dfloat.cuh", "kernels.cuh", "pcg_persist.cuh", "engine.h"]
 

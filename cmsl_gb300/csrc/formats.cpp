@@ -605,10 +605,13 @@ cmsl_status cmsl_evolve_schedule(double maxEz, double delEz, int num_steps, int 
     return CMSL_OK;
 }
 
-cmsl_status cmsl_voronoi_columnar(int nx, int ny, int nz, int ng, uint64_t seed, int32_t *omega, double *cent,
-                                  double *euler)
+}  // extern "C"
+
+// The seed points, centres and orientations of cmsl_voronoi_columnar (shared
+// with the device generator, grains.cu).
+void cmsl_internal_voronoi_seeds(int nx, int ny, int nz, int ng, uint64_t seed, double *sx, double *sy,
+                                 double *cent, double *euler)
 {
-    if (nx < 1 || ny < 1 || nz < 1 || ng < 1 || !omega) return io_fail(CMSL_ERR_ARG, "bad arguments");
     uint64_t st = seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
     auto next = [&]() {   // SplitMix64
         uint64_t z = (st += 0x9E3779B97F4A7C15ull);
@@ -617,8 +620,26 @@ cmsl_status cmsl_voronoi_columnar(int nx, int ny, int nz, int ng, uint64_t seed,
         return z ^ (z >> 31);
     };
     auto uni = [&]() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); };
-    std::vector<double> sx(ng), sy(ng);
     for (int g = 0; g < ng; ++g) { sx[g] = uni() * nx; sy[g] = uni() * ny; }
+    for (int g = 0; g < ng; ++g) {
+        if (cent) { cent[3 * g] = sx[g]; cent[3 * g + 1] = sy[g]; cent[3 * g + 2] = 0.5 * (nz - 1); }
+        if (euler) {
+            const double phi = 2.0 * M_PI * uni();
+            const double c = (0.3 + 0.7 * uni()) * (uni() < 0.5 ? -1.0 : 1.0);
+            const double psi = 2.0 * M_PI * uni();
+            euler[3 * g] = phi; euler[3 * g + 1] = std::acos(c); euler[3 * g + 2] = psi;
+        }
+    }
+}
+
+extern "C" {
+
+cmsl_status cmsl_voronoi_columnar(int nx, int ny, int nz, int ng, uint64_t seed, int32_t *omega, double *cent,
+                                  double *euler)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || ng < 1 || !omega) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    std::vector<double> sx(ng), sy(ng);
+    cmsl_internal_voronoi_seeds(nx, ny, nz, ng, seed, sx.data(), sy.data(), cent, euler);
     const long long plane = (long long)nx * ny;
     for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i) {
@@ -634,15 +655,6 @@ cmsl_status cmsl_voronoi_columnar(int nx, int ny, int nz, int ng, uint64_t seed,
             }
             for (int k = 0; k < nz; ++k) omega[i + (long long)nx * j + plane * k] = best;
         }
-    for (int g = 0; g < ng; ++g) {
-        if (cent) { cent[3 * g] = sx[g]; cent[3 * g + 1] = sy[g]; cent[3 * g + 2] = 0.5 * (nz - 1); }
-        if (euler) {
-            const double phi = 2.0 * M_PI * uni();
-            const double c = (0.3 + 0.7 * uni()) * (uni() < 0.5 ? -1.0 : 1.0);
-            const double psi = 2.0 * M_PI * uni();
-            euler[3 * g] = phi; euler[3 * g + 1] = std::acos(c); euler[3 * g + 2] = psi;
-        }
-    }
     return CMSL_OK;
 }
 

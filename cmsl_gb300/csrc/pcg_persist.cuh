@@ -89,6 +89,7 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
     const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Film constants held in registers for the whole solve (the compiler would
 // otherwise reload them from global memory after every float store).
@@ -272,129 +273,87 @@ __device__ __forceinline__ void cg2_point(const FilmC &F, const CgBuf &B, const 
     }
 }
 
-// Brick geometry of the thread (column) for the staging and stencil steps.
-struct BrickCol {
-    int pl, col, wx, wy;
-    bool own, need;
-};
-
-__device__ __forceinline__ BrickCol brick_col(const FilmC &F, int x0, int y0)
-{
-    BrickCol c;
-    const int nx = F.nx, ny = F.ny;
-    const int bx = threadIdx.x % PBX, by = threadIdx.x / PBX;
-    c.wx = min(TX, nx - x0);
-    c.wy = min(TY, ny - y0);
-    c.own = bx >= 1 && bx <= c.wx && by >= 1 && by <= c.wy;
-    const bool ex = bx == 0 || bx == c.wx + 1, ey = by == 0 || by == c.wy + 1;
-    c.need = bx <= c.wx + 1 && by <= c.wy + 1 && !(ex && ey);
-    const int gx = (x0 - 1 + bx + nx) % nx, gy = (y0 - 1 + by + ny) % ny;
-    c.pl = gx + nx * gy;
-    c.col = by * PBX + bx;
-    return c;
-}
-
-// Issues the cp.async copies of one brick's u (and material codes) with a
-// one-cell halo into one staging buffer (not waited for).
+// Phase S on one brick: stage u (and material codes) with a one-cell halo,
+// then w = A u and delta += w.u on own cells.
 template <bool UNI>
-__device__ __forceinline__ void cg2_stage(const FilmC &F, const CgBuf &B, const uint32_t *__restrict__ code,
-                                          int4 it, float *sUb, uint32_t *sCb)
+__device__ __forceinline__ void cg2_brick(const FilmC &F, const CgBuf &B, const uint32_t *__restrict__ code,
+                                          int x0, int y0, int z0, int z1, float &dacc, float *sUb,
+                                          uint32_t *sCb, const float *sEps)
 {
-    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    const BrickCol c = brick_col(F, it.y, it.z);
+    const int nx = F.nx, ny = F.ny, nz = F.nz, plane = F.plane;
+    const int bx = threadIdx.x % PBX, by = threadIdx.x / PBX;
+    const int wx = min(TX, nx - x0), wy = min(TY, ny - y0);
+    const bool own = bx >= 1 && bx <= wx && by >= 1 && by <= wy;
+    const bool ex = bx == 0 || bx == wx + 1, ey = by == 0 || by == wy + 1;
+    const bool need = bx <= wx + 1 && by <= wy + 1 && !(ex && ey);
+    const int gx = (x0 - 1 + bx + nx) % nx, gy = (y0 - 1 + by + ny) % ny;
+    const int pl = gx + nx * gy;
     const float *__restrict__ u = B.r[1] + F.off;
+    float *__restrict__ w = B.w[0] + F.off;
     constexpr int PP = PBY * PBX;
-    if (c.need) {
-        const int klo = c.own ? max(z0 - 1, 0) : z0;
-        const int khi = c.own ? min(z1, F.nz - 1) : z1 - 1;
+    const int col = by * PBX + bx;
+    if (need) {
+        const int klo = own ? max(z0 - 1, 0) : z0;
+        const int khi = own ? min(z1, nz - 1) : z1 - 1;
         for (int k = klo; k <= khi; ++k) {
-            const int o = c.pl + k * F.plane;
-            const int si = (k - z0 + 1) * PP + c.col;
+            const int o = pl + k * plane;
+            const int si = (k - z0 + 1) * PP + col;
             cp_async4(sUb + si, u + o);
             if (!UNI) cp_async4(sCb + si, code + o);
         }
     }
-}
-
-// w = A u and delta += w.u on the own cells of a staged brick.
-template <bool UNI>
-__device__ __forceinline__ void cg2_apply(const FilmC &F, const CgBuf &B, int4 it, float &dacc, const float *sUb,
-                                          const uint32_t *sCb, const float *sEps)
-{
-    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    const BrickCol c = brick_col(F, it.y, it.z);
-    if (!c.own) return;
-    const int nz = F.nz;
-    float *__restrict__ w = B.w[0] + F.off;
-    constexpr int PP = PBY * PBX;
-    for (int k = z0; k < z1; ++k) {
-        const int zi = k - z0 + 1;
-        const int si = zi * PP + c.col;
-        const float uc = sUb[si];
-        float wv;
-        if (id_row(F, k, c.pl)) {
-            wv = uc;
-        } else {
-            int zu = zi + 1, zd = zi - 1;
-            if (F.zbc != 0) {
-                if (k == 0) zd = zu;
-                else if (k == nz - 1) zu = zd;
-            }
-            const int su = zu * PP + c.col, sd = zd * PP + c.col;
-            const float ue = sUb[si + 1], uw = sUb[si - 1], un = sUb[si + PBX], us = sUb[si - PBX];
-            const float uu = sUb[su], ud = sUb[sd];
-            float a;
-            if (UNI) {
-                a = sEps[0] * ((((((ue - uc) - (uc - uw)) + (un - uc)) - (uc - us)) + (uu - uc)) - (uc - ud));
+    cp_async_wait_all();
+    __syncthreads();
+    if (own) {
+        for (int k = z0; k < z1; ++k) {
+            const int zi = k - z0 + 1;
+            const int si = zi * PP + col;
+            const float uc = sUb[si];
+            float wv;
+            if (id_row(F, k, pl)) {
+                wv = uc;
             } else {
-                const int mc = code_mat(sCb[si]) * 3;
-                a = sEps[mc + code_mat(sCb[si + 1])] * (ue - uc) - sEps[mc + code_mat(sCb[si - 1])] * (uc - uw);
-                a += sEps[mc + code_mat(sCb[si + PBX])] * (un - uc);
-                a -= sEps[mc + code_mat(sCb[si - PBX])] * (uc - us);
-                a += sEps[mc + code_mat(sCb[su])] * (uu - uc);
-                a -= sEps[mc + code_mat(sCb[sd])] * (uc - ud);
+                int zu = zi + 1, zd = zi - 1;
+                if (F.zbc != 0) {
+                    if (k == 0) zd = zu;
+                    else if (k == nz - 1) zu = zd;
+                }
+                const int su = zu * PP + col, sd = zd * PP + col;
+                const float ue = sUb[si + 1], uw = sUb[si - 1], un = sUb[si + PBX], us = sUb[si - PBX];
+                const float uu = sUb[su], ud = sUb[sd];
+                float a;
+                if (UNI) {
+                    a = sEps[0] * ((((((ue - uc) - (uc - uw)) + (un - uc)) - (uc - us)) + (uu - uc)) - (uc - ud));
+                } else {
+                    const int mc = code_mat(sCb[si]) * 3;
+                    a = sEps[mc + code_mat(sCb[si + 1])] * (ue - uc) - sEps[mc + code_mat(sCb[si - 1])] * (uc - uw);
+                    a += sEps[mc + code_mat(sCb[si + PBX])] * (un - uc);
+                    a -= sEps[mc + code_mat(sCb[si - PBX])] * (uc - us);
+                    a += sEps[mc + code_mat(sCb[su])] * (uu - uc);
+                    a -= sEps[mc + code_mat(sCb[sd])] * (uc - ud);
+                }
+                wv = -(a * F.inv_h2);
             }
-            wv = -(a * F.inv_h2);
+            w[pl + k * plane] = wv;
+            dacc = fmaf(wv, uc, dacc);
         }
-        w[c.pl + k * F.plane] = wv;
-        dacc = fmaf(wv, uc, dacc);
     }
+    __syncthreads();
 }
 
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-// Phase S over the bricks [first, end) of the film, stride nb (its blocks):
-// the next brick is staged into the other buffer while this one is applied.
+// Phase S over the bricks [first, end) of the film, stride nb (its blocks).
 template <bool UNI>
 __device__ __forceinline__ void cg2_stencil(const Dev &d, const FilmC &F, const CgBuf &B, int first, int end,
                                             int nb, float &dacc, float *sUb, uint32_t *sCb, const float *sEps)
 {
     const uint32_t *code = d.code + F.off;
-    if (first >= end) return;
-    int4 cur = B.bricks[first];
-    cg2_stage<UNI>(F, B, code, cur, sUb, sCb);
-    cp_async_commit();
-    int buf = 0;
     for (int i = first; i < end; i += nb) {
-        const int nxt = i + nb;
-        int4 next = cur;
-        if (nxt < end) {
-            next = B.bricks[nxt];
-            cg2_stage<UNI>(F, B, code, next, sUb + (buf ^ 1) * PNPL, sCb + (buf ^ 1) * PNPL);
-        }
-        cp_async_commit();
-        cp_async_wait_prev();           // this brick's group has landed
-        __syncthreads();
-        cg2_apply<UNI>(F, B, cur, dacc, sUb + buf * PNPL, sCb + buf * PNPL, sEps);
-        __syncthreads();                // the buffer is free for the brick after next
-        cur = next;
-        buf ^= 1;
+        const int4 it = B.bricks[i];
+        cg2_brick<UNI>(F, B, code, it.y, it.z, it.w & 0xffff, it.w >> 16, dacc, sUb, sCb, sEps);
     }
 }
 
-// Two staging buffers of u and of the material codes.
-constexpr size_t P2SMEM_BYTES = sizeof(float) * 4 * PNPL;
+constexpr size_t P2SMEM_BYTES = sizeof(float) * 2 * PNPL;
 
 // Films one persistent launch can carry (their scalars live in shared memory
 // behind the brick staging area: dynamic size P2SMEM_BYTES + films * 72 B).
@@ -533,10 +492,10 @@ __global__ void __launch_bounds__(PNT, 2) k_pcg_cg2(Dev d, CgBuf B, const float 
 {
     extern __shared__ float4 dsm4[];
     float *sUb = (float *)dsm4;
-    uint32_t *sCb = (uint32_t *)(sUb + 2 * PNPL);
+    uint32_t *sCb = (uint32_t *)(sUb + PNPL);
     __shared__ double sRed[PNW][2];
     __shared__ float sEps[9];
-    FilmState *st = reinterpret_cast<FilmState *>(sCb + 2 * PNPL);
+    FilmState *st = reinterpret_cast<FilmState *>(sCb + PNPL);
     const int nf = min(d.n_films, CG_MAX_FILMS);
     for (int i = threadIdx.x; i < nf; i += blockDim.x) {
         const FilmDev *ff = d.films + i;

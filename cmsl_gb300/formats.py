@@ -73,6 +73,7 @@ def _bind():
     L.cmsl_evolve_schedule.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
                                        _dp, _ip, C.POINTER(C.c_int), _dp, _ip, C.POINTER(C.c_int)]
     L.cmsl_voronoi_columnar.argtypes = [C.c_int] * 4 + [C.c_uint64, _ip, _dp, _dp]
+    L.cmsl_voronoi_columnar_gpu.argtypes = [C.c_int] * 4 + [C.c_uint64, _ip, _dp, _dp]
     L.cmsl_checkpoint_write.argtypes = [C.c_char_p] + [C.c_int] * 5 + [C.c_double, C.c_double, C.POINTER(_dp),
                                                                        C.POINTER(_dp)]
     L.cmsl_checkpoint_read.argtypes = [C.c_char_p] + [C.c_int] * 3 + [C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -215,12 +216,14 @@ def evolve_schedule(maxEz, delEz, num_steps, n_periods=1, single_crystal=False, 
     return Ez, rows, rE[: nr.value], rc[: nr.value]
 
 
-def voronoi_columnar(nx, ny, nz, n_grains, seed):
-    """-> omega [N], cent [ng, 3], euler [ng, 3]."""
+def voronoi_columnar(nx, ny, nz, n_grains, seed, device=False):
+    """-> omega [N], cent [ng, 3], euler [ng, 3]; device=True computes the map
+    on the GPU (identical result)."""
     L = _bind()
     om = np.zeros(nx * ny * nz, np.int32)
     cent, eul = np.zeros(3 * n_grains), np.zeros(3 * n_grains)
-    check(L.cmsl_voronoi_columnar(nx, ny, nz, n_grains, int(seed), _i(om), _d(cent), _d(eul)))
+    fn = L.cmsl_voronoi_columnar_gpu if device else L.cmsl_voronoi_columnar
+    check(fn(nx, ny, nz, n_grains, int(seed), _i(om), _d(cent), _d(eul)))
     return om, cent.reshape(n_grains, 3), eul.reshape(n_grains, 3)
 
 

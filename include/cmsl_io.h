@@ -118,6 +118,12 @@ cmsl_status cmsl_evolve_schedule(double maxEz, double delEz, int num_steps, int 
 cmsl_status cmsl_voronoi_columnar(int nx, int ny, int nz, int n_grains, uint64_t seed, int32_t *omega,
                                   double *cent, double *euler);
 
+/* cmsl_voronoi_columnar computed on the GPU (one thread per column, seeds in
+ * shared memory, distances in explicitly rounded FP64): the same map, centres
+ * and orientations as the host generator.  omega, cent, euler are host arrays. */
+cmsl_status cmsl_voronoi_columnar_gpu(int nx, int ny, int nz, int n_grains, uint64_t seed, int32_t *omega,
+                                      double *cent, double *euler);
+
 /* Checkpoint file of the reference (generate.cu:90-264, write_checkpoint /
  * read_checkpoint): header int nx, ny, nz, peloop, count; double Ez_ext,
  * incEz; then Pmx, Pmy, Pmz, Psx, Psy, Psz, Ex, Ey, Ez (N doubles each), host

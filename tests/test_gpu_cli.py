@@ -130,3 +130,12 @@ def test_campaign_driver_matches_oracle(cli, tmp_path):
                 st[8] * Ps, st[9]]
         assert int(got[11]) == cnt
         np.testing.assert_allclose(got[:11], want, rtol=2e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("dims", [(32, 24, 5, 13, 7), (257, 130, 3, 600, 11), (64, 64, 16, 1, 2)])
+def test_gpu_voronoi_equals_host(cli, dims):
+    """The device grain-map generator gives the host generator's map bit for bit."""
+    nx, ny, nz, ng, seed = dims
+    a = fm.voronoi_columnar(nx, ny, nz, ng, seed)
+    b = fm.voronoi_columnar(nx, ny, nz, ng, seed, device=True)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
