@@ -41,11 +41,14 @@ CONFIG_ID = 1
 #   update:   (FP64) read x, p, r, q, dinv, write x, r
 #   pcg_iter: (FP32, one single-reduction iteration of the persistent solver)
 #             read x, p, r, s, w, dinv, code, write x, p, r, s, w
+#   spec:     (FP32, direct inner solve) x-FFT: read r, write spectra; y-FFT, z-solve (with its
+#             coefficient scratch) and y-FFT: read and write the spectra (8 B); x-FFT: read
+#             the spectra, write x -> 12 + 16 + 24 + 16 + 12 B
 #   spmv32:   (FP32 batch, masked two-kernel PCG) read r, p_old, dinv, code, write p, q
 #   update32: (FP32 batch) read x, p, r, q, dinv, write x, r
 BYTES = {
     "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4, "setup": 8 + 4 + 12 + 4 + 4 + 8 + 4, "pcg_iter": 7 * 4 + 5 * 4,
-             "spmv32": 4 * 4 + 2 * 4, "update32": 5 * 4 + 2 * 4},
+             "spmv32": 4 * 4 + 2 * 4, "update32": 5 * 4 + 2 * 4, "spec": 80},
     "fp64": {"tdgl": 6 * 8 * 2 + 8 + 4, "setup": 24 + 8 + 4 + 8 + 8, "spmv": 8 * 3 + 4 + 16,
              "update": 5 * 8 + 2 * 8},
 }
@@ -278,8 +281,9 @@ def run_ours(args):
     mode = "fp64" if fp64 else "fp32"
     n_iter = float(np.mean(it))
     n_ref = float(np.mean(rf))
-    names = KERNELS[mode]
-    count = {"tdgl": 1.0, "setup": n_ref, "spmv": n_iter, "update": n_iter, "pcg_iter": n_iter}
+    direct = film.inner_solver == cg.INNER_DIRECT
+    names = ["tdgl", "setup", "spec"] if direct else KERNELS[mode]
+    count = {"tdgl": 1.0, "setup": n_ref, "spmv": n_iter, "update": n_iter, "pcg_iter": n_iter, "spec": n_iter}
     per_step = {k: kms[i] * count[k] for i, k in enumerate(names)}
     top = max(per_step, key=per_step.get)
     ki = names.index(top)
@@ -292,7 +296,12 @@ def run_ours(args):
             "traffic": (traffic * w.N) if traffic is not None else None,
             "kernel_ms": {k: float(kms[i]) for i, k in enumerate(names)},
             "share": {k: per_step[k] / sum(per_step.values()) for k in per_step}}
-    launches = int(K * 2 + 2 * rf.sum()) if not fp64 else int(K * 3 + 2 * it.sum())
+    if fp64:
+        launches = int(K * 3 + 2 * it.sum())
+    elif direct:
+        launches = int(K * 2 + rf.sum() + 6 * it.sum())
+    else:
+        launches = int(K * 2 + 2 * rf.sum())
 
     # end to end through the C ABI: host state in, K steps, host rows + state out
     film.set_state(w.P_init)
@@ -327,6 +336,8 @@ def run_ours(args):
                        "precision": "fp64" if fp64 else "fp32-refined (fp64 phi, refine to 1e-8)",
                        "pcg": "||b-A phi|| <= 1e-8 ||b||", "parallelism": "replicas" if world > 1 else "single",
                        "l2": "no flush: per-step state %.0f MB > 129 MB L2" % (film.device_bytes() / 1e6)},
+            "inner_solver": "direct (in-plane FFT + tridiagonal z, one solve per refinement pass)" if direct
+            else ("pcg (Jacobi, reference algorithm)" if fp64 else "pcg (persistent single-reduction Jacobi-PCG)"),
             "pcg_iters_per_step": n_iter, "refine_passes_per_step": n_ref,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
         }

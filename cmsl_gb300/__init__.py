@@ -9,6 +9,7 @@ formats and set-up (``formats``), the P-E loop schedule of ``Evolve``
 (``workloads``).
 """
 from ._lib import (  # noqa: F401
-    FP64, FP32_REFINED, DIRICHLET, NEUMANN, CRIT_REF, CRIT_RELRES, CmslError, LIB_PATH,
+    FP64, FP32_REFINED, DIRICHLET, NEUMANN, CRIT_REF, CRIT_RELRES, INNER_AUTO, INNER_PCG, INNER_DIRECT,
+    CmslError, LIB_PATH,
 )
 from .film import Batch, Film  # noqa: F401

@@ -18,6 +18,7 @@ STATUS_NAMES = {0: "CMSL_OK", 1: "CMSL_ERR_ARG", 2: "CMSL_ERR_CUDA", 3: "CMSL_ER
 FP64, FP32_REFINED = 0, 1
 DIRICHLET, NEUMANN = 0, 1
 CRIT_REF, CRIT_RELRES = 0, 1
+INNER_AUTO, INNER_PCG, INNER_DIRECT = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -39,6 +40,7 @@ class FilmDesc(C.Structure):
         ("tol_abs", C.c_double), ("tol_rel", C.c_double), ("max_iter", C.c_int),
         ("refine_tol", C.c_double), ("max_refine", C.c_int),
         ("inner_tol", C.c_double), ("inner_max_iter", C.c_int), ("warm_start", C.c_int),
+        ("inner_solver", C.c_int),
     ]
 
 
@@ -76,6 +78,7 @@ def lib() -> C.CDLL:
     L.cmsl_film_diag_inv.argtypes = [fp, _dp]
     L.cmsl_film_time_kernels.argtypes = [fp, C.c_int, C.c_void_p, _dp]
     L.cmsl_film_device_bytes.argtypes = [fp, C.POINTER(C.c_size_t)]
+    L.cmsl_film_inner_solver.argtypes = [fp, C.POINTER(C.c_int)]
     L.cmsl_film_checkpoint_write.argtypes = [fp, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double]
     L.cmsl_film_checkpoint_read.argtypes = [fp, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp, _dp]
     L.cmsl_film_loop_gradient.argtypes = [fp, C.c_int, _dp, _ip, _dp, C.c_int, C.c_int, _dp, _dp]
@@ -106,7 +109,7 @@ EXPORTS = [
     "cmsl_last_error", "cmsl_version", "cmsl_film_create", "cmsl_film_destroy", "cmsl_film_set_state",
     "cmsl_film_get_state", "cmsl_film_run", "cmsl_film_sync", "cmsl_film_get_rows", "cmsl_film_get_iters",
     "cmsl_film_tdgl_step", "cmsl_film_depol", "cmsl_film_apply_operator", "cmsl_film_efield",
-    "cmsl_film_diag_inv", "cmsl_film_time_kernels", "cmsl_film_device_bytes", "cmsl_film_checkpoint_write",
+    "cmsl_film_diag_inv", "cmsl_film_time_kernels", "cmsl_film_device_bytes", "cmsl_film_inner_solver", "cmsl_film_checkpoint_write",
     "cmsl_film_checkpoint_read", "cmsl_film_loop_gradient",
     "cmsl_batch_create",
     "cmsl_batch_destroy", "cmsl_batch_set_state", "cmsl_batch_get_state", "cmsl_batch_run", "cmsl_batch_sync",

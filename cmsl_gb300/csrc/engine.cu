@@ -83,6 +83,24 @@ int pick_zchunk(long long xy_tiles, int nz)
     return std::min(zc, nz);
 }
 
+// n = 2^a 3^b <= 4096 (the FFT radices of spectral.cuh)
+bool spec_radix_ok(int n)
+{
+    if (n < 1 || n > 4096) return false;
+    while (n % 3 == 0) n /= 3;
+    while (n % 2 == 0) n /= 2;
+    return n == 1;
+}
+
+SpecAxis spec_plan(int n)
+{
+    SpecAxis a{};
+    a.n = n;
+    while (n % 3 == 0) { a.rad[a.nst++] = 3; n /= 3; }
+    while (n % 2 == 0) { a.rad[a.nst++] = 2; n /= 2; }
+    return a;
+}
+
 template <class T> void fill_coef(Coef<T> &c, const cmsl_material &mt, int iface, double h, double dt)
 {
     // kernels_evol.cu:139-153, :212, :223 -- reference operation order
@@ -163,6 +181,8 @@ cmsl_status check_desc(const cmsl_film_desc *dsc, int idx, int n)
     if (dsc->precision != CMSL_FP64 && dsc->precision != CMSL_FP32_REFINED)
         return fail(CMSL_ERR_ARG, "%sprecision %d unknown", who, dsc->precision);
     if (dsc->zbc != CMSL_DIRICHLET && dsc->zbc != CMSL_NEUMANN) return fail(CMSL_ERR_ARG, "%szbc %d", who, dsc->zbc);
+    if (dsc->inner_solver < CMSL_INNER_AUTO || dsc->inner_solver > CMSL_INNER_DIRECT)
+        return fail(CMSL_ERR_ARG, "%sinner_solver %d unknown", who, dsc->inner_solver);
     if (!(dsc->del_h > 0.0) || !(dsc->del_t > 0.0)) return fail(CMSL_ERR_ARG, "%sdel_h and del_t must be > 0", who);
     for (int g = 0; g < dsc->n_grains; ++g)
         if (dsc->grain_mat[g] < 0 || dsc->grain_mat[g] > 2)
@@ -278,6 +298,30 @@ cmsl_status build_graph(Engine *e)
             TRY(add_kernel(body, &n_sp, nullptr, 0, (void *)k_spmv<double, Exact>, nit, NT, args64));
             TRY(add_kernel(body, &n_up, &n_sp, 1, (void *)k_update<double, Exact, false>, nit, NT, args64));
             last = n_solve;
+        } else if (e->spectral) {
+            // refinement pass: residual, then the direct solve of the correction
+            cudaGraph_t outer;
+            cudaGraphNode_t n_ref;
+            TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
+            a.d = e->dev(1, 0, h_outer);
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
+            void *a_x[] = {&a.d, &a.F32, &e->spec};
+            void *a_s[] = {&a.d, &e->spec};
+            void *a_d[] = {&a.d};
+            struct Node { void *fn; int grid, block; void **args; size_t smem; } seq[] = {
+                {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
+                {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
+                {(void *)k_spec_z, e->spec_grid[2], SPEC_NT, a_s, 0},
+                {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
+                {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
+                {(void *)k_spec_done, 1, 32, a_d, 0}};
+            cudaGraphNode_t prev = n_ref;
+            for (const Node &q : seq) {
+                cudaGraphNode_t nd;
+                TRY(add_kernel(outer, &nd, &prev, 1, q.fn, q.grid, q.block, q.args, q.smem));
+                prev = nd;
+            }
+            last = n_solve;
         } else if (e->persistent) {
             cudaGraph_t outer;
             cudaGraphNode_t n_ref, n_cg;
@@ -329,6 +373,20 @@ cmsl_status read_flags(Engine *e, cudaStream_t st, bool *active, bool *outer)
     return CMSL_OK;
 }
 
+// The direct spectral solve of the correction, launched from the host.
+cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<float> &F32)
+{
+    const SpecDev &sp = e->spec;
+    k_spec_x<true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
+    k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
+    k_spec_z<<<e->spec_grid[2], SPEC_NT, 0, st>>>(d, sp);
+    k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
+    k_spec_x<false><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
+    k_spec_done<<<1, 32, 0, st>>>(d);
+    CK(cudaGetLastError());
+    return CMSL_OK;
+}
+
 // The depolarisation solve launched from the host, one kernel at a time,
 // reading the loop flags back after each iteration.  Used by the
 // single-piece test hooks and when graphs are disabled (CMSL_NO_GRAPH=1).
@@ -354,6 +412,10 @@ cmsl_status solve_direct(Engine *e, cudaStream_t st, const Dev &d, const Fields<
             k_refine<<<nit, NT, 0, st>>>(d, F32);
             CK(cudaGetLastError());
             TRY(read_flags(e, st, &act, &out));
+            if (act && e->spectral) {
+                TRY(spec_launch(e, st, d, F32));
+                TRY(read_flags(e, st, &act, &out));
+            }
             if (act && e->persistent) {
                 Dev dd = d;
                 CgBuf B = e->cg;
@@ -362,7 +424,7 @@ cmsl_status solve_direct(Engine *e, cudaStream_t st, const Dev &d, const Fields<
                 CK(cudaLaunchCooperativeKernel(e->cg_fn, e->cg_grid, PNT, args, e->cg_smem, st));
                 TRY(read_flags(e, st, &act, &out));
             }
-            for (int guard = 0; act && !e->persistent; ++guard) {
+            for (int guard = 0; act && !e->persistent && !e->spectral; ++guard) {
                 if (guard > e->inner_max_cap + 1) return fail(CMSL_ERR_STATE, "inner PCG loop did not stop");
                 k_spmv<float, Fast><<<nit, NT, 0, st>>>(d, F32);
                 k_update<float, Fast, true><<<nit, NT, 0, st>>>(d, F32);
@@ -456,8 +518,24 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         all_dirichlet &= descs[i].zbc == CMSL_DIRICHLET;
         all_uni &= descs[i].mats[0].eps_r == descs[i].mats[1].eps_r && descs[i].mats[1].eps_r == descs[i].mats[2].eps_r;
     }
+    // direct (spectral) inner solve: one film, Dirichlet, one eps, 2^a 3^b sides
+    {
+        bool want = false, forced = false;
+        for (int i = 0; i < n; ++i) {
+            forced |= descs[i].inner_solver == CMSL_INNER_DIRECT;
+            want |= descs[i].inner_solver != CMSL_INNER_PCG;
+        }
+        const cmsl_film_desc &d0 = descs[0];
+        const bool ok = e->precision != CMSL_FP64 && n == 1 && d0.dep_flag && d0.zbc == CMSL_DIRICHLET && all_uni &&
+                        spec_radix_ok(d0.nx) && spec_radix_ok(d0.ny);
+        if (forced && !ok)
+            return fail(CMSL_ERR_ARG, "inner_solver DIRECT needs one FP32_REFINED film with dep_flag, the Dirichlet "
+                                      "z boundary, one eps for all materials and nx, ny of the form 2^a 3^b <= 4096");
+        e->spectral = ok && want;
+    }
     int cg_per = 0, cg_nsm = 0;
-    e->persistent = e->precision != CMSL_FP64 && all_dirichlet && n <= CG_MAX_FILMS && !(tk && atoi(tk) != 0);
+    e->persistent = e->precision != CMSL_FP64 && !e->spectral && all_dirichlet && n <= CG_MAX_FILMS &&
+                    !(tk && atoi(tk) != 0);
     if (e->persistent) {
         int dev = 0;
         CK(cudaGetDevice(&dev));
@@ -613,6 +691,47 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(e->alloc((void **)&B.part, sizeof(float4) * 2 * e->cg_grid));
         TRY(e->alloc((void **)&B.arrive, sizeof(unsigned int) * 2));
         TRY(e->alloc((void **)&B.err, sizeof(int) * 2));
+    }
+    if (e->spectral) {
+        const FilmHost &h = e->fh[0];
+        SpecDev &sp = e->spec;
+        sp.nx = h.nx; sp.ny = h.ny; sp.nz = h.nz; sp.M = h.nz - 2;
+        sp.ax = spec_plan(h.nx);
+        sp.ay = spec_plan(h.ny);
+        const double eps = descs[0].mats[0].eps_r;   // harm(eps, eps) = eps on every face
+        sp.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
+        const size_t modes = (size_t)h.nx * h.ny;
+        TRY(e->alloc((void **)&sp.C, sizeof(float2) * modes * sp.M));
+        TRY(e->alloc((void **)&sp.cp, sizeof(float) * modes * sp.M));
+        auto table = [&](int nn, const float2 **tw, const float **lam) -> cmsl_status {
+            std::vector<float2> t((size_t)nn);
+            std::vector<float> l((size_t)nn);
+            for (int q = 0; q < nn; ++q) {
+                const double a = 2.0 * M_PI * q / nn;
+                t[q] = make_float2((float)std::cos(a), (float)-std::sin(a));
+                const double sn = std::sin(M_PI * q / nn);
+                l[q] = (float)(4.0 * sn * sn);                 // 2 - 2 cos(2 pi q / n)
+            }
+            void *pt = nullptr, *pl = nullptr;
+            TRY(e->alloc(&pt, sizeof(float2) * nn));
+            TRY(e->alloc(&pl, sizeof(float) * nn));
+            CK(cudaMemcpy(pt, t.data(), sizeof(float2) * nn, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(pl, l.data(), sizeof(float) * nn, cudaMemcpyHostToDevice));
+            *tw = (const float2 *)pt;
+            *lam = (const float *)pl;
+            return CMSL_OK;
+        };
+        TRY(table(h.nx, &sp.twx, &sp.lamx));
+        TRY(table(h.ny, &sp.twy, &sp.lamy));
+        const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
+        e->spec_grid[0] = (int)(((long long)sp.M * h.ny + rbx - 1) / rbx);
+        e->spec_grid[1] = sp.M * ((h.nx + cby - 1) / cby);
+        e->spec_grid[2] = (int)((modes + SPEC_NT - 1) / SPEC_NT);
+        e->spec_smem[0] = sizeof(float2) * 2 * rbx * h.nx;
+        e->spec_smem[1] = sizeof(float2) * 2 * cby * h.ny;
+        CK(cudaFuncSetAttribute(k_spec_x<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
+        CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
+        CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));
     }
     TRY(e->alloc((void **)&e->d_phi[0], sizeof(double) * cells));
     TRY(e->alloc((void **)&e->d_phi[1], sizeof(double) * cells));
@@ -835,6 +954,8 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
             case 2:
                 if (fp64) {
                     k_spmv<double, Exact><<<nit, NT, 0, st>>>(d, F64);
+                } else if (e->spectral) {
+                    TRY(spec_launch(e, st, d, F32));
                 } else if (e->persistent) {
                     // one persistent solve of CG_TIMING_ITERS iterations
                     Dev dd = d;
@@ -850,7 +971,7 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
                 break;
             default:
                 if (fp64) k_update<double, Exact, false><<<nit, NT, 0, st>>>(d, F64);
-                else if (e->persistent) k_step_end<<<1, 32, 0, st>>>(d);   // no fourth kernel
+                else if (e->persistent || e->spectral) k_step_end<<<1, 32, 0, st>>>(d);   // no fourth kernel
                 else k_update<float, Fast, true><<<nit, NT, 0, st>>>(d, F32);
                 break;
             }
@@ -1080,6 +1201,13 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *f, int reps, void *stream, double 
 {
     if (!f) return fail(CMSL_ERR_ARG, "bad arguments");
     return time_kernels(f, reps, stream, ms);
+}
+
+cmsl_status cmsl_film_inner_solver(cmsl_film *f, int *solver)
+{
+    if (!f || !solver) return fail(CMSL_ERR_ARG, "NULL argument");
+    *solver = f->spectral ? CMSL_INNER_DIRECT : CMSL_INNER_PCG;
+    return CMSL_OK;
 }
 
 cmsl_status cmsl_film_device_bytes(cmsl_film *f, size_t *bytes)

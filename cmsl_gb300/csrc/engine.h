@@ -8,6 +8,7 @@
 #include "cmsl.h"
 #include "kernels.cuh"
 #include "pcg_persist.cuh"
+#include "spectral.cuh"
 
 namespace cmsl_eng {
 
@@ -75,6 +76,10 @@ struct Engine {
     cudaStream_t stream = nullptr;
     // FP32_REFINED inner solver: the persistent cooperative kernel, or the
     // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
+    bool spectral = false;      // FP32 inner solve by the direct spectral solve (one film, uniform eps)
+    SpecDev spec{};
+    int spec_grid[3] = {0, 0, 0};
+    size_t spec_smem[2] = {0, 0};
     bool persistent = false;
     CgBuf cg{};
     int cg_grid = 0;

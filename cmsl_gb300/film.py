@@ -33,7 +33,8 @@ class _Desc:
     def __init__(self, nx, ny, nz, omega, grain_mat, TR, mats, *, del_h, del_t, dep_flag=1,
                  zbc=_lib.DIRICHLET, eps_0_nd=0.0, is_interface=None, precision=_lib.FP64,
                  pcg_crit=_lib.CRIT_REF, tol_abs=1e-3, tol_rel=1e-2, max_iter=4000,
-                 refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000, warm_start=3):
+                 refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000, warm_start=3,
+                 inner_solver=_lib.INNER_AUTO):
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
         self.N = self.nx * self.ny * self.nz
         self.precision = precision
@@ -59,6 +60,7 @@ class _Desc:
         d.refine_tol, d.max_refine = float(refine_tol), int(max_refine)
         d.inner_tol, d.inner_max_iter = float(inner_tol), int(inner_max_iter)
         d.warm_start = int(warm_start)
+        d.inner_solver = int(inner_solver)
         self.d = d
 
 
@@ -217,6 +219,13 @@ class Film:
         b = C.c_size_t()
         check(lib().cmsl_film_device_bytes(self._h, C.byref(b)))
         return int(b.value)
+
+    @property
+    def inner_solver(self):
+        """INNER_DIRECT (spectral direct solve) or INNER_PCG."""
+        v = C.c_int()
+        check(lib().cmsl_film_inner_solver(self._h, C.byref(v)))
+        return v.value
 
 
 class Batch:

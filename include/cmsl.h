@@ -82,7 +82,17 @@ typedef struct {
                                      extrapolation 2 phi_n - phi_{n-1}, 2 = quadratic
                                      3 phi_n - 3 phi_{n-1} + phi_{n-2}, 3 = cubic
                                      4 phi_n - 6 phi_{n-1} + 4 phi_{n-2} - phi_{n-3} */
+    int inner_solver;             /* FP32_REFINED inner solve: CMSL_INNER_AUTO (direct
+                                     spectral solve where it applies, else PCG),
+                                     CMSL_INNER_PCG, CMSL_INNER_DIRECT (CMSL_ERR_ARG where
+                                     it does not apply) */
 } cmsl_film_desc;
+
+/* The direct inner solve applies to a single FP32_REFINED film with the
+ * Dirichlet z boundary, one permittivity for all materials and nx, ny of the
+ * form 2^a 3^b (<= 4096): an in-plane FFT, a tridiagonal solve along z per
+ * mode and the inverse FFT (exact for that operator up to FP32 rounding). */
+typedef enum { CMSL_INNER_AUTO = 0, CMSL_INNER_PCG = 1, CMSL_INNER_DIRECT = 2 } cmsl_inner_solver;
 
 typedef struct cmsl_film cmsl_film;
 
@@ -144,6 +154,11 @@ cmsl_status cmsl_film_diag_inv(cmsl_film *film, double *dinv);
  * r.z.  The PCG kernels run with the solve forced active, so the call
  * changes the film's work vectors; run it after the steps being measured. */
 cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, double *ms);
+
+/* The FP32_REFINED inner solve the film uses: CMSL_INNER_DIRECT or
+ * CMSL_INNER_PCG (CMSL_INNER_PCG for FP64 films, whose solve is the
+ * reference's PCG). */
+cmsl_status cmsl_film_inner_solver(cmsl_film *film, int *solver);
 
 /* Bytes of device memory the film holds. */
 cmsl_status cmsl_film_device_bytes(cmsl_film *film, size_t *bytes);

@@ -1,0 +1,94 @@
+"""The direct (spectral) inner solve of CMSL_FP32_REFINED: films whose
+materials share one permittivity, Dirichlet z boundary, 2^a 3^b sides.
+Against the FP64 oracle solved to ||r|| <= 1e-12 ||b|| with the tolerances
+of the other FP32_REFINED tests (P within 2e-5 of max |P|, phi 1e-4, rows
+1e-5), and against the same film with the PCG inner solve."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.films import MATS_DEFAULT, random_film
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cmsl_gb300 import build
+    build.build()
+    import cmsl_gb300
+    return cmsl_gb300
+
+
+def _uniform(shape, seed, eps=30.0):
+    mats = MATS_DEFAULT.copy()
+    mats[:, 7] = eps
+    f, P = random_film(*shape, seed=seed, eps_0_nd=4.0, mats=mats, p_scale=0.2, layered=True)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    return f, P
+
+
+@pytest.mark.parametrize("shape", [(32, 24, 8), (48, 36, 10), (64, 16, 5), (96, 12, 7), (8, 9, 3)])
+def test_direct_solve_run_vs_oracle(gpu, shape):
+    f, P = _uniform(shape, seed=sum(shape))
+    n = 16
+    Ez = np.linspace(0.0, 0.35, n)
+    rows = np.arange(n, dtype=np.int32)
+    Pw, _, phiw, statw, _, rc = oracle.load().run(f, P, np.zeros(f.N), Ez, rows)
+    assert rc == 0
+    kw = dict(precision=gpu.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-5)
+    with gpu.Film.from_oracle_film(f, **kw) as g:
+        assert g.inner_solver == gpu.INNER_DIRECT
+        g.set_state(P)
+        g.run(Ez, rows)
+        Pg, phig = g.get_state()
+        rg = g.rows()
+        it, rf = g.iters()
+    for a, b in zip(Pg, Pw):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+    assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
+    assert np.abs(rg[:, :10] - statw[:, :10]).max() <= 1e-5
+    # one direct solve per refinement pass, a few passes per step
+    assert (rf >= 2).all() and (rf <= 4).all() and (it == rf - 1).all()
+    with gpu.Film.from_oracle_film(f, inner_solver=gpu.INNER_PCG, **kw) as g:
+        assert g.inner_solver == gpu.INNER_PCG
+        g.set_state(P)
+        g.run(Ez, rows)
+        Pp, _ = g.get_state()
+    for a, b in zip(Pg, Pp):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+
+
+def test_direct_solve_reaches_refine_tolerance(gpu):
+    """One refined depolarisation solve: ||b - A phi|| <= 1e-8 ||b|| in FP64."""
+    f, P = _uniform((48, 24, 12), seed=3)
+    orc = oracle.load()
+    with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED, refine_tol=1e-8) as g:
+        assert g.inner_solver == gpu.INNER_DIRECT
+        g.set_state(P)
+        res = g.depol()
+        Pg, phi = g.get_state()
+    assert res["status"] == 0 and res["refine"] <= 4
+    b = -orc.divergence(f, Pg[0], Pg[1], Pg[2])
+    k = np.repeat(np.arange(f.nz), f.nx * f.ny)
+    b[(k == 0) | (k == f.nz - 1)] = 0.0
+    r = b - orc.apply_A(f, phi)
+    assert np.linalg.norm(r) <= 1.2e-8 * np.linalg.norm(b)
+
+
+def test_direct_solve_selection(gpu):
+    kw = dict(precision=gpu.FP32_REFINED)
+    f, P = _uniform((30, 24, 6), seed=4)             # 30 = 2 * 3 * 5: not 2^a 3^b
+    with gpu.Film.from_oracle_film(f, **kw) as g:
+        assert g.inner_solver == gpu.INNER_PCG
+    with pytest.raises(gpu.CmslError):
+        gpu.Film.from_oracle_film(f, inner_solver=gpu.INNER_DIRECT, **kw)
+    f2, _ = random_film(32, 24, 6, seed=5)          # three permittivities
+    with gpu.Film.from_oracle_film(f2, **kw) as g:
+        assert g.inner_solver == gpu.INNER_PCG
+    f3, _ = _uniform((32, 24, 6), seed=6)
+    with gpu.Film.from_oracle_film(f3) as g:          # FP64: the reference's PCG
+        assert g.inner_solver == gpu.INNER_PCG
