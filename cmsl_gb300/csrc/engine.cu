@@ -96,9 +96,19 @@ SpecAxis spec_plan(int n)
 {
     SpecAxis a{};
     a.n = n;
+    a.lg = (n & (n - 1)) == 0 ? __builtin_ctz((unsigned)n) : -1;
     while (n % 3 == 0) { a.rad[a.nst++] = 3; n /= 3; }
     while (n % 2 == 0) { a.rad[a.nst++] = 2; n /= 2; }
     return a;
+}
+
+// Threads per block of the z solve: its [M][threads] elimination arrays
+// (12 bytes per entry) stay within 96 KB of shared memory; 0 if M is too large.
+int spec_zthreads(int M)
+{
+    for (int t = 128; t >= 32; t /= 2)
+        if ((size_t)t * M * 12 <= 96 * 1024) return t;
+    return 0;
 }
 
 template <class T> void fill_coef(Coef<T> &c, const cmsl_material &mt, int iface, double h, double dt)
@@ -311,7 +321,7 @@ cmsl_status build_graph(Engine *e)
             struct Node { void *fn; int grid, block; void **args; size_t smem; } seq[] = {
                 {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
                 {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
-                {(void *)k_spec_z, e->spec_grid[2], SPEC_NT, a_s, 0},
+                {(void *)k_spec_z, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
                 {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
                 {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
                 {(void *)k_spec_done, 1, 32, a_d, 0}};
@@ -379,7 +389,7 @@ cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<f
     const SpecDev &sp = e->spec;
     k_spec_x<true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
     k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
-    k_spec_z<<<e->spec_grid[2], SPEC_NT, 0, st>>>(d, sp);
+    k_spec_z<<<e->spec_grid[2], e->spec_zt, e->spec_smem[2], st>>>(d, sp);
     k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
     k_spec_x<false><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
     k_spec_done<<<1, 32, 0, st>>>(d);
@@ -527,7 +537,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         }
         const cmsl_film_desc &d0 = descs[0];
         const bool ok = e->precision != CMSL_FP64 && n == 1 && d0.dep_flag && d0.zbc == CMSL_DIRICHLET && all_uni &&
-                        spec_radix_ok(d0.nx) && spec_radix_ok(d0.ny);
+                        spec_radix_ok(d0.nx) && spec_radix_ok(d0.ny) && spec_zthreads(d0.nz - 2) > 0;
         if (forced && !ok)
             return fail(CMSL_ERR_ARG, "inner_solver DIRECT needs one FP32_REFINED film with dep_flag, the Dirichlet "
                                       "z boundary, one eps for all materials and nx, ny of the form 2^a 3^b <= 4096");
@@ -702,7 +712,6 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         sp.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
         const size_t modes = (size_t)h.nx * h.ny;
         TRY(e->alloc((void **)&sp.C, sizeof(float2) * modes * sp.M));
-        TRY(e->alloc((void **)&sp.cp, sizeof(float) * modes * sp.M));
         auto table = [&](int nn, const float2 **tw, const float **lam) -> cmsl_status {
             std::vector<float2> t((size_t)nn);
             std::vector<float> l((size_t)nn);
@@ -726,12 +735,15 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
         e->spec_grid[0] = (int)(((long long)sp.M * h.ny + rbx - 1) / rbx);
         e->spec_grid[1] = sp.M * ((h.nx + cby - 1) / cby);
-        e->spec_grid[2] = (int)((modes + SPEC_NT - 1) / SPEC_NT);
-        e->spec_smem[0] = sizeof(float2) * 2 * rbx * h.nx;
-        e->spec_smem[1] = sizeof(float2) * 2 * cby * h.ny;
+        e->spec_zt = spec_zthreads(sp.M);
+        e->spec_grid[2] = (int)((modes + e->spec_zt - 1) / e->spec_zt);
+        e->spec_smem[0] = sizeof(float2) * (2 * rbx * h.nx + h.nx);      // two tiles + twiddles
+        e->spec_smem[1] = sizeof(float2) * (2 * cby * h.ny + h.ny);
+        e->spec_smem[2] = (size_t)12 * sp.M * e->spec_zt;
         CK(cudaFuncSetAttribute(k_spec_x<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));
+        CK(cudaFuncSetAttribute(k_spec_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[2]));
     }
     TRY(e->alloc((void **)&e->d_phi[0], sizeof(double) * cells));
     TRY(e->alloc((void **)&e->d_phi[1], sizeof(double) * cells));

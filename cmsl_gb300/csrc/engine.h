@@ -79,7 +79,8 @@ struct Engine {
     bool spectral = false;      // FP32 inner solve by the direct spectral solve (one film, uniform eps)
     SpecDev spec{};
     int spec_grid[3] = {0, 0, 0};
-    size_t spec_smem[2] = {0, 0};
+    int spec_zt = 0;            // threads per block of the z solve
+    size_t spec_smem[3] = {0, 0, 0};
     bool persistent = false;
     CgBuf cg{};
     int cg_grid = 0;

@@ -13,9 +13,12 @@
 // so one solve per refinement pass replaces the PCG iterations; the outer
 // double-float refinement keeps the potential at the reference's tolerance.
 //
-// FFTs: mixed radix-2/3 self-sorting (Stockham) passes in shared memory, one
-// block per group of rows (x) or of columns (y); twiddles exp(-2 pi i t / n)
-// and eigenvalues come from host tables computed in double.
+// FFTs: self-sorting (Stockham) passes in shared memory -- radix 4 (and one
+// radix 2) for powers of two, radix 3 and 2 otherwise -- one block per group
+// of rows (x) or of columns (y); twiddles exp(-2 pi i t / n) and eigenvalues
+// come from host tables computed in double.  The z solve keeps the Thomas
+// elimination in shared memory, so each spectrum value is read and written
+// once per sweep.
 #pragma once
 #include "kernels.cuh"
 
@@ -27,12 +30,12 @@ constexpr int SPEC_NT = 256;
 
 struct SpecAxis {
     int n, nst;
+    int lg;                     // log2(n) when n is a power of two, else -1
     int rad[SPEC_MAX_STAGES];
 };
 
 struct SpecDev {
     float2 *C;                  // [M][ny][nx] spectra of the interior planes
-    float *cp;                  // [M][ny*nx] Thomas coefficients
     const float2 *twx, *twy;    // exp(-2 pi i t / n)
     const float *lamx, *lamy;   // 2 - 2 cos(2 pi t / n)
     SpecAxis ax, ay;
@@ -47,10 +50,66 @@ __device__ __forceinline__ float2 c_mul(float2 a, float2 b)
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// nseq sequences of length n, [seq][n] in a; transforms them with scratch b;
-// returns the buffer holding the result.  All threads of the block call it.
-__device__ __forceinline__ float2 *fft_seqs(float2 *a, float2 *b, int nseq, const SpecAxis &pl,
-                                            const float2 *__restrict__ tw)
+// Element e of sequence s of a block's tile sits at a[e * es + s * ss].  The
+// transforms run in place between two such tiles (a, b) and return the one
+// holding the result.  SEQ_FAST: consecutive threads take consecutive
+// sequences (interleaved tiles, the y pass); otherwise consecutive butterflies
+// of one sequence (the x pass).  Both keep shared-memory accesses of a warp on
+// distinct banks for the loads.  tw: the n twiddles, staged in shared memory.
+
+// n = 2^lgn: radix-4 passes (one radix-2 pass when lgn is odd), shifts and masks.
+template <bool SEQ_FAST>
+__device__ __forceinline__ float2 *fft_pow2(float2 *a, float2 *b, int nseq, int lgn, int es, int ss,
+                                            const float2 *tw)
+{
+    int lgNs = 0;
+    while (lgNs < lgn) {
+        const int lgR = (lgn - lgNs >= 2) ? 2 : 1;
+        const int lgnbf = lgn - lgR, nbf = 1 << lgnbf;
+        const int Ns = 1 << lgNs;
+        const int lgstep = lgn - lgNs - lgR;          // twiddle stride n / (Ns R)
+        const int total = nseq << lgnbf;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            int sq, j;
+            if (SEQ_FAST) { j = t / nseq; sq = t - j * nseq; }
+            else { sq = t >> lgnbf; j = t & (nbf - 1); }
+            const int jm = j & (Ns - 1);
+            const int o = ((j >> lgNs) << (lgNs + lgR)) + jm;
+            const float2 *src = a + sq * ss;
+            float2 *dst = b + sq * ss;
+            const int tj = jm << lgstep;
+            if (lgR == 2) {
+                const float2 v0 = src[j * es];
+                const float2 v1 = c_mul(src[(j + nbf) * es], tw[tj]);
+                const float2 v2 = c_mul(src[(j + 2 * nbf) * es], tw[2 * tj]);
+                const float2 v3 = c_mul(src[(j + 3 * nbf) * es], tw[3 * tj]);
+                const float2 s02 = c_add(v0, v2), d02 = c_sub(v0, v2);
+                const float2 s13 = c_add(v1, v3), d13 = c_sub(v1, v3);
+                const float2 rot = make_float2(d13.y, -d13.x);     // -i (v1 - v3)
+                dst[o * es] = c_add(s02, s13);
+                dst[(o + Ns) * es] = c_add(d02, rot);
+                dst[(o + 2 * Ns) * es] = c_sub(s02, s13);
+                dst[(o + 3 * Ns) * es] = c_sub(d02, rot);
+            } else {
+                const float2 v0 = src[j * es];
+                const float2 v1 = c_mul(src[(j + nbf) * es], tw[tj]);
+                dst[o * es] = c_add(v0, v1);
+                dst[(o + Ns) * es] = c_sub(v0, v1);
+            }
+        }
+        __syncthreads();
+        float2 *tmp = a;
+        a = b;
+        b = tmp;
+        lgNs += lgR;
+    }
+    return a;
+}
+
+// Any 2^a 3^b length: radix-3 and radix-2 passes.
+template <bool SEQ_FAST>
+__device__ __forceinline__ float2 *fft_mixed(float2 *a, float2 *b, int nseq, const SpecAxis &pl, int es, int ss,
+                                             const float2 *tw)
 {
     const int n = pl.n;
     int Ns = 1;
@@ -59,34 +118,44 @@ __device__ __forceinline__ float2 *fft_seqs(float2 *a, float2 *b, int nseq, cons
         const int nbf = n / R;
         const int tstride = n / (Ns * R);
         for (int t = threadIdx.x; t < nseq * nbf; t += blockDim.x) {
-            const int s = t / nbf, j = t - s * nbf;
+            int sq, j;
+            if (SEQ_FAST) { j = t / nseq; sq = t - j * nseq; }
+            else { sq = t / nbf; j = t - sq * nbf; }
             const int jm = j % Ns;
-            const float2 *src = a + s * n;
-            float2 *dst = b + s * n;
+            const float2 *src = a + sq * ss;
+            float2 *dst = b + sq * ss;
             const int o = (j / Ns) * Ns * R + jm;
-            const float2 v0 = src[j];
-            const float2 v1 = c_mul(src[j + nbf], __ldg(tw + jm * tstride));
+            const float2 v0 = src[j * es];
+            const float2 v1 = c_mul(src[(j + nbf) * es], tw[jm * tstride]);
             if (R == 2) {
-                dst[o] = c_add(v0, v1);
-                dst[o + Ns] = c_sub(v0, v1);
+                dst[o * es] = c_add(v0, v1);
+                dst[(o + Ns) * es] = c_sub(v0, v1);
             } else {
-                const float2 v2 = c_mul(src[j + 2 * nbf], __ldg(tw + 2 * jm * tstride));
+                const float2 v2 = c_mul(src[(j + 2 * nbf) * es], tw[2 * jm * tstride]);
                 const float2 s12 = c_add(v1, v2), d12 = c_sub(v1, v2);
                 const float2 m = make_float2(v0.x - 0.5f * s12.x, v0.y - 0.5f * s12.y);
                 const float k3 = 0.86602540378443865f;   // sin(2 pi / 3)
                 const float2 rot = make_float2(k3 * d12.y, -k3 * d12.x);
-                dst[o] = c_add(v0, s12);
-                dst[o + Ns] = c_add(m, rot);
-                dst[o + 2 * Ns] = c_sub(m, rot);
+                dst[o * es] = c_add(v0, s12);
+                dst[(o + Ns) * es] = c_add(m, rot);
+                dst[(o + 2 * Ns) * es] = c_sub(m, rot);
             }
         }
         __syncthreads();
-        float2 *t = a;
+        float2 *tmp = a;
         a = b;
-        b = t;
+        b = tmp;
         Ns *= R;
     }
     return a;
+}
+
+template <bool SEQ_FAST>
+__device__ __forceinline__ float2 *fft_tile(float2 *a, float2 *b, int nseq, const SpecAxis &pl, int es, int ss,
+                                            const float2 *tw)
+{
+    if (pl.lg >= 0) return fft_pow2<SEQ_FAST>(a, b, nseq, pl.lg, es, ss, tw);
+    return fft_mixed<SEQ_FAST>(a, b, nseq, pl, es, ss, tw);
 }
 
 // Whether the film's inner solve runs through the spectra this step.
@@ -97,7 +166,8 @@ __device__ __forceinline__ bool spec_run(const Dev &d)
 
 // x transforms of rows (kk, y), kk = interior plane - 1.  IN_REAL: from the
 // FP32 residual r into the spectra; otherwise from the spectra into the real
-// correction x (and x = 0 on the Dirichlet planes).
+// correction x (and x = 0 on the Dirichlet planes).  Shared memory: two tiles
+// of rb rows and the twiddles.
 template <bool IN_REAL>
 __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
@@ -106,7 +176,8 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     const int nx = sp.nx, rows = sp.M * sp.ny, rb = max(1, SPEC_ELEMS / nx);
     const int r0 = blockIdx.x * rb, nr = min(rb, rows - r0);
     const long long plane = (long long)nx * sp.ny;
-    float2 *a = sm2, *b = sm2 + rb * nx;
+    float2 *a = sm2, *b = sm2 + rb * nx, *tw = sm2 + 2 * rb * nx;
+    for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.twx + t);
     for (int t = threadIdx.x; t < nr * nx; t += blockDim.x) {
         const int s = t / nx, i = t - s * nx;
         const long long row = r0 + s;              // (kk, y)
@@ -114,17 +185,17 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
             const long long kk = row / sp.ny, y = row - kk * sp.ny;
             a[t] = make_float2(F.r[(kk + 1) * plane + y * nx + i], 0.f);
         } else {
-            a[t] = sp.C[row * nx + i];
+            a[t] = sp.C[(long long)r0 * nx + t];
         }
     }
     __syncthreads();
-    const float2 *res = fft_seqs(a, b, nr, sp.ax, sp.twx);
+    const float2 *res = fft_tile<false>(a, b, nr, sp.ax, 1, nx, tw);
     for (int t = threadIdx.x; t < nr * nx; t += blockDim.x) {
-        const int s = t / nx, i = t - s * nx;
-        const long long row = r0 + s;
         if (IN_REAL) {
-            sp.C[row * nx + i] = res[t];
+            sp.C[(long long)r0 * nx + t] = res[t];
         } else {
+            const int s = t / nx, i = t - s * nx;
+            const long long row = r0 + s;
             const long long kk = row / sp.ny, y = row - kk * sp.ny;
             F.x[(kk + 1) * plane + y * nx + i] = res[t].x;
             if (kk == 0) F.x[y * nx + i] = 0.f;
@@ -133,7 +204,8 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     }
 }
 
-// y transforms of column groups of one interior plane, in place on the spectra.
+// y transforms of column groups of one interior plane, in place on the
+// spectra; the tile keeps the plane's row-major layout (sequences interleaved).
 static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
@@ -142,49 +214,55 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
     const int groups = (nx + cb - 1) / cb;
     const int kk = blockIdx.x / groups, x0 = (blockIdx.x - kk * groups) * cb, nc = min(cb, nx - x0);
     float2 *base = sp.C + (long long)kk * nx * ny;
-    float2 *a = sm2, *b = sm2 + cb * ny;
+    float2 *a = sm2, *b = sm2 + cb * ny, *tw = sm2 + 2 * cb * ny;
+    for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.twy + t);
     for (int t = threadIdx.x; t < nc * ny; t += blockDim.x) {
         const int y = t / nc, c = t - y * nc;      // coalesced along x
-        a[c * ny + y] = base[(long long)y * nx + x0 + c];
+        a[t] = base[(long long)y * nx + x0 + c];
     }
     __syncthreads();
-    const float2 *res = fft_seqs(a, b, nc, sp.ay, sp.twy);
+    const float2 *res = fft_tile<true>(a, b, nc, sp.ay, nc, 1, tw);
     for (int t = threadIdx.x; t < nc * ny; t += blockDim.x) {
         const int y = t / nc, c = t - y * nc;
-        base[(long long)y * nx + x0 + c] = res[c * ny + y];
+        base[(long long)y * nx + x0 + c] = res[t];
     }
 }
 
-// Thomas algorithm along z for every in-plane mode; writes the conjugate of
-// the scaled solution so that the next forward transforms invert.
-static __global__ void __launch_bounds__(SPEC_NT) k_spec_z(Dev d, SpecDev sp)
+// Thomas algorithm along z for every in-plane mode, one thread per mode, the
+// elimination coefficients in shared memory ([M][blockDim] of d' and c');
+// writes the conjugate of the scaled solution so that the next forward
+// transforms invert.
+static __global__ void k_spec_z(Dev d, SpecDev sp)
 {
+    extern __shared__ float2 sm2[];
     if (!spec_run(d)) return;
+    const int M = sp.M, T = blockDim.x;
+    float2 *dps = sm2;
+    float *cps = (float *)(sm2 + (size_t)M * T);
     const long long modes = (long long)sp.nx * sp.ny;
-    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long m = (long long)blockIdx.x * T + threadIdx.x;
     if (m >= modes) return;
     const int x = (int)(m % sp.nx), y = (int)(m / sp.nx);
     const float dg = __ldg(sp.lamx + x) + __ldg(sp.lamy + y) + 2.f;
     const float s = sp.scale;
     float2 *C = sp.C + m;
-    float *cp = sp.cp + m;
     float c_prev = 0.f;
     float2 d_prev = make_float2(0.f, 0.f);
-    for (int k = 0; k < sp.M; ++k) {                 // forward sweep (sub/super-diagonal -1)
-        const float piv = dg + c_prev;
-        const float inv = 1.f / piv;
+    #pragma unroll 8
+    for (int k = 0; k < M; ++k) {                    // forward sweep (sub/super-diagonal -1)
         const float2 rk = C[k * modes];
+        const float inv = 1.f / (dg + c_prev);
         const float2 dk = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
         c_prev = -inv;
-        cp[k * modes] = c_prev;
-        C[k * modes] = dk;
+        cps[k * T + threadIdx.x] = c_prev;
+        dps[k * T + threadIdx.x] = dk;
         d_prev = dk;
     }
     float2 xn = d_prev;                              // back substitution
-    C[(sp.M - 1) * modes] = make_float2(xn.x, -xn.y);
-    for (int k = sp.M - 2; k >= 0; --k) {
-        const float2 dk = C[k * modes];
-        const float c = cp[k * modes];
+    C[(M - 1) * modes] = make_float2(xn.x, -xn.y);
+    for (int k = M - 2; k >= 0; --k) {
+        const float2 dk = dps[k * T + threadIdx.x];
+        const float c = cps[k * T + threadIdx.x];
         xn = make_float2(dk.x - c * xn.x, dk.y - c * xn.y);
         C[k * modes] = make_float2(xn.x, -xn.y);
     }
