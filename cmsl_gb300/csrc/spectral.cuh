@@ -25,7 +25,8 @@
 namespace cmsl {
 
 constexpr int SPEC_MAX_STAGES = 13;       // 2^12 = 4096
-constexpr int SPEC_ELEMS = 4096;          // complex values staged per block
+constexpr int SPEC_ELEMS = 2048;          // complex values staged per block (6 blocks per SM)
+constexpr int SPEC_LB = 8;                // global loads in flight per thread
 constexpr int SPEC_NT = 256;
 
 struct SpecAxis {
@@ -178,28 +179,39 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     const long long plane = (long long)nx * sp.ny;
     float2 *a = sm2, *b = sm2 + rb * nx, *tw = sm2 + 2 * rb * nx;
     for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.twx + t);
-    for (int t = threadIdx.x; t < nr * nx; t += blockDim.x) {
-        const int s = t / nx, i = t - s * nx;
-        const long long row = r0 + s;              // (kk, y)
-        if (IN_REAL) {
-            const long long kk = row / sp.ny, y = row - kk * sp.ny;
-            a[t] = make_float2(F.r[(kk + 1) * plane + y * nx + i], 0.f);
-        } else {
-            a[t] = sp.C[(long long)r0 * nx + t];
+    // rows r0 .. r0+nr-1 are consecutive: (kk, y) runs over whole planes, so
+    // the residual rows of one interior plane are contiguous in r
+    const int total = nr * nx;
+    for (int t0 = threadIdx.x; t0 < total; t0 += SPEC_LB * blockDim.x) {
+        float2 v[SPEC_LB];
+        #pragma unroll
+        for (int u = 0; u < SPEC_LB; ++u) {
+            const int t = t0 + u * blockDim.x;
+            if (t < total) {
+                if (IN_REAL) {
+                    const long long e = (long long)r0 * nx + t;        // (kk, y, x) of the interior stack
+                    v[u] = make_float2(F.r[plane + e], 0.f);
+                } else {
+                    v[u] = sp.C[(long long)r0 * nx + t];
+                }
+            }
+        }
+        #pragma unroll
+        for (int u = 0; u < SPEC_LB; ++u) {
+            const int t = t0 + u * blockDim.x;
+            if (t < total) a[t] = v[u];
         }
     }
     __syncthreads();
     const float2 *res = fft_tile<false>(a, b, nr, sp.ax, 1, nx, tw);
-    for (int t = threadIdx.x; t < nr * nx; t += blockDim.x) {
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const long long e = (long long)r0 * nx + t;
         if (IN_REAL) {
-            sp.C[(long long)r0 * nx + t] = res[t];
+            sp.C[e] = res[t];
         } else {
-            const int s = t / nx, i = t - s * nx;
-            const long long row = r0 + s;
-            const long long kk = row / sp.ny, y = row - kk * sp.ny;
-            F.x[(kk + 1) * plane + y * nx + i] = res[t].x;
-            if (kk == 0) F.x[y * nx + i] = 0.f;
-            if (kk == sp.M - 1) F.x[(sp.nz - 1) * plane + y * nx + i] = 0.f;
+            F.x[plane + e] = res[t].x;
+            if (e < plane) F.x[e] = 0.f;                                // first Dirichlet plane
+            if (e >= (long long)(sp.M - 1) * plane) F.x[e + 2 * plane] = 0.f;   // last one
         }
     }
 }
@@ -216,9 +228,22 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
     float2 *base = sp.C + (long long)kk * nx * ny;
     float2 *a = sm2, *b = sm2 + cb * ny, *tw = sm2 + 2 * cb * ny;
     for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.twy + t);
-    for (int t = threadIdx.x; t < nc * ny; t += blockDim.x) {
-        const int y = t / nc, c = t - y * nc;      // coalesced along x
-        a[t] = base[(long long)y * nx + x0 + c];
+    const int total = nc * ny;
+    for (int t0 = threadIdx.x; t0 < total; t0 += SPEC_LB * blockDim.x) {
+        float2 v[SPEC_LB];
+        #pragma unroll
+        for (int u = 0; u < SPEC_LB; ++u) {
+            const int t = t0 + u * blockDim.x;
+            if (t < total) {
+                const int y = t / nc, c = t - y * nc;      // coalesced along x
+                v[u] = base[(long long)y * nx + x0 + c];
+            }
+        }
+        #pragma unroll
+        for (int u = 0; u < SPEC_LB; ++u) {
+            const int t = t0 + u * blockDim.x;
+            if (t < total) a[t] = v[u];
+        }
     }
     __syncthreads();
     const float2 *res = fft_tile<true>(a, b, nc, sp.ay, nc, 1, tw);
