@@ -392,14 +392,16 @@ def run_batch(args):
     rfs = np.stack([b.iters(i, K)[1] for i in range(len(ws))])
     value = cells * K / (ms * 1e-3)
     kms = b.time_kernels(reps=10, stream=sp)
-    # Dirichlet films share the persistent inner solver (ms[2] = one iteration
-    # over every film); otherwise the masked two-kernel PCG (ms[2], ms[3])
-    persistent = len(ws) <= 128 and os.environ.get("CMSL_PCG_TWO_KERNEL", "0") in ("", "0")
-    names = ["tdgl", "setup", "pcg_iter"] if persistent else ["tdgl", "setup", "spmv32", "update32"]
+    # inner solve: the direct spectral solve (ms[2] = one solve of every
+    # film), or the persistent PCG (ms[2] = one iteration over every film)
+    direct = b.inner_solver == cg.INNER_DIRECT
+    persistent = not direct and len(ws) <= 128 and os.environ.get("CMSL_PCG_TWO_KERNEL", "0") in ("", "0")
+    names = (["tdgl", "setup", "spec"] if direct else
+             ["tdgl", "setup", "pcg_iter"] if persistent else ["tdgl", "setup", "spmv32", "update32"])
     # the loops run while any film is active: per step, the most demanding film
     n_ref = float(np.mean(rfs.max(axis=0)))
     n_it = float(np.mean(its.max(axis=0)))
-    count = {"tdgl": 1.0, "setup": n_ref, "spmv32": n_it, "update32": n_it, "pcg_iter": n_it}
+    count = {"tdgl": 1.0, "setup": n_ref, "spmv32": n_it, "update32": n_it, "pcg_iter": n_it, "spec": n_it}
     per_step = {k: kms[i] * count[k] for i, k in enumerate(names)}
     top = max(per_step, key=per_step.get)
     ki = names.index(top)
@@ -465,9 +467,12 @@ def run_batch(args):
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": cells * K / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d // K,
                 "d2h_bytes_per_step": d2h // K},
-        "inner_solver": "persistent (one cooperative launch per refinement pass)" if persistent else "two-kernel",
+        "inner_solver": ("direct (in-plane FFT + tridiagonal z for every film, one launch set per refinement pass)"
+                         if direct else "persistent PCG (one cooperative launch per refinement pass)" if persistent
+                         else "two-kernel PCG"),
         "clocks": clk,
-        "gpu_launches": int(K * 2 + 2 * K * n_ref) if persistent else int(K * 2 + K * n_ref + 2 * K * n_it),
+        "gpu_launches": (int(K * 2 + K * n_ref + 6 * K * n_it) if direct else
+                         int(K * 2 + 2 * K * n_ref) if persistent else int(K * 2 + K * n_ref + 2 * K * n_it)),
     }
     print(json.dumps(line))
     return 0

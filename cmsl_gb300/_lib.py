@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
     L.cmsl_batch_get_iters.argtypes = [fp, C.c_int, C.c_int, _ip, _ip]
     L.cmsl_batch_time_kernels.argtypes = [fp, C.c_int, C.c_void_p, _dp]
     L.cmsl_batch_device_bytes.argtypes = [fp, C.POINTER(C.c_size_t)]
+    L.cmsl_batch_inner_solver.argtypes = [fp, C.POINTER(C.c_int)]
     L.cmsl_depol_solve_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double,
                                            C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, _ip, _ip]
@@ -114,5 +115,6 @@ EXPORTS = [
     "cmsl_batch_create",
     "cmsl_batch_destroy", "cmsl_batch_set_state", "cmsl_batch_get_state", "cmsl_batch_run", "cmsl_batch_sync",
     "cmsl_batch_get_rows", "cmsl_batch_get_iters", "cmsl_batch_time_kernels", "cmsl_batch_device_bytes",
+    "cmsl_batch_inner_solver",
     "cmsl_depol_solve_noalloc",
 ]

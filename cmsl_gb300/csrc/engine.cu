@@ -528,19 +528,26 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         all_dirichlet &= descs[i].zbc == CMSL_DIRICHLET;
         all_uni &= descs[i].mats[0].eps_r == descs[i].mats[1].eps_r && descs[i].mats[1].eps_r == descs[i].mats[2].eps_r;
     }
-    // direct (spectral) inner solve: one film, Dirichlet, one eps, 2^a 3^b sides
+    // direct (spectral) inner solve: every film with a depolarisation solve
+    // has the Dirichlet z boundary, one eps and 2^a 3^b sides
+    int spec_mmax = 1;
     {
-        bool want = false, forced = false;
+        bool want = false, forced = false, ok = e->precision != CMSL_FP64, anydep = false;
         for (int i = 0; i < n; ++i) {
-            forced |= descs[i].inner_solver == CMSL_INNER_DIRECT;
-            want |= descs[i].inner_solver != CMSL_INNER_PCG;
+            const cmsl_film_desc &d = descs[i];
+            forced |= d.inner_solver == CMSL_INNER_DIRECT;
+            want |= d.inner_solver != CMSL_INNER_PCG;
+            if (!d.dep_flag) continue;
+            anydep = true;
+            const bool uni = d.mats[0].eps_r == d.mats[1].eps_r && d.mats[1].eps_r == d.mats[2].eps_r;
+            ok &= d.zbc == CMSL_DIRICHLET && uni && spec_radix_ok(d.nx) && spec_radix_ok(d.ny);
+            spec_mmax = std::max(spec_mmax, d.nz - 2);
         }
-        const cmsl_film_desc &d0 = descs[0];
-        const bool ok = e->precision != CMSL_FP64 && n == 1 && d0.dep_flag && d0.zbc == CMSL_DIRICHLET && all_uni &&
-                        spec_radix_ok(d0.nx) && spec_radix_ok(d0.ny) && spec_zthreads(d0.nz - 2) > 0;
+        ok &= anydep && spec_zthreads(spec_mmax) > 0;
         if (forced && !ok)
-            return fail(CMSL_ERR_ARG, "inner_solver DIRECT needs one FP32_REFINED film with dep_flag, the Dirichlet "
-                                      "z boundary, one eps for all materials and nx, ny of the form 2^a 3^b <= 4096");
+            return fail(CMSL_ERR_ARG, "inner_solver DIRECT needs FP32_REFINED films whose depolarisation solves have "
+                                      "the Dirichlet z boundary, one eps for all materials and nx, ny of the form "
+                                      "2^a 3^b <= 4096");
         e->spectral = ok && want;
     }
     int cg_per = 0, cg_nsm = 0;
@@ -703,43 +710,70 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(e->alloc((void **)&B.err, sizeof(int) * 2));
     }
     if (e->spectral) {
-        const FilmHost &h = e->fh[0];
-        SpecDev &sp = e->spec;
-        sp.nx = h.nx; sp.ny = h.ny; sp.nz = h.nz; sp.M = h.nz - 2;
-        sp.ax = spec_plan(h.nx);
-        sp.ay = spec_plan(h.ny);
-        const double eps = descs[0].mats[0].eps_r;   // harm(eps, eps) = eps on every face
-        sp.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
-        const size_t modes = (size_t)h.nx * h.ny;
-        TRY(e->alloc((void **)&sp.C, sizeof(float2) * modes * sp.M));
-        auto table = [&](int nn, const float2 **tw, const float **lam) -> cmsl_status {
-            std::vector<float2> t((size_t)nn);
-            std::vector<float> l((size_t)nn);
+        // per-film plans, tables and block ranges of the three passes
+        const int zt = spec_zthreads(spec_mmax);
+        std::vector<SpecFilm> sf((size_t)n);
+        std::vector<int> bxf, byf, bzf;
+        std::vector<float2> tw;
+        std::vector<float> lam;
+        long long coff = 0;
+        size_t smx = 0, smy = 0;
+        auto tables = [&](int nn, int *two, int *lamo) {
+            *two = (int)tw.size();
+            *lamo = (int)lam.size();
             for (int q = 0; q < nn; ++q) {
-                const double a = 2.0 * M_PI * q / nn;
-                t[q] = make_float2((float)std::cos(a), (float)-std::sin(a));
+                const double ang = 2.0 * M_PI * q / nn;
+                tw.push_back(make_float2((float)std::cos(ang), (float)-std::sin(ang)));
                 const double sn = std::sin(M_PI * q / nn);
-                l[q] = (float)(4.0 * sn * sn);                 // 2 - 2 cos(2 pi q / n)
+                lam.push_back((float)(4.0 * sn * sn));                 // 2 - 2 cos(2 pi q / n)
             }
-            void *pt = nullptr, *pl = nullptr;
-            TRY(e->alloc(&pt, sizeof(float2) * nn));
-            TRY(e->alloc(&pl, sizeof(float) * nn));
-            CK(cudaMemcpy(pt, t.data(), sizeof(float2) * nn, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(pl, l.data(), sizeof(float) * nn, cudaMemcpyHostToDevice));
-            *tw = (const float2 *)pt;
-            *lam = (const float *)pl;
+        };
+        for (int fi = 0; fi < n; ++fi) {
+            const FilmHost &h = e->fh[fi];
+            SpecFilm &P = sf[fi];
+            P.nx = h.nx; P.ny = h.ny; P.nz = h.nz; P.off = h.off;
+            P.bx0 = (int)bxf.size(); P.by0 = (int)byf.size(); P.bz0 = (int)bzf.size();
+            if (!h.dep) continue;                                    // no solve, no blocks
+            P.M = h.nz - 2;
+            P.ax = spec_plan(h.nx);
+            P.ay = spec_plan(h.ny);
+            P.coff = coff;
+            coff += (long long)P.M * h.nx * h.ny;
+            const double eps = descs[fi].mats[0].eps_r;              // harm(eps, eps) = eps on every face
+            P.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
+            tables(h.nx, &P.twx, &P.lamx);
+            tables(h.ny, &P.twy, &P.lamy);
+            const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
+            const long long gx = ((long long)P.M * h.ny + rbx - 1) / rbx;
+            const long long gy = (long long)P.M * ((h.nx + cby - 1) / cby);
+            const long long gz = ((long long)h.nx * h.ny + zt - 1) / zt;
+            bxf.insert(bxf.end(), (size_t)gx, fi);
+            byf.insert(byf.end(), (size_t)gy, fi);
+            bzf.insert(bzf.end(), (size_t)gz, fi);
+            smx = std::max(smx, sizeof(float2) * (2 * rbx * h.nx + h.nx));   // two tiles + twiddles
+            smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
+        }
+        SpecDev &sp = e->spec;
+        auto upload = [&](const void *src, size_t bytes, void **dst) -> cmsl_status {
+            TRY(e->alloc(dst, bytes));
+            CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
             return CMSL_OK;
         };
-        TRY(table(h.nx, &sp.twx, &sp.lamx));
-        TRY(table(h.ny, &sp.twy, &sp.lamy));
-        const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
-        e->spec_grid[0] = (int)(((long long)sp.M * h.ny + rbx - 1) / rbx);
-        e->spec_grid[1] = sp.M * ((h.nx + cby - 1) / cby);
-        e->spec_zt = spec_zthreads(sp.M);
-        e->spec_grid[2] = (int)((modes + e->spec_zt - 1) / e->spec_zt);
-        e->spec_smem[0] = sizeof(float2) * (2 * rbx * h.nx + h.nx);      // two tiles + twiddles
-        e->spec_smem[1] = sizeof(float2) * (2 * cby * h.ny + h.ny);
-        e->spec_smem[2] = (size_t)12 * sp.M * e->spec_zt;
+        void *p = nullptr;
+        TRY(upload(sf.data(), sizeof(SpecFilm) * sf.size(), &p)); sp.films = (const SpecFilm *)p;
+        TRY(upload(bxf.data(), sizeof(int) * bxf.size(), &p)); sp.bx_film = (const int *)p;
+        TRY(upload(byf.data(), sizeof(int) * byf.size(), &p)); sp.by_film = (const int *)p;
+        TRY(upload(bzf.data(), sizeof(int) * bzf.size(), &p)); sp.bz_film = (const int *)p;
+        TRY(upload(tw.data(), sizeof(float2) * tw.size(), &p)); sp.tw = (const float2 *)p;
+        TRY(upload(lam.data(), sizeof(float) * lam.size(), &p)); sp.lam = (const float *)p;
+        TRY(e->alloc((void **)&sp.C, sizeof(float2) * (size_t)coff));
+        e->spec_zt = zt;
+        e->spec_grid[0] = (int)bxf.size();
+        e->spec_grid[1] = (int)byf.size();
+        e->spec_grid[2] = (int)bzf.size();
+        e->spec_smem[0] = smx;
+        e->spec_smem[1] = smy;
+        e->spec_smem[2] = (size_t)12 * spec_mmax * zt;
         CK(cudaFuncSetAttribute(k_spec_x<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));
@@ -1291,6 +1325,13 @@ cmsl_status cmsl_batch_time_kernels(cmsl_batch *b, int reps, void *stream, doubl
 {
     if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
     return time_kernels(b, reps, stream, ms);
+}
+
+cmsl_status cmsl_batch_inner_solver(cmsl_batch *b, int *solver)
+{
+    if (!b || !solver) return fail(CMSL_ERR_ARG, "NULL argument");
+    *solver = b->spectral ? CMSL_INNER_DIRECT : CMSL_INNER_PCG;
+    return CMSL_OK;
 }
 
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *b, size_t *bytes)

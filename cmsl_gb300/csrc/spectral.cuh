@@ -35,13 +35,23 @@ struct SpecAxis {
     int rad[SPEC_MAX_STAGES];
 };
 
-struct SpecDev {
-    float2 *C;                  // [M][ny][nx] spectra of the interior planes
-    const float2 *twx, *twy;    // exp(-2 pi i t / n)
-    const float *lamx, *lamy;   // 2 - 2 cos(2 pi t / n)
+// One film of the direct solve.
+struct SpecFilm {
     SpecAxis ax, ay;
+    long long off;              // first cell of the film
+    long long coff;             // first spectrum value: [M][ny][nx] of the interior planes
     int nx, ny, nz, M;
+    int twx, twy, lamx, lamy;   // offsets into the twiddle / eigenvalue tables
     float scale;                // h^2 / (eps nx ny)
+    int bx0, by0, bz0;          // first block of the film in the x, y and z grids
+};
+
+struct SpecDev {
+    const SpecFilm *films;
+    float2 *C;                  // spectra of every film
+    const float2 *tw;           // exp(-2 pi i t / n) per film and axis
+    const float *lam;           // 2 - 2 cos(2 pi t / n) per film and axis
+    const int *bx_film, *by_film, *bz_film;   // film of every block of the three grids
 };
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -159,10 +169,10 @@ __device__ __forceinline__ float2 *fft_tile(float2 *a, float2 *b, int nseq, cons
     return fft_mixed<SEQ_FAST>(a, b, nseq, pl, es, ss, tw);
 }
 
-// Whether the film's inner solve runs through the spectra this step.
-__device__ __forceinline__ bool spec_run(const Dev &d)
+// Whether film f's inner solve runs through the spectra in this pass.
+__device__ __forceinline__ bool spec_run(const Dev &d, int f)
 {
-    return d.force || *(volatile const int *)&d.solve[0].active != 0;
+    return d.force || *(volatile const int *)&d.solve[f].active != 0;
 }
 
 // x transforms of rows (kk, y), kk = interior plane - 1.  IN_REAL: from the
@@ -173,12 +183,19 @@ template <bool IN_REAL>
 __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
-    if (!spec_run(d)) return;
-    const int nx = sp.nx, rows = sp.M * sp.ny, rb = max(1, SPEC_ELEMS / nx);
-    const int r0 = blockIdx.x * rb, nr = min(rb, rows - r0);
-    const long long plane = (long long)nx * sp.ny;
+    const int f = __ldg(sp.bx_film + blockIdx.x);
+    if (!spec_run(d, f)) return;
+    const SpecFilm &P = sp.films[f];
+    const int nx = P.nx, rows = P.M * P.ny, rb = max(1, SPEC_ELEMS / nx);
+    const int r0 = (blockIdx.x - P.bx0) * rb, nr = min(rb, rows - r0);
+    const long long plane = (long long)nx * P.ny;
+    const float *rr = F.r + P.off;
+    float *xx = F.x + P.off;
+    float2 *Cf = sp.C + P.coff;
+    const SpecAxis ax = P.ax;
+    const int M = P.M;
     float2 *a = sm2, *b = sm2 + rb * nx, *tw = sm2 + 2 * rb * nx;
-    for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.twx + t);
+    for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twx + t);
     // rows r0 .. r0+nr-1 are consecutive: (kk, y) runs over whole planes, so
     // the residual rows of one interior plane are contiguous in r
     const int total = nr * nx;
@@ -190,9 +207,9 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
             if (t < total) {
                 if (IN_REAL) {
                     const long long e = (long long)r0 * nx + t;        // (kk, y, x) of the interior stack
-                    v[u] = make_float2(F.r[plane + e], 0.f);
+                    v[u] = make_float2(rr[plane + e], 0.f);
                 } else {
-                    v[u] = sp.C[(long long)r0 * nx + t];
+                    v[u] = Cf[(long long)r0 * nx + t];
                 }
             }
         }
@@ -203,15 +220,15 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
         }
     }
     __syncthreads();
-    const float2 *res = fft_tile<false>(a, b, nr, sp.ax, 1, nx, tw);
+    const float2 *res = fft_tile<false>(a, b, nr, ax, 1, nx, tw);
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         const long long e = (long long)r0 * nx + t;
         if (IN_REAL) {
-            sp.C[e] = res[t];
+            Cf[e] = res[t];
         } else {
-            F.x[plane + e] = res[t].x;
-            if (e < plane) F.x[e] = 0.f;                                // first Dirichlet plane
-            if (e >= (long long)(sp.M - 1) * plane) F.x[e + 2 * plane] = 0.f;   // last one
+            xx[plane + e] = res[t].x;
+            if (e < plane) xx[e] = 0.f;                                  // first Dirichlet plane
+            if (e >= (long long)(M - 1) * plane) xx[e + 2 * plane] = 0.f;   // last one
         }
     }
 }
@@ -221,13 +238,17 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
 static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
-    if (!spec_run(d)) return;
-    const int nx = sp.nx, ny = sp.ny, cb = max(1, SPEC_ELEMS / ny);
+    const int f = __ldg(sp.by_film + blockIdx.x);
+    if (!spec_run(d, f)) return;
+    const SpecFilm &P = sp.films[f];
+    const int nx = P.nx, ny = P.ny, cb = max(1, SPEC_ELEMS / ny);
     const int groups = (nx + cb - 1) / cb;
-    const int kk = blockIdx.x / groups, x0 = (blockIdx.x - kk * groups) * cb, nc = min(cb, nx - x0);
-    float2 *base = sp.C + (long long)kk * nx * ny;
+    const int lb = blockIdx.x - P.by0;
+    const int kk = lb / groups, x0 = (lb - kk * groups) * cb, nc = min(cb, nx - x0);
+    const SpecAxis ay = P.ay;
+    float2 *base = sp.C + P.coff + (long long)kk * nx * ny;
     float2 *a = sm2, *b = sm2 + cb * ny, *tw = sm2 + 2 * cb * ny;
-    for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.twy + t);
+    for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twy + t);
     const int total = nc * ny;
     for (int t0 = threadIdx.x; t0 < total; t0 += SPEC_LB * blockDim.x) {
         float2 v[SPEC_LB];
@@ -246,7 +267,7 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
         }
     }
     __syncthreads();
-    const float2 *res = fft_tile<true>(a, b, nc, sp.ay, nc, 1, tw);
+    const float2 *res = fft_tile<true>(a, b, nc, ay, nc, 1, tw);
     for (int t = threadIdx.x; t < nc * ny; t += blockDim.x) {
         const int y = t / nc, c = t - y * nc;
         base[(long long)y * nx + x0 + c] = res[t];
@@ -260,17 +281,19 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
 static __global__ void k_spec_z(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
-    if (!spec_run(d)) return;
-    const int M = sp.M, T = blockDim.x;
+    const int f = __ldg(sp.bz_film + blockIdx.x);
+    if (!spec_run(d, f)) return;
+    const SpecFilm &P = sp.films[f];
+    const int M = P.M, T = blockDim.x;
     float2 *dps = sm2;
     float *cps = (float *)(sm2 + (size_t)M * T);
-    const long long modes = (long long)sp.nx * sp.ny;
-    const long long m = (long long)blockIdx.x * T + threadIdx.x;
+    const long long modes = (long long)P.nx * P.ny;
+    const long long m = (long long)(blockIdx.x - P.bz0) * T + threadIdx.x;
     if (m >= modes) return;
-    const int x = (int)(m % sp.nx), y = (int)(m / sp.nx);
-    const float dg = __ldg(sp.lamx + x) + __ldg(sp.lamy + y) + 2.f;
-    const float s = sp.scale;
-    float2 *C = sp.C + m;
+    const int x = (int)(m % P.nx), y = (int)(m / P.nx);
+    const float dg = __ldg(sp.lam + P.lamx + x) + __ldg(sp.lam + P.lamy + y) + 2.f;
+    const float s = P.scale;
+    float2 *C = sp.C + P.coff + m;
     float c_prev = 0.f;
     float2 d_prev = make_float2(0.f, 0.f);
     #pragma unroll 8
@@ -296,11 +319,14 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
 // After the solve: the inner solve of this pass is done (one "iteration").
 static __global__ void k_spec_done(Dev d)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0 && spec_run(d) && !d.force) {
-        SolveDev *S = d.solve;
-        S->iters = 1;
-        S->total_iters += 1;
-        S->active = 0;
+    if (d.force) return;
+    for (int f = threadIdx.x; f < d.n_films; f += blockDim.x) {
+        SolveDev *S = d.solve + f;
+        if (S->active) {
+            S->iters = 1;
+            S->total_iters += 1;
+            S->active = 0;
+        }
     }
 }
 

@@ -334,6 +334,13 @@ class Batch:
         check(lib().cmsl_batch_time_kernels(self._h, int(reps), C.c_void_p(stream) if stream else None, _d(ms)))
         return ms
 
+    @property
+    def inner_solver(self):
+        """INNER_DIRECT (spectral direct solve) or INNER_PCG."""
+        v = C.c_int()
+        check(lib().cmsl_batch_inner_solver(self._h, C.byref(v)))
+        return v.value
+
     def device_bytes(self):
         b = C.c_size_t()
         check(lib().cmsl_batch_device_bytes(self._h, C.byref(b)))

@@ -88,10 +88,11 @@ typedef struct {
                                      it does not apply) */
 } cmsl_film_desc;
 
-/* The direct inner solve applies to a single FP32_REFINED film with the
- * Dirichlet z boundary, one permittivity for all materials and nx, ny of the
- * form 2^a 3^b (<= 4096): an in-plane FFT, a tridiagonal solve along z per
- * mode and the inverse FFT (exact for that operator up to FP32 rounding). */
+/* The direct inner solve applies to FP32_REFINED films (or batches) whose
+ * depolarisation solves have the Dirichlet z boundary, one permittivity for
+ * all materials and nx, ny of the form 2^a 3^b (<= 4096): an in-plane FFT, a
+ * tridiagonal solve along z per mode and the inverse FFT (exact for that
+ * operator up to FP32 rounding). */
 typedef enum { CMSL_INNER_AUTO = 0, CMSL_INNER_PCG = 1, CMSL_INNER_DIRECT = 2 } cmsl_inner_solver;
 
 typedef struct cmsl_film cmsl_film;
@@ -205,6 +206,8 @@ cmsl_status cmsl_batch_get_iters(cmsl_batch *batch, int film, int n, int32_t *pc
  * masked PCG's SpMV and update kernels in FP32_REFINED mode). */
 cmsl_status cmsl_batch_time_kernels(cmsl_batch *batch, int reps, void *stream, double *ms);
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *batch, size_t *bytes);
+/* The batch's FP32_REFINED inner solve, as cmsl_film_inner_solver. */
+cmsl_status cmsl_batch_inner_solver(cmsl_batch *batch, int *solver);
 
 /* Restart files in the reference's checkpoint layout (generate.cu:90-264;
  * cmsl_io.h cmsl_checkpoint_write/read).  write: P and E = -grad(phi) of the

@@ -92,3 +92,44 @@ def test_direct_solve_selection(gpu):
     f3, _ = _uniform((32, 24, 6), seed=6)
     with gpu.Film.from_oracle_film(f3) as g:          # FP64: the reference's PCG
         assert g.inner_solver == gpu.INNER_PCG
+
+
+def test_direct_solve_batch(gpu):
+    """A batch of uneven one-eps films (one without depolarisation) takes the
+    direct solve; every film against its oracle run and its solo run."""
+    shapes = [(32, 24, 8), (48, 36, 6), (64, 16, 5), (24, 27, 7)]
+    films = []
+    for i, sh in enumerate(shapes):
+        f, P = _uniform(sh, seed=40 + i, eps=20.0 + 5 * i)
+        if i == 2:
+            f.dep_flag = 0
+        films.append((f, P))
+    n = 12
+    Ez = np.stack([np.linspace(0.0, 0.2 + 0.05 * i, n) for i in range(len(films))])
+    rows = np.tile(np.arange(n, dtype=np.int32), (len(films), 1))
+    kw = dict(precision=gpu.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-5)
+    orc = oracle.load()
+    with gpu.Batch.from_oracle_films([f for f, _ in films], **kw) as b:
+        assert b.inner_solver == gpu.INNER_DIRECT
+        for i, (_, P) in enumerate(films):
+            b.set_state(i, P)
+        st = b.run(Ez, rows)
+        assert (st == 0).all()
+        for i, (f, P) in enumerate(films):
+            Pw, _, phiw, statw, _, rc = orc.run(f, P, np.zeros(f.N), Ez[i], rows[i])
+            assert rc == 0
+            Pg, phig = b.get_state(i)
+            for a, w in zip(Pg, Pw):
+                assert np.abs(a - w).max() <= 2e-5 * np.abs(w).max(), i
+            if f.dep_flag:
+                assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max(), i
+            assert np.abs(b.rows(i)[:, :10] - statw[:, :10]).max() <= 1e-5, i
+            it, rf = b.iters(i)
+            if f.dep_flag:
+                assert (rf >= 2).all() and (it == rf - 1).all(), i
+            with gpu.Film.from_oracle_film(f, **kw) as g:
+                g.set_state(P)
+                g.run(Ez[i])
+                Ps, _ = g.get_state()
+            for a, w in zip(Pg, Ps):
+                assert np.abs(a - w).max() <= 2e-5 * max(np.abs(w).max(), 1e-30), i
