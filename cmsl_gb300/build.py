@@ -16,7 +16,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CUDA_SOURCES = ["engine.cu", "noalloc.cu", "adjoint.cu", "grains.cu"]
 HOST_SOURCES = ["formats.cpp"]
-HEADERS = ["cmsl_dev.cuh", "dfloat.cuh", "kernels.cuh", "pcg_persist.cuh", "engine.h"]
+HEADERS = ["cmsl_dev.cuh", "dfloat.cuh", "kernels.cuh", "pcg_persist.cuh", "spectral.cuh", "engine.h"]
 
 
 def nvcc() -> str:

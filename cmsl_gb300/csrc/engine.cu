@@ -70,16 +70,19 @@ double harm(double a, double b)   // depol_varEPS.cu:10-15
 
 namespace {
 
-// z chunk: enough items to fill the 152 SMs a few times over (all films of
-// the handle together), chunks >= 4 planes.
+// z chunk of the stencil items (xy_tiles: the column tiles of all films of
+// the handle together); CMSL_ZCHUNK overrides.
 int pick_zchunk(long long xy_tiles, int nz)
 {
     const char *env = getenv("CMSL_ZCHUNK");
     if (env && atoi(env) > 0) return std::min(nz, atoi(env));
-    const long long target = 8LL * 152;
+    // about 1.5 waves of the stencil passes (4 resident blocks on each of
+    // 152 SMs), chunks of at least 8 planes: the ring prologue and the two
+    // halo planes of a chunk cost more than the tail of a partial wave
+    const long long target = 6LL * 152;
     const long long chunks = (target + xy_tiles - 1) / xy_tiles;
     int zc = (int)std::max<long long>(1, (nz + chunks - 1) / chunks);
-    zc = std::max(zc, std::min(nz, 4));
+    zc = std::max(zc, std::min(nz, 8));
     return std::min(zc, nz);
 }
 
@@ -297,7 +300,7 @@ cmsl_status build_graph(Engine *e)
     void *args32[] = {&a.d, &a.F32};
     void *args_d[] = {&a.d};
     if (fp64) TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl<double, Exact>, nit, NT, args64));
-    else TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl<float, Fast>, nit, NT, args32));
+    else TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl32<T32_NS>, nit, NT, args32, T32_SMEM));
     cudaGraphNode_t last = n_tdgl;
     if (e->any_dep) {
         if (fp64) {
@@ -314,7 +317,7 @@ cmsl_status build_graph(Engine *e)
             cudaGraphNode_t n_ref;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             a.d = e->dev(1, 0, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, NT, args32, e->refine_smem));
             void *a_x[] = {&a.d, &a.F32, &e->spec};
             void *a_s[] = {&a.d, &e->spec};
             void *a_d[] = {&a.d};
@@ -337,7 +340,7 @@ cmsl_status build_graph(Engine *e)
             cudaGraphNode_t n_ref, n_cg;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             a.d = e->dev(1, 0, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, NT, args32, e->refine_smem));
             void *args_cg[] = {&a.d, &e->cg, &e->d_dinv};
             TRY(add_kernel(outer, &n_cg, &n_ref, 1, e->cg_fn, e->cg_grid, PNT, args_cg, e->cg_smem));
             cudaLaunchAttributeValue av{};
@@ -351,7 +354,7 @@ cmsl_status build_graph(Engine *e)
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
             a.d = e->dev(1, h_inner, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, (void *)k_refine, nit, NT, args32));
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, NT, args32, e->refine_smem));
             TRY(add_while(outer, &n_in, &n_ref, 1, h_inner, &inner));
             TRY(add_kernel(inner, &n_sp, nullptr, 0, (void *)k_spmv<float, Fast>, nit, NT, args32));
             TRY(add_kernel(inner, &n_up, &n_sp, 1, (void *)k_update<float, Fast, true>, nit, NT, args32));
@@ -380,6 +383,23 @@ cmsl_status read_flags(Engine *e, cudaStream_t st, bool *active, bool *outer)
         *active |= s.active != 0;
         if (outer) *outer |= s.outer_active != 0;
     }
+    return CMSL_OK;
+}
+
+// One FP32 residual pass (k_refine32) launched from the host.
+cmsl_status launch_refine(Engine *e, cudaStream_t st, const Dev &d, const Fields<float> &F32)
+{
+    Dev dd = d;
+    Fields<float> ff = F32;
+    void *args[] = {&dd, &ff};
+    CK(cudaLaunchKernel(e->refine_fn, dim3((unsigned)e->items.size()), dim3(NT), args, e->refine_smem, st));
+    return CMSL_OK;
+}
+
+cmsl_status launch_tdgl32(Engine *e, cudaStream_t st, const Dev &d, const Fields<float> &F32)
+{
+    k_tdgl32<T32_NS><<<(unsigned)e->items.size(), NT, T32_SMEM, st>>>(d, F32);
+    CK(cudaGetLastError());
     return CMSL_OK;
 }
 
@@ -419,8 +439,7 @@ cmsl_status solve_direct(Engine *e, cudaStream_t st, const Dev &d, const Fields<
     } else {
         for (int og = 0;; ++og) {
             if (og > e->max_refine_cap + 1) return fail(CMSL_ERR_STATE, "refinement loop did not stop");
-            k_refine<<<nit, NT, 0, st>>>(d, F32);
-            CK(cudaGetLastError());
+            TRY(launch_refine(e, st, d, F32));
             TRY(read_flags(e, st, &act, &out));
             if (act && e->spectral) {
                 TRY(spec_launch(e, st, d, F32));
@@ -454,7 +473,7 @@ cmsl_status step_direct(Engine *e, cudaStream_t st)
     const Fields<double> F64 = e->fields<double>();
     const Fields<float> F32 = e->fields<float>();
     if (e->precision == CMSL_FP64) k_tdgl<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-    else k_tdgl<float, Fast><<<nit, NT, 0, st>>>(d, F32);
+    else TRY(launch_tdgl32(e, st, d, F32));
     CK(cudaGetLastError());
     if (e->any_dep) TRY(solve_direct(e, st, d, F64, F32));
     k_step_end<<<1, 32, 0, st>>>(d);
@@ -792,6 +811,15 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     TRY(e->alloc((void **)&e->d_ctl, sizeof(Ctl)));
     TRY(ensure_schedule(e, 16, 16));
 
+    if (e->precision != CMSL_FP64) {
+        bool uni = true;
+        for (int fi = 0; fi < n; ++fi) uni &= !e->fh[fi].dep || fds[fi].uni_eps != 0;
+        e->refine_fn = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
+        e->refine_smem = uni ? r32_smem<true>() : r32_smem<false>();
+        CK(cudaFuncSetAttribute(e->refine_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem));
+        CK(cudaFuncSetAttribute((const void *)k_tdgl32<T32_NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)T32_SMEM));
+    }
     const Dev d = e->dev(0);
     if (e->precision == CMSL_FP64) k_dinv<double><<<(int)e->items.size(), NT>>>(d, (double *)e->d_dinv);
     else k_dinv<float><<<(int)e->items.size(), NT>>>(d, (float *)e->d_dinv);
@@ -991,11 +1019,11 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
             switch (kind) {
             case 0:
                 if (fp64) k_tdgl<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-                else k_tdgl<float, Fast><<<nit, NT, 0, st>>>(d, F32);
+                else TRY(launch_tdgl32(e, st, d, F32));
                 break;
             case 1:
                 if (fp64) k_rhs<double, Exact><<<nit, NT, 0, st>>>(d, F64);
-                else k_refine<<<nit, NT, 0, st>>>(d, F32);
+                else TRY(launch_refine(e, st, d, F32));
                 break;
             case 2:
                 if (fp64) {
@@ -1115,7 +1143,7 @@ cmsl_status cmsl_film_tdgl_step(cmsl_film *f, double Ez)
     const int nit = (int)f->items.size();
     const Dev d = f->dev(0);
     if (f->precision == CMSL_FP64) k_tdgl<double, Exact><<<nit, NT>>>(d, f->fields<double>());
-    else k_tdgl<float, Fast><<<nit, NT>>>(d, f->fields<float>());
+    else TRY(launch_tdgl32(f, nullptr, d, f->fields<float>()));
     k_step_end<<<1, 32>>>(d);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
@@ -1140,6 +1168,11 @@ cmsl_status cmsl_film_depol(cmsl_film *f, int32_t *iters, int32_t *status)
     S.outer_active = 1; S.active = 0; S.refine = 0; S.total_iters = 0; S.iters = 0; S.status = 0;
     CK(cudaMemcpy(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice));
     const Dev d = f->dev(0);
+    if (f->precision != CMSL_FP64) {
+        // the first residual pass reads the warm start from the free buffer
+        k_extrap<<<(unsigned)f->items.size(), NT>>>(d);
+        CK(cudaGetLastError());
+    }
     TRY(solve_direct(f, nullptr, d, F64, F32));
     CK(cudaDeviceSynchronize());
     CK(cudaMemcpy(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost));

@@ -9,6 +9,7 @@
 #include "kernels.cuh"
 #include "pcg_persist.cuh"
 #include "spectral.cuh"
+#include "stencil32.cuh"
 
 namespace cmsl_eng {
 
@@ -76,6 +77,10 @@ struct Engine {
     cudaStream_t stream = nullptr;
     // FP32_REFINED inner solver: the persistent cooperative kernel, or the
     // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
+    // FP32_REFINED stencil passes (stencil32.cuh): the residual pass for
+    // one-eps films (all films) or the general one, and their ring sizes
+    void *refine_fn = nullptr;
+    size_t refine_smem = 0;
     bool spectral = false;      // FP32 inner solve by the direct spectral solve (one film, uniform eps)
     SpecDev spec{};
     int spec_grid[3] = {0, 0, 0};

@@ -228,6 +228,8 @@ __device__ __forceinline__ void op_z(const FilmDev *f, int k, V up, V dn, V &u, 
     else { u = dn; dd = dn; }
 }
 
+__device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)[7], double (&sTot)[7]);
+
 // ---------------------------------------------------------- TDGL kernel
 // kernelCalc_antiferro (kernels_evol.cu:47-231) + Calc_EfieldMag
 // (depol_varEPS.cu:223-276) of the previous potential + the sweep-row sums
@@ -431,7 +433,14 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
         }
     }
     if (!ticket_last(d.counter)) return;
-    // last block: finish the rows, reset the per-step solver state
+    tdgl_finish(d, rs, sRed, sTot);
+}
+
+// Last block of a TDGL step: every film's sweep row from its items' partial
+// sums (evolve.cu:256-357 scaled as in :391-400), and the per-step reset of
+// the solver state.
+__device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)[7], double (&sTot)[7])
+{
     for (int fi = 0; fi < d.n_films; ++fi) {
         const FilmDev *ff = d.films + fi;
         const int frow = d.rows[(long long)fi * d.wstride + rs];
@@ -609,146 +618,17 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
     start_solves(d, sRed, sTot);
 }
 
-// ----------------------------- FP32 refinement: double-float residual pass
+// ----------------------------- FP32 refinement: end of a residual pass
 // The potential of CMSL_FP32_REFINED is stored as double-float (hi half at
-// cell c, lo half at cell ncells + c of the same buffer).  This pass applies
-// the pending FP32 correction (phi += delta) -- or, on the first pass of a
-// step, the extrapolated warm start -- forms b from the new Pm and the
-// residual r = b - A phi in double-float, tests ||r|| <= refine_tol ||b||, and
-// seeds the next inner FP32 solve with r.  No FP64 instruction is executed.
-__device__ __forceinline__ df phi_ld(const float *h, const float *l, long long o) { return df{h[o], l[o]}; }
-
-static __global__ void __launch_bounds__(NT) k_refine(Dev d, Fields<float> F)
+// cell c, lo half at cell ncells + c of the same buffer) in five rotating
+// buffers: the current one, the three before it (extrapolated warm start) and
+// a free one.  A residual pass (k_refine32, stencil32.cuh) forms r = b - A phi
+// in double-float; in the last block this function takes every film's
+// reduced r.r, b.b and r.D^-1.r, applies the refinement stop test
+// ||r|| <= refine_tol ||b||, rotates the buffers and sets the next inner
+// solve's target.
+__device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], double (&sTot)[3])
 {
-    __shared__ float sX[SPL], sY[SPL], sFh[SPL], sFl[SPL];
-    __shared__ int sM[SPL];
-    __shared__ float sCh[9], sCl[9];
-    __shared__ double sRedA[NT / 32][3];
-    __shared__ double sRed[NT / 32][3];
-    __shared__ double sTot[3];
-    const int4 it = d.items[blockIdx.x];
-    const FilmDev *f = d.films + it.x;
-    const SolveDev *S0 = d.solve + it.x;
-    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    const Geom g = make_geom(f, it.y, it.z);
-    const int nz = g.nz;
-    const bool run = f->dep_flag != 0 && (d.force || S0->outer_active);
-    const bool apply = S0->refine > 0;   // a correction is pending after the first pass
-    const int cur = d.ctl->cur, pc = S0->phi_cur, pp = S0->phi_prev, pq = S0->phi_prev2, pr = S0->phi_prev3;
-    const int pf = 10 - pc - pp - pq - pr;        // the free buffer of the five
-    // first pass: extrapolated warm start (linear, quadratic or cubic)
-    const int extrap = apply ? 0 : f->warm;
-    const long long off = f->off, lo = d.ncells;
-    if (threadIdx.x < 9) { sCh[threadIdx.x] = f->cf_h[threadIdx.x]; sCl[threadIdx.x] = f->cf_l[threadIdx.x]; }
-    const float *Pmx = F.P[cur ^ 1][0] + off, *Pmy = F.P[cur ^ 1][1] + off, *Pmz = F.P[cur ^ 1][2] + off;
-    const float *ph = (const float *)phi_sel(d, pc) + off, *pl_ = ph + lo;
-    const float *qh = (const float *)phi_sel(d, pp) + off, *ql = qh + lo;
-    const float *uh = (const float *)phi_sel(d, pq) + off, *ul = uh + lo;
-    const float *vh = (const float *)phi_sel(d, pr) + off, *vl = vh + lo;
-    float *nh = (float *)phi_sel(d, pf) + off, *nl = nh + lo;
-    const float *dx = F.x + off;
-    const uint32_t *code = d.code + off;
-    float *r = F.r + off;
-    const float *dinv = F.dinv + off;
-    const df cb = df{f->cb_h, f->cb_l};
-    float acc[3] = {0.f, 0.f, 0.f};
-    __syncthreads();
-    if (run) {
-        df xd{0, 0}, xc{0, 0}, xu{0, 0}, hx{0, 0};
-        float zd = 0, zc = 0, zu = 0, hPx = 0, hPy = 0;
-        int md = 0, mc = 0, mu = 0, hm = 0;
-        auto eff = [&](long long o) -> df {
-            const df a = phi_ld(ph, pl_, o);
-            if (apply) return df_add_f(a, dx[o]);
-            if (extrap == 1) return df_sub(df{2.f * a.h, 2.f * a.l}, phi_ld(qh, ql, o));
-            if (extrap == 2) return df_add(df_mul_f(df_sub(a, phi_ld(qh, ql, o)), 3.f), phi_ld(uh, ul, o));
-            if (extrap == 3)
-                return df_sub(df_sub(df_mul_f(df_add(a, phi_ld(uh, ul, o)), 4.f), df_mul_f(phi_ld(qh, ql, o), 6.f)),
-                              phi_ld(vh, vl, o));
-            return a;
-        };
-        auto ld_own = [&](int k, df &xv, float &zv, int &mv) {
-            const long long o = g.own_pl + (long long)k * g.plane;
-            xv = eff(o); zv = Pmz[o]; mv = code_mat(code[o]);
-        };
-        if (g.valid) {
-            ld_own(z0, xc, zc, mc);
-            ld_own(z0 > 0 ? z0 - 1 : z0, xd, zd, md);
-            ld_own(z0 + 1 < nz ? z0 + 1 : z0, xu, zu, mu);
-        }
-        auto ld_halo = [&](int k) {
-            const long long o = g.halo_pl + (long long)k * g.plane;
-            hx = eff(o); hPx = Pmx[o]; hPy = Pmy[o]; hm = code_mat(code[o]);
-        };
-        if (g.halo) ld_halo(z0);
-        for (int k = z0; k < z1; ++k) {
-            __syncthreads();
-            if (g.valid) {
-                const long long o = g.own_pl + (long long)k * g.plane;
-                sFh[g.own_slot] = xc.h; sFl[g.own_slot] = xc.l;
-                sX[g.own_slot] = Pmx[o]; sY[g.own_slot] = Pmy[o]; sM[g.own_slot] = mc;
-            }
-            if (g.halo) {
-                sFh[g.halo_slot] = hx.h; sFl[g.halo_slot] = hx.l;
-                sX[g.halo_slot] = hPx; sY[g.halo_slot] = hPy; sM[g.halo_slot] = hm;
-            }
-            __syncthreads();
-            df xn2{0, 0}; float zn2 = 0; int mn2 = 0;
-            const bool pre = g.valid && (k + 2 < nz) && (k + 1 < z1);
-            if (pre) ld_own(k + 2, xn2, zn2, mn2);
-            if (g.halo && k + 1 < z1) ld_halo(k + 1);
-            if (g.valid) {
-                const int s0 = g.own_slot;
-                const long long o = g.own_pl + (long long)k * g.plane;
-                df b, ax;
-                if (identity_row(f, k, g.own_pl)) {
-                    b = df{0.f, 0.f};
-                    ax = xc;                             // x - g, g = 0
-                } else {
-                    // b = -eps_0_nd div(Pm), differences of FP32 values are exact in df
-                    const float pzu = (k == nz - 1) ? zc : zu, pzd = (k == 0) ? zc : zd;
-                    df dv = df_add(df_add(two_sum(sX[s0 + 1], -sX[s0 - 1]), two_sum(sY[s0 + SX], -sY[s0 - SX])),
-                                   two_sum(pzu, -pzd));
-                    b = df_neg(df_mul(dv, cb));
-                    df u, dd; int mmu, mmd;
-                    op_z<df>(f, k, xu, xd, u, dd);
-                    op_z<int>(f, k, mu, md, mmu, mmd);
-                    const df xe{sFh[s0 + 1], sFl[s0 + 1]}, xw{sFh[s0 - 1], sFl[s0 - 1]};
-                    const df xn{sFh[s0 + SX], sFl[s0 + SX]}, xs{sFh[s0 - SX], sFl[s0 - SX]};
-                    const int m3 = mc * 3;
-                    auto cf = [&](int mnb) { return df{sCh[m3 + mnb], sCl[m3 + mnb]}; };
-                    df a = df_sub(df_mul(cf(sM[s0 + 1]), df_sub(xe, xc)), df_mul(cf(sM[s0 - 1]), df_sub(xc, xw)));
-                    a = df_add(a, df_mul(cf(sM[s0 + SX]), df_sub(xn, xc)));
-                    a = df_sub(a, df_mul(cf(sM[s0 - SX]), df_sub(xc, xs)));
-                    a = df_add(a, df_mul(cf(mmu), df_sub(u, xc)));
-                    a = df_sub(a, df_mul(cf(mmd), df_sub(xc, dd)));
-                    ax = df_neg(a);
-                }
-                const df rr = df_sub(b, ax);
-                nh[o] = xc.h; nl[o] = xc.l;
-                const float rv = rr.h + rr.l;
-                r[o] = rv;
-                acc[0] = fmaf(rv, rv, acc[0]);
-                acc[1] = fmaf(b.h, b.h, acc[1]);
-                const float dd = f->uni_eps ? (identity_row(f, k, g.own_pl) ? 1.f : f->dinv_uni) : dinv[o];
-                acc[2] = fmaf(rv, rv * dd, acc[2]);
-            }
-            if (g.valid) {
-                xd = xc; xc = xu; zd = zc; zc = zu; md = mc; mc = mu;
-                if (pre) { xu = xn2; zu = zn2; mu = mn2; }
-            }
-        }
-    }
-    {
-        double t[3];
-        block_sum<3, float>(acc, sRedA, t);
-        if (threadIdx.x == 0) {
-            d.partial[(long long)blockIdx.x * NPART + 0] = t[0];
-            d.partial[(long long)blockIdx.x * NPART + 1] = t[1];
-            d.partial[(long long)blockIdx.x * NPART + 2] = t[2];
-        }
-    }
-    if (!ticket_last(d.counter)) return;
     int any_outer = 0, any_inner = 0;
     for (int fi = 0; fi < d.n_films; ++fi) {
         const FilmDev *ff = d.films + fi;

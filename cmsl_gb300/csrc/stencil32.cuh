@@ -1,0 +1,463 @@
+// stencil32.cuh -- the CMSL_FP32_REFINED stencil passes: the TDGL step and
+// the double-float residual pass of the depolarisation solve.
+//
+// Same work items as the FP64 kernels (a TX x TY column tile of one film
+// marching through z0..z1), but every plane of every field a pass reads is
+// brought into a ring of NS shared-memory stages by 4-byte cp.async copies
+// (each thread its own cell and at most one x/y halo cell), NS-3 planes ahead
+// of the plane being computed.  The z neighbours are read from the ring as
+// well, so a thread carries no plane-to-plane state beyond its partial sums,
+// several blocks share an SM, and each plane costs one barrier.
+//
+// Ring protocol (identical in both kernels): planes zlo = max(z0-1, 0) ..
+// zhi = min(z1, nz-1) are staged, plane p in stage (p - zlo) % NS, one
+// commit group per plane (empty groups keep the count uniform across
+// threads).  Before computing plane k a thread waits until plane k+1 has
+// landed (NS-4 younger groups may still be in flight), the block syncs --
+// which also retires every read of plane k-2 -- and plane k+NS-2 is issued
+// into that stage.
+#pragma once
+#include "kernels.cuh"
+
+namespace cmsl {
+
+__device__ __forceinline__ void cp4(void *dst, const void *src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Warm start of a step's first refinement pass (own cell): 0 the previous
+// potential a, 1 linear 2a - q, 2 quadratic 3(a - q) + u, 3 cubic
+// 4(a + u) - 6q - v, with a, q, u, v the potentials of steps n .. n-3.
+__device__ __forceinline__ df extrap_phi(int warm, df a, df q, df u, df v)
+{
+    if (warm == 1) return df_sub(df{2.f * a.h, 2.f * a.l}, q);
+    if (warm == 2) return df_add(df_mul_f(df_sub(a, q), 3.f), u);
+    if (warm == 3) return df_sub(df_sub(df_mul_f(df_add(a, u), 4.f), df_mul_f(q, 6.f)), v);
+    return a;
+}
+
+// The free one of the five potential buffers of film S.
+__device__ __forceinline__ int phi_free(const SolveDev *S)
+{
+    return 10 - S->phi_cur - S->phi_prev - S->phi_prev2 - S->phi_prev3;
+}
+
+// ------------------------------------------------------------ TDGL step
+// kernelCalc_antiferro (kernels_evol.cu:47-231) with E_dep of the current
+// potential (depol_varEPS.cu:223-276) and the sweep-row sums
+// (evolve.cu:256-357) in FP32, plus the warm start of the coming solve:
+// the extrapolated potential is written to the film's free buffer, which the
+// step's first residual pass then reads.
+constexpr int T32_NS = 4;
+constexpr int T32_STAGE = 8 * SPL + NT;      // floats: P[6], phi hi, phi lo (own + halo); code (own)
+constexpr size_t T32_SMEM = sizeof(float) * T32_NS * T32_STAGE;
+
+template <int NS>
+__global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
+{
+    static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
+    extern __shared__ float4 smem_t32[];
+    float *ring = (float *)smem_t32;
+    __shared__ Coef<float> sC[6];
+    __shared__ double sRed[NT / 32][7];
+    __shared__ double sTot[7];
+    const int4 it = d.items[blockIdx.x];
+    const FilmDev *f = d.films + it.x;
+    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
+    if (threadIdx.x < 6) sC[threadIdx.x] = f->coef32[threadIdx.x];
+    const Geom g = make_geom(f, it.y, it.z);
+    const int cur = d.ctl->cur, rs = d.ctl->run_step;
+    const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
+    const int row = d.rows[(long long)it.x * d.wstride + rs];
+    const int dep = f->dep_flag, nz = g.nz;
+    const long long off = f->off, lo = d.ncells;
+    const SolveDev *S = d.solve + it.x;
+    const float *ph = (const float *)phi_sel(d, S->phi_cur) + off;
+    const float *qh = (const float *)phi_sel(d, S->phi_prev) + off;
+    const float *uh = (const float *)phi_sel(d, S->phi_prev2) + off;
+    const float *vh = (const float *)phi_sel(d, S->phi_prev3) + off;
+    float *nh = (float *)phi_sel(d, phi_free(S)) + off;
+    const int warm = f->warm;
+    const uint32_t *code = d.code + off;
+    const float inv_2hf = f->inv_2hf;
+    const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
+
+    auto Pold = [&](int q) { return (cur ? F.P[1][q] : F.P[0][q]) + off; };
+    auto stage = [&](int p) { return ring + ((p - zlo) % NS) * T32_STAGE; };
+    auto issue = [&](int p) {
+        if (p <= zhi) {
+            float *st = stage(p);
+            const long long pp = (long long)p * g.plane;
+            if (g.valid) {
+                const long long o = g.own_pl + pp;
+                #pragma unroll
+                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.own_slot, Pold(q) + o);
+                if (dep) {
+                    cp4(st + 6 * SPL + g.own_slot, ph + o);
+                    cp4(st + 7 * SPL + g.own_slot, ph + lo + o);
+                }
+                cp4(st + 8 * SPL + threadIdx.x, code + o);
+            }
+            if (g.halo) {
+                const long long o = g.halo_pl + pp;
+                #pragma unroll
+                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.halo_slot, Pold(q) + o);
+                if (dep) {
+                    cp4(st + 6 * SPL + g.halo_slot, ph + o);
+                    cp4(st + 7 * SPL + g.halo_slot, ph + lo + o);
+                }
+            }
+        }
+        cp_commit();
+    };
+    for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p);
+
+    float acc[7];
+    #pragma unroll
+    for (int q = 0; q < 7; ++q) acc[q] = 0.f;
+    const int s0 = g.own_slot;
+    for (int k = z0; k < z1; ++k) {
+        cp_wait<NS - 4>();
+        __syncthreads();
+        issue(k + NS - 2);
+        if (!g.valid) continue;
+        const long long o = g.own_pl + (long long)k * g.plane;
+        // older potentials for the warm start (consumed after the step's arithmetic)
+        df wq{0.f, 0.f}, wu{0.f, 0.f}, wv{0.f, 0.f};
+        if (dep && warm >= 1) wq = df{qh[o], qh[lo + o]};
+        if (dep && warm >= 2) wu = df{uh[o], uh[lo + o]};
+        if (dep && warm >= 3) wv = df{vh[o], vh[lo + o]};
+        const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
+        const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
+        const uint32_t c = ((const uint32_t *)sk)[8 * SPL + threadIdx.x];
+        const int gid = code_gid(c), mat = code_mat(c);
+        const Coef<float> K = sC[mat * 2 + code_iface(c)];
+        const float *trp = F.TR + 9LL * (f->g_off + gid);
+        float t[9];
+        #pragma unroll
+        for (int q = 0; q < 9; ++q) t[q] = __ldg(trp + q);
+        float pc[6], sum[6];
+        #pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float *a = sk + q * SPL;
+            pc[q] = a[s0];
+            // neighbour sums e, w, n, s, u, d (kernels_evol.cu:101-122); z clamped
+            float sm = a[s0 + 1] + a[s0 - 1];
+            sm = sm + a[s0 + SX];
+            sm = sm + a[s0 - SX];
+            sm = sm + su[q * SPL + s0];
+            sum[q] = sm + sd[q * SPL + s0];
+        }
+        float ex = 0.f, ey = 0.f, ez = 0.f;
+        df a0{0.f, 0.f};
+        if (dep) {
+            const float *fh = sk + 6 * SPL, *fl = sk + 7 * SPL;
+            a0 = df{fh[s0], fl[s0]};
+            const df fu{su[6 * SPL + s0], su[7 * SPL + s0]}, fd{sd[6 * SPL + s0], sd[7 * SPL + s0]};
+            df pu, pd;
+            if (f->zbc == 0) {
+                pu = (k == nz - 1) ? df{0.f, 0.f} : fu;
+                pd = (k == 0) ? df{0.f, 0.f} : fd;
+            } else {
+                op_z<df>(f, k, fu, fd, pu, pd);
+            }
+            // -1 * E with E = -(phi_+ - phi_-) / (2h)  (depol_varEPS.cu:246-273)
+            ex = phi_diff(df{fh[s0 + 1], fl[s0 + 1]}, df{fh[s0 - 1], fl[s0 - 1]}) * inv_2hf;
+            ey = phi_diff(df{fh[s0 + SX], fl[s0 + SX]}, df{fh[s0 - SX], fl[s0 - SX]}) * inv_2hf;
+            ez = phi_diff(pu, pd) * inv_2hf;
+        }
+        // crystal frame (kernels_evol.cu:162-168)
+        const float pMXl = t[0] * pc[0] + t[1] * pc[1] + t[2] * pc[2];
+        const float pMYl = t[3] * pc[0] + t[4] * pc[1] + t[5] * pc[2];
+        const float pMZl = t[6] * pc[0] + t[7] * pc[1] + t[8] * pc[2];
+        const float pSXl = t[0] * pc[3] + t[1] * pc[4] + t[2] * pc[5];
+        const float pSYl = t[3] * pc[3] + t[4] * pc[4] + t[5] * pc[5];
+        const float pSZl = t[6] * pc[3] + t[7] * pc[4] + t[8] * pc[5];
+        // two-sublattice Landau derivative (kernels_evol.cu:178-199)
+        const float dmx = K.a02 * pMXl, dmy = K.a02 * pMYl;
+        const float dsx = K.a02 * pSXl, dsy = K.a02 * pSYl;
+        const float m2 = pMZl * pMZl, m3 = m2 * pMZl, m4 = m3 * pMZl, m5 = m4 * pMZl;
+        const float q2 = pSZl * pSZl, q3 = q2 * pSZl, q4 = q3 * pSZl, q5 = q4 * pSZl;
+        float dmz = K.ag * pMZl + K.b4 * m3;
+        dmz = dmz + K.b12 * pMZl * q2;
+        dmz = dmz + K.g6 * (m5 + 10.f * m3 * q2 + 5.f * pMZl * q4);
+        float dsz = K.ags * pSZl + K.b4 * q3;
+        dsz = dsz + K.b12 * pSZl * m2;
+        dsz = dsz + K.g6 * (q5 + 10.f * m2 * q3 + 5.f * pSZl * m4);
+        // back to the lab frame (kernels_evol.cu:202-208) + fields (:210-220)
+        float b[6];
+        b[0] = t[0] * dmx + t[3] * dmy + t[6] * dmz + ex;
+        b[1] = t[1] * dmx + t[4] * dmy + t[7] * dmz + ey;
+        b[2] = t[2] * dmx + t[5] * dmy + t[8] * dmz + (mEz + ez);
+        b[3] = t[0] * dsx + t[3] * dsy + t[6] * dsz;
+        b[4] = t[1] * dsx + t[4] * dsy + t[7] * dsz;
+        b[5] = t[2] * dsx + t[5] * dsy + t[8] * dsz;
+        // explicit Euler with the 6-neighbour Laplacian (kernels_evol.cu:223-229)
+        float pn[6];
+        #pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            pn[q] = pc[q] * K.relax + K.A * sum[q] - K.LdT * b[q];
+            (cur ? F.P[0][q] : F.P[1][q])[off + o] = pn[q];
+        }
+        if (row >= 0) {
+            acc[0] += pn[2];
+            acc[1] += pn[5];
+            acc[2] += pMZl;
+            acc[3] += pSZl;
+            acc[4] += (mat == 1) ? pn[2] : 0.f;
+            acc[5] += (mat == 0) ? pn[2] : 0.f;
+            acc[6] += (mat == 2) ? pn[2] : 0.f;
+        }
+        if (dep) {
+            const df w = extrap_phi(warm, a0, wq, wu, wv);
+            nh[o] = w.h;
+            nh[lo + o] = w.l;
+        }
+    }
+    cp_wait<0>();
+
+    if (row >= 0) {
+        double tot[7];
+        block_sum<7, float>(acc, sRed, tot);
+        if (threadIdx.x == 0) {
+            #pragma unroll
+            for (int q = 0; q < 7; ++q) d.partial[(long long)blockIdx.x * NPART + q] = tot[q];
+        }
+    }
+    if (!ticket_last(d.counter)) return;
+    tdgl_finish(d, rs, sRed, sTot);
+}
+
+// Warm start alone (own cells): the free buffer of every depolarised film
+// gets the extrapolated potential.  Used before a solve that does not follow
+// a TDGL step (cmsl_film_depol).
+static __global__ void __launch_bounds__(NT) k_extrap(Dev d)
+{
+    const int4 it = d.items[blockIdx.x];
+    const FilmDev *f = d.films + it.x;
+    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
+    const Geom g = make_geom(f, it.y, it.z);
+    if (!f->dep_flag || !g.valid) return;
+    const SolveDev *S = d.solve + it.x;
+    const long long off = f->off, lo = d.ncells;
+    const float *ph = (const float *)phi_sel(d, S->phi_cur) + off;
+    const float *qh = (const float *)phi_sel(d, S->phi_prev) + off;
+    const float *uh = (const float *)phi_sel(d, S->phi_prev2) + off;
+    const float *vh = (const float *)phi_sel(d, S->phi_prev3) + off;
+    float *nh = (float *)phi_sel(d, phi_free(S)) + off;
+    for (int k = z0; k < z1; ++k) {
+        const long long o = g.own_pl + (long long)k * g.plane;
+        const df w = extrap_phi(f->warm, df{ph[o], ph[lo + o]}, df{qh[o], qh[lo + o]}, df{uh[o], uh[lo + o]},
+                                df{vh[o], vh[lo + o]});
+        nh[o] = w.h;
+        nh[lo + o] = w.l;
+    }
+}
+
+// ------------------------------------------------- double-float residual
+// One refinement pass of CMSL_FP32_REFINED's depolarisation solve: with x the
+// potential -- on a step's first pass the warm start in the free buffer, on
+// later passes the current potential plus the pending FP32 correction dx of
+// the inner solve, written to the free buffer -- form b = -eps_0_nd div Pm
+// (depol_varEPS.cu:279-329, zero on the Dirichlet planes / Neumann pin) and
+// r = b - A x in double-float, and the partial sums r.r, b.b, r.D^-1.r.
+// A x is split as A phi (double-float) + A dx (FP32: |A dx| ~ |r| is small,
+// so FP32 rounding there is far below the refinement target).  UNI: every
+// material has the same eps, the operator is eps/h^2 times the 7-point
+// Laplacian (one double-float product per cell, no material codes).
+// No FP64 instruction is executed.
+constexpr int R32_NS = 5;
+template <bool UNI> struct R32Lay {
+    static constexpr int FH = 0, FL = SPL, DX = 2 * SPL, PX = 3 * SPL, PY = 4 * SPL, PZ = 5 * SPL;
+    static constexpr int CODE = 5 * SPL + NT, DINV = 6 * SPL + NT;   // general eps only
+    static constexpr int STAGE = UNI ? 5 * SPL + NT : 6 * SPL + 2 * NT;
+};
+template <bool UNI> constexpr size_t r32_smem() { return sizeof(float) * R32_NS * R32Lay<UNI>::STAGE; }
+
+// sum of six double-float values minus 6 c; the hi parts are summed error-free
+__device__ __forceinline__ df lap7(df e, df w, df n, df s, df u, df dn, df c)
+{
+    df t = two_sum(e.h, w.h);
+    float l = t.l + (e.l + w.l);
+    df t2 = two_sum(t.h, n.h);
+    l += t2.l + n.l;
+    t = two_sum(t2.h, s.h);
+    l += t.l + s.l;
+    t2 = two_sum(t.h, u.h);
+    l += t2.l + u.l;
+    t = two_sum(t2.h, dn.h);
+    l += t.l + dn.l;
+    const df p = two_prod(c.h, -6.f);
+    l += fmaf(c.l, -6.f, p.l);
+    t2 = two_sum(t.h, p.h);
+    l += t2.l;
+    return fast_two_sum(t2.h, l);
+}
+
+// (a - b) + (c - e) + (g - h) of FP32 values as double-float (hi parts error-free)
+__device__ __forceinline__ df div3(float a, float b, float c, float e, float g, float h)
+{
+    const df x = two_sum(a, -b), y = two_sum(c, -e), z = two_sum(g, -h);
+    const df s = two_sum(x.h, y.h);
+    float l = s.l + (x.l + y.l);
+    const df s2 = two_sum(s.h, z.h);
+    l += s2.l + z.l;
+    return fast_two_sum(s2.h, l);
+}
+
+template <bool UNI, int NS>
+__global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
+{
+    static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
+    using L = R32Lay<UNI>;
+    extern __shared__ float4 smem_r32[];
+    float *ring = (float *)smem_r32;
+    __shared__ double sRed[NT / 32][3];
+    __shared__ double sTot[3];
+    const int4 it = d.items[blockIdx.x];
+    const FilmDev *f = d.films + it.x;
+    const SolveDev *S = d.solve + it.x;
+    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
+    const Geom g = make_geom(f, it.y, it.z);
+    const int nz = g.nz;
+    const bool run = f->dep_flag != 0 && (d.force || S->outer_active);
+    const bool apply = S->refine > 0;     // later pass: x = phi + dx; first pass: x = the warm start
+    const int cur = d.ctl->cur;
+    const int fr = phi_free(S);
+    const long long off = f->off, lo = d.ncells;
+    const float *xh = (const float *)phi_sel(d, apply ? S->phi_cur : fr) + off;
+    float *nh = (float *)phi_sel(d, fr) + off;
+    const float *dx = F.x + off;
+    const float *Pmx = (cur ? F.P[0][0] : F.P[1][0]) + off;
+    const float *Pmy = (cur ? F.P[0][1] : F.P[1][1]) + off;
+    const float *Pmz = (cur ? F.P[0][2] : F.P[1][2]) + off;
+    const uint32_t *code = d.code + off;
+    const float *dinv = F.dinv + off;
+    float *r = F.r + off;
+    const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
+
+    auto stage = [&](int p) { return ring + ((p - zlo) % NS) * L::STAGE; };
+    auto issue = [&](int p) {
+        if (run && p <= zhi) {
+            float *st = stage(p);
+            const long long pp = (long long)p * g.plane;
+            if (g.valid) {
+                const long long o = g.own_pl + pp;
+                const int s = g.own_slot;
+                cp4(st + L::FH + s, xh + o);
+                cp4(st + L::FL + s, xh + lo + o);
+                if (apply) cp4(st + L::DX + s, dx + o);
+                cp4(st + L::PX + s, Pmx + o);
+                cp4(st + L::PY + s, Pmy + o);
+                cp4(st + L::PZ + threadIdx.x, Pmz + o);
+                if (!UNI) {
+                    cp4(st + L::CODE + s, code + o);
+                    cp4(st + L::DINV + threadIdx.x, dinv + o);
+                }
+            }
+            if (g.halo) {
+                const long long o = g.halo_pl + pp;
+                const int s = g.halo_slot;
+                cp4(st + L::FH + s, xh + o);
+                cp4(st + L::FL + s, xh + lo + o);
+                if (apply) cp4(st + L::DX + s, dx + o);
+                cp4(st + L::PX + s, Pmx + o);
+                cp4(st + L::PY + s, Pmy + o);
+                if (!UNI) cp4(st + L::CODE + s, code + o);
+            }
+        }
+        cp_commit();
+    };
+    for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p);
+
+    const df cb{f->cb_h, f->cb_l};
+    const df cu{f->cf_h[0], f->cf_l[0]};     // UNI: eps/h^2 on every face
+    const float dinv_uni = f->dinv_uni;
+    const int s0 = g.own_slot;
+    float acc[3] = {0.f, 0.f, 0.f};
+    for (int k = z0; k < z1; ++k) {
+        cp_wait<NS - 4>();
+        __syncthreads();
+        issue(k + NS - 2);
+        if (!run || !g.valid) continue;
+        const long long o = g.own_pl + (long long)k * g.plane;
+        const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
+        const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
+        auto X = [&](const float *st, int s) { return df{st[L::FH + s], st[L::FL + s]}; };
+        auto D = [&](const float *st, int s) { return apply ? st[L::DX + s] : 0.f; };
+        const df xc = X(sk, s0);
+        const float dc = D(sk, s0);
+        float rv, bh, dd;
+        if (identity_row(f, k, g.own_pl)) {
+            // x - g with g = 0, b = 0
+            rv = -(xc.h + (xc.l + dc));
+            bh = 0.f;
+            dd = 1.f;
+        } else {
+            const int tz = threadIdx.x;
+            const df bm = df_mul(div3(sk[L::PX + s0 + 1], sk[L::PX + s0 - 1], sk[L::PY + s0 + SX],
+                                      sk[L::PY + s0 - SX], su[L::PZ + tz], sd[L::PZ + tz]),
+                                 cb);   // -b
+            df xu, xd;
+            op_z<df>(f, k, X(su, s0), X(sd, s0), xu, xd);
+            float du, ddn;
+            op_z<float>(f, k, D(su, s0), D(sd, s0), du, ddn);
+            const df xe = X(sk, s0 + 1), xw = X(sk, s0 - 1), xn = X(sk, s0 + SX), xs = X(sk, s0 - SX);
+            const float de = D(sk, s0 + 1), dw = D(sk, s0 - 1), dn = D(sk, s0 + SX), ds = D(sk, s0 - SX);
+            df s;            // b - A phi
+            float rd;        // - A dx
+            if (UNI) {
+                s = df_sub(df_mul(cu, lap7(xe, xw, xn, xs, xu, xd, xc)), bm);
+                rd = cu.h * ((de + dw) + (dn + ds) + (du + ddn) - 6.f * dc);
+                dd = dinv_uni;
+            } else {
+                const uint32_t *cs = (const uint32_t *)sk;
+                const int m3 = code_mat(cs[L::CODE + s0]) * 3;
+                int mu, md;
+                op_z<int>(f, k, code_mat(((const uint32_t *)su)[L::CODE + s0]),
+                          code_mat(((const uint32_t *)sd)[L::CODE + s0]), mu, md);
+                const int me = m3 + code_mat(cs[L::CODE + s0 + 1]), mw = m3 + code_mat(cs[L::CODE + s0 - 1]);
+                const int mn = m3 + code_mat(cs[L::CODE + s0 + SX]), ms = m3 + code_mat(cs[L::CODE + s0 - SX]);
+                auto cf = [&](int i) { return df{f->cf_h[i], f->cf_l[i]}; };
+                df a = df_sub(df_mul(cf(me), df_sub(xe, xc)), df_mul(cf(mw), df_sub(xc, xw)));
+                a = df_add(a, df_mul(cf(mn), df_sub(xn, xc)));
+                a = df_sub(a, df_mul(cf(ms), df_sub(xc, xs)));
+                a = df_add(a, df_mul(cf(m3 + mu), df_sub(xu, xc)));
+                a = df_sub(a, df_mul(cf(m3 + md), df_sub(xc, xd)));
+                s = df_sub(a, bm);
+                rd = f->cf_h[me] * (de - dc) - f->cf_h[mw] * (dc - dw) + f->cf_h[mn] * (dn - dc) -
+                     f->cf_h[ms] * (dc - ds) + f->cf_h[m3 + mu] * (du - dc) - f->cf_h[m3 + md] * (dc - ddn);
+                dd = sk[L::DINV + tz];
+            }
+            rv = s.h + (s.l + rd);
+            bh = -bm.h;
+        }
+        r[o] = rv;
+        if (apply) {
+            const df nv = df_add_f(xc, dc);
+            nh[o] = nv.h;
+            nh[lo + o] = nv.l;
+        }
+        acc[0] = fmaf(rv, rv, acc[0]);
+        acc[1] = fmaf(bh, bh, acc[1]);
+        acc[2] = fmaf(rv, rv * dd, acc[2]);
+    }
+    cp_wait<0>();
+    {
+        double t[3];
+        block_sum<3, float>(acc, sRed, t);
+        if (threadIdx.x == 0) {
+            d.partial[(long long)blockIdx.x * NPART + 0] = t[0];
+            d.partial[(long long)blockIdx.x * NPART + 1] = t[1];
+            d.partial[(long long)blockIdx.x * NPART + 2] = t[2];
+        }
+    }
+    if (!ticket_last(d.counter)) return;
+    refine_finish(d, sRed, sTot);
+}
+
+}  // namespace cmsl
