@@ -559,7 +559,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             if (!d.dep_flag) continue;
             anydep = true;
             const bool uni = d.mats[0].eps_r == d.mats[1].eps_r && d.mats[1].eps_r == d.mats[2].eps_r;
-            ok &= d.zbc == CMSL_DIRICHLET && uni && spec_radix_ok(d.nx) && spec_radix_ok(d.ny);
+            ok &= d.zbc == CMSL_DIRICHLET && uni && d.nz >= 3 && spec_radix_ok(d.nx) && spec_radix_ok(d.ny);
             spec_mmax = std::max(spec_mmax, d.nz - 2);
         }
         ok &= anydep && spec_zthreads(spec_mmax) > 0;
@@ -754,17 +754,18 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             P.bx0 = (int)bxf.size(); P.by0 = (int)byf.size(); P.bz0 = (int)bzf.size();
             if (!h.dep) continue;                                    // no solve, no blocks
             P.M = h.nz - 2;
+            P.Mp = (P.M + 1) / 2;
             P.ax = spec_plan(h.nx);
             P.ay = spec_plan(h.ny);
             P.coff = coff;
-            coff += (long long)P.M * h.nx * h.ny;
+            coff += (long long)P.Mp * h.nx * h.ny;
             const double eps = descs[fi].mats[0].eps_r;              // harm(eps, eps) = eps on every face
             P.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
             tables(h.nx, &P.twx, &P.lamx);
             tables(h.ny, &P.twy, &P.lamy);
             const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
-            const long long gx = ((long long)P.M * h.ny + rbx - 1) / rbx;
-            const long long gy = (long long)P.M * ((h.nx + cby - 1) / cby);
+            const long long gx = ((long long)P.Mp * h.ny + rbx - 1) / rbx;
+            const long long gy = (long long)P.Mp * ((h.nx + cby - 1) / cby);
             const long long gz = ((long long)h.nx * h.ny + zt - 1) / zt;
             bxf.insert(bxf.end(), (size_t)gx, fi);
             byf.insert(byf.end(), (size_t)gy, fi);

@@ -7,10 +7,15 @@
 // Fourier transform diagonalises the x/y part (eigenvalues 2 - 2 cos(2 pi m / n)),
 // which leaves one real tridiagonal system along z per in-plane mode:
 //   (lam_x + lam_y + 2) X_k - X_{k-1} - X_{k+1} = (h^2 / eps) R_k.
-// The solve is: 2D FFT of every interior plane of r -> Thomas algorithm per
-// mode -> inverse 2D FFT (as the forward transform of the conjugate, the
-// system being real) -> x.  It is exact up to FP32 rounding (~1e-6 relative),
-// so one solve per refinement pass replaces the PCG iterations; the outer
+// The solve is: 2D FFT of the interior planes of r -> Thomas algorithm per
+// mode -> inverse 2D FFT (as the forward transform of the conjugate) -> x.
+// r and x are real, so interior planes 2j and 2j+1 travel as the real and
+// imaginary parts of one complex plane j (half the transforms); the z solve
+// separates a mode m and its mirror -m of the packed spectrum into the two
+// real planes' spectra (R_2j = (Z(m) + conj Z(-m))/2, R_2j+1 = (Z(m) -
+// conj Z(-m))/2i), solves for m (the mirror's solution is the conjugate) and
+// packs the pair back.  It is exact up to FP32 rounding (~1e-6 relative), so
+// one solve per refinement pass replaces the PCG iterations; the outer
 // double-float refinement keeps the potential at the reference's tolerance.
 //
 // FFTs: self-sorting (Stockham) passes in shared memory -- radix 4 (and one
@@ -39,8 +44,8 @@ struct SpecAxis {
 struct SpecFilm {
     SpecAxis ax, ay;
     long long off;              // first cell of the film
-    long long coff;             // first spectrum value: [M][ny][nx] of the interior planes
-    int nx, ny, nz, M;
+    long long coff;             // first spectrum value: [Mp][ny][nx], plane j = interior planes 2j, 2j+1
+    int nx, ny, nz, M, Mp;      // M = nz - 2 interior planes, Mp = ceil(M / 2) packed planes
     int twx, twy, lamx, lamy;   // offsets into the twiddle / eigenvalue tables
     float scale;                // h^2 / (eps nx ny)
     int bx0, by0, bz0;          // first block of the film in the x, y and z grids
@@ -175,10 +180,11 @@ __device__ __forceinline__ bool spec_run(const Dev &d, int f)
     return d.force || *(volatile const int *)&d.solve[f].active != 0;
 }
 
-// x transforms of rows (kk, y), kk = interior plane - 1.  IN_REAL: from the
-// FP32 residual r into the spectra; otherwise from the spectra into the real
-// correction x (and x = 0 on the Dirichlet planes).  Shared memory: two tiles
-// of rb rows and the twiddles.
+// x transforms of rows (j, y) of the packed planes, j = 0 .. Mp-1.  IN_REAL:
+// from the FP32 residual r (interior planes 2j and 2j+1, i.e. z planes 2j+1
+// and 2j+2, as real and imaginary parts) into the spectra; otherwise from the
+// spectra into the real correction x (and x = 0 on the Dirichlet planes).
+// Shared memory: two tiles of rb rows and the twiddles.
 template <bool IN_REAL>
 __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     const int f = __ldg(sp.bx_film + blockIdx.x);
     if (!spec_run(d, f)) return;
     const SpecFilm &P = sp.films[f];
-    const int nx = P.nx, rows = P.M * P.ny, rb = max(1, SPEC_ELEMS / nx);
+    const int nx = P.nx, rows = P.Mp * P.ny, rb = max(1, SPEC_ELEMS / nx);
     const int r0 = (blockIdx.x - P.bx0) * rb, nr = min(rb, rows - r0);
     const long long plane = (long long)nx * P.ny;
     const float *rr = F.r + P.off;
@@ -196,9 +202,10 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     const int M = P.M;
     float2 *a = sm2, *b = sm2 + rb * nx, *tw = sm2 + 2 * rb * nx;
     for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twx + t);
-    // rows r0 .. r0+nr-1 are consecutive: (kk, y) runs over whole planes, so
-    // the residual rows of one interior plane are contiguous in r
+    // rows r0 .. r0+nr-1 are consecutive: (j, y) runs over whole planes, so
+    // the residual rows of one packed plane are contiguous in r
     const int total = nr * nx;
+    const int ny = P.ny;
     for (int t0 = threadIdx.x; t0 < total; t0 += SPEC_LB * blockDim.x) {
         float2 v[SPEC_LB];
         #pragma unroll
@@ -206,8 +213,10 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
             const int t = t0 + u * blockDim.x;
             if (t < total) {
                 if (IN_REAL) {
-                    const long long e = (long long)r0 * nx + t;        // (kk, y, x) of the interior stack
-                    v[u] = make_float2(rr[plane + e], 0.f);
+                    const int rw = r0 + t / nx, j = rw / ny;           // packed plane
+                    const long long yx = (long long)(rw - j * ny) * nx + (t - (t / nx) * nx);
+                    const long long e = (long long)(2 * j + 1) * plane + yx;
+                    v[u] = make_float2(rr[e], 2 * j + 1 < M ? rr[e + plane] : 0.f);
                 } else {
                     v[u] = Cf[(long long)r0 * nx + t];
                 }
@@ -222,13 +231,17 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     __syncthreads();
     const float2 *res = fft_tile<false>(a, b, nr, ax, 1, nx, tw);
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const long long e = (long long)r0 * nx + t;
         if (IN_REAL) {
-            Cf[e] = res[t];
+            Cf[(long long)r0 * nx + t] = res[t];
         } else {
-            xx[plane + e] = res[t].x;
-            if (e < plane) xx[e] = 0.f;                                  // first Dirichlet plane
-            if (e >= (long long)(M - 1) * plane) xx[e + 2 * plane] = 0.f;   // last one
+            // the transform of conj(W) is conj(x_2j + i x_2j+1) (scale folded into the z solve)
+            const int rw = r0 + t / nx, j = rw / ny;
+            const long long yx = (long long)(rw - j * ny) * nx + (t - (t / nx) * nx);
+            const long long e = (long long)(2 * j + 1) * plane + yx;
+            xx[e] = res[t].x;
+            if (2 * j + 1 < M) xx[e + plane] = -res[t].y;
+            if (j == 0) xx[yx] = 0.f;                                        // first Dirichlet plane
+            if (j == P.Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;    // last one
         }
     }
 }
@@ -274,10 +287,11 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
     }
 }
 
-// Thomas algorithm along z for every in-plane mode, one thread per mode, the
-// elimination coefficients in shared memory ([M][blockDim] of d' and c');
-// writes the conjugate of the scaled solution so that the next forward
-// transforms invert.
+// Thomas algorithm along z, one thread per in-plane mode m whose mirror -m
+// has an index >= m's (the mirror's solution is the conjugate), the
+// elimination coefficients in shared memory ([M][blockDim] of d' and c').
+// Reads the packed spectra at m and -m, writes the conjugates of the packed
+// scaled solutions there, so that the next forward transforms invert.
 static __global__ void k_spec_z(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
@@ -291,28 +305,55 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
     const long long m = (long long)(blockIdx.x - P.bz0) * T + threadIdx.x;
     if (m >= modes) return;
     const int x = (int)(m % P.nx), y = (int)(m / P.nx);
+    const int xm = x == 0 ? 0 : P.nx - x, ym = y == 0 ? 0 : P.ny - y;
+    const long long mm = (long long)ym * P.nx + xm;
+    if (mm < m) return;                               // solved by the thread of -m
     const float dg = __ldg(sp.lam + P.lamx + x) + __ldg(sp.lam + P.lamy + y) + 2.f;
-    const float s = P.scale;
-    float2 *C = sp.C + P.coff + m;
+    const float s = 0.5f * P.scale;
+    float2 *Ca = sp.C + P.coff + m, *Cb = sp.C + P.coff + mm;
     float c_prev = 0.f;
     float2 d_prev = make_float2(0.f, 0.f);
-    #pragma unroll 8
-    for (int k = 0; k < M; ++k) {                    // forward sweep (sub/super-diagonal -1)
-        const float2 rk = C[k * modes];
+    auto sweep = [&](int k, float2 rk) {             // forward elimination (sub/super-diagonal -1)
         const float inv = 1.f / (dg + c_prev);
         const float2 dk = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
         c_prev = -inv;
         cps[k * T + threadIdx.x] = c_prev;
         dps[k * T + threadIdx.x] = dk;
         d_prev = dk;
+    };
+    #pragma unroll 4
+    for (int j = 0; 2 * j < M; ++j) {
+        const float2 a = Ca[j * modes], b = Cb[j * modes];
+        sweep(2 * j, make_float2(a.x + b.x, a.y - b.y));                 // 2 (Z(m) + conj Z(-m)) / 2
+        if (2 * j + 1 < M) sweep(2 * j + 1, make_float2(a.y + b.y, b.x - a.x));   // (Z(m) - conj Z(-m)) / i
     }
-    float2 xn = d_prev;                              // back substitution
-    C[(M - 1) * modes] = make_float2(xn.x, -xn.y);
-    for (int k = M - 2; k >= 0; --k) {
-        const float2 dk = dps[k * T + threadIdx.x];
-        const float c = cps[k * T + threadIdx.x];
+    // back substitution, two planes at a time; store conj of the packed pair
+    // W(m) = X_2j + i X_2j+1 and W(-m) = conj X_2j + i conj X_2j+1
+    float2 xn = d_prev;
+    float2 u, v = make_float2(0.f, 0.f);
+    auto put = [&](int j, float2 p0, float2 p1) {
+        Ca[j * modes] = make_float2(p0.x - p1.y, -(p0.y + p1.x));
+        Cb[j * modes] = make_float2(p0.x + p1.y, p0.y - p1.x);
+    };
+    int k = M - 1;
+    if ((M & 1) == 0) {
+        v = xn;                                       // plane M-1 is the odd member of the last pair
+        const float2 dk = dps[(k - 1) * T + threadIdx.x];
+        const float c = cps[(k - 1) * T + threadIdx.x];
         xn = make_float2(dk.x - c * xn.x, dk.y - c * xn.y);
-        C[k * modes] = make_float2(xn.x, -xn.y);
+        --k;
+    }
+    u = xn;                                           // plane k (even)
+    put(k >> 1, u, v);
+    for (k -= 2; k >= 0; k -= 2) {
+        float2 dk = dps[(k + 1) * T + threadIdx.x];
+        float c = cps[(k + 1) * T + threadIdx.x];
+        v = make_float2(dk.x - c * xn.x, dk.y - c * xn.y);
+        dk = dps[k * T + threadIdx.x];
+        c = cps[k * T + threadIdx.x];
+        u = make_float2(dk.x - c * v.x, dk.y - c * v.y);
+        xn = u;
+        put(k >> 1, u, v);
     }
 }
 
