@@ -203,11 +203,15 @@ cmsl_status check_desc(const cmsl_film_desc *dsc, int idx, int n)
     return CMSL_OK;
 }
 
+// Rotations per grain: 9 values (FP64), or 9 values and 3 zeros (FP32: three
+// 16-byte loads per cell in the TDGL step).
 template <class T> cmsl_status upload_TR(Engine *e, const cmsl_film_desc *descs, int n)
 {
+    constexpr int stride = sizeof(T) == 4 ? TR32 : 9;
     std::vector<T> tr;
     for (int i = 0; i < n; ++i)
-        for (int q = 0; q < 9 * descs[i].n_grains; ++q) tr.push_back((T)descs[i].TR[q]);
+        for (int g = 0; g < descs[i].n_grains; ++g)
+            for (int q = 0; q < stride; ++q) tr.push_back(q < 9 ? (T)descs[i].TR[9 * g + q] : (T)0);
     TRY(e->alloc(&e->d_TR, tr.size() * sizeof(T)));
     CK(cudaMemcpy(e->d_TR, tr.data(), tr.size() * sizeof(T), cudaMemcpyHostToDevice));
     return CMSL_OK;
@@ -278,6 +282,19 @@ cmsl_status add_while(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_
     return CMSL_OK;
 }
 
+cmsl_status add_if(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *dep, int ndep,
+                   cudaGraphConditionalHandle h, cudaGraph_t *body)
+{
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    CK(cudaGraphAddNode(node, g, dep, nullptr, ndep, &cp));
+    *body = cp.conditional.phGraph_out[0];
+    return CMSL_OK;
+}
+
 // Arguments must outlive graph instantiation only (node params are copied).
 cmsl_status build_graph(Engine *e)
 {
@@ -300,7 +317,7 @@ cmsl_status build_graph(Engine *e)
     void *args32[] = {&a.d, &a.F32};
     void *args_d[] = {&a.d};
     if (fp64) TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl<double, Exact>, nit, NT, args64));
-    else TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl32<T32_NS>, nit, NT, args32, T32_SMEM));
+    else TRY(add_kernel(g, &n_tdgl, nullptr, 0, e->tdgl_fn, nit, e->tdgl_nt, args32, e->tdgl_smem));
     cudaGraphNode_t last = n_tdgl;
     if (e->any_dep) {
         if (fp64) {
@@ -312,37 +329,41 @@ cmsl_status build_graph(Engine *e)
             TRY(add_kernel(body, &n_up, &n_sp, 1, (void *)k_update<double, Exact, false>, nit, NT, args64));
             last = n_solve;
         } else if (e->spectral) {
-            // refinement pass: residual, then the direct solve of the correction
-            cudaGraph_t outer;
-            cudaGraphNode_t n_ref;
+            // refinement pass: residual, then -- while a film is not yet
+            // converged -- the direct solve of the correction (IF node)
+            cudaGraph_t outer, solve;
+            cudaGraphNode_t n_ref, n_if;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
-            a.d = e->dev(1, 0, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, NT, args32, e->refine_smem));
+            CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
+            a.d = e->dev(1, h_inner, h_outer);
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_if(outer, &n_if, &n_ref, 1, h_inner, &solve));
             void *a_x[] = {&a.d, &a.F32, &e->spec};
             void *a_s[] = {&a.d, &e->spec};
-            void *a_d[] = {&a.d};
             struct Node { void *fn; int grid, block; void **args; size_t smem; } seq[] = {
                 {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
                 {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
                 {(void *)k_spec_z, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
                 {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
-                {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
-                {(void *)k_spec_done, 1, 32, a_d, 0}};
-            cudaGraphNode_t prev = n_ref;
+                {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
+            cudaGraphNode_t prev = nullptr;
             for (const Node &q : seq) {
                 cudaGraphNode_t nd;
-                TRY(add_kernel(outer, &nd, &prev, 1, q.fn, q.grid, q.block, q.args, q.smem));
+                TRY(add_kernel(solve, &nd, prev ? &prev : nullptr, prev ? 1 : 0, q.fn, q.grid, q.block, q.args,
+                               q.smem));
                 prev = nd;
             }
             last = n_solve;
         } else if (e->persistent) {
-            cudaGraph_t outer;
-            cudaGraphNode_t n_ref, n_cg;
+            cudaGraph_t outer, solve;
+            cudaGraphNode_t n_ref, n_if, n_cg;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
-            a.d = e->dev(1, 0, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, NT, args32, e->refine_smem));
+            CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
+            a.d = e->dev(1, h_inner, h_outer);
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_if(outer, &n_if, &n_ref, 1, h_inner, &solve));
             void *args_cg[] = {&a.d, &e->cg, &e->d_dinv};
-            TRY(add_kernel(outer, &n_cg, &n_ref, 1, e->cg_fn, e->cg_grid, PNT, args_cg, e->cg_smem));
+            TRY(add_kernel(solve, &n_cg, nullptr, 0, e->cg_fn, e->cg_grid, PNT, args_cg, e->cg_smem));
             cudaLaunchAttributeValue av{};
             av.cooperative = 1;
             CK(cudaGraphKernelNodeSetAttribute(n_cg, cudaLaunchAttributeCooperative, &av));
@@ -354,7 +375,7 @@ cmsl_status build_graph(Engine *e)
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
             a.d = e->dev(1, h_inner, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, NT, args32, e->refine_smem));
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
             TRY(add_while(outer, &n_in, &n_ref, 1, h_inner, &inner));
             TRY(add_kernel(inner, &n_sp, nullptr, 0, (void *)k_spmv<float, Fast>, nit, NT, args32));
             TRY(add_kernel(inner, &n_up, &n_sp, 1, (void *)k_update<float, Fast, true>, nit, NT, args32));
@@ -392,14 +413,17 @@ cmsl_status launch_refine(Engine *e, cudaStream_t st, const Dev &d, const Fields
     Dev dd = d;
     Fields<float> ff = F32;
     void *args[] = {&dd, &ff};
-    CK(cudaLaunchKernel(e->refine_fn, dim3((unsigned)e->items.size()), dim3(NT), args, e->refine_smem, st));
+    CK(cudaLaunchKernel(e->refine_fn, dim3((unsigned)e->items.size()), dim3(e->refine_nt), args, e->refine_smem, st));
     return CMSL_OK;
 }
 
+// One FP32 TDGL step (k_tdgl32 / k_tdgl32p) launched from the host.
 cmsl_status launch_tdgl32(Engine *e, cudaStream_t st, const Dev &d, const Fields<float> &F32)
 {
-    k_tdgl32<T32_NS><<<(unsigned)e->items.size(), NT, T32_SMEM, st>>>(d, F32);
-    CK(cudaGetLastError());
+    Dev dd = d;
+    Fields<float> ff = F32;
+    void *args[] = {&dd, &ff};
+    CK(cudaLaunchKernel(e->tdgl_fn, dim3((unsigned)e->items.size()), dim3(e->tdgl_nt), args, e->tdgl_smem, st));
     return CMSL_OK;
 }
 
@@ -412,7 +436,6 @@ cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<f
     k_spec_z<<<e->spec_grid[2], e->spec_zt, e->spec_smem[2], st>>>(d, sp);
     k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
     k_spec_x<false><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
-    k_spec_done<<<1, 32, 0, st>>>(d);
     CK(cudaGetLastError());
     return CMSL_OK;
 }
@@ -813,13 +836,17 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     TRY(ensure_schedule(e, 16, 16));
 
     if (e->precision != CMSL_FP64) {
+        // FP32 stencil passes: the one-eps residual pass when every
+        // depolarised film has one eps
         bool uni = true;
         for (int fi = 0; fi < n; ++fi) uni &= !e->fh[fi].dep || fds[fi].uni_eps != 0;
         e->refine_fn = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
         e->refine_smem = uni ? r32_smem<true>() : r32_smem<false>();
+        e->tdgl_fn = (void *)k_tdgl32<T32_NS>;
+        e->tdgl_smem = T32_SMEM;
+        e->refine_nt = e->tdgl_nt = NT;
         CK(cudaFuncSetAttribute(e->refine_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem));
-        CK(cudaFuncSetAttribute((const void *)k_tdgl32<T32_NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)T32_SMEM));
+        CK(cudaFuncSetAttribute(e->tdgl_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem));
     }
     const Dev d = e->dev(0);
     if (e->precision == CMSL_FP64) k_dinv<double><<<(int)e->items.size(), NT>>>(d, (double *)e->d_dinv);

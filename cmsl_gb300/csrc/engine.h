@@ -79,8 +79,9 @@ struct Engine {
     // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
     // FP32_REFINED stencil passes (stencil32.cuh): the residual pass for
     // one-eps films (all films) or the general one, and their ring sizes
-    void *refine_fn = nullptr;
-    size_t refine_smem = 0;
+    void *refine_fn = nullptr, *tdgl_fn = nullptr;
+    size_t refine_smem = 0, tdgl_smem = 0;
+    int refine_nt = 0, tdgl_nt = 0;     // threads per block
     bool spectral = false;      // FP32 inner solve by the direct spectral solve (one film, uniform eps)
     SpecDev spec{};
     int spec_grid[3] = {0, 0, 0};

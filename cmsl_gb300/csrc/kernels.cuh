@@ -129,10 +129,11 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], double (*sm)[NV], double (
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        const int nw = (int)(blockDim.x >> 5);      // any block of up to NT threads
         #pragma unroll
         for (int i = 0; i < NV; ++i) {
             double s = 0.0;
-            for (int q = 0; q < NT / 32; ++q) s += sm[q][i];
+            for (int q = 0; q < nw; ++q) s += sm[q][i];
             out[i] = s;
         }
     }
@@ -164,7 +165,7 @@ __device__ __forceinline__ void film_total(const Dev &d, const FilmDev *f, doubl
     double v[NV];
     #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = 0.0;
-    for (int it = f->item_begin + (int)threadIdx.x; it < f->item_end; it += NT) {
+    for (int it = f->item_begin + (int)threadIdx.x; it < f->item_end; it += (int)blockDim.x) {
         #pragma unroll
         for (int i = 0; i < NV; ++i) v[i] += __ldcg(d.partial + (long long)it * NPART + i);
     }

@@ -185,12 +185,34 @@ __device__ __forceinline__ bool spec_run(const Dev &d, int f)
 // and 2j+2, as real and imaginary parts) into the spectra; otherwise from the
 // spectra into the real correction x (and x = 0 on the Dirichlet planes).
 // Shared memory: two tiles of rb rows and the twiddles.
+// The inverse transform (IN_REAL false) closes the solve: its last block
+// marks every active film's inner solve done (one "iteration").
+__device__ __forceinline__ void spec_finish(const Dev &d)
+{
+    if (!ticket_last(d.counter)) return;
+    if (threadIdx.x == 0) {
+        if (!d.force)
+            for (int f = 0; f < d.n_films; ++f) {
+                SolveDev *S = d.solve + f;
+                if (S->active) {
+                    S->iters = 1;
+                    S->total_iters += 1;
+                    S->active = 0;
+                }
+            }
+        *d.counter = 0u;
+    }
+}
+
 template <bool IN_REAL>
 __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
     const int f = __ldg(sp.bx_film + blockIdx.x);
-    if (!spec_run(d, f)) return;
+    if (!spec_run(d, f)) {
+        if (!IN_REAL) spec_finish(d);
+        return;
+    }
     const SpecFilm &P = sp.films[f];
     const int nx = P.nx, rows = P.Mp * P.ny, rb = max(1, SPEC_ELEMS / nx);
     const int r0 = (blockIdx.x - P.bx0) * rb, nr = min(rb, rows - r0);
@@ -244,6 +266,7 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
             if (j == P.Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;    // last one
         }
     }
+    if (!IN_REAL) spec_finish(d);
 }
 
 // y transforms of column groups of one interior plane, in place on the
@@ -354,20 +377,6 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
         u = make_float2(dk.x - c * v.x, dk.y - c * v.y);
         xn = u;
         put(k >> 1, u, v);
-    }
-}
-
-// After the solve: the inner solve of this pass is done (one "iteration").
-static __global__ void k_spec_done(Dev d)
-{
-    if (d.force) return;
-    for (int f = threadIdx.x; f < d.n_films; f += blockDim.x) {
-        SolveDev *S = d.solve + f;
-        if (S->active) {
-            S->iters = 1;
-            S->total_iters += 1;
-            S->active = 0;
-        }
     }
 }
 

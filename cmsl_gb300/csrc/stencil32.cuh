@@ -3,11 +3,15 @@
 //
 // Same work items as the FP64 kernels (a TX x TY column tile of one film
 // marching through z0..z1), but every plane of every field a pass reads is
-// brought into a ring of NS shared-memory stages by 4-byte cp.async copies
-// (each thread its own cell and at most one x/y halo cell), NS-3 planes ahead
-// of the plane being computed.  The z neighbours are read from the ring as
-// well, so a thread carries no plane-to-plane state beyond its partial sums,
-// several blocks share an SM, and each plane costs one barrier.
+// brought into a ring of NS shared-memory stages by cp.async copies, NS-3
+// planes ahead of the plane being computed.  The z neighbours are read from
+// the ring as well, so a thread carries no plane-to-plane state beyond its
+// partial sums, several blocks share an SM, and each plane costs one barrier.
+//
+// Each thread owns one cell of the tile and copies it (4 bytes per field)
+// and at most one x/y halo cell.  (Pair tiles -- two x-adjacent cells per
+// thread with 8-byte copies -- execute a third fewer instructions but halve
+// the warps an SM holds within the same shared memory, and measured slower.)
 //
 // Ring protocol (identical in both kernels): planes zlo = max(z0-1, 0) ..
 // zhi = min(z1, nz-1) are staged, plane p in stage (p - zlo) % NS, one
@@ -28,6 +32,8 @@ __device__ __forceinline__ void cp4(void *dst, const void *src)
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int TR32 = 12;     // FP32 rotation per grain: 9 values + 3 pad (three 16-byte loads)
 
 // Warm start of a step's first refinement pass (own cell): 0 the previous
 // potential a, 1 linear 2a - q, 2 quadratic 3(a - q) + u, 3 cubic
@@ -52,6 +58,84 @@ __device__ __forceinline__ int phi_free(const SolveDev *S)
 // (evolve.cu:256-357) in FP32, plus the warm start of the coming solve:
 // the extrapolated potential is written to the film's free buffer, which the
 // step's first residual pass then reads.
+
+// Coefficients of one (material, interface) class as three float4:
+// (relax, A, LdT, ag), (ags, b4, b12, g6), (a02, -, -, -).
+__device__ __forceinline__ void load_coef4(const FilmDev *f, float4 (*sC)[3])
+{
+    if (threadIdx.x < 6) {
+        const Coef<float> &c = f->coef32[threadIdx.x];
+        sC[threadIdx.x][0] = make_float4(c.relax, c.A, c.LdT, c.ag);
+        sC[threadIdx.x][1] = make_float4(c.ags, c.b4, c.b12, c.g6);
+        sC[threadIdx.x][2] = make_float4(c.a02, 0.f, 0.f, 0.f);
+    }
+}
+
+// One cell: P^{n+1} (pn) from P^n (pc), the 6-neighbour sums, -E (ex, ey, ez)
+// and -Ez_applied (mEz); pMZl, pSZl (crystal frame) for the sweep rows.
+__device__ __forceinline__ void tdgl_cell32(const float4 *K, const float4 *tr, const float (&pc)[6],
+                                            const float (&sum)[6], float ex, float ey, float ez, float mEz,
+                                            float (&pn)[6], float &pMZl, float &pSZl)
+{
+    const float4 t0 = __ldg(tr), t1 = __ldg(tr + 1), t2 = __ldg(tr + 2);
+    const float t[9] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x};
+    const float4 ka = K[0], kb = K[1], kc = K[2];
+    const float relax = ka.x, A = ka.y, LdT = ka.z, ag = ka.w, ags = kb.x, b4 = kb.y, b12 = kb.z, g6 = kb.w;
+    const float a02 = kc.x;
+    // crystal frame (kernels_evol.cu:162-168)
+    const float pMXl = t[0] * pc[0] + t[1] * pc[1] + t[2] * pc[2];
+    const float pMYl = t[3] * pc[0] + t[4] * pc[1] + t[5] * pc[2];
+    pMZl = t[6] * pc[0] + t[7] * pc[1] + t[8] * pc[2];
+    const float pSXl = t[0] * pc[3] + t[1] * pc[4] + t[2] * pc[5];
+    const float pSYl = t[3] * pc[3] + t[4] * pc[4] + t[5] * pc[5];
+    pSZl = t[6] * pc[3] + t[7] * pc[4] + t[8] * pc[5];
+    // two-sublattice Landau derivative (kernels_evol.cu:178-199)
+    const float dmx = a02 * pMXl, dmy = a02 * pMYl;
+    const float dsx = a02 * pSXl, dsy = a02 * pSYl;
+    const float m2 = pMZl * pMZl, m3 = m2 * pMZl, m4 = m3 * pMZl, m5 = m4 * pMZl;
+    const float q2 = pSZl * pSZl, q3 = q2 * pSZl, q4 = q3 * pSZl, q5 = q4 * pSZl;
+    float dmz = ag * pMZl + b4 * m3;
+    dmz = dmz + b12 * pMZl * q2;
+    dmz = dmz + g6 * (m5 + 10.f * m3 * q2 + 5.f * pMZl * q4);
+    float dsz = ags * pSZl + b4 * q3;
+    dsz = dsz + b12 * pSZl * m2;
+    dsz = dsz + g6 * (q5 + 10.f * m2 * q3 + 5.f * pSZl * m4);
+    // back to the lab frame (kernels_evol.cu:202-208) + fields (:210-220)
+    float b[6];
+    b[0] = t[0] * dmx + t[3] * dmy + t[6] * dmz + ex;
+    b[1] = t[1] * dmx + t[4] * dmy + t[7] * dmz + ey;
+    b[2] = t[2] * dmx + t[5] * dmy + t[8] * dmz + (mEz + ez);
+    b[3] = t[0] * dsx + t[3] * dsy + t[6] * dsz;
+    b[4] = t[1] * dsx + t[4] * dsy + t[7] * dsz;
+    b[5] = t[2] * dsx + t[5] * dsy + t[8] * dsz;
+    // explicit Euler with the 6-neighbour Laplacian (kernels_evol.cu:223-229)
+    #pragma unroll
+    for (int q = 0; q < 6; ++q) pn[q] = pc[q] * relax + A * sum[q] - LdT * b[q];
+}
+
+// z neighbours of the potential for E (depol_varEPS.cu:246-273): zero beyond
+// the Dirichlet planes, mirrored for the Neumann boundary.
+__device__ __forceinline__ void efield_z(const FilmDev *f, int k, df fu, df fd, df &pu, df &pd)
+{
+    if (f->zbc == 0) {
+        pu = (k == f->nz - 1) ? df{0.f, 0.f} : fu;
+        pd = (k == 0) ? df{0.f, 0.f} : fd;
+    } else {
+        op_z<df>(f, k, fu, fd, pu, pd);
+    }
+}
+
+__device__ __forceinline__ void row_acc(float (&acc)[7], int mat, const float (&pn)[6], float pMZl, float pSZl)
+{
+    acc[0] += pn[2];
+    acc[1] += pn[5];
+    acc[2] += pMZl;
+    acc[3] += pSZl;
+    acc[4] += (mat == 1) ? pn[2] : 0.f;
+    acc[5] += (mat == 0) ? pn[2] : 0.f;
+    acc[6] += (mat == 2) ? pn[2] : 0.f;
+}
+
 constexpr int T32_NS = 4;
 constexpr int T32_STAGE = 8 * SPL + NT;      // floats: P[6], phi hi, phi lo (own + halo); code (own)
 constexpr size_t T32_SMEM = sizeof(float) * T32_NS * T32_STAGE;
@@ -62,13 +146,13 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
     extern __shared__ float4 smem_t32[];
     float *ring = (float *)smem_t32;
-    __shared__ Coef<float> sC[6];
+    __shared__ float4 sC[6][3];
     __shared__ double sRed[NT / 32][7];
     __shared__ double sTot[7];
     const int4 it = d.items[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    if (threadIdx.x < 6) sC[threadIdx.x] = f->coef32[threadIdx.x];
+    load_coef4(f, sC);
     const Geom g = make_geom(f, it.y, it.z);
     const int cur = d.ctl->cur, rs = d.ctl->run_step;
     const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
@@ -83,6 +167,7 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
     float *nh = (float *)phi_sel(d, phi_free(S)) + off;
     const int warm = f->warm;
     const uint32_t *code = d.code + off;
+    const float4 *TR4 = (const float4 *)(F.TR + (long long)TR32 * f->g_off);
     const float inv_2hf = f->inv_2hf;
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
 
@@ -134,12 +219,6 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
         const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
         const uint32_t c = ((const uint32_t *)sk)[8 * SPL + threadIdx.x];
-        const int gid = code_gid(c), mat = code_mat(c);
-        const Coef<float> K = sC[mat * 2 + code_iface(c)];
-        const float *trp = F.TR + 9LL * (f->g_off + gid);
-        float t[9];
-        #pragma unroll
-        for (int q = 0; q < 9; ++q) t[q] = __ldg(trp + q);
         float pc[6], sum[6];
         #pragma unroll
         for (int q = 0; q < 6; ++q) {
@@ -157,61 +236,19 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         if (dep) {
             const float *fh = sk + 6 * SPL, *fl = sk + 7 * SPL;
             a0 = df{fh[s0], fl[s0]};
-            const df fu{su[6 * SPL + s0], su[7 * SPL + s0]}, fd{sd[6 * SPL + s0], sd[7 * SPL + s0]};
             df pu, pd;
-            if (f->zbc == 0) {
-                pu = (k == nz - 1) ? df{0.f, 0.f} : fu;
-                pd = (k == 0) ? df{0.f, 0.f} : fd;
-            } else {
-                op_z<df>(f, k, fu, fd, pu, pd);
-            }
-            // -1 * E with E = -(phi_+ - phi_-) / (2h)  (depol_varEPS.cu:246-273)
+            efield_z(f, k, df{su[6 * SPL + s0], su[7 * SPL + s0]}, df{sd[6 * SPL + s0], sd[7 * SPL + s0]}, pu, pd);
+            // -1 * E with E = -(phi_+ - phi_-) / (2h)
             ex = phi_diff(df{fh[s0 + 1], fl[s0 + 1]}, df{fh[s0 - 1], fl[s0 - 1]}) * inv_2hf;
             ey = phi_diff(df{fh[s0 + SX], fl[s0 + SX]}, df{fh[s0 - SX], fl[s0 - SX]}) * inv_2hf;
             ez = phi_diff(pu, pd) * inv_2hf;
         }
-        // crystal frame (kernels_evol.cu:162-168)
-        const float pMXl = t[0] * pc[0] + t[1] * pc[1] + t[2] * pc[2];
-        const float pMYl = t[3] * pc[0] + t[4] * pc[1] + t[5] * pc[2];
-        const float pMZl = t[6] * pc[0] + t[7] * pc[1] + t[8] * pc[2];
-        const float pSXl = t[0] * pc[3] + t[1] * pc[4] + t[2] * pc[5];
-        const float pSYl = t[3] * pc[3] + t[4] * pc[4] + t[5] * pc[5];
-        const float pSZl = t[6] * pc[3] + t[7] * pc[4] + t[8] * pc[5];
-        // two-sublattice Landau derivative (kernels_evol.cu:178-199)
-        const float dmx = K.a02 * pMXl, dmy = K.a02 * pMYl;
-        const float dsx = K.a02 * pSXl, dsy = K.a02 * pSYl;
-        const float m2 = pMZl * pMZl, m3 = m2 * pMZl, m4 = m3 * pMZl, m5 = m4 * pMZl;
-        const float q2 = pSZl * pSZl, q3 = q2 * pSZl, q4 = q3 * pSZl, q5 = q4 * pSZl;
-        float dmz = K.ag * pMZl + K.b4 * m3;
-        dmz = dmz + K.b12 * pMZl * q2;
-        dmz = dmz + K.g6 * (m5 + 10.f * m3 * q2 + 5.f * pMZl * q4);
-        float dsz = K.ags * pSZl + K.b4 * q3;
-        dsz = dsz + K.b12 * pSZl * m2;
-        dsz = dsz + K.g6 * (q5 + 10.f * m2 * q3 + 5.f * pSZl * m4);
-        // back to the lab frame (kernels_evol.cu:202-208) + fields (:210-220)
-        float b[6];
-        b[0] = t[0] * dmx + t[3] * dmy + t[6] * dmz + ex;
-        b[1] = t[1] * dmx + t[4] * dmy + t[7] * dmz + ey;
-        b[2] = t[2] * dmx + t[5] * dmy + t[8] * dmz + (mEz + ez);
-        b[3] = t[0] * dsx + t[3] * dsy + t[6] * dsz;
-        b[4] = t[1] * dsx + t[4] * dsy + t[7] * dsz;
-        b[5] = t[2] * dsx + t[5] * dsy + t[8] * dsz;
-        // explicit Euler with the 6-neighbour Laplacian (kernels_evol.cu:223-229)
-        float pn[6];
+        float pn[6], pMZl, pSZl;
+        tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
+                    pMZl, pSZl);
         #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            pn[q] = pc[q] * K.relax + K.A * sum[q] - K.LdT * b[q];
-            (cur ? F.P[0][q] : F.P[1][q])[off + o] = pn[q];
-        }
-        if (row >= 0) {
-            acc[0] += pn[2];
-            acc[1] += pn[5];
-            acc[2] += pMZl;
-            acc[3] += pSZl;
-            acc[4] += (mat == 1) ? pn[2] : 0.f;
-            acc[5] += (mat == 0) ? pn[2] : 0.f;
-            acc[6] += (mat == 2) ? pn[2] : 0.f;
-        }
+        for (int q = 0; q < 6; ++q) (cur ? F.P[0][q] : F.P[1][q])[off + o] = pn[q];
+        if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
         if (dep) {
             const df w = extrap_phi(warm, a0, wq, wu, wv);
             nh[o] = w.h;
@@ -271,12 +308,6 @@ static __global__ void __launch_bounds__(NT) k_extrap(Dev d)
 // Laplacian (one double-float product per cell, no material codes).
 // No FP64 instruction is executed.
 constexpr int R32_NS = 5;
-template <bool UNI> struct R32Lay {
-    static constexpr int FH = 0, FL = SPL, DX = 2 * SPL, PX = 3 * SPL, PY = 4 * SPL, PZ = 5 * SPL;
-    static constexpr int CODE = 5 * SPL + NT, DINV = 6 * SPL + NT;   // general eps only
-    static constexpr int STAGE = UNI ? 5 * SPL + NT : 6 * SPL + 2 * NT;
-};
-template <bool UNI> constexpr size_t r32_smem() { return sizeof(float) * R32_NS * R32Lay<UNI>::STAGE; }
 
 // sum of six double-float values minus 6 c; the hi parts are summed error-free
 __device__ __forceinline__ df lap7(df e, df w, df n, df s, df u, df dn, df c)
@@ -309,6 +340,118 @@ __device__ __forceinline__ df div3(float a, float b, float c, float e, float g, 
     return fast_two_sum(s2.h, l);
 }
 
+// The neighbourhood of one cell as a residual pass sees it.
+struct RCell {
+    df xc, xe, xw, xn, xs, xu, xd;          // potential (z neighbours as loaded, k+1 / k-1 clamped)
+    float dc, de, dw, dn, ds, du, dd;        // pending correction (0 on a first pass)
+    float pxe, pxw, pyn, pys, pzu, pzd;      // Pm for the divergence (z clamped)
+    int mc, me, mw, mn, ms, mu, md;          // materials (general eps only)
+};
+
+// r (FP32 value of b - A x), b.h and the Jacobi weight of one non-identity row.
+template <bool UNI>
+__device__ __forceinline__ void refine_row(const FilmDev *f, int k, const RCell &c, float dinv, float &rv,
+                                           float &bh, float &wj)
+{
+    const df cb{f->cb_h, f->cb_l};
+    const df bm = df_mul(div3(c.pxe, c.pxw, c.pyn, c.pys, c.pzu, c.pzd), cb);   // -b
+    df xu, xd;
+    op_z<df>(f, k, c.xu, c.xd, xu, xd);
+    float du, ddn;
+    op_z<float>(f, k, c.du, c.dd, du, ddn);
+    df s;            // b - A phi
+    float rd;        // - A dx
+    if (UNI) {
+        const df cu{f->cf_h[0], f->cf_l[0]};   // eps/h^2 on every face
+        s = df_sub(df_mul(cu, lap7(c.xe, c.xw, c.xn, c.xs, xu, xd, c.xc)), bm);
+        rd = cu.h * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
+        wj = f->dinv_uni;
+    } else {
+        int mu, md;
+        op_z<int>(f, k, c.mu, c.md, mu, md);
+        const int m3 = c.mc * 3;
+        auto cf = [&](int i) { return df{f->cf_h[m3 + i], f->cf_l[m3 + i]}; };
+        df a = df_sub(df_mul(cf(c.me), df_sub(c.xe, c.xc)), df_mul(cf(c.mw), df_sub(c.xc, c.xw)));
+        a = df_add(a, df_mul(cf(c.mn), df_sub(c.xn, c.xc)));
+        a = df_sub(a, df_mul(cf(c.ms), df_sub(c.xc, c.xs)));
+        a = df_add(a, df_mul(cf(mu), df_sub(xu, c.xc)));
+        a = df_sub(a, df_mul(cf(md), df_sub(c.xc, xd)));
+        s = df_sub(a, bm);
+        const float *ch = f->cf_h + m3;
+        rd = ch[c.me] * (c.de - c.dc) - ch[c.mw] * (c.dc - c.dw) + ch[c.mn] * (c.dn - c.dc) -
+             ch[c.ms] * (c.dc - c.ds) + ch[mu] * (du - c.dc) - ch[md] * (c.dc - ddn);
+        wj = dinv;
+    }
+    rv = s.h + (s.l + rd);
+    bh = -bm.h;
+}
+
+// The last part of a residual pass of one cell: r and the partial sums.
+template <bool UNI>
+__device__ __forceinline__ void refine_cell(const FilmDev *f, int k, bool ident, const RCell &c, float dinv,
+                                            float &rv, float (&acc)[3])
+{
+    float bh, wj;
+    if (ident) {
+        rv = -(c.xc.h + (c.xc.l + c.dc));     // x - g with g = 0, b = 0
+        bh = 0.f;
+        wj = 1.f;
+    } else {
+        refine_row<UNI>(f, k, c, dinv, rv, bh, wj);
+    }
+    acc[0] = fmaf(rv, rv, acc[0]);
+    acc[1] = fmaf(bh, bh, acc[1]);
+    acc[2] = fmaf(rv, rv * wj, acc[2]);
+}
+
+// Common set-up of a residual pass.
+struct RefineSrc {
+    const float *xh, *dx, *Pmx, *Pmy, *Pmz, *dinv;
+    const uint32_t *code;
+    float *nh, *r;
+    long long lo;
+    bool run, apply;
+};
+
+__device__ __forceinline__ RefineSrc refine_src(const Dev &d, const Fields<float> &F, const FilmDev *f,
+                                                const SolveDev *S)
+{
+    RefineSrc q;
+    q.run = f->dep_flag != 0 && (d.force || S->outer_active);
+    q.apply = S->refine > 0;     // later pass: x = phi + dx; first pass: x = the warm start
+    const int cur = d.ctl->cur, fr = phi_free(S);
+    const long long off = f->off;
+    q.lo = d.ncells;
+    q.xh = (const float *)phi_sel(d, q.apply ? S->phi_cur : fr) + off;
+    q.nh = (float *)phi_sel(d, fr) + off;
+    q.dx = F.x + off;
+    q.Pmx = (cur ? F.P[0][0] : F.P[1][0]) + off;
+    q.Pmy = (cur ? F.P[0][1] : F.P[1][1]) + off;
+    q.Pmz = (cur ? F.P[0][2] : F.P[1][2]) + off;
+    q.code = d.code + off;
+    q.dinv = F.dinv + off;
+    q.r = F.r + off;
+    return q;
+}
+
+__device__ __forceinline__ void refine_partials(const Dev &d, float (&acc)[3], double (*sRed)[3])
+{
+    double t[3];
+    block_sum<3, float>(acc, sRed, t);
+    if (threadIdx.x == 0) {
+        d.partial[(long long)blockIdx.x * NPART + 0] = t[0];
+        d.partial[(long long)blockIdx.x * NPART + 1] = t[1];
+        d.partial[(long long)blockIdx.x * NPART + 2] = t[2];
+    }
+}
+
+template <bool UNI> struct R32Lay {
+    static constexpr int FH = 0, FL = SPL, DX = 2 * SPL, PX = 3 * SPL, PY = 4 * SPL, PZ = 5 * SPL;
+    static constexpr int CODE = 5 * SPL + NT, DINV = 6 * SPL + NT;   // general eps only
+    static constexpr int STAGE = UNI ? 5 * SPL + NT : 6 * SPL + 2 * NT;
+};
+template <bool UNI> constexpr size_t r32_smem() { return sizeof(float) * R32_NS * R32Lay<UNI>::STAGE; }
+
 template <bool UNI, int NS>
 __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
 {
@@ -320,142 +463,82 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
     __shared__ double sTot[3];
     const int4 it = d.items[blockIdx.x];
     const FilmDev *f = d.films + it.x;
-    const SolveDev *S = d.solve + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
     const Geom g = make_geom(f, it.y, it.z);
     const int nz = g.nz;
-    const bool run = f->dep_flag != 0 && (d.force || S->outer_active);
-    const bool apply = S->refine > 0;     // later pass: x = phi + dx; first pass: x = the warm start
-    const int cur = d.ctl->cur;
-    const int fr = phi_free(S);
-    const long long off = f->off, lo = d.ncells;
-    const float *xh = (const float *)phi_sel(d, apply ? S->phi_cur : fr) + off;
-    float *nh = (float *)phi_sel(d, fr) + off;
-    const float *dx = F.x + off;
-    const float *Pmx = (cur ? F.P[0][0] : F.P[1][0]) + off;
-    const float *Pmy = (cur ? F.P[0][1] : F.P[1][1]) + off;
-    const float *Pmz = (cur ? F.P[0][2] : F.P[1][2]) + off;
-    const uint32_t *code = d.code + off;
-    const float *dinv = F.dinv + off;
-    float *r = F.r + off;
+    const RefineSrc q = refine_src(d, F, f, d.solve + it.x);
+    const long long lo = q.lo;
+    const bool apply = q.apply;
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
 
     auto stage = [&](int p) { return ring + ((p - zlo) % NS) * L::STAGE; };
     auto issue = [&](int p) {
-        if (run && p <= zhi) {
+        if (q.run && p <= zhi) {
             float *st = stage(p);
             const long long pp = (long long)p * g.plane;
             if (g.valid) {
                 const long long o = g.own_pl + pp;
                 const int s = g.own_slot;
-                cp4(st + L::FH + s, xh + o);
-                cp4(st + L::FL + s, xh + lo + o);
-                if (apply) cp4(st + L::DX + s, dx + o);
-                cp4(st + L::PX + s, Pmx + o);
-                cp4(st + L::PY + s, Pmy + o);
-                cp4(st + L::PZ + threadIdx.x, Pmz + o);
+                cp4(st + L::FH + s, q.xh + o);
+                cp4(st + L::FL + s, q.xh + lo + o);
+                if (apply) cp4(st + L::DX + s, q.dx + o);
+                cp4(st + L::PX + s, q.Pmx + o);
+                cp4(st + L::PY + s, q.Pmy + o);
+                cp4(st + L::PZ + threadIdx.x, q.Pmz + o);
                 if (!UNI) {
-                    cp4(st + L::CODE + s, code + o);
-                    cp4(st + L::DINV + threadIdx.x, dinv + o);
+                    cp4(st + L::CODE + s, q.code + o);
+                    cp4(st + L::DINV + threadIdx.x, q.dinv + o);
                 }
             }
             if (g.halo) {
                 const long long o = g.halo_pl + pp;
                 const int s = g.halo_slot;
-                cp4(st + L::FH + s, xh + o);
-                cp4(st + L::FL + s, xh + lo + o);
-                if (apply) cp4(st + L::DX + s, dx + o);
-                cp4(st + L::PX + s, Pmx + o);
-                cp4(st + L::PY + s, Pmy + o);
-                if (!UNI) cp4(st + L::CODE + s, code + o);
+                cp4(st + L::FH + s, q.xh + o);
+                cp4(st + L::FL + s, q.xh + lo + o);
+                if (apply) cp4(st + L::DX + s, q.dx + o);
+                cp4(st + L::PX + s, q.Pmx + o);
+                cp4(st + L::PY + s, q.Pmy + o);
+                if (!UNI) cp4(st + L::CODE + s, q.code + o);
             }
         }
         cp_commit();
     };
     for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p);
 
-    const df cb{f->cb_h, f->cb_l};
-    const df cu{f->cf_h[0], f->cf_l[0]};     // UNI: eps/h^2 on every face
-    const float dinv_uni = f->dinv_uni;
-    const int s0 = g.own_slot;
+    const int s0 = g.own_slot, tz = threadIdx.x;
     float acc[3] = {0.f, 0.f, 0.f};
     for (int k = z0; k < z1; ++k) {
         cp_wait<NS - 4>();
         __syncthreads();
         issue(k + NS - 2);
-        if (!run || !g.valid) continue;
+        if (!q.run || !g.valid) continue;
         const long long o = g.own_pl + (long long)k * g.plane;
         const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
         const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
         auto X = [&](const float *st, int s) { return df{st[L::FH + s], st[L::FL + s]}; };
         auto D = [&](const float *st, int s) { return apply ? st[L::DX + s] : 0.f; };
-        const df xc = X(sk, s0);
-        const float dc = D(sk, s0);
-        float rv, bh, dd;
-        if (identity_row(f, k, g.own_pl)) {
-            // x - g with g = 0, b = 0
-            rv = -(xc.h + (xc.l + dc));
-            bh = 0.f;
-            dd = 1.f;
-        } else {
-            const int tz = threadIdx.x;
-            const df bm = df_mul(div3(sk[L::PX + s0 + 1], sk[L::PX + s0 - 1], sk[L::PY + s0 + SX],
-                                      sk[L::PY + s0 - SX], su[L::PZ + tz], sd[L::PZ + tz]),
-                                 cb);   // -b
-            df xu, xd;
-            op_z<df>(f, k, X(su, s0), X(sd, s0), xu, xd);
-            float du, ddn;
-            op_z<float>(f, k, D(su, s0), D(sd, s0), du, ddn);
-            const df xe = X(sk, s0 + 1), xw = X(sk, s0 - 1), xn = X(sk, s0 + SX), xs = X(sk, s0 - SX);
-            const float de = D(sk, s0 + 1), dw = D(sk, s0 - 1), dn = D(sk, s0 + SX), ds = D(sk, s0 - SX);
-            df s;            // b - A phi
-            float rd;        // - A dx
-            if (UNI) {
-                s = df_sub(df_mul(cu, lap7(xe, xw, xn, xs, xu, xd, xc)), bm);
-                rd = cu.h * ((de + dw) + (dn + ds) + (du + ddn) - 6.f * dc);
-                dd = dinv_uni;
-            } else {
-                const uint32_t *cs = (const uint32_t *)sk;
-                const int m3 = code_mat(cs[L::CODE + s0]) * 3;
-                int mu, md;
-                op_z<int>(f, k, code_mat(((const uint32_t *)su)[L::CODE + s0]),
-                          code_mat(((const uint32_t *)sd)[L::CODE + s0]), mu, md);
-                const int me = m3 + code_mat(cs[L::CODE + s0 + 1]), mw = m3 + code_mat(cs[L::CODE + s0 - 1]);
-                const int mn = m3 + code_mat(cs[L::CODE + s0 + SX]), ms = m3 + code_mat(cs[L::CODE + s0 - SX]);
-                auto cf = [&](int i) { return df{f->cf_h[i], f->cf_l[i]}; };
-                df a = df_sub(df_mul(cf(me), df_sub(xe, xc)), df_mul(cf(mw), df_sub(xc, xw)));
-                a = df_add(a, df_mul(cf(mn), df_sub(xn, xc)));
-                a = df_sub(a, df_mul(cf(ms), df_sub(xc, xs)));
-                a = df_add(a, df_mul(cf(m3 + mu), df_sub(xu, xc)));
-                a = df_sub(a, df_mul(cf(m3 + md), df_sub(xc, xd)));
-                s = df_sub(a, bm);
-                rd = f->cf_h[me] * (de - dc) - f->cf_h[mw] * (dc - dw) + f->cf_h[mn] * (dn - dc) -
-                     f->cf_h[ms] * (dc - ds) + f->cf_h[m3 + mu] * (du - dc) - f->cf_h[m3 + md] * (dc - ddn);
-                dd = sk[L::DINV + tz];
-            }
-            rv = s.h + (s.l + rd);
-            bh = -bm.h;
-        }
-        r[o] = rv;
+        auto M = [&](const float *st, int s) { return UNI ? 0 : code_mat(((const uint32_t *)st)[L::CODE + s]); };
+        RCell c;
+        c.xc = X(sk, s0); c.xe = X(sk, s0 + 1); c.xw = X(sk, s0 - 1); c.xn = X(sk, s0 + SX); c.xs = X(sk, s0 - SX);
+        c.xu = X(su, s0); c.xd = X(sd, s0);
+        c.dc = D(sk, s0); c.de = D(sk, s0 + 1); c.dw = D(sk, s0 - 1); c.dn = D(sk, s0 + SX); c.ds = D(sk, s0 - SX);
+        c.du = D(su, s0); c.dd = D(sd, s0);
+        c.pxe = sk[L::PX + s0 + 1]; c.pxw = sk[L::PX + s0 - 1];
+        c.pyn = sk[L::PY + s0 + SX]; c.pys = sk[L::PY + s0 - SX];
+        c.pzu = su[L::PZ + tz]; c.pzd = sd[L::PZ + tz];
+        c.mc = M(sk, s0); c.me = M(sk, s0 + 1); c.mw = M(sk, s0 - 1); c.mn = M(sk, s0 + SX); c.ms = M(sk, s0 - SX);
+        c.mu = M(su, s0); c.md = M(sd, s0);
+        float rv;
+        refine_cell<UNI>(f, k, identity_row(f, k, g.own_pl), c, UNI ? 0.f : sk[L::DINV + tz], rv, acc);
+        q.r[o] = rv;
         if (apply) {
-            const df nv = df_add_f(xc, dc);
-            nh[o] = nv.h;
-            nh[lo + o] = nv.l;
+            const df nv = df_add_f(c.xc, c.dc);
+            q.nh[o] = nv.h;
+            q.nh[lo + o] = nv.l;
         }
-        acc[0] = fmaf(rv, rv, acc[0]);
-        acc[1] = fmaf(bh, bh, acc[1]);
-        acc[2] = fmaf(rv, rv * dd, acc[2]);
     }
     cp_wait<0>();
-    {
-        double t[3];
-        block_sum<3, float>(acc, sRed, t);
-        if (threadIdx.x == 0) {
-            d.partial[(long long)blockIdx.x * NPART + 0] = t[0];
-            d.partial[(long long)blockIdx.x * NPART + 1] = t[1];
-            d.partial[(long long)blockIdx.x * NPART + 2] = t[2];
-        }
-    }
+    refine_partials(d, acc, sRed);
     if (!ticket_last(d.counter)) return;
     refine_finish(d, sRed, sTot);
 }
