@@ -328,45 +328,57 @@ cmsl_status build_graph(Engine *e)
             TRY(add_kernel(body, &n_sp, nullptr, 0, (void *)k_spmv<double, Exact>, nit, NT, args64));
             TRY(add_kernel(body, &n_up, &n_sp, 1, (void *)k_update<double, Exact, false>, nit, NT, args64));
             last = n_solve;
-        } else if (e->spectral) {
-            // refinement pass: residual, then -- while a film is not yet
-            // converged -- the direct solve of the correction (IF node)
-            cudaGraph_t outer, solve;
-            cudaGraphNode_t n_ref, n_if;
-            TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
-            CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
-            a.d = e->dev(1, h_inner, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
-            TRY(add_if(outer, &n_if, &n_ref, 1, h_inner, &solve));
+        } else if (e->spectral || e->persistent) {
+            // A step almost always takes two refinement passes (the warm
+            // start's residual, then the check after one inner solve), so
+            // they are laid out flat: pass -> solve -> pass -> WHILE(some
+            // film not converged) { solve -> pass } for the rare further
+            // passes.  The direct solve's kernels skip converged films; the
+            // cooperative PCG launch sits under an IF node.  (Programmatic
+            // edges along this chain measured no gain.)
             void *a_x[] = {&a.d, &a.F32, &e->spec};
             void *a_s[] = {&a.d, &e->spec};
-            struct Node { void *fn; int grid, block; void **args; size_t smem; } seq[] = {
-                {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
-                {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
-                {(void *)k_spec_z, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
-                {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
-                {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
-            cudaGraphNode_t prev = nullptr;
-            for (const Node &q : seq) {
-                cudaGraphNode_t nd;
-                TRY(add_kernel(solve, &nd, prev ? &prev : nullptr, prev ? 1 : 0, q.fn, q.grid, q.block, q.args,
-                               q.smem));
-                prev = nd;
-            }
-            last = n_solve;
-        } else if (e->persistent) {
-            cudaGraph_t outer, solve;
-            cudaGraphNode_t n_ref, n_if, n_cg;
-            TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
-            CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
+            void *a_cg[] = {&a.d, &e->cg, &e->d_dinv};
+            // the inner solve of one pass, after *dep (or first in graph gs)
+            auto add_solve = [&](cudaGraph_t gs, const cudaGraphNode_t *dep, cudaGraphNode_t *out) -> cmsl_status {
+                if (e->persistent) {
+                    TRY(add_kernel(gs, out, dep, dep ? 1 : 0, e->cg_fn, e->cg_grid, PNT, a_cg, e->cg_smem));
+                    cudaLaunchAttributeValue av{};
+                    av.cooperative = 1;
+                    CK(cudaGraphKernelNodeSetAttribute(*out, cudaLaunchAttributeCooperative, &av));
+                    return CMSL_OK;
+                }
+                struct Node { void *fn; int grid, block; void **args; size_t smem; } seq[] = {
+                    {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
+                    {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
+                    {(void *)k_spec_z, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
+                    {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
+                    {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
+                const cudaGraphNode_t *prev = dep;
+                for (const Node &q : seq) {
+                    TRY(add_kernel(gs, out, prev, prev ? 1 : 0, q.fn, q.grid, q.block, q.args, q.smem));
+                    prev = out;
+                }
+                return CMSL_OK;
+            };
+            cudaGraphNode_t n_r1, n_s1, n_r2, n_sb, n_rb;
+            cudaGraph_t body;
+            if (e->persistent) CK(cudaGraphConditionalHandleCreate(&h_inner, g, 0, cudaGraphCondAssignDefault));
             a.d = e->dev(1, h_inner, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
-            TRY(add_if(outer, &n_if, &n_ref, 1, h_inner, &solve));
-            void *args_cg[] = {&a.d, &e->cg, &e->d_dinv};
-            TRY(add_kernel(solve, &n_cg, nullptr, 0, e->cg_fn, e->cg_grid, PNT, args_cg, e->cg_smem));
-            cudaLaunchAttributeValue av{};
-            av.cooperative = 1;
-            CK(cudaGraphKernelNodeSetAttribute(n_cg, cudaLaunchAttributeCooperative, &av));
+            TRY(add_kernel(g, &n_r1, &last, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            if (e->persistent) {
+                cudaGraph_t solve1;
+                cudaGraphNode_t n_c1;
+                TRY(add_if(g, &n_s1, &n_r1, 1, h_inner, &solve1));
+                TRY(add_solve(solve1, nullptr, &n_c1));
+            } else {
+                TRY(add_solve(g, &n_r1, &n_s1));
+            }
+            TRY(add_kernel(g, &n_r2, &n_s1, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_while(g, &n_solve, &n_r2, 1, h_outer, &body));
+            a.d = e->dev(1, 0, h_outer);
+            TRY(add_solve(body, nullptr, &n_sb));
+            TRY(add_kernel(body, &n_rb, &n_sb, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
             last = n_solve;
         } else {
             // the inner loop's handle belongs to the outer body graph it lives in
