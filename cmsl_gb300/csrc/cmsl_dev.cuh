@@ -63,6 +63,8 @@ struct FilmDev {
     float inv_h2f, inv_2hf, eps0f;
     float dinv_uni;             // Jacobi D^-1 of non-identity rows when every material has one eps
     int uni_eps;                // all materials share eps_r
+    int upd_ok;                 // FP32_REFINED: the inner solve leaves r intact (direct solve), so a
+                                // later refinement pass may update r instead of recomputing it
     double n_mat[3];            // voxels per material (sum of the reference's masks)
     Coef<double> coef[6];       // index mat*2 + iface
     Coef<float> coef32[6];
@@ -87,7 +89,8 @@ struct SolveDev {               // per film, lives in device memory
     int sticky;                 // first non-zero status seen since set_state
     double inner_tol2;          // inner target of the current refinement pass
     int inner_max;              // inner iteration cap of the current pass
-    int pad2;
+    int upd;                    // the next refinement pass updates r <- r - A dx (FP32) instead of
+                                // forming b - A phi in double-float
 };
 
 // Extra vectors of the single-reduction FP32 PCG (FP32_REFINED mode).

@@ -653,6 +653,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         }
         FilmDev &fd = fds[fi];
         fill_film(fd, dsc, e->precision);
+        fd.upd_ok = e->spectral ? 1 : 0;
         fd.off = h.off;
         fd.g_off = g_off;
         g_off += h.ng;
@@ -1048,7 +1049,7 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
     for (int kind = 0; kind < 4; ++kind) {
         CK(cudaMemcpy(S.data(), e->d_solve, sizeof(SolveDev) * F, cudaMemcpyDeviceToHost));
         for (SolveDev &s : S) {
-            s.outer_active = 1; s.active = 1; s.iters = 1; s.refine = 1; s.status = 0;
+            s.outer_active = 1; s.active = 1; s.iters = 1; s.refine = 1; s.status = 0; s.upd = 0;
             s.alpha = 1e-3; s.beta = 0.5; s.rz = s.rz0 = 1.0;
             s.inner_tol2 = 0.0; s.inner_max = CG_TIMING_ITERS;
         }
@@ -1205,7 +1206,7 @@ cmsl_status cmsl_film_depol(cmsl_film *f, int32_t *iters, int32_t *status)
     }
     SolveDev S;
     CK(cudaMemcpy(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost));
-    S.outer_active = 1; S.active = 0; S.refine = 0; S.total_iters = 0; S.iters = 0; S.status = 0;
+    S.outer_active = 1; S.active = 0; S.refine = 0; S.total_iters = 0; S.iters = 0; S.status = 0; S.upd = 0;
     CK(cudaMemcpy(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice));
     const Dev d = f->dev(0);
     if (f->precision != CMSL_FP64) {

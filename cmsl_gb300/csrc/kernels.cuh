@@ -470,6 +470,7 @@ __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)
             S->active = 0;
             S->status = 0;
             S->refine = 0;
+            S->upd = 0;
             S->total_iters = 0;
             S->iters = 0;
         }
@@ -637,6 +638,9 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
         if (was) film_total<3>(d, ff, sRed, sTot);
         if (threadIdx.x == 0 && was) {
+            // an update pass (r <- r - A dx) leaves b.b as the last full pass formed it
+            const bool was_upd = ff->upd_ok && S->upd && S->refine > 0;
+            const double bb = was_upd ? S->bb : sTot[1];
             const int c0 = S->phi_cur, p0 = S->phi_prev, q0 = S->phi_prev2, r0 = S->phi_prev3;
             const int fr = 10 - c0 - p0 - q0 - r0;
             if (S->refine == 0) {            // keep phi_n .. phi_{n-2} for the next step's extrapolation
@@ -648,8 +652,13 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
             S->phi_cur = fr;                 // this pass wrote the free buffer
             S->refine += 1;
             S->rr64 = sTot[0];
-            S->bb = sTot[1];
-            const bool conv = sTot[0] <= ff->refine_tol2 * sTot[1] || sTot[0] == 0.0;
+            S->bb = bb;
+            const bool conv = sTot[0] <= ff->refine_tol2 * bb || sTot[0] == 0.0;
+            // the next pass may update r when this one formed it in full and
+            // ||r|| <= 1e-4 ||b||: the FP32 rounding of A dx (relative ~1e-7,
+            // times the stencil's cancellation) then stays far below the
+            // refinement target; never two update passes in a row
+            S->upd = !was_upd && ff->upd_ok && sTot[0] <= 1e-8 * bb;
             S->iters = 0;
             S->rz = S->rz0 = sTot[2];
             if (conv || !isfinite(sTot[0])) {
@@ -666,7 +675,7 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
                 // inner target: just enough reduction to reach the refinement
                 // tolerance in this pass (half-margin), between the FP32 floor
                 // inner_tol and 1e-2
-                double want = 0.25 * ff->refine_tol2 * sTot[1] / sTot[0];
+                double want = 0.25 * ff->refine_tol2 * bb / sTot[0];
                 want = fmax(want, ff->inner_tol2);
                 S->inner_tol2 = fmin(want, 1e-4);
                 S->inner_max = ff->inner_max;

@@ -302,10 +302,13 @@ static __global__ void __launch_bounds__(NT) k_extrap(Dev d)
 // the inner solve, written to the free buffer -- form b = -eps_0_nd div Pm
 // (depol_varEPS.cu:279-329, zero on the Dirichlet planes / Neumann pin) and
 // r = b - A x in double-float, and the partial sums r.r, b.b, r.D^-1.r.
-// A x is split as A phi (double-float) + A dx (FP32: |A dx| ~ |r| is small,
-// so FP32 rounding there is far below the refinement target).  UNI: every
-// material has the same eps, the operator is eps/h^2 times the 7-point
+// x = phi + dx is formed in double-float at every stencil point (dx can be
+// as large as phi itself, e.g. the first solve after a cold start).  UNI:
+// every material has the same eps, the operator is eps/h^2 times the 7-point
 // Laplacian (one double-float product per cell, no material codes).
+// An update pass (after the direct solve, once ||r|| <= 1e-4 ||b||) instead
+// forms r <- r - A dx in FP32: dx is then small, and the FP32 rounding of
+// A dx stays far below the refinement target.
 // No FP64 instruction is executed.
 constexpr int R32_NS = 5;
 
@@ -342,30 +345,38 @@ __device__ __forceinline__ df div3(float a, float b, float c, float e, float g, 
 
 // The neighbourhood of one cell as a residual pass sees it.
 struct RCell {
-    df xc, xe, xw, xn, xs, xu, xd;          // potential (z neighbours as loaded, k+1 / k-1 clamped)
-    float dc, de, dw, dn, ds, du, dd;        // pending correction (0 on a first pass)
+    df xc, xe, xw, xn, xs, xu, xd;          // x = phi + dx (z neighbours as loaded, k+1 / k-1 clamped)
+    float dc, de, dw, dn, ds, du, dd;        // pending correction (update passes)
     float pxe, pxw, pyn, pys, pzu, pzd;      // Pm for the divergence (z clamped)
     int mc, me, mw, mn, ms, mu, md;          // materials (general eps only)
 };
 
-// r (FP32 value of b - A x), b.h and the Jacobi weight of one non-identity row.
+// -A dx of one non-identity row in FP32 (dx: the pending correction).
 template <bool UNI>
-__device__ __forceinline__ void refine_row(const FilmDev *f, int k, const RCell &c, float dinv, float &rv,
-                                           float &bh, float &wj)
+__device__ __forceinline__ float minus_adx(const FilmDev *f, int k, const RCell &c)
+{
+    float du, ddn;
+    op_z<float>(f, k, c.du, c.dd, du, ddn);
+    if (UNI) return f->cf_h[0] * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
+    int mu, md;
+    op_z<int>(f, k, c.mu, c.md, mu, md);
+    const float *ch = f->cf_h + c.mc * 3;
+    return ch[c.me] * (c.de - c.dc) - ch[c.mw] * (c.dc - c.dw) + ch[c.mn] * (c.dn - c.dc) -
+           ch[c.ms] * (c.dc - c.ds) + ch[mu] * (du - c.dc) - ch[md] * (c.dc - ddn);
+}
+
+// r (FP32 value of b - A x, double-float arithmetic) and b.h of one non-identity row.
+template <bool UNI>
+__device__ __forceinline__ void refine_row(const FilmDev *f, int k, const RCell &c, float &rv, float &bh)
 {
     const df cb{f->cb_h, f->cb_l};
     const df bm = df_mul(div3(c.pxe, c.pxw, c.pyn, c.pys, c.pzu, c.pzd), cb);   // -b
     df xu, xd;
     op_z<df>(f, k, c.xu, c.xd, xu, xd);
-    float du, ddn;
-    op_z<float>(f, k, c.du, c.dd, du, ddn);
     df s;            // b - A phi
-    float rd;        // - A dx
     if (UNI) {
         const df cu{f->cf_h[0], f->cf_l[0]};   // eps/h^2 on every face
         s = df_sub(df_mul(cu, lap7(c.xe, c.xw, c.xn, c.xs, xu, xd, c.xc)), bm);
-        rd = cu.h * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
-        wj = f->dinv_uni;
     } else {
         int mu, md;
         op_z<int>(f, k, c.mu, c.md, mu, md);
@@ -377,27 +388,24 @@ __device__ __forceinline__ void refine_row(const FilmDev *f, int k, const RCell 
         a = df_add(a, df_mul(cf(mu), df_sub(xu, c.xc)));
         a = df_sub(a, df_mul(cf(md), df_sub(c.xc, xd)));
         s = df_sub(a, bm);
-        const float *ch = f->cf_h + m3;
-        rd = ch[c.me] * (c.de - c.dc) - ch[c.mw] * (c.dc - c.dw) + ch[c.mn] * (c.dn - c.dc) -
-             ch[c.ms] * (c.dc - c.ds) + ch[mu] * (du - c.dc) - ch[md] * (c.dc - ddn);
-        wj = dinv;
     }
-    rv = s.h + (s.l + rd);
+    rv = s.h + s.l;
     bh = -bm.h;
 }
 
 // The last part of a residual pass of one cell: r and the partial sums.
+// upd: r = r_old - A dx (b.b is not formed); otherwise r = b - A x.
 template <bool UNI>
-__device__ __forceinline__ void refine_cell(const FilmDev *f, int k, bool ident, const RCell &c, float dinv,
-                                            float &rv, float (&acc)[3])
+__device__ __forceinline__ void refine_cell(const FilmDev *f, int k, bool ident, bool upd, const RCell &c,
+                                            float r_old, float dinv, float &rv, float (&acc)[3])
 {
-    float bh, wj;
+    float bh = 0.f, wj = 1.f;
     if (ident) {
-        rv = -(c.xc.h + (c.xc.l + c.dc));     // x - g with g = 0, b = 0
-        bh = 0.f;
-        wj = 1.f;
+        rv = -(c.xc.h + c.xc.l);              // x - g with g = 0, b = 0
     } else {
-        refine_row<UNI>(f, k, c, dinv, rv, bh, wj);
+        if (upd) rv = r_old + minus_adx<UNI>(f, k, c);
+        else refine_row<UNI>(f, k, c, rv, bh);
+        wj = UNI ? f->dinv_uni : dinv;
     }
     acc[0] = fmaf(rv, rv, acc[0]);
     acc[1] = fmaf(bh, bh, acc[1]);
@@ -410,7 +418,7 @@ struct RefineSrc {
     const uint32_t *code;
     float *nh, *r;
     long long lo;
-    bool run, apply;
+    bool run, apply, upd;
 };
 
 __device__ __forceinline__ RefineSrc refine_src(const Dev &d, const Fields<float> &F, const FilmDev *f,
@@ -419,6 +427,7 @@ __device__ __forceinline__ RefineSrc refine_src(const Dev &d, const Fields<float
     RefineSrc q;
     q.run = f->dep_flag != 0 && (d.force || S->outer_active);
     q.apply = S->refine > 0;     // later pass: x = phi + dx; first pass: x = the warm start
+    q.upd = q.apply && S->upd && f->upd_ok;   // r <- r - A dx
     const int cur = d.ctl->cur, fr = phi_free(S);
     const long long off = f->off;
     q.lo = d.ncells;
@@ -468,12 +477,34 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
     const int nz = g.nz;
     const RefineSrc q = refine_src(d, F, f, d.solve + it.x);
     const long long lo = q.lo;
-    const bool apply = q.apply;
+    const bool apply = q.apply, upd = UNI && q.upd;   // update passes follow the direct solve (one eps)
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
 
     auto stage = [&](int p) { return ring + ((p - zlo) % NS) * L::STAGE; };
     auto issue = [&](int p) {
-        if (q.run && p <= zhi) {
+        if (q.run && p <= zhi && upd) {
+            // update pass: dx with its halo; phi and the old r of the own cell
+            float *st = stage(p);
+            const long long pp = (long long)p * g.plane;
+            if (g.valid) {
+                const long long o = g.own_pl + pp;
+                const int s = g.own_slot;
+                cp4(st + L::FH + s, q.xh + o);
+                cp4(st + L::FL + s, q.xh + lo + o);
+                cp4(st + L::DX + s, q.dx + o);
+                cp4(st + L::PX + s, q.r + o);
+                if (!UNI) {
+                    cp4(st + L::CODE + s, q.code + o);
+                    cp4(st + L::DINV + threadIdx.x, q.dinv + o);
+                }
+            }
+            if (g.halo) {
+                const long long o = g.halo_pl + pp;
+                const int s = g.halo_slot;
+                cp4(st + L::DX + s, q.dx + o);
+                if (!UNI) cp4(st + L::CODE + s, q.code + o);
+            }
+        } else if (q.run && p <= zhi) {
             float *st = stage(p);
             const long long pp = (long long)p * g.plane;
             if (g.valid) {
@@ -515,26 +546,33 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
         const long long o = g.own_pl + (long long)k * g.plane;
         const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
         const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
-        auto X = [&](const float *st, int s) { return df{st[L::FH + s], st[L::FL + s]}; };
-        auto D = [&](const float *st, int s) { return apply ? st[L::DX + s] : 0.f; };
+        auto D = [&](const float *st, int s) { return st[L::DX + s]; };
+        auto X = [&](const float *st, int s) {        // x = phi (+ dx on later passes)
+            const df p{st[L::FH + s], st[L::FL + s]};
+            return apply ? df_add_f(p, D(st, s)) : p;
+        };
         auto M = [&](const float *st, int s) { return UNI ? 0 : code_mat(((const uint32_t *)st)[L::CODE + s]); };
         RCell c;
-        c.xc = X(sk, s0); c.xe = X(sk, s0 + 1); c.xw = X(sk, s0 - 1); c.xn = X(sk, s0 + SX); c.xs = X(sk, s0 - SX);
-        c.xu = X(su, s0); c.xd = X(sd, s0);
-        c.dc = D(sk, s0); c.de = D(sk, s0 + 1); c.dw = D(sk, s0 - 1); c.dn = D(sk, s0 + SX); c.ds = D(sk, s0 - SX);
-        c.du = D(su, s0); c.dd = D(sd, s0);
-        c.pxe = sk[L::PX + s0 + 1]; c.pxw = sk[L::PX + s0 - 1];
-        c.pyn = sk[L::PY + s0 + SX]; c.pys = sk[L::PY + s0 - SX];
-        c.pzu = su[L::PZ + tz]; c.pzd = sd[L::PZ + tz];
+        c.xc = X(sk, s0);
         c.mc = M(sk, s0); c.me = M(sk, s0 + 1); c.mw = M(sk, s0 - 1); c.mn = M(sk, s0 + SX); c.ms = M(sk, s0 - SX);
         c.mu = M(su, s0); c.md = M(sd, s0);
+        if (upd) {
+            c.dc = D(sk, s0); c.de = D(sk, s0 + 1); c.dw = D(sk, s0 - 1); c.dn = D(sk, s0 + SX);
+            c.ds = D(sk, s0 - SX); c.du = D(su, s0); c.dd = D(sd, s0);
+        } else {
+            c.xe = X(sk, s0 + 1); c.xw = X(sk, s0 - 1); c.xn = X(sk, s0 + SX); c.xs = X(sk, s0 - SX);
+            c.xu = X(su, s0); c.xd = X(sd, s0);
+            c.pxe = sk[L::PX + s0 + 1]; c.pxw = sk[L::PX + s0 - 1];
+            c.pyn = sk[L::PY + s0 + SX]; c.pys = sk[L::PY + s0 - SX];
+            c.pzu = su[L::PZ + tz]; c.pzd = sd[L::PZ + tz];
+        }
         float rv;
-        refine_cell<UNI>(f, k, identity_row(f, k, g.own_pl), c, UNI ? 0.f : sk[L::DINV + tz], rv, acc);
+        refine_cell<UNI>(f, k, identity_row(f, k, g.own_pl), upd, c, upd ? sk[L::PX + s0] : 0.f,
+                         UNI ? 0.f : sk[L::DINV + tz], rv, acc);
         q.r[o] = rv;
         if (apply) {
-            const df nv = df_add_f(c.xc, c.dc);
-            q.nh[o] = nv.h;
-            q.nh[lo + o] = nv.l;
+            q.nh[o] = c.xc.h;
+            q.nh[lo + o] = c.xc.l;
         }
     }
     cp_wait<0>();

@@ -1,5 +1,7 @@
 """The direct (spectral) inner solve of CMSL_FP32_REFINED: films whose
-materials share one permittivity, Dirichlet z boundary, 2^a 3^b sides.
+materials share one permittivity, Dirichlet z boundary, 2^a 3^b sides; the
+refinement passes after it (full double-float residuals, or FP32 updates
+r <- r - A dx once the residual is small).
 Against the FP64 oracle solved to ||r|| <= 1e-12 ||b|| with the tolerances
 of the other FP32_REFINED tests (P within 2e-5 of max |P|, phi 1e-4, rows
 1e-5), and against the same film with the PCG inner solve."""
@@ -53,6 +55,13 @@ def test_direct_solve_run_vs_oracle(gpu, shape):
     assert np.abs(rg[:, :10] - statw[:, :10]).max() <= 1e-5
     # one direct solve per refinement pass, a few passes per step
     assert (rf >= 2).all() and (rf <= 4).all() and (it == rf - 1).all()
+    # the last step ended on an update pass (r <- r - A dx) or a full one:
+    # either way the potential meets the refinement target in FP64
+    orc = oracle.load()
+    b = -orc.divergence(f, Pg[0], Pg[1], Pg[2])
+    k = np.repeat(np.arange(f.nz), f.nx * f.ny)
+    b[(k == 0) | (k == f.nz - 1)] = 0.0
+    assert np.linalg.norm(b - orc.apply_A(f, phig)) <= 1.5e-8 * np.linalg.norm(b)
     with gpu.Film.from_oracle_film(f, inner_solver=gpu.INNER_PCG, **kw) as g:
         assert g.inner_solver == gpu.INNER_PCG
         g.set_state(P)
