@@ -105,12 +105,16 @@ SpecAxis spec_plan(int n)
     return a;
 }
 
-// Threads per block of the z solve: its [M][threads] elimination arrays
-// (12 bytes per entry) stay within 96 KB of shared memory; 0 if M is too large.
+// Shared memory of the z solve per thread: the staged / eliminated plane
+// pairs (16 bytes each) and c' per plane (4 bytes).
+size_t spec_zbytes(int M) { return (size_t)16 * ((M + 1) / 2) + (size_t)4 * M; }
+
+// Threads per block of the z solve: its shared memory stays within 96 KB;
+// 0 if M is too large.
 int spec_zthreads(int M)
 {
     for (int t = 128; t >= 32; t /= 2)
-        if ((size_t)t * M * 12 <= 96 * 1024) return t;
+        if ((size_t)t * spec_zbytes(M) <= 96 * 1024) return t;
     return 0;
 }
 
@@ -802,11 +806,11 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
             const long long gx = ((long long)P.Mp * h.ny + rbx - 1) / rbx;
             const long long gy = (long long)P.Mp * ((h.nx + cby - 1) / cby);
-            const long long gz = ((long long)h.nx * h.ny + zt - 1) / zt;
+            const long long gz = (spec_canon_count(h.nx, h.ny) + zt - 1) / zt;   // one thread per mode pair
             bxf.insert(bxf.end(), (size_t)gx, fi);
             byf.insert(byf.end(), (size_t)gy, fi);
             bzf.insert(bzf.end(), (size_t)gz, fi);
-            smx = std::max(smx, sizeof(float2) * (2 * rbx * h.nx + h.nx));   // two tiles + twiddles
+            smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * h.nx) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }
         SpecDev &sp = e->spec;
@@ -829,7 +833,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         e->spec_grid[2] = (int)bzf.size();
         e->spec_smem[0] = smx;
         e->spec_smem[1] = smy;
-        e->spec_smem[2] = (size_t)12 * spec_mmax * zt;
+        e->spec_smem[2] = spec_zbytes(spec_mmax) * zt;
         CK(cudaFuncSetAttribute(k_spec_x<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));

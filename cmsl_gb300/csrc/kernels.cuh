@@ -76,6 +76,22 @@ __device__ __forceinline__ float phi_diff(df a, df b)
     return d.h + d.l;
 }
 
+// Asynchronous global -> shared copies (cp.async, 4 or 8 bytes, both
+// addresses aligned to the size), grouped per commit; cp_wait<N> returns
+// once at most N of this thread's groups are still in flight.
+__device__ __forceinline__ void cp4(void *dst, const void *src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp8(void *dst, const void *src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // ------------------------------------------------------------------ tiles
 struct Geom {
     int nx, ny, nz, x0, y0, wx, wy;

@@ -70,14 +70,17 @@ __device__ __forceinline__ float2 c_mul(float2 a, float2 b)
 // transforms run in place between two such tiles (a, b) and return the one
 // holding the result.  SEQ_FAST: consecutive threads take consecutive
 // sequences (interleaved tiles, the y pass); otherwise consecutive butterflies
-// of one sequence (the x pass).  Both keep shared-memory accesses of a warp on
-// distinct banks for the loads.  tw: the n twiddles, staged in shared memory.
+// of one sequence (the x pass), whose tiles are padded by one element every
+// 16 (spec_pad) so that the strided Stockham writes of a warp fall on
+// distinct banks.  tw: the n twiddles, staged in shared memory.
+__host__ __device__ __forceinline__ int spec_pad(int i) { return i + (i >> 4); }
 
 // n = 2^lgn: radix-4 passes (one radix-2 pass when lgn is odd), shifts and masks.
 template <bool SEQ_FAST>
 __device__ __forceinline__ float2 *fft_pow2(float2 *a, float2 *b, int nseq, int lgn, int es, int ss,
                                             const float2 *tw)
 {
+    const int lgs = (nseq & (nseq - 1)) == 0 ? __ffs(nseq) - 1 : -1;   // sequences per tile, as a shift
     int lgNs = 0;
     while (lgNs < lgn) {
         const int lgR = (lgn - lgNs >= 2) ? 2 : 1;
@@ -87,30 +90,34 @@ __device__ __forceinline__ float2 *fft_pow2(float2 *a, float2 *b, int nseq, int 
         const int total = nseq << lgnbf;
         for (int t = threadIdx.x; t < total; t += blockDim.x) {
             int sq, j;
-            if (SEQ_FAST) { j = t / nseq; sq = t - j * nseq; }
-            else { sq = t >> lgnbf; j = t & (nbf - 1); }
+            if (SEQ_FAST) {
+                if (lgs >= 0) { j = t >> lgs; sq = t & (nseq - 1); }
+                else { j = t / nseq; sq = t - j * nseq; }
+            } else {
+                sq = t >> lgnbf; j = t & (nbf - 1);
+            }
             const int jm = j & (Ns - 1);
             const int o = ((j >> lgNs) << (lgNs + lgR)) + jm;
-            const float2 *src = a + sq * ss;
-            float2 *dst = b + sq * ss;
+            const int base = sq * ss;
+            auto at = [&](int e) { return SEQ_FAST ? base + e * es : spec_pad(base + e * es); };
             const int tj = jm << lgstep;
             if (lgR == 2) {
-                const float2 v0 = src[j * es];
-                const float2 v1 = c_mul(src[(j + nbf) * es], tw[tj]);
-                const float2 v2 = c_mul(src[(j + 2 * nbf) * es], tw[2 * tj]);
-                const float2 v3 = c_mul(src[(j + 3 * nbf) * es], tw[3 * tj]);
+                const float2 v0 = a[at(j)];
+                const float2 v1 = c_mul(a[at(j + nbf)], tw[tj]);
+                const float2 v2 = c_mul(a[at(j + 2 * nbf)], tw[2 * tj]);
+                const float2 v3 = c_mul(a[at(j + 3 * nbf)], tw[3 * tj]);
                 const float2 s02 = c_add(v0, v2), d02 = c_sub(v0, v2);
                 const float2 s13 = c_add(v1, v3), d13 = c_sub(v1, v3);
                 const float2 rot = make_float2(d13.y, -d13.x);     // -i (v1 - v3)
-                dst[o * es] = c_add(s02, s13);
-                dst[(o + Ns) * es] = c_add(d02, rot);
-                dst[(o + 2 * Ns) * es] = c_sub(s02, s13);
-                dst[(o + 3 * Ns) * es] = c_sub(d02, rot);
+                b[at(o)] = c_add(s02, s13);
+                b[at(o + Ns)] = c_add(d02, rot);
+                b[at(o + 2 * Ns)] = c_sub(s02, s13);
+                b[at(o + 3 * Ns)] = c_sub(d02, rot);
             } else {
-                const float2 v0 = src[j * es];
-                const float2 v1 = c_mul(src[(j + nbf) * es], tw[tj]);
-                dst[o * es] = c_add(v0, v1);
-                dst[(o + Ns) * es] = c_sub(v0, v1);
+                const float2 v0 = a[at(j)];
+                const float2 v1 = c_mul(a[at(j + nbf)], tw[tj]);
+                b[at(o)] = c_add(v0, v1);
+                b[at(o + Ns)] = c_sub(v0, v1);
             }
         }
         __syncthreads();
@@ -138,23 +145,23 @@ __device__ __forceinline__ float2 *fft_mixed(float2 *a, float2 *b, int nseq, con
             if (SEQ_FAST) { j = t / nseq; sq = t - j * nseq; }
             else { sq = t / nbf; j = t - sq * nbf; }
             const int jm = j % Ns;
-            const float2 *src = a + sq * ss;
-            float2 *dst = b + sq * ss;
+            const int base = sq * ss;
+            auto at = [&](int e) { return SEQ_FAST ? base + e * es : spec_pad(base + e * es); };
             const int o = (j / Ns) * Ns * R + jm;
-            const float2 v0 = src[j * es];
-            const float2 v1 = c_mul(src[(j + nbf) * es], tw[jm * tstride]);
+            const float2 v0 = a[at(j)];
+            const float2 v1 = c_mul(a[at(j + nbf)], tw[jm * tstride]);
             if (R == 2) {
-                dst[o * es] = c_add(v0, v1);
-                dst[(o + Ns) * es] = c_sub(v0, v1);
+                b[at(o)] = c_add(v0, v1);
+                b[at(o + Ns)] = c_sub(v0, v1);
             } else {
-                const float2 v2 = c_mul(src[(j + 2 * nbf) * es], tw[2 * jm * tstride]);
+                const float2 v2 = c_mul(a[at(j + 2 * nbf)], tw[2 * jm * tstride]);
                 const float2 s12 = c_add(v1, v2), d12 = c_sub(v1, v2);
                 const float2 m = make_float2(v0.x - 0.5f * s12.x, v0.y - 0.5f * s12.y);
                 const float k3 = 0.86602540378443865f;   // sin(2 pi / 3)
                 const float2 rot = make_float2(k3 * d12.y, -k3 * d12.x);
-                dst[o * es] = c_add(v0, s12);
-                dst[(o + Ns) * es] = c_add(m, rot);
-                dst[(o + 2 * Ns) * es] = c_sub(m, rot);
+                b[at(o)] = c_add(v0, s12);
+                b[at(o + Ns)] = c_add(m, rot);
+                b[at(o + 2 * Ns)] = c_sub(m, rot);
             }
         }
         __syncthreads();
@@ -180,13 +187,8 @@ __device__ __forceinline__ bool spec_run(const Dev &d, int f)
     return d.force || *(volatile const int *)&d.solve[f].active != 0;
 }
 
-// x transforms of rows (j, y) of the packed planes, j = 0 .. Mp-1.  IN_REAL:
-// from the FP32 residual r (interior planes 2j and 2j+1, i.e. z planes 2j+1
-// and 2j+2, as real and imaginary parts) into the spectra; otherwise from the
-// spectra into the real correction x (and x = 0 on the Dirichlet planes).
-// Shared memory: two tiles of rb rows and the twiddles.
-// The inverse transform (IN_REAL false) closes the solve: its last block
-// marks every active film's inner solve done (one "iteration").
+// The inverse transform closes the solve: its last block marks every active
+// film's inner solve done (one "iteration").
 __device__ __forceinline__ void spec_finish(const Dev &d)
 {
     if (!ticket_last(d.counter)) return;
@@ -204,6 +206,11 @@ __device__ __forceinline__ void spec_finish(const Dev &d)
     }
 }
 
+// x transforms of rows (j, y) of the packed planes, j = 0 .. Mp-1.  IN_REAL:
+// from the FP32 residual r (interior planes 2j and 2j+1, i.e. z planes 2j+1
+// and 2j+2, as real and imaginary parts) into the spectra; otherwise from the
+// spectra into the real correction x (and x = 0 on the Dirichlet planes).
+// Shared memory: two padded tiles of rb rows and the twiddles.
 template <bool IN_REAL>
 __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
@@ -222,7 +229,8 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
     float2 *Cf = sp.C + P.coff;
     const SpecAxis ax = P.ax;
     const int M = P.M;
-    float2 *a = sm2, *b = sm2 + rb * nx, *tw = sm2 + 2 * rb * nx;
+    const int tile = spec_pad(rb * nx) + 1;
+    float2 *a = sm2, *b = sm2 + tile, *tw = sm2 + 2 * tile;
     for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twx + t);
     // rows r0 .. r0+nr-1 are consecutive: (j, y) runs over whole planes, so
     // the residual rows of one packed plane are contiguous in r
@@ -247,21 +255,22 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
         #pragma unroll
         for (int u = 0; u < SPEC_LB; ++u) {
             const int t = t0 + u * blockDim.x;
-            if (t < total) a[t] = v[u];
+            if (t < total) a[spec_pad(t)] = v[u];
         }
     }
     __syncthreads();
     const float2 *res = fft_tile<false>(a, b, nr, ax, 1, nx, tw);
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const float2 rv = res[spec_pad(t)];
         if (IN_REAL) {
-            Cf[(long long)r0 * nx + t] = res[t];
+            Cf[(long long)r0 * nx + t] = rv;
         } else {
             // the transform of conj(W) is conj(x_2j + i x_2j+1) (scale folded into the z solve)
             const int rw = r0 + t / nx, j = rw / ny;
             const long long yx = (long long)(rw - j * ny) * nx + (t - (t / nx) * nx);
             const long long e = (long long)(2 * j + 1) * plane + yx;
-            xx[e] = res[t].x;
-            if (2 * j + 1 < M) xx[e + plane] = -res[t].y;
+            xx[e] = rv.x;
+            if (2 * j + 1 < M) xx[e + plane] = -rv.y;
             if (j == 0) xx[yx] = 0.f;                                        // first Dirichlet plane
             if (j == P.Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;    // last one
         }
@@ -310,73 +319,92 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
     }
 }
 
-// Thomas algorithm along z, one thread per in-plane mode m whose mirror -m
-// has an index >= m's (the mirror's solution is the conjugate), the
-// elimination coefficients in shared memory ([M][blockDim] of d' and c').
-// Reads the packed spectra at m and -m, writes the conjugates of the packed
-// scaled solutions there, so that the next forward transforms invert.
+// In-plane modes m whose mirror -m has an index >= m's, one per z solve:
+// rows y = 1 .. (ny-1)/2 in full, then row 0 and, for even ny, row ny/2
+// with x = 0 .. nx/2.  Returns false past the last one.
+__device__ __forceinline__ bool spec_canon_mode(long long t, int nx, int ny, int &x, int &y)
+{
+    const long long full = (long long)((ny - 1) / 2) * nx;
+    if (t < full) {
+        y = 1 + (int)(t / nx);
+        x = (int)(t - (long long)(y - 1) * nx);
+        return true;
+    }
+    const int hx = nx / 2 + 1, t2 = (int)(t - full);
+    if (t2 < hx) { y = 0; x = t2; return true; }
+    if ((ny & 1) == 0 && t2 < 2 * hx) { y = ny / 2; x = t2 - hx; return true; }
+    return false;
+}
+__host__ __device__ inline long long spec_canon_count(int nx, int ny)
+{
+    return (long long)((ny - 1) / 2) * nx + (long long)(nx / 2 + 1) * ((ny & 1) == 0 ? 2 : 1);
+}
+
+// Thomas algorithm along z, one thread per canonical mode m (the mirror's
+// solution is the conjugate).  The thread's packed spectra at m and -m for
+// every plane pair are first copied into shared memory at once (cp.async),
+// then eliminated there: [Mp][blockDim] float4 (Z(m), Z(-m)), overwritten by
+// the eliminated right-hand sides (d'_2j, d'_2j+1), and [M][blockDim] of c'.
+// Writes the conjugates of the packed scaled solutions, so that the next
+// forward transforms invert.
 static __global__ void k_spec_z(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
     const int f = __ldg(sp.bz_film + blockIdx.x);
     if (!spec_run(d, f)) return;
     const SpecFilm &P = sp.films[f];
-    const int M = P.M, T = blockDim.x;
-    float2 *dps = sm2;
-    float *cps = (float *)(sm2 + (size_t)M * T);
+    const int M = P.M, Mp = P.Mp, T = blockDim.x, tx = threadIdx.x;
+    float4 *dp = (float4 *)sm2;
+    float *cps = (float *)(dp + (size_t)Mp * T);
+    int x, y;
+    if (!spec_canon_mode((long long)(blockIdx.x - P.bz0) * T + tx, P.nx, P.ny, x, y)) return;
     const long long modes = (long long)P.nx * P.ny;
-    const long long m = (long long)(blockIdx.x - P.bz0) * T + threadIdx.x;
-    if (m >= modes) return;
-    const int x = (int)(m % P.nx), y = (int)(m / P.nx);
-    const int xm = x == 0 ? 0 : P.nx - x, ym = y == 0 ? 0 : P.ny - y;
-    const long long mm = (long long)ym * P.nx + xm;
-    if (mm < m) return;                               // solved by the thread of -m
+    const long long m = (long long)y * P.nx + x;
+    const long long mm = (long long)(y == 0 ? 0 : P.ny - y) * P.nx + (x == 0 ? 0 : P.nx - x);
+    float2 *Ca = sp.C + P.coff + m, *Cb = sp.C + P.coff + mm;
+    for (int j = 0; j < Mp; ++j) {
+        float2 *s = (float2 *)(dp + (size_t)j * T + tx);
+        cp8(s, Ca + j * modes);
+        cp8(s + 1, Cb + j * modes);
+    }
+    cp_commit();
     const float dg = __ldg(sp.lam + P.lamx + x) + __ldg(sp.lam + P.lamy + y) + 2.f;
     const float s = 0.5f * P.scale;
-    float2 *Ca = sp.C + P.coff + m, *Cb = sp.C + P.coff + mm;
+    cp_wait<0>();
     float c_prev = 0.f;
     float2 d_prev = make_float2(0.f, 0.f);
     auto sweep = [&](int k, float2 rk) {             // forward elimination (sub/super-diagonal -1)
         const float inv = 1.f / (dg + c_prev);
-        const float2 dk = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
+        d_prev = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
         c_prev = -inv;
-        cps[k * T + threadIdx.x] = c_prev;
-        dps[k * T + threadIdx.x] = dk;
-        d_prev = dk;
+        cps[k * T + tx] = c_prev;
+        return d_prev;
     };
-    #pragma unroll 4
-    for (int j = 0; 2 * j < M; ++j) {
-        const float2 a = Ca[j * modes], b = Cb[j * modes];
-        sweep(2 * j, make_float2(a.x + b.x, a.y - b.y));                 // 2 (Z(m) + conj Z(-m)) / 2
-        if (2 * j + 1 < M) sweep(2 * j + 1, make_float2(a.y + b.y, b.x - a.x));   // (Z(m) - conj Z(-m)) / i
+    for (int j = 0; j < Mp; ++j) {
+        const float4 ab = dp[(size_t)j * T + tx];    // a = Z(m), b = Z(-m)
+        const float2 d0 = sweep(2 * j, make_float2(ab.x + ab.z, ab.y - ab.w));   // 2 (Z(m) + conj Z(-m)) / 2
+        float2 d1 = make_float2(0.f, 0.f);
+        if (2 * j + 1 < M) d1 = sweep(2 * j + 1, make_float2(ab.y + ab.w, ab.z - ab.x));   // (Z(m) - conj Z(-m)) / i
+        dp[(size_t)j * T + tx] = make_float4(d0.x, d0.y, d1.x, d1.y);
     }
     // back substitution, two planes at a time; store conj of the packed pair
     // W(m) = X_2j + i X_2j+1 and W(-m) = conj X_2j + i conj X_2j+1
-    float2 xn = d_prev;
-    float2 u, v = make_float2(0.f, 0.f);
     auto put = [&](int j, float2 p0, float2 p1) {
         Ca[j * modes] = make_float2(p0.x - p1.y, -(p0.y + p1.x));
         Cb[j * modes] = make_float2(p0.x + p1.y, p0.y - p1.x);
     };
-    int k = M - 1;
-    if ((M & 1) == 0) {
-        v = xn;                                       // plane M-1 is the odd member of the last pair
-        const float2 dk = dps[(k - 1) * T + threadIdx.x];
-        const float c = cps[(k - 1) * T + threadIdx.x];
-        xn = make_float2(dk.x - c * xn.x, dk.y - c * xn.y);
-        --k;
-    }
-    u = xn;                                           // plane k (even)
-    put(k >> 1, u, v);
-    for (k -= 2; k >= 0; k -= 2) {
-        float2 dk = dps[(k + 1) * T + threadIdx.x];
-        float c = cps[(k + 1) * T + threadIdx.x];
-        v = make_float2(dk.x - c * xn.x, dk.y - c * xn.y);
-        dk = dps[k * T + threadIdx.x];
-        c = cps[k * T + threadIdx.x];
-        u = make_float2(dk.x - c * v.x, dk.y - c * v.y);
+    float2 xn = make_float2(0.f, 0.f);               // x_{k+1} of the plane above the pair
+    for (int j = Mp - 1; j >= 0; --j) {
+        const float4 dd = dp[(size_t)j * T + tx];
+        float2 v = make_float2(0.f, 0.f);
+        if (2 * j + 1 < M) {
+            const float c = cps[(2 * j + 1) * T + tx];
+            v = make_float2(dd.z - c * xn.x, dd.w - c * xn.y);
+        }
+        const float c = cps[2 * j * T + tx];
+        const float2 u = make_float2(dd.x - c * v.x, dd.y - c * v.y);
+        put(j, u, v);
         xn = u;
-        put(k >> 1, u, v);
     }
 }
 

@@ -25,14 +25,6 @@
 
 namespace cmsl {
 
-__device__ __forceinline__ void cp4(void *dst, const void *src)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
 constexpr int TR32 = 12;     // FP32 rotation per grain: 9 values + 3 pad (three 16-byte loads)
 
 // Warm start of a step's first refinement pass (own cell): 0 the previous
