@@ -6,7 +6,8 @@
 //     the vectorised passes) and are in the reference's C order
 //     i + nx*(j + ny*k);
 //   * P fields: two ping-pong sets of six SoA arrays (Pmx..Psz) in the
-//     compute type T (double for CMSL_FP64, float for CMSL_FP32_REFINED);
+//     compute type T (double for CMSL_FP64, float for CMSL_FP32_REFINED),
+//     each set one allocation with field q at q * ncells;
 //   * code[c]: grain id (bits 0-23, film-local) | material (bits 24-25) |
 //     interface flag (bit 26) -- replaces the reference's seven per-voxel FP64
 //     parameter arrays, omega and is_interface (kernels_evol.cu:133-146);

@@ -739,8 +739,11 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     CK(cudaMemcpy(e->d_code, code.data(), sizeof(uint32_t) * cells, cudaMemcpyHostToDevice));
     if (e->precision == CMSL_FP64) TRY(upload_TR<double>(e, descs, n));
     else TRY(upload_TR<float>(e, descs, n));
-    for (int s = 0; s < 2; ++s)
-        for (int q = 0; q < 6; ++q) TRY(e->alloc(&e->d_P[s][q], e->esz * cells));
+    for (int s = 0; s < 2; ++s) {
+        // the six fields of a set back to back (field q at q * cells)
+        TRY(e->alloc(&e->d_P[s][0], 6 * e->esz * cells));
+        for (int q = 1; q < 6; ++q) e->d_P[s][q] = (char *)e->d_P[s][0] + q * e->esz * cells;
+    }
     TRY(e->alloc(&e->d_r, e->esz * cells));
     TRY(e->alloc(&e->d_q, e->esz * cells));
     TRY(e->alloc(&e->d_dinv, e->esz * cells));

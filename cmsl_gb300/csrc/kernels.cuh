@@ -78,18 +78,21 @@ __device__ __forceinline__ float phi_diff(df a, df b)
 
 // Asynchronous global -> shared copies (cp.async, 4 or 8 bytes, both
 // addresses aligned to the size), grouped per commit; cp_wait<N> returns
-// once at most N of this thread's groups are still in flight.
+// once at most N of this thread's groups are still in flight.  The copies
+// carry no compiler memory clobber: their destinations are read only after
+// cp_wait (which has one) and a barrier, and their sources are not written
+// while they are in flight.
 __device__ __forceinline__ void cp4(void *dst, const void *src)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src));
 }
 __device__ __forceinline__ void cp8(void *dst, const void *src)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src));
 }
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n"); }
 template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // ------------------------------------------------------------------ tiles

@@ -44,6 +44,15 @@ __device__ __forceinline__ int phi_free(const SolveDev *S)
     return 10 - S->phi_cur - S->phi_prev - S->phi_prev2 - S->phi_prev3;
 }
 
+// Stage bookkeeping of the ring: s is the stage of the plane being computed.
+template <int NS> struct RingIdx {
+    int s;
+    __device__ __forceinline__ int up(bool top) const { return top ? s : (s + 1 == NS ? 0 : s + 1); }
+    __device__ __forceinline__ int dn(bool bottom) const { return bottom ? s : (s == 0 ? NS - 1 : s - 1); }
+    __device__ __forceinline__ int ahead() const { return s >= 2 ? s - 2 : s + NS - 2; }   // plane k + NS - 2
+    __device__ __forceinline__ void next() { s = s + 1 == NS ? 0 : s + 1; }
+};
+
 // ------------------------------------------------------------ TDGL step
 // kernelCalc_antiferro (kernels_evol.cu:47-231) with E_dep of the current
 // potential (depol_varEPS.cu:223-276) and the sweep-row sums
@@ -107,13 +116,14 @@ __device__ __forceinline__ void tdgl_cell32(const float4 *K, const float4 *tr, c
 
 // z neighbours of the potential for E (depol_varEPS.cu:246-273): zero beyond
 // the Dirichlet planes, mirrored for the Neumann boundary.
-__device__ __forceinline__ void efield_z(const FilmDev *f, int k, df fu, df fd, df &pu, df &pd)
+__device__ __forceinline__ void efield_z(bool neumann, int k, int nz, df fu, df fd, df &pu, df &pd)
 {
-    if (f->zbc == 0) {
-        pu = (k == f->nz - 1) ? df{0.f, 0.f} : fu;
+    if (!neumann) {
+        pu = (k == nz - 1) ? df{0.f, 0.f} : fu;
         pd = (k == 0) ? df{0.f, 0.f} : fd;
     } else {
-        op_z<df>(f, k, fu, fd, pu, pd);
+        pu = (k == nz - 1) ? fd : fu;         // mirrored (depol_varEPS.cu:86-99)
+        pd = (k == 0) ? fu : fd;
     }
 }
 
@@ -149,67 +159,69 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
     const int cur = d.ctl->cur, rs = d.ctl->run_step;
     const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
     const int row = d.rows[(long long)it.x * d.wstride + rs];
-    const int dep = f->dep_flag, nz = g.nz;
-    const long long off = f->off, lo = d.ncells;
+    // film constants in registers (the stores below might alias the film table)
+    const int dep = f->dep_flag, nz = g.nz, warm = f->warm;
+    const bool neu = f->zbc != 0;
+    const float inv_2hf = f->inv_2hf;
+    const long long off = f->off, lo = d.ncells, fs = d.ncells;
     const SolveDev *S = d.solve + it.x;
     const float *ph = (const float *)phi_sel(d, S->phi_cur) + off;
     const float *qh = (const float *)phi_sel(d, S->phi_prev) + off;
     const float *uh = (const float *)phi_sel(d, S->phi_prev2) + off;
     const float *vh = (const float *)phi_sel(d, S->phi_prev3) + off;
     float *nh = (float *)phi_sel(d, phi_free(S)) + off;
-    const int warm = f->warm;
     const uint32_t *code = d.code + off;
     const float4 *TR4 = (const float4 *)(F.TR + (long long)TR32 * f->g_off);
-    const float inv_2hf = f->inv_2hf;
+    const float *Po = (cur ? F.P[1][0] : F.P[0][0]) + off;   // the six fields of a set at q * fs
+    float *Pn = (cur ? F.P[0][0] : F.P[1][0]) + off;
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
 
-    auto Pold = [&](int q) { return (cur ? F.P[1][q] : F.P[0][q]) + off; };
-    auto stage = [&](int p) { return ring + ((p - zlo) % NS) * T32_STAGE; };
-    auto issue = [&](int p) {
+    // copies of plane p (planes are issued in order, p = zlo, zlo + 1, ...)
+    long long own_o = g.own_pl + (long long)zlo * g.plane, halo_o = g.halo_pl + (long long)zlo * g.plane;
+    auto issue = [&](int p, float *st) {
         if (p <= zhi) {
-            float *st = stage(p);
-            const long long pp = (long long)p * g.plane;
             if (g.valid) {
-                const long long o = g.own_pl + pp;
                 #pragma unroll
-                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.own_slot, Pold(q) + o);
+                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.own_slot, Po + q * fs + own_o);
                 if (dep) {
-                    cp4(st + 6 * SPL + g.own_slot, ph + o);
-                    cp4(st + 7 * SPL + g.own_slot, ph + lo + o);
+                    cp4(st + 6 * SPL + g.own_slot, ph + own_o);
+                    cp4(st + 7 * SPL + g.own_slot, ph + lo + own_o);
                 }
-                cp4(st + 8 * SPL + threadIdx.x, code + o);
+                cp4(st + 8 * SPL + threadIdx.x, code + own_o);
             }
             if (g.halo) {
-                const long long o = g.halo_pl + pp;
                 #pragma unroll
-                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.halo_slot, Pold(q) + o);
+                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.halo_slot, Po + q * fs + halo_o);
                 if (dep) {
-                    cp4(st + 6 * SPL + g.halo_slot, ph + o);
-                    cp4(st + 7 * SPL + g.halo_slot, ph + lo + o);
+                    cp4(st + 6 * SPL + g.halo_slot, ph + halo_o);
+                    cp4(st + 7 * SPL + g.halo_slot, ph + lo + halo_o);
                 }
             }
         }
         cp_commit();
+        own_o += g.plane;
+        halo_o += g.plane;
     };
-    for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p);
+    for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p, ring + (p - zlo) * T32_STAGE);
 
     float acc[7];
     #pragma unroll
     for (int q = 0; q < 7; ++q) acc[q] = 0.f;
     const int s0 = g.own_slot;
-    for (int k = z0; k < z1; ++k) {
+    RingIdx<NS> ri{z0 - zlo};
+    long long o = g.own_pl + (long long)z0 * g.plane;
+    for (int k = z0; k < z1; ++k, o += g.plane, ri.next()) {
         cp_wait<NS - 4>();
         __syncthreads();
-        issue(k + NS - 2);
+        issue(k + NS - 2, ring + ri.ahead() * T32_STAGE);
         if (!g.valid) continue;
-        const long long o = g.own_pl + (long long)k * g.plane;
         // older potentials for the warm start (consumed after the step's arithmetic)
         df wq{0.f, 0.f}, wu{0.f, 0.f}, wv{0.f, 0.f};
         if (dep && warm >= 1) wq = df{qh[o], qh[lo + o]};
         if (dep && warm >= 2) wu = df{uh[o], uh[lo + o]};
         if (dep && warm >= 3) wv = df{vh[o], vh[lo + o]};
-        const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
-        const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
+        const float *sk = ring + ri.s * T32_STAGE;
+        const float *su = ring + ri.up(k == nz - 1) * T32_STAGE, *sd = ring + ri.dn(k == 0) * T32_STAGE;
         const uint32_t c = ((const uint32_t *)sk)[8 * SPL + threadIdx.x];
         float pc[6], sum[6];
         #pragma unroll
@@ -229,7 +241,8 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
             const float *fh = sk + 6 * SPL, *fl = sk + 7 * SPL;
             a0 = df{fh[s0], fl[s0]};
             df pu, pd;
-            efield_z(f, k, df{su[6 * SPL + s0], su[7 * SPL + s0]}, df{sd[6 * SPL + s0], sd[7 * SPL + s0]}, pu, pd);
+            efield_z(neu, k, nz, df{su[6 * SPL + s0], su[7 * SPL + s0]}, df{sd[6 * SPL + s0], sd[7 * SPL + s0]},
+                     pu, pd);
             // -1 * E with E = -(phi_+ - phi_-) / (2h)
             ex = phi_diff(df{fh[s0 + 1], fl[s0 + 1]}, df{fh[s0 - 1], fl[s0 - 1]}) * inv_2hf;
             ey = phi_diff(df{fh[s0 + SX], fl[s0 + SX]}, df{fh[s0 - SX], fl[s0 - SX]}) * inv_2hf;
@@ -239,7 +252,7 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
                     pMZl, pSZl);
         #pragma unroll
-        for (int q = 0; q < 6; ++q) (cur ? F.P[0][q] : F.P[1][q])[off + o] = pn[q];
+        for (int q = 0; q < 6; ++q) Pn[q * fs + o] = pn[q];
         if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
         if (dep) {
             const df w = extrap_phi(warm, a0, wq, wu, wv);
@@ -343,37 +356,55 @@ struct RCell {
     int mc, me, mw, mn, ms, mu, md;          // materials (general eps only)
 };
 
+// Film constants of a residual pass, held in registers.
+struct RConst {
+    df cb, cu;                  // eps_0_nd / (2h); eps / h^2 on every face (one eps)
+    float dinv_u;               // Jacobi weight of the non-identity rows (one eps)
+    int nz;
+    bool neu;                   // Neumann z boundary (mirrored end rows, one pinned cell)
+    long long ref;              // the pinned cell (film-local)
+    const float *cf_h, *cf_l;   // general eps: face coefficient tables (through the film table)
+};
+
+// z neighbours of the operator (depol_varEPS.cu:86-99), given the loaded
+// k+1 and k-1 values (clamped at the ends).
+template <class V>
+__device__ __forceinline__ void zpick(const RConst &rc, int k, V up, V dn, V &u, V &dd)
+{
+    if (!rc.neu || (k > 0 && k < rc.nz - 1)) { u = up; dd = dn; }
+    else if (k == 0) { u = up; dd = up; }
+    else { u = dn; dd = dn; }
+}
+
 // -A dx of one non-identity row in FP32 (dx: the pending correction).
 template <bool UNI>
-__device__ __forceinline__ float minus_adx(const FilmDev *f, int k, const RCell &c)
+__device__ __forceinline__ float minus_adx(const RConst &rc, int k, const RCell &c)
 {
     float du, ddn;
-    op_z<float>(f, k, c.du, c.dd, du, ddn);
-    if (UNI) return f->cf_h[0] * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
+    zpick<float>(rc, k, c.du, c.dd, du, ddn);
+    if (UNI) return rc.cu.h * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
     int mu, md;
-    op_z<int>(f, k, c.mu, c.md, mu, md);
-    const float *ch = f->cf_h + c.mc * 3;
+    zpick<int>(rc, k, c.mu, c.md, mu, md);
+    const float *ch = rc.cf_h + c.mc * 3;
     return ch[c.me] * (c.de - c.dc) - ch[c.mw] * (c.dc - c.dw) + ch[c.mn] * (c.dn - c.dc) -
            ch[c.ms] * (c.dc - c.ds) + ch[mu] * (du - c.dc) - ch[md] * (c.dc - ddn);
 }
 
 // r (FP32 value of b - A x, double-float arithmetic) and b.h of one non-identity row.
 template <bool UNI>
-__device__ __forceinline__ void refine_row(const FilmDev *f, int k, const RCell &c, float &rv, float &bh)
+__device__ __forceinline__ void refine_row(const RConst &rc, int k, const RCell &c, float &rv, float &bh)
 {
-    const df cb{f->cb_h, f->cb_l};
-    const df bm = df_mul(div3(c.pxe, c.pxw, c.pyn, c.pys, c.pzu, c.pzd), cb);   // -b
+    const df bm = df_mul(div3(c.pxe, c.pxw, c.pyn, c.pys, c.pzu, c.pzd), rc.cb);   // -b
     df xu, xd;
-    op_z<df>(f, k, c.xu, c.xd, xu, xd);
+    zpick<df>(rc, k, c.xu, c.xd, xu, xd);
     df s;            // b - A phi
     if (UNI) {
-        const df cu{f->cf_h[0], f->cf_l[0]};   // eps/h^2 on every face
-        s = df_sub(df_mul(cu, lap7(c.xe, c.xw, c.xn, c.xs, xu, xd, c.xc)), bm);
+        s = df_sub(df_mul(rc.cu, lap7(c.xe, c.xw, c.xn, c.xs, xu, xd, c.xc)), bm);
     } else {
         int mu, md;
-        op_z<int>(f, k, c.mu, c.md, mu, md);
+        zpick<int>(rc, k, c.mu, c.md, mu, md);
         const int m3 = c.mc * 3;
-        auto cf = [&](int i) { return df{f->cf_h[m3 + i], f->cf_l[m3 + i]}; };
+        auto cf = [&](int i) { return df{rc.cf_h[m3 + i], rc.cf_l[m3 + i]}; };
         df a = df_sub(df_mul(cf(c.me), df_sub(c.xe, c.xc)), df_mul(cf(c.mw), df_sub(c.xc, c.xw)));
         a = df_add(a, df_mul(cf(c.mn), df_sub(c.xn, c.xc)));
         a = df_sub(a, df_mul(cf(c.ms), df_sub(c.xc, c.xs)));
@@ -388,51 +419,20 @@ __device__ __forceinline__ void refine_row(const FilmDev *f, int k, const RCell 
 // The last part of a residual pass of one cell: r and the partial sums.
 // upd: r = r_old - A dx (b.b is not formed); otherwise r = b - A x.
 template <bool UNI>
-__device__ __forceinline__ void refine_cell(const FilmDev *f, int k, bool ident, bool upd, const RCell &c,
+__device__ __forceinline__ void refine_cell(const RConst &rc, int k, bool ident, bool upd, const RCell &c,
                                             float r_old, float dinv, float &rv, float (&acc)[3])
 {
     float bh = 0.f, wj = 1.f;
     if (ident) {
         rv = -(c.xc.h + c.xc.l);              // x - g with g = 0, b = 0
     } else {
-        if (upd) rv = r_old + minus_adx<UNI>(f, k, c);
-        else refine_row<UNI>(f, k, c, rv, bh);
-        wj = UNI ? f->dinv_uni : dinv;
+        if (upd) rv = r_old + minus_adx<UNI>(rc, k, c);
+        else refine_row<UNI>(rc, k, c, rv, bh);
+        wj = UNI ? rc.dinv_u : dinv;
     }
     acc[0] = fmaf(rv, rv, acc[0]);
     acc[1] = fmaf(bh, bh, acc[1]);
     acc[2] = fmaf(rv, rv * wj, acc[2]);
-}
-
-// Common set-up of a residual pass.
-struct RefineSrc {
-    const float *xh, *dx, *Pmx, *Pmy, *Pmz, *dinv;
-    const uint32_t *code;
-    float *nh, *r;
-    long long lo;
-    bool run, apply, upd;
-};
-
-__device__ __forceinline__ RefineSrc refine_src(const Dev &d, const Fields<float> &F, const FilmDev *f,
-                                                const SolveDev *S)
-{
-    RefineSrc q;
-    q.run = f->dep_flag != 0 && (d.force || S->outer_active);
-    q.apply = S->refine > 0;     // later pass: x = phi + dx; first pass: x = the warm start
-    q.upd = q.apply && S->upd && f->upd_ok;   // r <- r - A dx
-    const int cur = d.ctl->cur, fr = phi_free(S);
-    const long long off = f->off;
-    q.lo = d.ncells;
-    q.xh = (const float *)phi_sel(d, q.apply ? S->phi_cur : fr) + off;
-    q.nh = (float *)phi_sel(d, fr) + off;
-    q.dx = F.x + off;
-    q.Pmx = (cur ? F.P[0][0] : F.P[1][0]) + off;
-    q.Pmy = (cur ? F.P[0][1] : F.P[1][1]) + off;
-    q.Pmz = (cur ? F.P[0][2] : F.P[1][2]) + off;
-    q.code = d.code + off;
-    q.dinv = F.dinv + off;
-    q.r = F.r + off;
-    return q;
 }
 
 __device__ __forceinline__ void refine_partials(const Dev &d, float (&acc)[3], double (*sRed)[3])
@@ -464,80 +464,89 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
     __shared__ double sTot[3];
     const int4 it = d.items[blockIdx.x];
     const FilmDev *f = d.films + it.x;
+    const SolveDev *S = d.solve + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
     const Geom g = make_geom(f, it.y, it.z);
     const int nz = g.nz;
-    const RefineSrc q = refine_src(d, F, f, d.solve + it.x);
-    const long long lo = q.lo;
-    const bool apply = q.apply, upd = UNI && q.upd;   // update passes follow the direct solve (one eps)
+    // film constants in registers (the stores below might alias the film table)
+    RConst rc;
+    rc.cb = df{f->cb_h, f->cb_l};
+    rc.cu = df{f->cf_h[0], f->cf_l[0]};
+    rc.dinv_u = f->dinv_uni;
+    rc.nz = nz;
+    rc.neu = f->zbc != 0;
+    rc.ref = f->ref_id;
+    rc.cf_h = f->cf_h;
+    rc.cf_l = f->cf_l;
+    const bool run = f->dep_flag != 0 && (d.force || S->outer_active);
+    const bool apply = S->refine > 0;                   // later pass: x = phi + dx; first: the warm start
+    const bool upd = UNI && apply && S->upd && f->upd_ok;   // r <- r - A dx (after the direct solve, one eps)
+    const int cur = d.ctl->cur, fr = phi_free(S);
+    const long long off = f->off, lo = d.ncells, fs = d.ncells;
+    const float *xh = (const float *)phi_sel(d, apply ? S->phi_cur : fr) + off;
+    float *nh = (float *)phi_sel(d, fr) + off;
+    const float *dx = F.x + off;
+    const float *Pm = (cur ? F.P[0][0] : F.P[1][0]) + off;   // the new Pm: x, y, z at 0, fs, 2 fs
+    const uint32_t *code = d.code + off;
+    const float *dinv = F.dinv + off;
+    float *r = F.r + off;
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
 
-    auto stage = [&](int p) { return ring + ((p - zlo) % NS) * L::STAGE; };
-    auto issue = [&](int p) {
-        if (q.run && p <= zhi && upd) {
-            // update pass: dx with its halo; phi and the old r of the own cell
-            float *st = stage(p);
-            const long long pp = (long long)p * g.plane;
-            if (g.valid) {
-                const long long o = g.own_pl + pp;
-                const int s = g.own_slot;
-                cp4(st + L::FH + s, q.xh + o);
-                cp4(st + L::FL + s, q.xh + lo + o);
-                cp4(st + L::DX + s, q.dx + o);
-                cp4(st + L::PX + s, q.r + o);
-                if (!UNI) {
-                    cp4(st + L::CODE + s, q.code + o);
-                    cp4(st + L::DINV + threadIdx.x, q.dinv + o);
+    // copies of plane p (planes are issued in order, p = zlo, zlo + 1, ...)
+    long long own_o = g.own_pl + (long long)zlo * g.plane, halo_o = g.halo_pl + (long long)zlo * g.plane;
+    auto issue = [&](int p, float *st) {
+        if (run && p <= zhi) {
+            const int so = g.own_slot, sh = g.halo_slot;
+            if (upd) {
+                // update pass: dx with its halo; phi and the old r of the own cell
+                if (g.valid) {
+                    cp4(st + L::FH + so, xh + own_o);
+                    cp4(st + L::FL + so, xh + lo + own_o);
+                    cp4(st + L::DX + so, dx + own_o);
+                    cp4(st + L::PX + so, r + own_o);
                 }
-            }
-            if (g.halo) {
-                const long long o = g.halo_pl + pp;
-                const int s = g.halo_slot;
-                cp4(st + L::DX + s, q.dx + o);
-                if (!UNI) cp4(st + L::CODE + s, q.code + o);
-            }
-        } else if (q.run && p <= zhi) {
-            float *st = stage(p);
-            const long long pp = (long long)p * g.plane;
-            if (g.valid) {
-                const long long o = g.own_pl + pp;
-                const int s = g.own_slot;
-                cp4(st + L::FH + s, q.xh + o);
-                cp4(st + L::FL + s, q.xh + lo + o);
-                if (apply) cp4(st + L::DX + s, q.dx + o);
-                cp4(st + L::PX + s, q.Pmx + o);
-                cp4(st + L::PY + s, q.Pmy + o);
-                cp4(st + L::PZ + threadIdx.x, q.Pmz + o);
-                if (!UNI) {
-                    cp4(st + L::CODE + s, q.code + o);
-                    cp4(st + L::DINV + threadIdx.x, q.dinv + o);
+                if (g.halo) cp4(st + L::DX + sh, dx + halo_o);
+            } else {
+                if (g.valid) {
+                    cp4(st + L::FH + so, xh + own_o);
+                    cp4(st + L::FL + so, xh + lo + own_o);
+                    if (apply) cp4(st + L::DX + so, dx + own_o);
+                    cp4(st + L::PX + so, Pm + own_o);
+                    cp4(st + L::PY + so, Pm + fs + own_o);
+                    cp4(st + L::PZ + threadIdx.x, Pm + 2 * fs + own_o);
+                    if (!UNI) {
+                        cp4(st + L::CODE + so, code + own_o);
+                        cp4(st + L::DINV + threadIdx.x, dinv + own_o);
+                    }
                 }
-            }
-            if (g.halo) {
-                const long long o = g.halo_pl + pp;
-                const int s = g.halo_slot;
-                cp4(st + L::FH + s, q.xh + o);
-                cp4(st + L::FL + s, q.xh + lo + o);
-                if (apply) cp4(st + L::DX + s, q.dx + o);
-                cp4(st + L::PX + s, q.Pmx + o);
-                cp4(st + L::PY + s, q.Pmy + o);
-                if (!UNI) cp4(st + L::CODE + s, q.code + o);
+                if (g.halo) {
+                    cp4(st + L::FH + sh, xh + halo_o);
+                    cp4(st + L::FL + sh, xh + lo + halo_o);
+                    if (apply) cp4(st + L::DX + sh, dx + halo_o);
+                    cp4(st + L::PX + sh, Pm + halo_o);
+                    cp4(st + L::PY + sh, Pm + fs + halo_o);
+                    if (!UNI) cp4(st + L::CODE + sh, code + halo_o);
+                }
             }
         }
         cp_commit();
+        own_o += g.plane;
+        halo_o += g.plane;
     };
-    for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p);
+    for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p, ring + (p - zlo) * L::STAGE);
 
     const int s0 = g.own_slot, tz = threadIdx.x;
+    const long long pin = rc.neu ? rc.ref - g.own_pl : -1;   // the pinned cell's plane offset in this column
     float acc[3] = {0.f, 0.f, 0.f};
-    for (int k = z0; k < z1; ++k) {
+    RingIdx<NS> ri{z0 - zlo};
+    long long o = g.own_pl + (long long)z0 * g.plane;
+    for (int k = z0; k < z1; ++k, o += g.plane, ri.next()) {
         cp_wait<NS - 4>();
         __syncthreads();
-        issue(k + NS - 2);
-        if (!q.run || !g.valid) continue;
-        const long long o = g.own_pl + (long long)k * g.plane;
-        const int ku = k == nz - 1 ? k : k + 1, kd = k == 0 ? k : k - 1;
-        const float *sk = stage(k), *su = stage(ku), *sd = stage(kd);
+        issue(k + NS - 2, ring + ri.ahead() * L::STAGE);
+        if (!run || !g.valid) continue;
+        const float *sk = ring + ri.s * L::STAGE;
+        const float *su = ring + ri.up(k == nz - 1) * L::STAGE, *sd = ring + ri.dn(k == 0) * L::STAGE;
         auto D = [&](const float *st, int s) { return st[L::DX + s]; };
         auto X = [&](const float *st, int s) {        // x = phi (+ dx on later passes)
             const df p{st[L::FH + s], st[L::FL + s]};
@@ -558,13 +567,14 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
             c.pyn = sk[L::PY + s0 + SX]; c.pys = sk[L::PY + s0 - SX];
             c.pzu = su[L::PZ + tz]; c.pzd = sd[L::PZ + tz];
         }
+        // identity rows: the Dirichlet planes, or the Neumann pin
+        const bool ident = rc.neu ? (long long)k * g.plane == pin : (k == 0 || k == nz - 1);
         float rv;
-        refine_cell<UNI>(f, k, identity_row(f, k, g.own_pl), upd, c, upd ? sk[L::PX + s0] : 0.f,
-                         UNI ? 0.f : sk[L::DINV + tz], rv, acc);
-        q.r[o] = rv;
+        refine_cell<UNI>(rc, k, ident, upd, c, upd ? sk[L::PX + s0] : 0.f, UNI ? 0.f : sk[L::DINV + tz], rv, acc);
+        r[o] = rv;
         if (apply) {
-            q.nh[o] = c.xc.h;
-            q.nh[lo + o] = c.xc.l;
+            nh[o] = c.xc.h;
+            nh[lo + o] = c.xc.l;
         }
     }
     cp_wait<0>();
