@@ -18,12 +18,12 @@
 // one solve per refinement pass replaces the PCG iterations; the outer
 // double-float refinement keeps the potential at the reference's tolerance.
 //
-// FFTs: self-sorting (Stockham) passes in shared memory -- radix 4 (and one
-// radix 2) for powers of two, radix 3 and 2 otherwise -- one block per group
-// of rows (x) or of columns (y); twiddles exp(-2 pi i t / n) and eigenvalues
-// come from host tables computed in double.  The z solve keeps the Thomas
-// elimination in shared memory, so each spectrum value is read and written
-// once per sweep.
+// FFTs: self-sorting (Stockham) passes through shared memory, the butterflies
+// in registers -- radix 16 (8, 4 or 2 for the remainder) for powers of two,
+// radix 3 and 2 otherwise -- one block per group of rows (x) or of columns
+// (y); twiddles exp(-2 pi i t / n) and eigenvalues come from host tables
+// computed in double.  The z solve keeps the Thomas elimination in shared
+// memory, so each spectrum value is read and written once per sweep.
 #pragma once
 #include "kernels.cuh"
 
@@ -75,7 +75,126 @@ __device__ __forceinline__ float2 c_mul(float2 a, float2 b)
 // distinct banks.  tw: the n twiddles, staged in shared memory.
 __host__ __device__ __forceinline__ int spec_pad(int i) { return i + (i >> 4); }
 
-// n = 2^lgn: radix-4 passes (one radix-2 pass when lgn is odd), shifts and masks.
+// Forward DFTs of 4, 8 and 16 values held in registers, y_k = sum_n v_n
+// exp(-2 pi i n k / R).  dft4 and dft8 leave y in natural order; dft16 (4 x 4
+// split) leaves y_k at v[4 (k mod 4) + k / 4] (dft_out gives the slot's k).
+__device__ __forceinline__ void dft4(float2 &a, float2 &b, float2 &c, float2 &d)
+{
+    const float2 s02 = c_add(a, c), d02 = c_sub(a, c), s13 = c_add(b, d), d13 = c_sub(b, d);
+    const float2 rot = make_float2(d13.y, -d13.x);     // -i (b - d)
+    a = c_add(s02, s13);
+    b = c_add(d02, rot);
+    c = c_sub(s02, s13);
+    d = c_sub(d02, rot);
+}
+
+constexpr float SPEC_R2 = 0.70710678118654752f;    // cos(pi/4)
+constexpr float SPEC_C8 = 0.92387953251128676f;    // cos(pi/8)
+constexpr float SPEC_S8 = 0.38268343236508977f;    // sin(pi/8)
+
+__device__ __forceinline__ float2 c_mulc(float2 v, float wr, float wi)
+{
+    return make_float2(v.x * wr - v.y * wi, v.x * wi + v.y * wr);
+}
+
+__device__ __forceinline__ void dft2(float2 &a, float2 &b)
+{
+    const float2 t = a;
+    a = c_add(t, b);
+    b = c_sub(t, b);
+}
+
+__device__ __forceinline__ void dft8(float2 (&v)[8])
+{
+    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4(e0, e1, e2, e3);
+    dft4(o0, o1, o2, o3);
+    o1 = c_mulc(o1, SPEC_R2, -SPEC_R2);                // w8^1
+    o2 = make_float2(o2.y, -o2.x);                     // w8^2 = -i
+    o3 = c_mulc(o3, -SPEC_R2, -SPEC_R2);               // w8^3
+    v[0] = c_add(e0, o0); v[4] = c_sub(e0, o0);
+    v[1] = c_add(e1, o1); v[5] = c_sub(e1, o1);
+    v[2] = c_add(e2, o2); v[6] = c_sub(e2, o2);
+    v[3] = c_add(e3, o3); v[7] = c_sub(e3, o3);
+}
+
+// v * w16^e for the exponents e = n2 k1 (n2, k1 < 4) of the 4 x 4 split
+__device__ __forceinline__ float2 w16(int e, float2 v)
+{
+    switch (e) {
+    case 0: return v;
+    case 1: return c_mulc(v, SPEC_C8, -SPEC_S8);
+    case 2: return c_mulc(v, SPEC_R2, -SPEC_R2);
+    case 3: return c_mulc(v, SPEC_S8, -SPEC_C8);
+    case 4: return make_float2(v.y, -v.x);
+    case 6: return c_mulc(v, -SPEC_R2, -SPEC_R2);
+    default: return c_mulc(v, -SPEC_C8, SPEC_S8);     // e = 9
+    }
+}
+
+__device__ __forceinline__ void dft16(float2 (&v)[16])
+{
+    // n = 4 n1 + n2, k = k1 + 4 k2: DFT4 over n1, twiddle w16^(n2 k1), DFT4 over n2
+    #pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+    #pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1)
+        #pragma unroll
+        for (int n2 = 1; n2 < 4; ++n2) v[4 * k1 + n2] = w16(n2 * k1, v[4 * k1 + n2]);
+    #pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+}
+
+template <int R> __device__ __forceinline__ constexpr int dft_out(int i) { return R == 16 ? (i >> 2) + 4 * (i & 3) : i; }
+
+template <int R> __device__ __forceinline__ void dft_reg(float2 (&v)[R])
+{
+    if constexpr (R == 2) dft2(v[0], v[1]);
+    else if constexpr (R == 4) dft4(v[0], v[1], v[2], v[3]);
+    else if constexpr (R == 8) dft8(v);
+    else dft16(v);
+}
+
+// One self-sorting (Stockham) pass of radix R on a tile: butterfly j of a
+// sequence takes elements j + r n/R (r < R), twiddled by w_n^(r (j mod Ns)
+// n / (Ns R)), and writes its DFT to (j / Ns) Ns R + (j mod Ns) + k Ns.
+template <int R, bool SEQ_FAST>
+__device__ __forceinline__ void stockham_pass(const float2 *a, float2 *b, int nseq, int lgs, int lgn, int lgNs,
+                                              int es, int ss, const float2 *tw)
+{
+    constexpr int lgR = R == 16 ? 4 : R == 8 ? 3 : R == 4 ? 2 : 1;
+    const int lgnbf = lgn - lgR, nbf = 1 << lgnbf;
+    const int Ns = 1 << lgNs;
+    const int lgstep = lgn - lgNs - lgR;              // twiddle stride n / (Ns R)
+    const int total = nseq << lgnbf;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int sq, j;
+        if (SEQ_FAST) {
+            if (lgs >= 0) { j = t >> lgs; sq = t & (nseq - 1); }
+            else { j = t / nseq; sq = t - j * nseq; }
+        } else {
+            sq = t >> lgnbf; j = t & (nbf - 1);
+        }
+        const int jm = j & (Ns - 1);
+        const int o = ((j >> lgNs) << (lgNs + lgR)) + jm;
+        const int base = sq * ss;
+        auto at = [&](int e) { return SEQ_FAST ? base + e * es : spec_pad(base + e * es); };
+        const int tj = jm << lgstep;
+        float2 v[R];
+        #pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = a[at(j + r * nbf)];
+        if (lgNs > 0) {
+            #pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], tw[r * tj]);
+        }
+        dft_reg<R>(v);
+        #pragma unroll
+        for (int i = 0; i < R; ++i) b[at(o + dft_out<R>(i) * Ns)] = v[i];
+    }
+}
+
+// n = 2^lgn: passes of radix 16 (8, 4 or 2 for the remainder; a radix-8
+// pass first when the remainder would be a lone radix-2).
 template <bool SEQ_FAST>
 __device__ __forceinline__ float2 *fft_pow2(float2 *a, float2 *b, int nseq, int lgn, int es, int ss,
                                             const float2 *tw)
@@ -83,42 +202,20 @@ __device__ __forceinline__ float2 *fft_pow2(float2 *a, float2 *b, int nseq, int 
     const int lgs = (nseq & (nseq - 1)) == 0 ? __ffs(nseq) - 1 : -1;   // sequences per tile, as a shift
     int lgNs = 0;
     while (lgNs < lgn) {
-        const int lgR = (lgn - lgNs >= 2) ? 2 : 1;
-        const int lgnbf = lgn - lgR, nbf = 1 << lgnbf;
-        const int Ns = 1 << lgNs;
-        const int lgstep = lgn - lgNs - lgR;          // twiddle stride n / (Ns R)
-        const int total = nseq << lgnbf;
-        for (int t = threadIdx.x; t < total; t += blockDim.x) {
-            int sq, j;
-            if (SEQ_FAST) {
-                if (lgs >= 0) { j = t >> lgs; sq = t & (nseq - 1); }
-                else { j = t / nseq; sq = t - j * nseq; }
-            } else {
-                sq = t >> lgnbf; j = t & (nbf - 1);
-            }
-            const int jm = j & (Ns - 1);
-            const int o = ((j >> lgNs) << (lgNs + lgR)) + jm;
-            const int base = sq * ss;
-            auto at = [&](int e) { return SEQ_FAST ? base + e * es : spec_pad(base + e * es); };
-            const int tj = jm << lgstep;
-            if (lgR == 2) {
-                const float2 v0 = a[at(j)];
-                const float2 v1 = c_mul(a[at(j + nbf)], tw[tj]);
-                const float2 v2 = c_mul(a[at(j + 2 * nbf)], tw[2 * tj]);
-                const float2 v3 = c_mul(a[at(j + 3 * nbf)], tw[3 * tj]);
-                const float2 s02 = c_add(v0, v2), d02 = c_sub(v0, v2);
-                const float2 s13 = c_add(v1, v3), d13 = c_sub(v1, v3);
-                const float2 rot = make_float2(d13.y, -d13.x);     // -i (v1 - v3)
-                b[at(o)] = c_add(s02, s13);
-                b[at(o + Ns)] = c_add(d02, rot);
-                b[at(o + 2 * Ns)] = c_sub(s02, s13);
-                b[at(o + 3 * Ns)] = c_sub(d02, rot);
-            } else {
-                const float2 v0 = a[at(j)];
-                const float2 v1 = c_mul(a[at(j + nbf)], tw[tj]);
-                b[at(o)] = c_add(v0, v1);
-                b[at(o + Ns)] = c_sub(v0, v1);
-            }
+        const int rem = lgn - lgNs;
+        int lgR;
+        if (rem >= 4 && (rem & 3) != 1) {
+            stockham_pass<16, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
+            lgR = 4;
+        } else if (rem >= 3) {
+            stockham_pass<8, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
+            lgR = 3;
+        } else if (rem == 2) {
+            stockham_pass<4, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
+            lgR = 2;
+        } else {
+            stockham_pass<2, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
+            lgR = 1;
         }
         __syncthreads();
         float2 *tmp = a;
