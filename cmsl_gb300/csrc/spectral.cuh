@@ -31,7 +31,6 @@ namespace cmsl {
 
 constexpr int SPEC_MAX_STAGES = 13;       // 2^12 = 4096
 constexpr int SPEC_ELEMS = 2048;          // complex values staged per block (6 blocks per SM)
-constexpr int SPEC_LB = 8;                // global loads in flight per thread
 constexpr int SPEC_NT = 256;
 
 struct SpecAxis {
@@ -158,9 +157,14 @@ template <int R> __device__ __forceinline__ void dft_reg(float2 (&v)[R])
 // One self-sorting (Stockham) pass of radix R on a tile: butterfly j of a
 // sequence takes elements j + r n/R (r < R), twiddled by w_n^(r (j mod Ns)
 // n / (Ns R)), and writes its DFT to (j / Ns) Ns R + (j mod Ns) + k Ns.
-template <int R, bool SEQ_FAST>
+// The first pass reads through ld(sequence, element) instead of tile a, the
+// last writes through st(sequence, element, value) instead of tile b, so the
+// data goes from global memory to registers and back with one shared-memory
+// exchange per further pass.
+template <int R, bool SEQ_FAST, class LD, class ST>
 __device__ __forceinline__ void stockham_pass(const float2 *a, float2 *b, int nseq, int lgs, int lgn, int lgNs,
-                                              int es, int ss, const float2 *tw)
+                                              int es, int ss, const float2 *tw, bool first, bool last, LD &ld,
+                                              ST &st)
 {
     constexpr int lgR = R == 16 ? 4 : R == 8 ? 3 : R == 4 ? 2 : 1;
     const int lgnbf = lgn - lgR, nbf = 1 << lgnbf;
@@ -181,49 +185,54 @@ __device__ __forceinline__ void stockham_pass(const float2 *a, float2 *b, int ns
         auto at = [&](int e) { return SEQ_FAST ? base + e * es : spec_pad(base + e * es); };
         const int tj = jm << lgstep;
         float2 v[R];
-        #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = a[at(j + r * nbf)];
+        if (first) {
+            #pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = ld(sq, j + r * nbf);
+        } else {
+            #pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = a[at(j + r * nbf)];
+        }
         if (lgNs > 0) {
             #pragma unroll
             for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], tw[r * tj]);
         }
         dft_reg<R>(v);
-        #pragma unroll
-        for (int i = 0; i < R; ++i) b[at(o + dft_out<R>(i) * Ns)] = v[i];
+        if (last) {
+            #pragma unroll
+            for (int i = 0; i < R; ++i) st(sq, o + dft_out<R>(i) * Ns, v[i]);
+        } else {
+            #pragma unroll
+            for (int i = 0; i < R; ++i) b[at(o + dft_out<R>(i) * Ns)] = v[i];
+        }
     }
 }
 
 // n = 2^lgn: passes of radix 16 (8, 4 or 2 for the remainder; a radix-8
-// pass first when the remainder would be a lone radix-2).
-template <bool SEQ_FAST>
-__device__ __forceinline__ float2 *fft_pow2(float2 *a, float2 *b, int nseq, int lgn, int es, int ss,
-                                            const float2 *tw)
+// pass first when the remainder would be a lone radix-2), between ld and st
+// (see stockham_pass) with tiles a and b for the exchanges.  The twiddles
+// must be visible to the block (a barrier after staging them).
+template <bool SEQ_FAST, class LD, class ST>
+__device__ __forceinline__ void fft_pow2(float2 *a, float2 *b, int nseq, int lgn, int es, int ss, const float2 *tw,
+                                         LD ld, ST st)
 {
     const int lgs = (nseq & (nseq - 1)) == 0 ? __ffs(nseq) - 1 : -1;   // sequences per tile, as a shift
+    if (lgn == 0)                                                     // n = 1: the identity
+        for (int t = threadIdx.x; t < nseq; t += blockDim.x) st(t, 0, ld(t, 0));
     int lgNs = 0;
     while (lgNs < lgn) {
         const int rem = lgn - lgNs;
-        int lgR;
-        if (rem >= 4 && (rem & 3) != 1) {
-            stockham_pass<16, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
-            lgR = 4;
-        } else if (rem >= 3) {
-            stockham_pass<8, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
-            lgR = 3;
-        } else if (rem == 2) {
-            stockham_pass<4, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
-            lgR = 2;
-        } else {
-            stockham_pass<2, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw);
-            lgR = 1;
-        }
-        __syncthreads();
+        const int lgR = (rem >= 4 && (rem & 3) != 1) ? 4 : rem >= 3 ? 3 : rem;
+        const bool first = lgNs == 0, last = lgNs + lgR == lgn;
+        if (lgR == 4) stockham_pass<16, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw, first, last, ld, st);
+        else if (lgR == 3) stockham_pass<8, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw, first, last, ld, st);
+        else if (lgR == 2) stockham_pass<4, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw, first, last, ld, st);
+        else stockham_pass<2, SEQ_FAST>(a, b, nseq, lgs, lgn, lgNs, es, ss, tw, first, last, ld, st);
+        if (!last) __syncthreads();
         float2 *tmp = a;
         a = b;
         b = tmp;
         lgNs += lgR;
     }
-    return a;
 }
 
 // Any 2^a 3^b length: radix-3 and radix-2 passes.
@@ -270,13 +279,6 @@ __device__ __forceinline__ float2 *fft_mixed(float2 *a, float2 *b, int nseq, con
     return a;
 }
 
-template <bool SEQ_FAST>
-__device__ __forceinline__ float2 *fft_tile(float2 *a, float2 *b, int nseq, const SpecAxis &pl, int es, int ss,
-                                            const float2 *tw)
-{
-    if (pl.lg >= 0) return fft_pow2<SEQ_FAST>(a, b, nseq, pl.lg, es, ss, tw);
-    return fft_mixed<SEQ_FAST>(a, b, nseq, pl, es, ss, tw);
-}
 
 // Whether film f's inner solve runs through the spectra in this pass.
 __device__ __forceinline__ bool spec_run(const Dev &d, int f)
@@ -309,7 +311,7 @@ __device__ __forceinline__ void spec_finish(const Dev &d)
 // spectra into the real correction x (and x = 0 on the Dirichlet planes).
 // Shared memory: two padded tiles of rb rows and the twiddles.
 template <bool IN_REAL>
-__global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
+__global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
     const int f = __ldg(sp.bx_film + blockIdx.x);
@@ -318,66 +320,54 @@ __global__ void __launch_bounds__(SPEC_NT) k_spec_x(Dev d, Fields<float> F, Spec
         return;
     }
     const SpecFilm &P = sp.films[f];
-    const int nx = P.nx, rows = P.Mp * P.ny, rb = max(1, SPEC_ELEMS / nx);
+    const int nx = P.nx, ny = P.ny, rows = P.Mp * ny, rb = max(1, SPEC_ELEMS / nx);
     const int r0 = (blockIdx.x - P.bx0) * rb, nr = min(rb, rows - r0);
-    const long long plane = (long long)nx * P.ny;
+    const long long plane = (long long)nx * ny;
     const float *rr = F.r + P.off;
     float *xx = F.x + P.off;
     float2 *Cf = sp.C + P.coff;
     const SpecAxis ax = P.ax;
-    const int M = P.M;
+    const int M = P.M, Mp = P.Mp;
     const int tile = spec_pad(rb * nx) + 1;
     float2 *a = sm2, *b = sm2 + tile, *tw = sm2 + 2 * tile;
     for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twx + t);
-    // rows r0 .. r0+nr-1 are consecutive: (j, y) runs over whole planes, so
-    // the residual rows of one packed plane are contiguous in r
-    const int total = nr * nx;
-    const int ny = P.ny;
-    for (int t0 = threadIdx.x; t0 < total; t0 += SPEC_LB * blockDim.x) {
-        float2 v[SPEC_LB];
-        #pragma unroll
-        for (int u = 0; u < SPEC_LB; ++u) {
-            const int t = t0 + u * blockDim.x;
-            if (t < total) {
-                if (IN_REAL) {
-                    const int rw = r0 + t / nx, j = rw / ny;           // packed plane
-                    const long long yx = (long long)(rw - j * ny) * nx + (t - (t / nx) * nx);
-                    const long long e = (long long)(2 * j + 1) * plane + yx;
-                    v[u] = make_float2(rr[e], 2 * j + 1 < M ? rr[e + plane] : 0.f);
-                } else {
-                    v[u] = Cf[(long long)r0 * nx + t];
-                }
-            }
-        }
-        #pragma unroll
-        for (int u = 0; u < SPEC_LB; ++u) {
-            const int t = t0 + u * blockDim.x;
-            if (t < total) a[spec_pad(t)] = v[u];
-        }
-    }
-    __syncthreads();
-    const float2 *res = fft_tile<false>(a, b, nr, ax, 1, nx, tw);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const float2 rv = res[spec_pad(t)];
+    // row r0 + sq is (j, y) = packed plane j, in-plane row y; its residual
+    // rows in r are z planes 2j+1 and 2j+2
+    auto ld = [&](int sq, int e) -> float2 {
+        if (!IN_REAL) return Cf[(long long)(r0 + sq) * nx + e];
+        const int rw = r0 + sq, j = rw / ny;
+        const long long o = (long long)(2 * j + 1) * plane + (long long)(rw - j * ny) * nx + e;
+        return make_float2(rr[o], 2 * j + 1 < M ? rr[o + plane] : 0.f);
+    };
+    auto st = [&](int sq, int e, float2 v) {
         if (IN_REAL) {
-            Cf[(long long)r0 * nx + t] = rv;
-        } else {
-            // the transform of conj(W) is conj(x_2j + i x_2j+1) (scale folded into the z solve)
-            const int rw = r0 + t / nx, j = rw / ny;
-            const long long yx = (long long)(rw - j * ny) * nx + (t - (t / nx) * nx);
-            const long long e = (long long)(2 * j + 1) * plane + yx;
-            xx[e] = rv.x;
-            if (2 * j + 1 < M) xx[e + plane] = -rv.y;
-            if (j == 0) xx[yx] = 0.f;                                        // first Dirichlet plane
-            if (j == P.Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;    // last one
+            Cf[(long long)(r0 + sq) * nx + e] = v;
+            return;
         }
+        // the transform of conj(W) is conj(x_2j + i x_2j+1) (scale folded into the z solve)
+        const int rw = r0 + sq, j = rw / ny;
+        const long long yx = (long long)(rw - j * ny) * nx + e, o = (long long)(2 * j + 1) * plane + yx;
+        xx[o] = v.x;
+        if (2 * j + 1 < M) xx[o + plane] = -v.y;
+        if (j == 0) xx[yx] = 0.f;                                        // first Dirichlet plane
+        if (j == Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;      // last one
+    };
+    if (ax.lg >= 0) {
+        __syncthreads();                                                 // twiddles
+        fft_pow2<false>(a, b, nr, ax.lg, 1, nx, tw, ld, st);
+    } else {
+        const int total = nr * nx;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) a[spec_pad(t)] = ld(t / nx, t - (t / nx) * nx);
+        __syncthreads();
+        const float2 *res = fft_mixed<false>(a, b, nr, ax, 1, nx, tw);
+        for (int t = threadIdx.x; t < total; t += blockDim.x) st(t / nx, t - (t / nx) * nx, res[spec_pad(t)]);
     }
     if (!IN_REAL) spec_finish(d);
 }
 
-// y transforms of column groups of one interior plane, in place on the
+// y transforms of column groups of one packed plane, in place on the
 // spectra; the tile keeps the plane's row-major layout (sequences interleaved).
-static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
+static __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_y(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
     const int f = __ldg(sp.by_film + blockIdx.x);
@@ -388,31 +378,21 @@ static __global__ void __launch_bounds__(SPEC_NT) k_spec_y(Dev d, SpecDev sp)
     const int lb = blockIdx.x - P.by0;
     const int kk = lb / groups, x0 = (lb - kk * groups) * cb, nc = min(cb, nx - x0);
     const SpecAxis ay = P.ay;
-    float2 *base = sp.C + P.coff + (long long)kk * nx * ny;
+    float2 *base = sp.C + P.coff + (long long)kk * nx * ny + x0;
     float2 *a = sm2, *b = sm2 + cb * ny, *tw = sm2 + 2 * cb * ny;
     for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twy + t);
-    const int total = nc * ny;
-    for (int t0 = threadIdx.x; t0 < total; t0 += SPEC_LB * blockDim.x) {
-        float2 v[SPEC_LB];
-        #pragma unroll
-        for (int u = 0; u < SPEC_LB; ++u) {
-            const int t = t0 + u * blockDim.x;
-            if (t < total) {
-                const int y = t / nc, c = t - y * nc;      // coalesced along x
-                v[u] = base[(long long)y * nx + x0 + c];
-            }
-        }
-        #pragma unroll
-        for (int u = 0; u < SPEC_LB; ++u) {
-            const int t = t0 + u * blockDim.x;
-            if (t < total) a[t] = v[u];
-        }
-    }
-    __syncthreads();
-    const float2 *res = fft_tile<true>(a, b, nc, ay, nc, 1, tw);
-    for (int t = threadIdx.x; t < nc * ny; t += blockDim.x) {
-        const int y = t / nc, c = t - y * nc;
-        base[(long long)y * nx + x0 + c] = res[t];
+    // sequence c = column x0 + c, element e = row y (coalesced along x)
+    auto ld = [&](int c, int e) { return base[(long long)e * nx + c]; };
+    auto st = [&](int c, int e, float2 v) { base[(long long)e * nx + c] = v; };
+    __syncthreads();                                                     // twiddles
+    if (ay.lg >= 0) {
+        fft_pow2<true>(a, b, nc, ay.lg, nc, 1, tw, ld, st);
+    } else {
+        const int total = nc * ny;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) a[t] = ld(t % nc, t / nc);
+        __syncthreads();
+        const float2 *res = fft_mixed<true>(a, b, nc, ay, nc, 1, tw);
+        for (int t = threadIdx.x; t < total; t += blockDim.x) st(t % nc, t / nc, res[t]);
     }
 }
 
