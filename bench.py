@@ -34,21 +34,24 @@ METRIC = "TDGL cell-steps/s incl. PCG, FP32-refined vs FP64 on GB300 at equal P-
 CONFIG_ID = 1
 
 # Algorithmic bytes per cell and launch (compulsory DRAM traffic of each kernel).
-#   tdgl:     read 6 P + phi (f64) + code, write 6 P
+#   tdgl:     read 6 P + phi + code, write 6 P (FP32 also: read the two older
+#             potentials of the quadratic warm start, write the warm start)
 #   setup:    FP64 rhs: read Pm(3) + phi + code + dinv, write r
-#             FP32 refine: read phi (f64) + delta + Pm(3) + code + dinv, write phi (f64) + r
-#   spmv:     (FP64) read r, p_old, dinv, code, write p, q
+#             FP32 first refinement pass (one eps): read x (double-float) + Pm(3), write r
 #   update:   (FP64) read x, p, r, q, dinv, write x, r
+#             (FP32 update pass after the direct solve) read phi (double-float), dx, r,
+#             write phi (double-float), r
+#   spmv:     (FP64) read r, p_old, dinv, code, write p, q
 #   pcg_iter: (FP32, one single-reduction iteration of the persistent solver)
 #             read x, p, r, s, w, dinv, code, write x, p, r, s, w
-#   spec:     (FP32, direct inner solve) x-FFT: read r, write spectra; y-FFT, z-solve (with its
-#             coefficient scratch) and y-FFT: read and write the spectra (8 B); x-FFT: read
-#             the spectra, write x -> 12 + 16 + 24 + 16 + 12 B
+#   spec:     (FP32, direct inner solve, two real planes per complex spectrum plane) x-FFT:
+#             read r, write spectra; y-FFT, z-solve, y-FFT: read and write the spectra;
+#             x-FFT: read the spectra, write x -> 5 x (4 + 4) B
 #   spmv32:   (FP32 batch, masked two-kernel PCG) read r, p_old, dinv, code, write p, q
 #   update32: (FP32 batch) read x, p, r, q, dinv, write x, r
 BYTES = {
-    "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4, "setup": 8 + 4 + 12 + 4 + 4 + 8 + 4, "pcg_iter": 7 * 4 + 5 * 4,
-             "spmv32": 4 * 4 + 2 * 4, "update32": 5 * 4 + 2 * 4, "spec": 80},
+    "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4 + 2 * 8 + 8, "setup": 8 + 12 + 4, "update": 8 + 4 + 4 + 4 + 8,
+             "pcg_iter": 7 * 4 + 5 * 4, "spmv32": 4 * 4 + 2 * 4, "update32": 5 * 4 + 2 * 4, "spec": 40},
     "fp64": {"tdgl": 6 * 8 * 2 + 8 + 4, "setup": 24 + 8 + 4 + 8 + 8, "spmv": 8 * 3 + 4 + 16,
              "update": 5 * 8 + 2 * 8},
 }
@@ -242,7 +245,7 @@ def run_ours(args):
     w = wl.config(args.config)
     kw = dict(precision=cg.FP64 if fp64 else cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8,
               max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000,
-              warm_start=3)
+              warm_start=2)
     film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **kw)
     film.set_state(w.P_init)
     K, W = args.steps, args.warmup
@@ -282,8 +285,10 @@ def run_ours(args):
     n_iter = float(np.mean(it))
     n_ref = float(np.mean(rf))
     direct = film.inner_solver == cg.INNER_DIRECT
-    names = ["tdgl", "setup", "spec"] if direct else KERNELS[mode]
-    count = {"tdgl": 1.0, "setup": n_ref, "spmv": n_iter, "update": n_iter, "pcg_iter": n_iter, "spec": n_iter}
+    # direct solve: one full pass per step, the later ones (almost always) update passes
+    names = ["tdgl", "setup", "spec", "update"] if direct else KERNELS[mode]
+    count = {"tdgl": 1.0, "setup": 1.0 if direct else n_ref, "spmv": n_iter,
+             "update": max(n_ref - 1.0, 0.0) if direct else n_iter, "pcg_iter": n_iter, "spec": n_iter}
     per_step = {k: kms[i] * count[k] for i, k in enumerate(names)}
     top = max(per_step, key=per_step.get)
     ki = names.index(top)
@@ -299,7 +304,7 @@ def run_ours(args):
     if fp64:
         launches = int(K * 3 + 2 * it.sum())
     elif direct:
-        launches = int(K * 2 + rf.sum() + 6 * it.sum())
+        launches = int(K * 2 + rf.sum() + 5 * it.sum())
     else:
         launches = int(K * 2 + 2 * rf.sum())
 
@@ -362,7 +367,7 @@ def run_batch(args):
 
     ws = wl.ensemble(64, 100)
     kw = dict(precision=cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8, max_iter=4000, refine_tol=1e-8,
-              max_refine=6, inner_tol=1e-5, inner_max_iter=2000, warm_start=3, dep_flag=1)
+              max_refine=6, inner_tol=1e-5, inner_max_iter=2000, warm_start=2, dep_flag=1)
     descs = [dict(nx=w.nx, ny=w.ny, nz=w.nz, omega=w.omega, grain_mat=w.grain_mat, TR=w.TR, mats=w.mats,
                   del_h=w.del_h, del_t=w.del_t, eps_0_nd=w.eps_0_nd, **kw) for w in ws]
     cells = sum(w.N for w in ws)
@@ -396,12 +401,13 @@ def run_batch(args):
     # film), or the persistent PCG (ms[2] = one iteration over every film)
     direct = b.inner_solver == cg.INNER_DIRECT
     persistent = not direct and len(ws) <= 128 and os.environ.get("CMSL_PCG_TWO_KERNEL", "0") in ("", "0")
-    names = (["tdgl", "setup", "spec"] if direct else
+    names = (["tdgl", "setup", "spec", "update"] if direct else
              ["tdgl", "setup", "pcg_iter"] if persistent else ["tdgl", "setup", "spmv32", "update32"])
     # the loops run while any film is active: per step, the most demanding film
     n_ref = float(np.mean(rfs.max(axis=0)))
     n_it = float(np.mean(its.max(axis=0)))
-    count = {"tdgl": 1.0, "setup": n_ref, "spmv32": n_it, "update32": n_it, "pcg_iter": n_it, "spec": n_it}
+    count = {"tdgl": 1.0, "setup": 1.0 if direct else n_ref, "update": max(n_ref - 1.0, 0.0), "spmv32": n_it,
+             "update32": n_it, "pcg_iter": n_it, "spec": n_it}
     per_step = {k: kms[i] * count[k] for i, k in enumerate(names)}
     top = max(per_step, key=per_step.get)
     ki = names.index(top)
@@ -471,7 +477,7 @@ def run_batch(args):
                          if direct else "persistent PCG (one cooperative launch per refinement pass)" if persistent
                          else "two-kernel PCG"),
         "clocks": clk,
-        "gpu_launches": (int(K * 2 + K * n_ref + 6 * K * n_it) if direct else
+        "gpu_launches": (int(K * 2 + K * n_ref + 5 * K * n_it) if direct else
                          int(K * 2 + 2 * K * n_ref) if persistent else int(K * 2 + K * n_ref + 2 * K * n_it)),
     }
     print(json.dumps(line))

@@ -187,7 +187,7 @@ int main(int argc, char **argv)
         for (int q = 0; q < 3; ++q) d.mats[q] = nd[q];
         d.precision = precision; d.pcg_crit = CMSL_CRIT_REF;
         d.tol_abs = 1e-3; d.tol_rel = 1e-2; d.max_iter = 4000;                    // global.cu:140-144
-        d.refine_tol = 1e-8; d.max_refine = 6; d.inner_tol = 1e-5; d.inner_max_iter = 2000; d.warm_start = 3;
+        d.refine_tol = 1e-8; d.max_refine = 6; d.inner_tol = 1e-5; d.inner_max_iter = 2000; d.warm_start = 2;
         cmsl_film *film = nullptr;
         if (cmsl_film_create(&d, &film) != CMSL_OK) return die(cmsl_last_error());
         const double *Pp[6] = {P[0].data(), P[1].data(), P[2].data(), P[3].data(), P[4].data(), P[5].data()};

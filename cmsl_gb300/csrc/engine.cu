@@ -1028,8 +1028,11 @@ cmsl_status get_iters(Engine *e, int film, int n, int32_t *iters, int32_t *refin
     return CMSL_OK;
 }
 
-// ms[0] TDGL, ms[1] solve set-up / refinement pass, ms[2] and ms[3] the PCG
-// kernels (persistent FP32 solver: ms[2] per iteration, ms[3] the step end).
+// ms[0] TDGL, ms[1] solve set-up / first refinement pass, ms[2] and ms[3] the
+// PCG kernels (persistent FP32 solver: ms[2] per iteration, ms[3] the step
+// end; direct solve: ms[2] the solve, ms[3] the update pass).  The
+// refinement passes run in force mode, which leaves the solver state as it
+// is, so every repetition times the same kind of pass.
 cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
 {
     if (!ms || reps < 1) return fail(CMSL_ERR_ARG, "bad arguments");
@@ -1056,7 +1059,11 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
     for (int kind = 0; kind < 4; ++kind) {
         CK(cudaMemcpy(S.data(), e->d_solve, sizeof(SolveDev) * F, cudaMemcpyDeviceToHost));
         for (SolveDev &s : S) {
-            s.outer_active = 1; s.active = 1; s.iters = 1; s.refine = 1; s.status = 0; s.upd = 0;
+            // FP32 passes: kind 1 a step's first residual pass, kind 3 (direct
+            // solve) the update pass that follows it
+            s.outer_active = 1; s.active = 1; s.iters = 1; s.status = 0;
+            s.refine = (!fp64 && kind == 1) ? 0 : 1;
+            s.upd = (e->spectral && kind == 3) ? 1 : 0;
             s.alpha = 1e-3; s.beta = 0.5; s.rz = s.rz0 = 1.0;
             s.inner_tol2 = 0.0; s.inner_max = CG_TIMING_ITERS;
         }
@@ -1093,7 +1100,8 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
                 break;
             default:
                 if (fp64) k_update<double, Exact, false><<<nit, NT, 0, st>>>(d, F64);
-                else if (e->persistent || e->spectral) k_step_end<<<1, 32, 0, st>>>(d);   // no fourth kernel
+                else if (e->spectral) TRY(launch_refine(e, st, d, F32));                 // update pass
+                else if (e->persistent) k_step_end<<<1, 32, 0, st>>>(d);                 // no fourth kernel
                 else k_update<float, Fast, true><<<nit, NT, 0, st>>>(d, F32);
                 break;
             }

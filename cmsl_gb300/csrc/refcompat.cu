@@ -84,7 +84,7 @@ cmsl_film *make_film(std::vector<int32_t> &gm)
     d.precision = (p && std::string(p) == "fp32") ? CMSL_FP32_REFINED : CMSL_FP64;
     d.pcg_crit = CMSL_CRIT_REF;
     d.tol_abs = 1.0e-3; d.tol_rel = 1.0e-2; d.max_iter = 4000;   // global.cu:140-144
-    d.refine_tol = 1e-8; d.max_refine = 6; d.inner_tol = 1e-5; d.inner_max_iter = 2000; d.warm_start = 3;
+    d.refine_tol = 1e-8; d.max_refine = 6; d.inner_tol = 1e-5; d.inner_max_iter = 2000; d.warm_start = 2;
     cmsl_film *f = nullptr;
     if (cmsl_film_create(&d, &f) != CMSL_OK) die("cmsl_film_create");
     return f;

@@ -33,7 +33,7 @@ class _Desc:
     def __init__(self, nx, ny, nz, omega, grain_mat, TR, mats, *, del_h, del_t, dep_flag=1,
                  zbc=_lib.DIRICHLET, eps_0_nd=0.0, is_interface=None, precision=_lib.FP64,
                  pcg_crit=_lib.CRIT_REF, tol_abs=1e-3, tol_rel=1e-2, max_iter=4000,
-                 refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000, warm_start=3,
+                 refine_tol=1e-8, max_refine=6, inner_tol=1e-4, inner_max_iter=2000, warm_start=2,
                  inner_solver=_lib.INNER_AUTO):
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
         self.N = self.nx * self.ny * self.nz

@@ -28,7 +28,7 @@ def run_loop(w, precision, tol=1e-8, inner_tol=1e-5, stream=None):
     kw = dict(pcg_crit=cg.CRIT_RELRES, tol_rel=tol, max_iter=20000)
     if precision == "fp32":
         kw.update(precision=cg.FP32_REFINED, refine_tol=tol, max_refine=6, inner_tol=inner_tol,
-                  inner_max_iter=2000, warm_start=3)
+                  inner_max_iter=2000, warm_start=2)
     else:
         kw.update(precision=cg.FP64)
     s = w.sched

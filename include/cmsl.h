@@ -81,7 +81,10 @@ typedef struct {
                                      start, depol_varEPS.cu:429-430), 1 = linear
                                      extrapolation 2 phi_n - phi_{n-1}, 2 = quadratic
                                      3 phi_n - 3 phi_{n-1} + phi_{n-2}, 3 = cubic
-                                     4 phi_n - 6 phi_{n-1} + 4 phi_{n-2} - phi_{n-3} */
+                                     4 phi_n - 6 phi_{n-1} + 4 phi_{n-2} - phi_{n-3}
+                                     (2 is the fastest with the direct inner solve: its
+                                     first residual is small enough for the FP32 update
+                                     pass, at two fewer potentials read per step) */
     int inner_solver;             /* FP32_REFINED inner solve: CMSL_INNER_AUTO (direct
                                      spectral solve where it applies, else PCG),
                                      CMSL_INNER_PCG, CMSL_INNER_DIRECT (CMSL_ERR_ARG where
