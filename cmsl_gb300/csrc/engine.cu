@@ -24,7 +24,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -84,6 +86,63 @@ int pick_zchunk(long long xy_tiles, int nz)
     int zc = (int)std::max<long long>(1, (nz + chunks - 1) / chunks);
     zc = std::max(zc, std::min(nz, 8));
     return std::min(zc, nz);
+}
+
+// Work items of every film for z chunk zc (0: pick_zchunk per film); how
+// many there are, or the items themselves with each film's item range.
+constexpr int ZCHUNK_MIN = 4;       // the finest chunk the autotuner tries
+
+int film_zchunk(const Engine *e, int fi, int zc)
+{
+    const int nz = e->fh[fi].nz;
+    return zc > 0 ? std::min(zc, nz) : pick_zchunk(e->xy_tiles, nz);
+}
+
+size_t count_items(const Engine *e, int zc)
+{
+    size_t n = 0;
+    for (int fi = 0; fi < e->n_films; ++fi) {
+        const FilmHost &h = e->fh[fi];
+        const int c = film_zchunk(e, fi, zc);
+        n += (size_t)((h.nx + TX - 1) / TX) * ((h.ny + TY - 1) / TY) * ((h.nz + c - 1) / c);
+    }
+    return n;
+}
+
+// Rebuilds and uploads the items for z chunk zc (the graph is rebuilt at the
+// next run).
+cmsl_status set_items(Engine *e, int zc)
+{
+    if (count_items(e, zc) > e->items_cap) return fail(CMSL_ERR_ARG, "z chunk %d: too many work items", zc);
+    e->items.clear();
+    for (int fi = 0; fi < e->n_films; ++fi) {
+        const FilmHost &h = e->fh[fi];
+        const int c = film_zchunk(e, fi, zc);
+        FilmDev &fd = e->fdh[fi];
+        fd.item_begin = (int)e->items.size();
+        for (int y0 = 0; y0 < h.ny; y0 += TY)
+            for (int x0 = 0; x0 < h.nx; x0 += TX)
+                for (int z0 = 0; z0 < h.nz; z0 += c)
+                    e->items.push_back(make_int4(fi, x0, y0, z0 | (std::min(h.nz, z0 + c) << 16)));
+        fd.item_end = (int)e->items.size();
+    }
+    CK(cudaMemcpy(e->d_films, e->fdh.data(), sizeof(FilmDev) * e->fdh.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_items, e->items.data(), sizeof(int4) * e->items.size(), cudaMemcpyHostToDevice));
+    e->zchunk = zc;
+    e->graph_valid = false;
+    return CMSL_OK;
+}
+
+// Tile shapes tuned in this process, by film-shape class.
+std::map<std::string, int> g_tuned;
+std::mutex g_tuned_mu;
+
+std::string shape_key(const Engine *e)
+{
+    std::string k = std::to_string(e->precision) + (e->spectral ? "s" : e->persistent ? "p" : "k");
+    for (const FilmHost &h : e->fh)
+        k += ":" + std::to_string(h.nx) + "x" + std::to_string(h.ny) + "x" + std::to_string(h.nz) + (h.dep ? "d" : "");
+    return k;
 }
 
 // n = 2^a 3^b <= 4096 (the FFT radices of spectral.cuh)
@@ -662,17 +721,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         fd.g_off = g_off;
         g_off += h.ng;
         for (int q = 0; q < 3; ++q) fd.n_mat[q] = nmat[q];
-        // items: TX x TY x zchunk tiles
-        const int zc = pick_zchunk(xy_tiles, h.nz);
-        fd.item_begin = (int)e->items.size();
-        for (int y0 = 0; y0 < h.ny; y0 += TY)
-            for (int x0 = 0; x0 < h.nx; x0 += TX)
-                for (int z0 = 0; z0 < h.nz; z0 += zc) {
-                    const int z1 = std::min(h.nz, z0 + zc);
-                    e->items.push_back(make_int4(fi, x0, y0, z0 | (z1 << 16)));
-                }
-        fd.item_end = (int)e->items.size();
     }
+    e->xy_tiles = xy_tiles;
 
     // persistent PCG partition: stencil bricks of PZ planes film by film;
     // each film gets a contiguous block range in proportion to its cells
@@ -729,12 +779,21 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         e->cg_grid = (int)blk_film.size();
     }
 
-    // device memory
+    // device memory; the work items (and their partial sums) are sized for
+    // the finest z chunk the autotuner tries
     const size_t cells = (size_t)e->ncells;
+    e->fdh = fds;
     TRY(e->alloc((void **)&e->d_films, sizeof(FilmDev) * n));
-    CK(cudaMemcpy(e->d_films, fds.data(), sizeof(FilmDev) * n, cudaMemcpyHostToDevice));
-    TRY(e->alloc((void **)&e->d_items, sizeof(int4) * e->items.size()));
-    CK(cudaMemcpy(e->d_items, e->items.data(), sizeof(int4) * e->items.size(), cudaMemcpyHostToDevice));
+    e->items_cap = std::max(count_items(e, ZCHUNK_MIN), count_items(e, 0));
+    TRY(e->alloc((void **)&e->d_items, sizeof(int4) * e->items_cap));
+    TRY(e->alloc((void **)&e->d_partial, sizeof(double) * NPART * e->items_cap));
+    {
+        int zc = 0;
+        std::lock_guard<std::mutex> lk(g_tuned_mu);
+        const auto hit = g_tuned.find(shape_key(e));
+        if (hit != g_tuned.end()) zc = hit->second;
+        TRY(set_items(e, zc));
+    }
     TRY(e->alloc((void **)&e->d_code, sizeof(uint32_t) * cells));
     CK(cudaMemcpy(e->d_code, code.data(), sizeof(uint32_t) * cells, cudaMemcpyHostToDevice));
     if (e->precision == CMSL_FP64) TRY(upload_TR<double>(e, descs, n));
@@ -849,7 +908,6 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(e->alloc((void **)&e->d_phi[3], sizeof(double) * cells));
         TRY(e->alloc((void **)&e->d_phi[4], sizeof(double) * cells));
     }
-    TRY(e->alloc((void **)&e->d_partial, sizeof(double) * NPART * e->items.size()));
     TRY(e->alloc((void **)&e->d_counter, sizeof(unsigned int) * 4));
     TRY(e->alloc((void **)&e->d_solve, sizeof(SolveDev) * n));
     TRY(e->alloc((void **)&e->d_ctl, sizeof(Ctl)));
@@ -1120,6 +1178,61 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
     return CMSL_OK;
 }
 
+cmsl_status autotune_items(Engine *e, int32_t *zchunk);
+
+// Tile-shape autotuner: times the stencil passes (TDGL step and the
+// item-based solve kernels: the FP32 first and update passes, the FP64 PCG
+// kernels) for z chunks 4, 8, 16, ... up to the thickest film, keeps the
+// fastest, and remembers it for handles of the same film-shape class.
+cmsl_status autotune(Engine *e, int32_t *zchunk)
+{
+    // the FP64 PCG kernels update the potential in place when timed: keep a copy
+    const size_t pbytes = sizeof(double) * (size_t)e->ncells;
+    double *saved = nullptr;
+    if (e->precision == CMSL_FP64) {
+        CK(cudaMalloc(&saved, 2 * pbytes));
+        CK(cudaMemcpy(saved, e->d_phi[0], pbytes, cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(saved + e->ncells, e->d_phi[1], pbytes, cudaMemcpyDeviceToDevice));
+    }
+    const cmsl_status st = autotune_items(e, zchunk);
+    if (saved) {
+        cudaMemcpy(e->d_phi[0], saved, pbytes, cudaMemcpyDeviceToDevice);
+        cudaMemcpy(e->d_phi[1], saved + e->ncells, pbytes, cudaMemcpyDeviceToDevice);
+        cudaFree(saved);
+    }
+    if (st != CMSL_OK) return st;
+    CK(cudaGetLastError());
+    return CMSL_OK;
+}
+
+cmsl_status autotune_items(Engine *e, int32_t *zchunk)
+{
+    int maxnz = 1;
+    for (const FilmHost &h : e->fh) maxnz = std::max(maxnz, h.nz);
+    std::vector<int> cands;
+    for (int c = ZCHUNK_MIN; c < maxnz; c *= 2) cands.push_back(c);
+    cands.push_back(maxnz);
+    int best = 0;
+    double best_ms = 0.0;
+    for (int c : cands) {
+        TRY(set_items(e, c));
+        double ms[4] = {0, 0, 0, 0};
+        TRY(time_kernels(e, 5, nullptr, ms));
+        double t = ms[0] + ms[1];                          // TDGL step + first pass (FP32) / set-up (FP64)
+        if (e->precision == CMSL_FP64) t += ms[2] + ms[3];
+        else if (e->spectral) t += ms[3];                  // update pass
+        else if (!e->persistent) t += ms[2] + ms[3];       // two-kernel PCG
+        if (best == 0 || t < best_ms) { best = c; best_ms = t; }
+    }
+    TRY(set_items(e, best));
+    {
+        std::lock_guard<std::mutex> lk(g_tuned_mu);
+        g_tuned[shape_key(e)] = best;
+    }
+    if (zchunk) *zchunk = best;
+    return CMSL_OK;
+}
+
 size_t device_bytes(const Engine *e)
 {
     return e->bytes + (size_t)e->n_films * ((size_t)e->wstride * (sizeof(double) + 3 * sizeof(int)) +
@@ -1345,6 +1458,12 @@ cmsl_status cmsl_film_inner_solver(cmsl_film *f, int *solver)
     return CMSL_OK;
 }
 
+cmsl_status cmsl_film_autotune(cmsl_film *f, int32_t *zchunk)
+{
+    if (!f) return fail(CMSL_ERR_ARG, "NULL film");
+    return autotune(f, zchunk);
+}
+
 cmsl_status cmsl_film_device_bytes(cmsl_film *f, size_t *bytes)
 {
     if (!f || !bytes) return fail(CMSL_ERR_ARG, "NULL argument");
@@ -1421,6 +1540,12 @@ cmsl_status cmsl_batch_inner_solver(cmsl_batch *b, int *solver)
     if (!b || !solver) return fail(CMSL_ERR_ARG, "NULL argument");
     *solver = b->spectral ? CMSL_INNER_DIRECT : CMSL_INNER_PCG;
     return CMSL_OK;
+}
+
+cmsl_status cmsl_batch_autotune(cmsl_batch *b, int32_t *zchunk)
+{
+    if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
+    return autotune(b, zchunk);
 }
 
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *b, size_t *bytes)

@@ -47,7 +47,11 @@ struct Engine {
     size_t esz = 8;
     int max_iter_cap = 0, max_refine_cap = 0, inner_max_cap = 0;
     std::vector<FilmHost> fh;
+    std::vector<FilmDev> fdh;           // host copy of the film tables
     std::vector<int4> items;
+    size_t items_cap = 0;               // items the device arrays hold
+    long long xy_tiles = 0;             // column tiles of all films
+    int zchunk = 0;                     // z chunk of the items (0: per-film heuristic)
     // device buffers
     std::vector<void *> allocs;
     size_t bytes = 0;

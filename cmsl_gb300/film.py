@@ -227,6 +227,13 @@ class Film:
         check(lib().cmsl_film_inner_solver(self._h, C.byref(v)))
         return v.value
 
+    def autotune(self):
+        """Times the stencil passes for several work-item z chunks, keeps the
+        fastest and returns it (cmsl_film_autotune)."""
+        v = C.c_int32()
+        check(lib().cmsl_film_autotune(self._h, C.byref(v)))
+        return int(v.value)
+
 
 class Batch:
     """Many independent films on the GPU advancing together (cmsl_batch_*).
@@ -340,6 +347,12 @@ class Batch:
         v = C.c_int()
         check(lib().cmsl_batch_inner_solver(self._h, C.byref(v)))
         return v.value
+
+    def autotune(self):
+        """The batch's tile-shape autotuner (cmsl_batch_autotune); returns the z chunk."""
+        v = C.c_int32()
+        check(lib().cmsl_batch_autotune(self._h, C.byref(v)))
+        return int(v.value)
 
     def device_bytes(self):
         b = C.c_size_t()

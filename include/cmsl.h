@@ -164,6 +164,14 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, doub
  * reference's PCG). */
 cmsl_status cmsl_film_inner_solver(cmsl_film *film, int *solver);
 
+/* Tile-shape autotuner: times the stencil passes of this film for work-item z
+ * chunks 4, 8, 16, ... up to nz on the device, keeps the fastest (reported in
+ * *zchunk, may be NULL) and remembers it for films of the same shape class
+ * created later in the process.  Leaves the state (P, phi) as it is; results
+ * of later steps equal the untuned ones up to the order of the row sums.
+ * CMSL_ZCHUNK=<n> in the environment fixes the chunk of untuned handles. */
+cmsl_status cmsl_film_autotune(cmsl_film *film, int32_t *zchunk);
+
 /* Bytes of device memory the film holds. */
 cmsl_status cmsl_film_device_bytes(cmsl_film *film, size_t *bytes);
 
@@ -211,6 +219,10 @@ cmsl_status cmsl_batch_time_kernels(cmsl_batch *batch, int reps, void *stream, d
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *batch, size_t *bytes);
 /* The batch's FP32_REFINED inner solve, as cmsl_film_inner_solver. */
 cmsl_status cmsl_batch_inner_solver(cmsl_batch *batch, int *solver);
+
+/* The batch's tile-shape autotuner, as cmsl_film_autotune (one z chunk for
+ * all films of the batch). */
+cmsl_status cmsl_batch_autotune(cmsl_batch *batch, int32_t *zchunk);
 
 /* Restart files in the reference's checkpoint layout (generate.cu:90-264;
  * cmsl_io.h cmsl_checkpoint_write/read).  write: P and E = -grad(phi) of the

@@ -1,0 +1,57 @@
+"""The tile-shape autotuner (cmsl_film_autotune / cmsl_batch_autotune): it
+picks a z chunk among 4, 8, 16, ... nz, leaves the state alone, and a tuned
+film advances like an untuned one.  The items set the order of the PCG dot
+products and row sums, so with the solve converged to 1e-12 the two runs
+agree to 1e-9 of max |P| (FP64) / 1e-6 (FP32_REFINED), rows to 1e-9."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.films import random_film
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cmsl_gb300 import build
+    build.build()
+    import cmsl_gb300
+    return cmsl_gb300
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_autotune_keeps_results(gpu, precision):
+    f, P = random_film(40, 24, 20, seed=91, eps_0_nd=4.0, p_scale=0.2, layered=True)
+    kw = dict(precision=gpu.FP64 if precision == "fp64" else gpu.FP32_REFINED)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    n = 12
+    Ez = np.linspace(0.0, 0.3, n)
+    rows = np.arange(n, dtype=np.int32)
+    out = []
+    for tune in (False, True):
+        with gpu.Film.from_oracle_film(f, **kw) as g:
+            g.set_state(P)
+            if tune:
+                zc = g.autotune()
+                assert zc in (4, 8, 16, 20)
+                Pt, _ = g.get_state()
+                for a, b in zip(Pt, P):
+                    assert np.array_equal(a, np.asarray(b, a.dtype)) or np.abs(a - b).max() <= 1e-7
+            g.run(Ez, rows)
+            out.append((g.get_state()[0], g.rows()))
+    (P0, r0), (P1, r1) = out
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    for a, b in zip(P0, P1):
+        assert np.abs(a - b).max() <= tol * np.abs(b).max()
+    assert np.abs(r0[:, :10] - r1[:, :10]).max() <= 1e-9 * max(np.abs(r1[:, :10]).max(), 1.0)
+
+
+def test_batch_autotune(gpu):
+    films = [random_film(*sh, seed=95 + i, eps_0_nd=3.0, p_scale=0.2)[0] for i, sh in
+             enumerate([(32, 16, 6), (24, 20, 12)])]
+    with gpu.Batch.from_oracle_films(films) as b:
+        assert b.autotune() in (4, 8, 12)
