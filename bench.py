@@ -247,7 +247,7 @@ def run_ours(args):
               max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000,
               warm_start=2)
     film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **kw)
-    zchunk = film.autotune()
+    zchunk = 0 if args.no_autotune else film.autotune()
     film.set_state(w.P_init)
     K, W = args.steps, args.warmup
     Ez = w.sched.Ez[: W + K]
@@ -341,7 +341,7 @@ def run_ours(args):
             "config": {"workload": w.name, "cells": w.N, "grid": [w.nx, w.ny, w.nz],
                        "precision": "fp64" if fp64 else "fp32-refined (fp64 phi, refine to 1e-8)",
                        "pcg": "||b-A phi|| <= 1e-8 ||b||", "parallelism": "replicas" if world > 1 else "single",
-                       "tile": {"x": 32, "y": 8, "z_chunk": zchunk, "chosen_by": "autotuner (cmsl_film_autotune)"},
+                       "tile": {"x": 32, "y": 8, "z_chunk": zchunk, "chosen_by": "heuristic" if args.no_autotune else "autotuner (cmsl_film_autotune)"},
                        "l2": "no flush: per-step state %.0f MB > 129 MB L2" % (film.device_bytes() / 1e6)},
             "inner_solver": "direct (in-plane FFT + tridiagonal z, one solve per refinement pass)" if direct
             else ("pcg (Jacobi, reference algorithm)" if fp64 else "pcg (persistent single-reduction Jacobi-PCG)"),
@@ -379,7 +379,7 @@ def run_batch(args):
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     b = cg.Batch(descs)
-    zchunk = b.autotune()
+    zchunk = 0 if args.no_autotune else b.autotune()
     for i, w in enumerate(ws):
         b.set_state(i, w.P_init)
     with torch.cuda.stream(stream):
@@ -437,7 +437,8 @@ def run_batch(args):
     with torch.cuda.stream(stream):
         for i, d in enumerate(descs):
             with cg.Film(**d) as f:
-                f.autotune()
+                if not args.no_autotune:
+                    f.autotune()
                 f.set_state(ws[i].P_init)
                 f.run(Ez[i, :W], rows[i, :W], stream=sp)
                 e0 = torch.cuda.Event(enable_timing=True)
@@ -470,7 +471,7 @@ def run_batch(args):
         "config": {"workload": "c3_ensemble64", "films": len(ws), "cells": cells,
                    "precision": "fp32-refined (fp64 phi, refine to 1e-8)", "pcg": "||b-A phi|| <= 1e-8 ||b|| per film",
                    "parallelism": "single", "l2": "no flush: batch state > 129 MB L2",
-                   "tile": {"x": 32, "y": 8, "z_chunk": zchunk, "chosen_by": "autotuner (cmsl_batch_autotune)"}},
+                   "tile": {"x": 32, "y": 8, "z_chunk": zchunk, "chosen_by": "heuristic" if args.no_autotune else "autotuner (cmsl_batch_autotune)"}},
         "sequential": {"value": seq, "unit": "cell-steps/s", "ms_per_step": seq_ms / K,
                        "speedup_batch_over_sequential": value / seq},
         "pcg_iters_per_step_max_film": n_it, "refine_passes_per_step_max_film": n_ref,
@@ -497,6 +498,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="heuristic z chunk instead of the tile autotuner")
     ap.add_argument("--config", type=int, default=CONFIG_ID, choices=[0, 1, 2, 3, 4],
                     help="benchmark configuration (default 1; 3 = the 64-film batched ensemble)")
     args = ap.parse_args()
