@@ -98,7 +98,7 @@ struct SolveDev {               // per film, lives in device memory
 struct CgBuf {
     float *r[2], *w[2], *s[2];  // ping-pong by iteration parity
     float *x, *p;
-    unsigned int *arrive;       // grid-barrier arrival counter (reset by k_refine)
+    unsigned int *arrive;       // grid-barrier arrival counter (reset by k_refine32)
     float4 *part;               // [2][grid] per-block partial sums (two double-float pairs), by parity
     int *err;                   // barrier timeout flag
     const int4 *bricks;         // stencil work list: TX x TY x (<= PZ planes) bricks, film by film

@@ -6,14 +6,17 @@
 // per-film quantity (solver scalars, convergence flags, waveform, sweep rows)
 // lives in per-film device slots.  One time step is one CUDA graph:
 //   CMSL_FP64:          k_tdgl -> k_rhs -> WHILE(inner){ k_spmv -> k_update } -> k_step_end
-//   CMSL_FP32_REFINED:  k_tdgl -> WHILE(outer){ k_refine -> inner solve } -> k_step_end
-// where the FP32 inner solve is one persistent cooperative PCG launch over
-// all films (each film on its own block range with its own convergence flag),
-// or, for films with the Neumann z boundary, WHILE(inner){ k_spmv -> k_update }
-// (films that have converged drop out of the masked kernels; the loop runs
-// while any film is active).  The WHILE conditions are set on the device by the last block of
-// k_rhs, k_refine and k_update, so a step never returns to the host: the PCG
-// loop of the reference (depol_varEPS.cu:472-522, two blocking Ddot per
+//   CMSL_FP32_REFINED:  k_tdgl32 -> k_refine32 -> solve -> k_refine32
+//                       -> WHILE(outer){ solve -> k_refine32 } -> k_step_end
+// where the FP32 inner solve is the direct spectral solve (films of one eps,
+// spectral.cuh), or one persistent cooperative PCG launch over all films
+// (each film on its own block range with its own convergence flag, under an
+// IF node), or, for films with the Neumann z boundary, the residual pass
+// followed by WHILE(inner){ k_spmv -> k_update } inside the outer WHILE.
+// Converged films drop out of the masked kernels; a loop runs while any film
+// is active.  The conditions are set on the device by the last block of
+// k_rhs, k_refine32 and k_update, so a step never returns to the host: the
+// PCG loop of the reference (depol_varEPS.cu:472-522, two blocking Ddot per
 // iteration) and its per-step cudaMalloc/cublasCreate churn (:373-393,
 // :585-593) are gone.  The applied field and the output-row schedule of the
 // P-E loop are device arrays indexed by a device step counter, so the same

@@ -481,7 +481,7 @@ __device__ __forceinline__ bool grid_allreduce_all(const CgBuf &B, int parity, u
 }
 
 // The inner FP32 solve of one refinement pass for every film whose solve is
-// active: starts from r_0 in B.r[0] (written by k_refine) and x = 0, runs
+// active: starts from r_0 in B.r[0] (written by k_refine32) and x = 0, runs
 // until (r,u) <= inner_tol2 (r_0,u_0) or inner_max iterations per film, and
 // leaves each film's correction in B.x.  Cooperative launch of PNT-thread
 // blocks; every block is co-resident.  MULTI = false is the single-film
