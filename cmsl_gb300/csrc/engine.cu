@@ -31,6 +31,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -466,6 +467,30 @@ cmsl_status build_graph(Engine *e)
     return CMSL_OK;
 }
 
+// State transfers.  Where the device reads the host's page tables
+// (cudaDevAttrPageableMemoryAccess: Grace-Blackwell's coherent NVLink-C2C),
+// kernels read the caller's double arrays in place and convert on the GPU.
+// Downloads go through one pinned array and are converted on the host cores
+// (a GPU writing fresh pageable pages pays a page fault per page).  Without
+// that device attribute the host converts and copies both ways.
+template <class T>
+__global__ void k_host_in(const double *__restrict__ src, T *__restrict__ dst, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (T)src[i];
+}
+// potential as double-float: hi = (float)x, lo = (float)(x - hi)
+__global__ void k_phi_in(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double x = src[i];
+        const float h = (float)x;
+        hi[i] = h;
+        lo[i] = (float)(x - (double)h);
+    }
+}
+constexpr int XFER_GRID = 152 * 8, XFER_NT = 256;
+
 }  // namespace cmsl_eng
 
 namespace {
@@ -582,23 +607,77 @@ cmsl_status step_direct(Engine *e, cudaStream_t st)
     return CMSL_OK;
 }
 
+
 template <class T>
 cmsl_status put_fields(Engine *e, int film, int set, const double *const P[6])
 {
     const FilmHost &h = e->fh[film];
+    for (int q = 0; q < 6; ++q)
+        if (!P[q]) return fail(CMSL_ERR_ARG, "P[%d] is NULL", q);
+    if (e->host_direct) {
+        for (int q = 0; q < 6; ++q)
+            k_host_in<T><<<XFER_GRID, XFER_NT>>>(P[q], (T *)e->d_P[set][q] + h.off, h.N);
+        CK(cudaGetLastError());
+        CK(cudaDeviceSynchronize());
+        return CMSL_OK;
+    }
     std::vector<T> tmp((size_t)h.N);
     for (int q = 0; q < 6; ++q) {
-        if (!P[q]) return fail(CMSL_ERR_ARG, "P[%d] is NULL", q);
         for (long long i = 0; i < h.N; ++i) tmp[i] = (T)P[q][i];
         CK(cudaMemcpy((T *)e->d_P[set][q] + h.off, tmp.data(), h.N * sizeof(T), cudaMemcpyHostToDevice));
     }
     return CMSL_OK;
 }
 
+// Pinned host array of the largest film's cells (two floats or one double per
+// cell), for state downloads (allocated on first use).
+cmsl_status pinned_stage(Engine *e, void **out)
+{
+    if (!e->h_stage) {
+        long long nmax = 0;
+        for (const FilmHost &h : e->fh) nmax = std::max(nmax, h.N);
+        CK(cudaMallocHost(&e->h_stage, sizeof(double) * (size_t)nmax));
+    }
+    *out = e->h_stage;
+    return CMSL_OK;
+}
+
+// fn(i0, i1) over [0, n) on the host cores: the conversion of a download is
+// dominated by the first touch of the caller's fresh output pages.
+template <class F> void parallel_for(long long n, F fn)
+{
+    const long long chunk = 1 << 20;
+    const int nt = (int)std::min<long long>(std::max(1u, std::thread::hardware_concurrency()), (n + chunk - 1) / chunk);
+    if (nt <= 1) {
+        fn(0LL, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] { fn(n * t / nt, n * (t + 1) / nt); });
+    for (std::thread &x : th) x.join();
+}
+
 template <class T>
 cmsl_status get_fields(Engine *e, int film, int set, double *const P[6])
 {
     const FilmHost &h = e->fh[film];
+    if (e->host_direct) {
+        // one DMA copy into pinned memory, then the conversion into the
+        // caller's arrays on the host cores
+        void *stg = nullptr;
+        TRY(pinned_stage(e, &stg));
+        const T *st = (const T *)stg;
+        for (int q = 0; q < 6; ++q) {
+            if (!P[q]) continue;
+            CK(cudaMemcpy((void *)st, (const T *)e->d_P[set][q] + h.off, sizeof(T) * h.N, cudaMemcpyDeviceToHost));
+            double *dst = P[q];
+            parallel_for(h.N, [&](long long i0, long long i1) {
+                for (long long i = i0; i < i1; ++i) dst[i] = (double)st[i];
+            });
+        }
+        return CMSL_OK;
+    }
     std::vector<T> tmp((size_t)h.N);
     for (int q = 0; q < 6; ++q) {
         if (!P[q]) continue;
@@ -785,6 +864,14 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     // device memory; the work items (and their partial sums) are sized for
     // the finest z chunk the autotuner tries
     const size_t cells = (size_t)e->ncells;
+    {
+        int dev = 0, pageable = 0, host_tables = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+        CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+        const char *hd = getenv("CMSL_HOST_COPY");   // 1: host-side conversion and copies
+        e->host_direct = pageable && host_tables && !(hd && atoi(hd) != 0);
+    }
     e->fdh = fds;
     TRY(e->alloc((void **)&e->d_films, sizeof(FilmDev) * n));
     e->items_cap = std::max(count_items(e, ZCHUNK_MIN), count_items(e, 0));
@@ -956,6 +1043,24 @@ cmsl_status set_state(Engine *e, int film, const double *const P[6], const doubl
         if (phi) CK(cudaMemcpy(dst, phi, sizeof(double) * h.N, cudaMemcpyHostToDevice));
         else CK(cudaMemset(dst, 0, sizeof(double) * h.N));
         CK(cudaMemcpy(e->d_phi[1] + h.off, dst, sizeof(double) * h.N, cudaMemcpyDeviceToDevice));
+    } else if (e->host_direct) {
+        // double-float: hi half at the cell, lo half ncells further on; the
+        // previous potentials start equal to the given one
+        float *b0 = (float *)e->d_phi[0];
+        if (phi) {
+            k_phi_in<<<XFER_GRID, XFER_NT>>>(phi, b0 + h.off, b0 + e->ncells + h.off, h.N);
+            CK(cudaGetLastError());
+        } else {
+            CK(cudaMemset(b0 + h.off, 0, sizeof(float) * h.N));
+            CK(cudaMemset(b0 + e->ncells + h.off, 0, sizeof(float) * h.N));
+        }
+        for (int q = 1; q < 4; ++q) {
+            float *b = (float *)e->d_phi[q];
+            CK(cudaMemcpy(b + h.off, b0 + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToDevice));
+            CK(cudaMemcpy(b + e->ncells + h.off, b0 + e->ncells + h.off, sizeof(float) * h.N,
+                          cudaMemcpyDeviceToDevice));
+        }
+        CK(cudaMemset((float *)e->d_x + h.off, 0, sizeof(float) * h.N));
     } else {
         // double-float: hi half at the cell, lo half ncells further on
         std::vector<float> hi((size_t)h.N, 0.f), lo((size_t)h.N, 0.f);
@@ -998,6 +1103,16 @@ cmsl_status get_state(Engine *e, int film, double *const P[6], double *phi)
     if (phi) {
         if (e->precision == CMSL_FP64) {
             CK(cudaMemcpy(phi, e->d_phi[S.phi_cur] + h.off, sizeof(double) * h.N, cudaMemcpyDeviceToHost));
+        } else if (e->host_direct) {
+            const float *b = (const float *)e->d_phi[S.phi_cur];
+            void *stg = nullptr;
+            TRY(pinned_stage(e, &stg));
+            float *hi = (float *)stg, *lo = hi + h.N;
+            CK(cudaMemcpy(hi, b + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(lo, b + e->ncells + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
+            parallel_for(h.N, [&](long long i0, long long i1) {
+                for (long long i = i0; i < i1; ++i) phi[i] = (double)hi[i] + (double)lo[i];
+            });
         } else {
             std::vector<float> hi((size_t)h.N), lo((size_t)h.N);
             const float *b = (const float *)e->d_phi[S.phi_cur];

@@ -78,6 +78,8 @@ struct Engine {
     cudaGraphExec_t exec = nullptr;
     bool graph_valid = false;
     bool use_graph = true;
+    bool host_direct = false;           // state uploads read the host arrays from kernels
+    void *h_stage = nullptr;            // pinned buffer of state downloads (first use)
     cudaStream_t stream = nullptr;
     // FP32_REFINED inner solver: the persistent cooperative kernel, or the
     // masked two-kernel PCG (Neumann films, or CMSL_PCG_TWO_KERNEL=1)
@@ -102,6 +104,7 @@ struct Engine {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         for (void *p : allocs) cudaFree(p);
+        if (h_stage) cudaFreeHost(h_stage);
         if (d_wave) cudaFree(d_wave);
         if (d_rows) cudaFree(d_rows);
         if (d_rowbuf) cudaFree(d_rowbuf);
