@@ -305,9 +305,11 @@ def run_ours(args):
     if fp64:
         launches = int(K * 3 + 2 * it.sum())
     elif direct:
-        launches = int(K * 2 + rf.sum() + 5 * it.sum())
+        # TDGL, the refinement passes (the last one ends the step), five per direct solve
+        launches = int(K + rf.sum() + 5 * it.sum())
     else:
-        launches = int(K * 2 + 2 * rf.sum())
+        # TDGL, the refinement passes, one persistent PCG launch per pass but the last
+        launches = int(2 * rf.sum())
 
     # end to end through the C ABI: host state in, K steps, host rows + state out
     film.set_state(w.P_init)
@@ -483,7 +485,7 @@ def run_batch(args):
                          if direct else "persistent PCG (one cooperative launch per refinement pass)" if persistent
                          else "two-kernel PCG"),
         "clocks": clk,
-        "gpu_launches": (int(K * 2 + K * n_ref + 5 * K * n_it) if direct else
+        "gpu_launches": (int(K + K * n_ref + 5 * K * n_it) if direct else
                          int(K * 2 + 2 * K * n_ref) if persistent else int(K * 2 + K * n_ref + 2 * K * n_it)),
     }
     print(json.dumps(line))

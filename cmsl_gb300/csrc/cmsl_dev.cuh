@@ -139,6 +139,7 @@ struct Dev {
     int wstride, rstride;
     int use_cond;
     int force;                  // run the PCG kernels whatever the flags (kernel timing)
+    int step_end;               // a residual pass that leaves no film active also ends the step
     unsigned int *arrive;       // grid-barrier counter of the persistent PCG (or null)
     cudaGraphConditionalHandle h_inner, h_outer;
 };

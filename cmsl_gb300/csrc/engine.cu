@@ -441,12 +441,15 @@ cmsl_status build_graph(Engine *e)
             } else {
                 TRY(add_solve(g, &n_r1, &n_s1));
             }
+            // the pass that leaves no film active ends the step (no k_step_end node)
+            a.d.step_end = 1;
             TRY(add_kernel(g, &n_r2, &n_s1, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
             TRY(add_while(g, &n_solve, &n_r2, 1, h_outer, &body));
             a.d = e->dev(1, 0, h_outer);
+            a.d.step_end = 1;
             TRY(add_solve(body, nullptr, &n_sb));
             TRY(add_kernel(body, &n_rb, &n_sb, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
-            last = n_solve;
+            last = nullptr;
         } else {
             // the inner loop's handle belongs to the outer body graph it lives in
             cudaGraph_t outer, inner;
@@ -461,7 +464,7 @@ cmsl_status build_graph(Engine *e)
             last = n_solve;
         }
     }
-    TRY(add_kernel(g, &n_end, &last, 1, (void *)k_step_end, 1, 32, args_d));
+    if (last) TRY(add_kernel(g, &n_end, &last, 1, (void *)k_step_end, 1, 32, args_d));
     CK(cudaGraphInstantiate(&e->exec, g, 0));
     e->graph_valid = true;
     return CMSL_OK;

@@ -639,6 +639,26 @@ __global__ void __launch_bounds__(NT) k_rhs(Dev d, Fields<T> F)
     start_solves(d, sRed, sTot);
 }
 
+// End of a time step (one block): every film's solve counts into the logs,
+// the first failure into its sticky status, then the step counters and the
+// P set advance.
+__device__ __forceinline__ void step_end(const Dev &d)
+{
+    for (int fi = threadIdx.x; fi < d.n_films; fi += blockDim.x) {
+        SolveDev *S = d.solve + fi;
+        const long long w = (long long)fi * d.wstride + d.ctl->run_step;
+        d.iters_log[w] = S->total_iters;
+        d.refine_log[w] = S->refine;
+        if (S->status != 0 && S->status != 3 && S->sticky == 0) S->sticky = S->status;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        d.ctl->step += 1;
+        d.ctl->run_step += 1;
+        d.ctl->cur ^= 1;
+    }
+}
+
 // ----------------------------- FP32 refinement: end of a residual pass
 // The potential of CMSL_FP32_REFINED is stored as double-float (hi half at
 // cell c, lo half at cell ncells + c of the same buffer) in five rotating
@@ -707,12 +727,16 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
             any_inner |= S->active;
         }
     }
+    __shared__ int s_any;
     if (threadIdx.x == 0) {
         set_cond(d, d.h_outer, any_outer);
         set_cond(d, d.h_inner, any_inner);
         if (d.arrive) *d.arrive = 0u;
         *d.counter = 0u;
+        s_any = any_outer;
     }
+    __syncthreads();
+    if (d.step_end && !s_any) step_end(d);
 }
 
 // ------------------------------------------- PCG: p-update + SpMV + p.Ap
@@ -912,19 +936,7 @@ __global__ void __launch_bounds__(NT) k_update(Dev d, Fields<T> F)
 // ------------------------------------------------------------ step end
 static __global__ void k_step_end(Dev d)
 {
-    for (int fi = threadIdx.x; fi < d.n_films; fi += blockDim.x) {
-        SolveDev *S = d.solve + fi;
-        const long long w = (long long)fi * d.wstride + d.ctl->run_step;
-        d.iters_log[w] = S->total_iters;
-        d.refine_log[w] = S->refine;
-        if (S->status != 0 && S->status != 3 && S->sticky == 0) S->sticky = S->status;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        d.ctl->step += 1;
-        d.ctl->run_step += 1;
-        d.ctl->cur ^= 1;
-    }
+    step_end(d);
 }
 
 // ----------------------------------------------------------- utilities
