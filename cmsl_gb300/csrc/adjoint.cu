@@ -267,9 +267,12 @@ struct AdjWork {
     }
 };
 
+__global__ void k_set_stop(Ctl *ctl, int stop) { ctl->stop = stop; }
+
 // Enqueues steps [0, len) of Ez_seg from the film's current state on st
-// (forward graph, one launch per step).  store: P^n before each step, as
-// [len][6][N].  cur: the film's current P set, advanced per step.
+// (forward graph, one launch per step, its step loop stopped after that
+// step).  store: P^n before each step, as [len][6][N].  cur: the film's
+// current P set, advanced per step.
 cmsl_status forward_segment(Engine *e, cudaStream_t st, const double *Ez_seg, const int32_t *rows_seg, int len,
                             double *store, int &cur)
 {
@@ -287,6 +290,7 @@ cmsl_status forward_segment(Engine *e, cudaStream_t st, const double *Ez_seg, co
             for (int q = 0; q < 6; ++q)
                 CK(cudaMemcpyAsync(store + ((size_t)s * 6 + q) * N, e->d_P[cur][q], sizeof(double) * N,
                                    cudaMemcpyDeviceToDevice, st));
+        k_set_stop<<<1, 1, 0, st>>>(e->d_ctl, s + 1);
         CK(cudaGraphLaunch(e->exec, st));
         cur ^= 1;
     }

@@ -110,7 +110,7 @@ struct Ctl {
     int step;                   // steps done since set_state
     int cur;                    // which P set is "old"
     int run_step;               // step index within the current run (waveform index)
-    int pad;
+    int stop;                   // run_step at which the step loop of a graph launch ends
 };
 
 template <class T> struct Fields {
@@ -142,6 +142,7 @@ struct Dev {
     int step_end;               // a residual pass that leaves no film active also ends the step
     unsigned int *arrive;       // grid-barrier counter of the persistent PCG (or null)
     cudaGraphConditionalHandle h_inner, h_outer;
+    cudaGraphConditionalHandle h_steps;   // the graph's step loop (0: one step per launch)
 };
 
 }  // namespace cmsl

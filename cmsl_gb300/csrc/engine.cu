@@ -367,9 +367,20 @@ cmsl_status build_graph(Engine *e)
 {
     if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
     if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
-    cudaGraph_t g;
-    CK(cudaGraphCreate(&g, 0));
-    e->graph = g;
+    cudaGraph_t top, g;
+    CK(cudaGraphCreate(&top, 0));
+    e->graph = top;
+    // One launch runs the steps of a run: a WHILE node whose body is one
+    // step; the TDGL kernel sets its condition (run_step + 1 < ctl->stop).
+    cudaGraphConditionalHandle h_steps = 0;
+    cudaGraphNode_t n_loop;
+    CK(cudaGraphConditionalHandleCreate(&h_steps, top, 1, cudaGraphCondAssignDefault));
+    TRY(add_while(top, &n_loop, nullptr, 0, h_steps, &g));
+    auto dev = [&](cudaGraphConditionalHandle hi, cudaGraphConditionalHandle ho) {
+        Dev d = e->dev(1, hi, ho);
+        d.h_steps = h_steps;
+        return d;
+    };
     const int nit = (int)e->items.size();
     KArgs a;
     a.F64 = e->fields<double>();
@@ -379,7 +390,7 @@ cmsl_status build_graph(Engine *e)
     cudaGraphNode_t n_tdgl, n_solve, n_end;
     if (!fp64 && e->any_dep) CK(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
     if (fp64 && e->any_dep) CK(cudaGraphConditionalHandleCreate(&h_inner, g, 0, cudaGraphCondAssignDefault));
-    a.d = e->dev(1, h_inner, h_outer);
+    a.d = dev(h_inner, h_outer);
     void *args64[] = {&a.d, &a.F64};
     void *args32[] = {&a.d, &a.F32};
     void *args_d[] = {&a.d};
@@ -431,7 +442,7 @@ cmsl_status build_graph(Engine *e)
             cudaGraphNode_t n_r1, n_s1, n_r2, n_sb, n_rb;
             cudaGraph_t body;
             if (e->persistent) CK(cudaGraphConditionalHandleCreate(&h_inner, g, 0, cudaGraphCondAssignDefault));
-            a.d = e->dev(1, h_inner, h_outer);
+            a.d = dev(h_inner, h_outer);
             TRY(add_kernel(g, &n_r1, &last, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
             if (e->persistent) {
                 cudaGraph_t solve1;
@@ -445,7 +456,7 @@ cmsl_status build_graph(Engine *e)
             a.d.step_end = 1;
             TRY(add_kernel(g, &n_r2, &n_s1, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
             TRY(add_while(g, &n_solve, &n_r2, 1, h_outer, &body));
-            a.d = e->dev(1, 0, h_outer);
+            a.d = dev(0, h_outer);
             a.d.step_end = 1;
             TRY(add_solve(body, nullptr, &n_sb));
             TRY(add_kernel(body, &n_rb, &n_sb, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
@@ -456,7 +467,7 @@ cmsl_status build_graph(Engine *e)
             cudaGraphNode_t n_ref, n_in, n_sp, n_up;
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
-            a.d = e->dev(1, h_inner, h_outer);
+            a.d = dev(h_inner, h_outer);
             TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
             TRY(add_while(outer, &n_in, &n_ref, 1, h_inner, &inner));
             TRY(add_kernel(inner, &n_sp, nullptr, 0, (void *)k_spmv<float, Fast>, nit, NT, args32));
@@ -465,7 +476,7 @@ cmsl_status build_graph(Engine *e)
         }
     }
     if (last) TRY(add_kernel(g, &n_end, &last, 1, (void *)k_step_end, 1, 32, args_d));
-    CK(cudaGraphInstantiate(&e->exec, g, 0));
+    CK(cudaGraphInstantiate(&e->exec, top, 0));
     e->graph_valid = true;
     return CMSL_OK;
 }
@@ -1152,7 +1163,9 @@ cmsl_status run(Engine *e, int n_steps, const double *Ez, const int32_t *row, vo
     e->last_steps = n_steps;
     if (e->use_graph) {
         if (!e->graph_valid) TRY(build_graph(e));
-        for (int s = 0; s < n_steps; ++s) CK(cudaGraphLaunch(e->exec, st));
+        // one launch: the graph's step loop runs until run_step == stop
+        CK(cudaMemcpyAsync(&e->d_ctl->stop, &n_steps, sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaGraphLaunch(e->exec, st));
     } else {
         for (int s = 0; s < n_steps; ++s) TRY(step_direct(e, st));
     }

@@ -136,25 +136,33 @@ template <class T> __device__ __forceinline__ T warp_sum(T v)
 }
 
 // Sums NV values over the block; the result is valid in thread 0.  Values are
-// summed in T within a warp and in FP64 across warps.
+// summed in T within a warp and in FP64 across warps, in warp order: thread
+// i of the first warp sums value i, so the FP64 adds of all NV values issue
+// together (FP64 instructions are scarce on this part).
 template <int NV, class T>
 __device__ __forceinline__ void block_sum(T (&v)[NV], double (*sm)[NV], double (&out)[NV])
 {
+    static_assert(NV <= 32, "one lane per value");
+    static_assert(sizeof(T) <= sizeof(double), "warp sums are kept in sm");
+    __shared__ double s_tot[NV];
+    T *ws = (T *)&sm[0][0];                       // [warps][NV] warp sums
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     #pragma unroll
     for (int i = 0; i < NV; ++i) {
         const T s = warp_sum(v[i]);
-        if (lane == 0) sm[w][i] = (double)s;
+        if (lane == 0) ws[w * NV + i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        const int nw = (int)(blockDim.x >> 5);      // any block of up to NT threads
+        double s = 0.0;
+        for (int q = 0; q < nw; ++q) s += (double)ws[q * NV + threadIdx.x];
+        s_tot[threadIdx.x] = s;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const int nw = (int)(blockDim.x >> 5);      // any block of up to NT threads
         #pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            double s = 0.0;
-            for (int q = 0; q < nw; ++q) s += sm[q][i];
-            out[i] = s;
-        }
+        for (int i = 0; i < NV; ++i) out[i] = s_tot[i];
     }
     __syncthreads();
 }
@@ -204,6 +212,16 @@ __device__ __forceinline__ bool uniform_flag(const int *p)
 __device__ __forceinline__ void set_cond(const Dev &d, cudaGraphConditionalHandle h, int value)
 {
     if (d.use_cond && h) cudaGraphSetConditional(h, value ? 1u : 0u);
+}
+
+// Step rs in a graph whose WHILE node runs the steps (one thread of the
+// TDGL launch's last block): whether another step follows, and the entry
+// value of the outer refinement loop (a handle's default is applied per
+// graph launch, not per step).
+__device__ __forceinline__ void step_begin(const Dev &d, int rs)
+{
+    set_cond(d, d.h_steps, rs + 1 < d.ctl->stop);
+    set_cond(d, d.h_outer, 1);
 }
 
 // ------------------------------------------------------------- operator
@@ -494,7 +512,10 @@ __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)
             S->iters = 0;
         }
     }
-    if (threadIdx.x == 0) *d.counter = 0u;
+    if (threadIdx.x == 0) {
+        step_begin(d, rs);
+        *d.counter = 0u;
+    }
 }
 
 // In the last block of a solve's set-up kernel (partials r.z, r.r, b.b per
