@@ -45,6 +45,18 @@ __device__ __forceinline__ df df_add(df a, df b)
     return fast_two_sum(s.h, s.l);
 }
 
+// Accurate double-float sum (both halves through TwoSum; the "IEEE" add of
+// Hida, Li and Bailey's QD library), for sums whose terms may cancel.
+__device__ __forceinline__ df df_add_acc(df a, df b)
+{
+    df s = two_sum(a.h, b.h);
+    const df t = two_sum(a.l, b.l);
+    s.l += t.h;
+    s = fast_two_sum(s.h, s.l);
+    s.l += t.l;
+    return fast_two_sum(s.h, s.l);
+}
+
 __device__ __forceinline__ df df_neg(df a) { return df{-a.h, -a.l}; }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
 

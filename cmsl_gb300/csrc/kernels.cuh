@@ -199,6 +199,79 @@ __device__ __forceinline__ void film_total(const Dev &d, const FilmDev *f, doubl
     block_sum<NV, double>(v, sm, out);
 }
 
+// FP32 passes: the partial sums of an item are double-float pairs (float2
+// in the item's double slots) formed and added with FP32 instructions only,
+// so that neither the blocks' epilogues nor the last block's film totals
+// queue on the FP64 pipe.  The summation order is fixed (deterministic).
+template <int NV>
+__device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], double (*sm)[NV])
+{
+    static_assert(NV <= 32, "one lane per value");
+    float *ws = (float *)&sm[0][0];               // [warps][NV] warp sums
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const float s = warp_sum(v[i]);
+        if (lane == 0) ws[w * NV + i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        const int nw = (int)(blockDim.x >> 5);
+        df s{0.f, 0.f};
+        for (int q = 0; q < nw; ++q) s = df_add_f(s, ws[q * NV + threadIdx.x]);
+        *(float2 *)(d.partial + (long long)blockIdx.x * NPART + threadIdx.x) = make_float2(s.h, s.l);
+    }
+    __syncthreads();
+}
+
+// In the last block: film f's totals of the block_partial32 pairs (item
+// order: thread-strided, warp tree, then warps in order), valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, double (*sm)[NV],
+                                             double (&out)[NV])
+{
+    static_assert(NV <= 32 && sizeof(float2) == sizeof(double), "one lane and one slot per value");
+    __shared__ double s_tot[NV];
+    float2 *ws = (float2 *)&sm[0][0];             // [warps][NV] warp totals
+    df v[NV];
+    #pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = df{0.f, 0.f};
+    for (int it = f->item_begin + (int)threadIdx.x; it < f->item_end; it += (int)blockDim.x) {
+        #pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const float2 p = __ldcg((const float2 *)(d.partial + (long long)it * NPART + i));
+            v[i] = df_add_acc(v[i], df{p.x, p.y});
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int UNR = NV > 4 ? 1 : NV;          // seven TDGL totals: one at a time (registers)
+    #pragma unroll UNR
+    for (int i = 0; i < NV; ++i) {
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const df u{__shfl_down_sync(0xffffffffu, v[i].h, o), __shfl_down_sync(0xffffffffu, v[i].l, o)};
+            v[i] = df_add_acc(v[i], u);
+        }
+        if (lane == 0) ws[w * NV + i] = make_float2(v[i].h, v[i].l);
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        const int nw = (int)(blockDim.x >> 5);
+        df s{0.f, 0.f};
+        for (int q = 0; q < nw; ++q) {
+            const float2 p = ws[q * NV + threadIdx.x];
+            s = df_add_acc(s, df{p.x, p.y});
+        }
+        s_tot[threadIdx.x] = (double)s.h + (double)s.l;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        #pragma unroll
+        for (int i = 0; i < NV; ++i) out[i] = s_tot[i];
+    }
+    __syncthreads();
+}
+
 // Block-uniform read of a flag another block may have written.
 __device__ __forceinline__ bool uniform_flag(const int *p)
 {
@@ -266,6 +339,7 @@ __device__ __forceinline__ void op_z(const FilmDev *f, int k, V up, V dn, V &u, 
     else { u = dn; dd = dn; }
 }
 
+template <bool DF>
 __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)[7], double (&sTot)[7]);
 
 // ---------------------------------------------------------- TDGL kernel
@@ -471,19 +545,22 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
         }
     }
     if (!ticket_last(d.counter)) return;
-    tdgl_finish(d, rs, sRed, sTot);
+    tdgl_finish<false>(d, rs, sRed, sTot);
 }
 
 // Last block of a TDGL step: every film's sweep row from its items' partial
 // sums (evolve.cu:256-357 scaled as in :391-400), and the per-step reset of
 // the solver state.
+// DF: the partials are block_partial32 pairs (FP32 kernel).
+template <bool DF>
 __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)[7], double (&sTot)[7])
 {
     for (int fi = 0; fi < d.n_films; ++fi) {
         const FilmDev *ff = d.films + fi;
         const int frow = d.rows[(long long)fi * d.wstride + rs];
         if (frow >= 0) {
-            film_total<7>(d, ff, sRed, sTot);
+            if (DF) film_total32<7>(d, ff, sRed, sTot);
+            else film_total<7>(d, ff, sRed, sTot);
             if (threadIdx.x == 0) {
                 double *R = d.rowbuf + ((long long)fi * d.rstride + frow) * 11;
                 const double N = (double)ff->nx * ff->ny * ff->nz;
@@ -700,7 +777,7 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
         const FilmDev *ff = d.films + fi;
         SolveDev *S = d.solve + fi;
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
-        if (was) film_total<3>(d, ff, sRed, sTot);
+        if (was) film_total32<3>(d, ff, sRed, sTot);
         if (threadIdx.x == 0 && was) {
             // an update pass (r <- r - A dx) leaves b.b as the last full pass formed it
             const bool was_upd = ff->upd_ok && S->upd && S->refine > 0;

@@ -262,16 +262,9 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
     }
     cp_wait<0>();
 
-    if (row >= 0) {
-        double tot[7];
-        block_sum<7, float>(acc, sRed, tot);
-        if (threadIdx.x == 0) {
-            #pragma unroll
-            for (int q = 0; q < 7; ++q) d.partial[(long long)blockIdx.x * NPART + q] = tot[q];
-        }
-    }
+    if (row >= 0) block_partial32<7>(d, acc, sRed);
     if (!ticket_last(d.counter)) return;
-    tdgl_finish(d, rs, sRed, sTot);
+    tdgl_finish<true>(d, rs, sRed, sTot);
 }
 
 // Warm start alone (own cells): the free buffer of every depolarised film
@@ -437,13 +430,7 @@ __device__ __forceinline__ void refine_cell(const RConst &rc, int k, bool ident,
 
 __device__ __forceinline__ void refine_partials(const Dev &d, float (&acc)[3], double (*sRed)[3])
 {
-    double t[3];
-    block_sum<3, float>(acc, sRed, t);
-    if (threadIdx.x == 0) {
-        d.partial[(long long)blockIdx.x * NPART + 0] = t[0];
-        d.partial[(long long)blockIdx.x * NPART + 1] = t[1];
-        d.partial[(long long)blockIdx.x * NPART + 2] = t[2];
-    }
+    block_partial32<3>(d, acc, sRed);
 }
 
 template <bool UNI> struct R32Lay {
