@@ -12,4 +12,4 @@ from ._lib import (  # noqa: F401
     FP64, FP32_REFINED, DIRICHLET, NEUMANN, CRIT_REF, CRIT_RELRES, INNER_AUTO, INNER_PCG, INNER_DIRECT,
     CmslError, LIB_PATH,
 )
-from .film import Batch, Film  # noqa: F401
+from .film import Batch, Film, pinned_empty  # noqa: F401

@@ -4,10 +4,11 @@
 // Their cells, grains and work items are concatenated; every kernel launch
 // covers all films, each work item carrying its film index, and every
 // per-film quantity (solver scalars, convergence flags, waveform, sweep rows)
-// lives in per-film device slots.  One time step is one CUDA graph:
+// lives in per-film device slots.  A run is one CUDA graph launch: a WHILE
+// node over the steps whose body is one time step,
 //   CMSL_FP64:          k_tdgl -> k_rhs -> WHILE(inner){ k_spmv -> k_update } -> k_step_end
 //   CMSL_FP32_REFINED:  k_tdgl32 -> k_refine32 -> solve -> k_refine32
-//                       -> WHILE(outer){ solve -> k_refine32 } -> k_step_end
+//                       -> WHILE(outer){ solve -> k_refine32 }
 // where the FP32 inner solve is the direct spectral solve (films of one eps,
 // spectral.cuh), or one persistent cooperative PCG launch over all films
 // (each film on its own block range with its own convergence flag, under an
@@ -15,12 +16,14 @@
 // followed by WHILE(inner){ k_spmv -> k_update } inside the outer WHILE.
 // Converged films drop out of the masked kernels; a loop runs while any film
 // is active.  The conditions are set on the device by the last block of
-// k_rhs, k_refine32 and k_update, so a step never returns to the host: the
+// k_tdgl32 / k_tdgl (the step loop), k_rhs, k_refine32 and k_update (the
+// residual pass that leaves no film active also ends the step, in place of
+// k_step_end), so a run never returns to the host: the
 // PCG loop of the reference (depol_varEPS.cu:472-522, two blocking Ddot per
 // iteration) and its per-step cudaMalloc/cublasCreate churn (:373-393,
 // :585-593) are gone.  The applied field and the output-row schedule of the
-// P-E loop are device arrays indexed by a device step counter, so the same
-// graph is relaunched for every step.
+// P-E loop are device arrays indexed by a device step counter, which the
+// step loop's condition compares with the run's length.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -484,9 +487,11 @@ cmsl_status build_graph(Engine *e)
 // State transfers.  Where the device reads the host's page tables
 // (cudaDevAttrPageableMemoryAccess: Grace-Blackwell's coherent NVLink-C2C),
 // kernels read the caller's double arrays in place and convert on the GPU.
-// Downloads go through one pinned array and are converted on the host cores
+// Downloads into page-locked caller arrays (cmsl_host_alloc, or registered
+// by the caller) are converted and written by kernels as well; other
+// downloads go through one pinned array and are converted on the host cores
 // (a GPU writing fresh pageable pages pays a page fault per page).  Without
-// that device attribute the host converts and copies both ways.
+// that device attribute uploads are converted on the host too.
 template <class T>
 __global__ void k_host_in(const double *__restrict__ src, T *__restrict__ dst, long long n)
 {
@@ -503,7 +508,31 @@ __global__ void k_phi_in(const double *__restrict__ src, float *__restrict__ hi,
         lo[i] = (float)(x - (double)h);
     }
 }
+template <class T>
+__global__ void k_host_out(const T *__restrict__ src, double *__restrict__ dst, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
+}
+__global__ void k_phi_out(const float *__restrict__ hi, const float *__restrict__ lo, double *__restrict__ dst,
+                          long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (double)hi[i] + (double)lo[i];
+}
 constexpr int XFER_GRID = 152 * 8, XFER_NT = 256;
+
+// The device address of page-locked host memory at p (null for pageable
+// memory, which cudaPointerGetAttributes reports as unregistered).
+inline double *locked_dst(double *p)
+{
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? (double *)a.devicePointer : nullptr;
+}
 
 }  // namespace cmsl_eng
 
@@ -676,6 +705,18 @@ template <class T>
 cmsl_status get_fields(Engine *e, int film, int set, double *const P[6])
 {
     const FilmHost &h = e->fh[film];
+    bool rest = false;                  // arrays left for the paths below
+    for (int q = 0; q < 6; ++q) {
+        double *dv = locked_dst(P[q]);
+        if (dv) k_host_out<T><<<XFER_GRID, XFER_NT>>>((const T *)e->d_P[set][q] + h.off, dv, h.N);
+        else rest = rest || P[q];
+    }
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if (!rest) return CMSL_OK;
+    double *Pr[6];
+    for (int q = 0; q < 6; ++q) Pr[q] = locked_dst(P[q]) ? nullptr : P[q];
+    P = Pr;
     if (e->host_direct) {
         // one DMA copy into pinned memory, then the conversion into the
         // caller's arrays on the host cores
@@ -1115,8 +1156,14 @@ cmsl_status get_state(Engine *e, int film, double *const P[6], double *phi)
     }
     const FilmHost &h = e->fh[film];
     if (phi) {
+        double *dv = e->precision == CMSL_FP64 ? nullptr : locked_dst(phi);
         if (e->precision == CMSL_FP64) {
             CK(cudaMemcpy(phi, e->d_phi[S.phi_cur] + h.off, sizeof(double) * h.N, cudaMemcpyDeviceToHost));
+        } else if (dv) {
+            const float *b = (const float *)e->d_phi[S.phi_cur];
+            k_phi_out<<<XFER_GRID, XFER_NT>>>(b + h.off, b + e->ncells + h.off, dv, h.N);
+            CK(cudaGetLastError());
+            CK(cudaDeviceSynchronize());
         } else if (e->host_direct) {
             const float *b = (const float *)e->d_phi[S.phi_cur];
             void *stg = nullptr;
@@ -1409,6 +1456,20 @@ cmsl_status cmsl_film_get_state(cmsl_film *f, double *const P[6], double *phi)
 {
     if (!f) return fail(CMSL_ERR_ARG, "NULL film");
     return get_state(f, 0, P, phi);
+}
+
+cmsl_status cmsl_host_alloc(size_t bytes, void **out)
+{
+    if (!out) return fail(CMSL_ERR_ARG, "NULL out");
+    *out = nullptr;
+    CK(cudaMallocHost(out, bytes ? bytes : 16));
+    return CMSL_OK;
+}
+
+cmsl_status cmsl_host_free(void *p)
+{
+    if (p) CK(cudaFreeHost(p));
+    return CMSL_OK;
 }
 
 cmsl_status cmsl_film_run(cmsl_film *f, int n_steps, const double *Ez, const int32_t *row, void *stream)

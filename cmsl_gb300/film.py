@@ -7,6 +7,7 @@ table a ``SetupAndRunSimulation`` call builds (HZO_Code_github/src/main.cu:
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -25,6 +26,34 @@ def _d(a):
 
 def _i(a):
     return a.ctypes.data_as(_ip)
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """An uninitialised numpy array in page-locked host memory
+    (cmsl_host_alloc), freed with the array.  ``get_state(out=...)`` converts
+    on the GPU straight into such arrays."""
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    p = C.c_void_p()
+    check(lib().cmsl_host_alloc(n, C.byref(p)))
+    buf = (C.c_char * max(n, 1)).from_address(p.value)
+    weakref.finalize(buf, lib().cmsl_host_free, C.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dt, count=n // dt.itemsize).reshape(shape)
+
+
+def _state_out(out, n):
+    """(P, phi) output arrays: fresh ones, or the caller's ``out`` checked."""
+    if out is None:
+        return [np.zeros(n) for _ in range(6)], np.zeros(n)
+    P, phi = out
+    P = list(P)
+    for a in P + [phi]:
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.size == n and a.flags.c_contiguous
+                and a.flags.writeable):
+            raise ValueError("out arrays must be writeable contiguous float64 arrays of %d cells" % n)
+    if len(P) != 6:
+        raise ValueError("out needs six P arrays")
+    return P, phi
 
 
 class _Desc:
@@ -118,9 +147,11 @@ class Film:
         ph = None if phi is None else np.ascontiguousarray(phi, np.float64)
         check(lib().cmsl_film_set_state(self._h, arr, _d(ph) if ph is not None else None))
 
-    def get_state(self):
-        P = [np.zeros(self.N) for _ in range(6)]
-        phi = np.zeros(self.N)
+    def get_state(self, out=None):
+        """(P, phi) as float64 arrays; ``out=(P, phi)`` fills the caller's
+        arrays instead (page-locked ones from ``pinned_empty`` are written by
+        the GPU directly)."""
+        P, phi = _state_out(out, self.N)
         arr = (_dp * 6)(*[_d(p) for p in P])
         check(lib().cmsl_film_get_state(self._h, arr, _d(phi)))
         return P, phi
@@ -289,10 +320,9 @@ class Batch:
         ph = None if phi is None else np.ascontiguousarray(phi, np.float64)
         check(lib().cmsl_batch_set_state(self._h, int(film), arr, _d(ph) if ph is not None else None))
 
-    def get_state(self, film):
-        n = self.N[film]
-        P = [np.zeros(n) for _ in range(6)]
-        phi = np.zeros(n)
+    def get_state(self, film, out=None):
+        """Film ``film``'s (P, phi), as ``Film.get_state``."""
+        P, phi = _state_out(out, self.N[film])
         arr = (_dp * 6)(*[_d(p) for p in P])
         check(lib().cmsl_batch_get_state(self._h, int(film), arr, _d(phi)))
         return P, phi

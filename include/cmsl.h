@@ -121,6 +121,15 @@ cmsl_status cmsl_film_destroy(cmsl_film *film);
 cmsl_status cmsl_film_set_state(cmsl_film *film, const double *const P[6], const double *phi);
 cmsl_status cmsl_film_get_state(cmsl_film *film, double *const P[6], double *phi);
 
+/* Page-locked host memory for state arrays (no reference counterpart: the
+ * reference keeps its state in its own globals).  get_state converts on the
+ * GPU straight into page-locked arrays (these, or memory the caller
+ * registered with CUDA) instead of converting on the host cores, and a
+ * caller that reuses its arrays across calls avoids first-touch page faults.
+ * cmsl_host_free(NULL) is a no-op. */
+cmsl_status cmsl_host_alloc(size_t bytes, void **out);
+cmsl_status cmsl_host_free(void *p);
+
 /* The P-E loop driver body (Evolve, evolve.cu:217-409): runs n_steps TDGL steps,
  * each followed by the depolarisation solve when dep_flag.  Ez[s] is the
  * applied non-dimensional field of step s (host array); row[s] >= 0 stores the

@@ -46,3 +46,48 @@ def test_state_round_trip_and_run(gpu, precision, monkeypatch):
     for a, b in zip(out[0][0], out[1][0]):
         assert np.array_equal(a, b)
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_page_locked_outputs(gpu, precision):
+    """get_state into page-locked arrays (written by the GPU) gives the same
+    values as into fresh pageable arrays, for a film and for a batch."""
+    f, P = random_film(36, 20, 10, seed=103, eps_0_nd=3.0, p_scale=0.2)
+    kw = dict(precision=gpu.FP64 if precision == "fp64" else gpu.FP32_REFINED)
+    Ez = np.linspace(0.0, 0.2, 6)
+    P_in = [gpu.pinned_empty(f.N) for _ in range(6)]
+    for a, p in zip(P_in, P):
+        a[:] = p
+    out = ([gpu.pinned_empty(f.N) for _ in range(6)], gpu.pinned_empty(f.N))
+    with gpu.Film.from_oracle_film(f, **kw) as g:
+        g.set_state(P_in)
+        g.run(Ez)
+        Pa, pha = g.get_state()
+        Pb, phb = g.get_state(out=out)
+        assert Pb[0] is out[0][0] and phb is out[1]
+        for a, b in zip(Pa, Pb):
+            assert np.array_equal(a, b)
+        assert np.array_equal(pha, phb)
+    f2, P2 = random_film(24, 24, 8, seed=104, eps_0_nd=3.0, p_scale=0.2)
+    with gpu.Batch.from_oracle_films([f, f2], **kw) as b:
+        b.set_state(0, P)
+        b.set_state(1, P2)
+        b.run(np.stack([Ez, Ez]))
+        for i, n in enumerate((f.N, f2.N)):
+            o = ([gpu.pinned_empty(n) for _ in range(6)], gpu.pinned_empty(n))
+            Pa, pha = b.get_state(i)
+            Pb, phb = b.get_state(i, out=o)
+            for a, c in zip(Pa, Pb):
+                assert np.array_equal(a, c)
+            assert np.array_equal(pha, phb)
+
+
+def test_bad_out_arrays(gpu):
+    f, P = random_film(12, 12, 4, seed=105, eps_0_nd=3.0, p_scale=0.2)
+    with gpu.Film.from_oracle_film(f) as g:
+        with pytest.raises(ValueError):
+            g.get_state(out=([np.zeros(f.N)] * 5, np.zeros(f.N)))
+        with pytest.raises(ValueError):
+            g.get_state(out=([np.zeros(f.N)] * 6, np.zeros(f.N - 1)))
+        with pytest.raises(ValueError):
+            g.get_state(out=([np.zeros(f.N, np.float32)] * 6, np.zeros(f.N)))
