@@ -81,3 +81,31 @@ def test_batch_rejects_bad_descriptors_without_gpu():
     assert _lib.lib().cmsl_batch_create(None, 1, _lib.C.byref(h)) == 1
     with pytest.raises(ValueError):
         cg.Batch([])
+
+
+def test_state_out_arrays_checked_without_gpu():
+    """get_state(out=...) validates the caller's arrays on the host (shape,
+    dtype, contiguity, count) before any CUDA call; cmsl_host_alloc rejects a
+    NULL out pointer, and cmsl_host_free(NULL) is a no-op."""
+    import numpy as np
+    from cmsl_gb300 import _lib
+    from cmsl_gb300.film import _state_out
+    n = 10
+    P, phi = _state_out(None, n)
+    assert len(P) == 6 and all(p.shape == (n,) and p.dtype == np.float64 for p in P) and phi.shape == (n,)
+    ok = ([np.zeros(n) for _ in range(6)], np.zeros(n))
+    P2, phi2 = _state_out(ok, n)
+    assert P2[3] is ok[0][3] and phi2 is ok[1]
+    bad = [([np.zeros(n)] * 5, np.zeros(n)),
+           ([np.zeros(n)] * 6, np.zeros(n + 1)),
+           ([np.zeros(n, np.float32)] * 6, np.zeros(n)),
+           ([np.zeros(2 * n)[::2]] * 6, np.zeros(n))]
+    ro = np.zeros(n)
+    ro.flags.writeable = False
+    bad.append(([ro] * 6, np.zeros(n)))
+    for out in bad:
+        with pytest.raises(ValueError):
+            _state_out(out, n)
+    L = _lib.lib()
+    assert L.cmsl_host_alloc(16, None) == 1
+    assert L.cmsl_host_free(None) == 0
