@@ -29,7 +29,10 @@ constexpr int TR32 = 12;     // FP32 rotation per grain: 9 values + 3 pad (three
 
 // Warm start of a step's first refinement pass (own cell): 0 the previous
 // potential a, 1 linear 2a - q, 2 quadratic 3(a - q) + u, 3 cubic
-// 4(a + u) - 6q - v, with a, q, u, v the potentials of steps n .. n-3.
+// 4(a + u) - 6q - v, with a, q, u, v the potentials of steps n .. n-3.  In
+// double-float: FP32 rounding noise in the start would be amplified by the
+// operator's high-frequency end (~12/h^2) well above the smooth truncation
+// error, and the first residual would miss the update pass's 1e-4 ||b||.
 __device__ __forceinline__ df extrap_phi(int warm, df a, df q, df u, df v)
 {
     if (warm == 1) return df_sub(df{2.f * a.h, 2.f * a.l}, q);
@@ -37,6 +40,13 @@ __device__ __forceinline__ df extrap_phi(int warm, df a, df q, df u, df v)
     if (warm == 3) return df_sub(df_sub(df_mul_f(df_add(a, u), 4.f), df_mul_f(q, 6.f)), v);
     return a;
 }
+
+// Difference of two double-float potentials rounded to FP32, for E: the hi
+// difference of neighbouring values is exact when they lie within a factor
+// of two of each other (Sterbenz) and one FP32 rounding off otherwise; the
+// lo difference is added.  E enters the FP32 step, which rounds at that
+// level anyway.
+__device__ __forceinline__ float phi_diff32(df a, df b) { return (a.h - b.h) + (a.l - b.l); }
 
 // The free one of the five potential buffers of film S.
 __device__ __forceinline__ int phi_free(const SolveDev *S)
@@ -139,7 +149,10 @@ __device__ __forceinline__ void row_acc(float (&acc)[7], int mat, const float (&
 }
 
 constexpr int T32_NS = 4;
-constexpr int T32_STAGE = 8 * SPL + NT;      // floats: P[6], phi hi, phi lo (own + halo); code (own)
+// Stage layout (own + halo slots): P as three float2 planes (P0, P1), (P2, P3),
+// (P4, P5), the potential as one (hi, lo) float2 plane, then the code (own):
+// a stencil point of a pair is one 8-byte shared load.
+constexpr int T32_STAGE = 8 * SPL + NT;      // floats
 constexpr size_t T32_SMEM = sizeof(float) * T32_NS * T32_STAGE;
 
 template <int NS>
@@ -182,19 +195,19 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         if (p <= zhi) {
             if (g.valid) {
                 #pragma unroll
-                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.own_slot, Po + q * fs + own_o);
+                for (int q = 0; q < 6; ++q) cp4(st + 2 * ((q >> 1) * SPL + g.own_slot) + (q & 1), Po + q * fs + own_o);
                 if (dep) {
-                    cp4(st + 6 * SPL + g.own_slot, ph + own_o);
-                    cp4(st + 7 * SPL + g.own_slot, ph + lo + own_o);
+                    cp4(st + 2 * (3 * SPL + g.own_slot), ph + own_o);
+                    cp4(st + 2 * (3 * SPL + g.own_slot) + 1, ph + lo + own_o);
                 }
                 cp4(st + 8 * SPL + threadIdx.x, code + own_o);
             }
             if (g.halo) {
                 #pragma unroll
-                for (int q = 0; q < 6; ++q) cp4(st + q * SPL + g.halo_slot, Po + q * fs + halo_o);
+                for (int q = 0; q < 6; ++q) cp4(st + 2 * ((q >> 1) * SPL + g.halo_slot) + (q & 1), Po + q * fs + halo_o);
                 if (dep) {
-                    cp4(st + 6 * SPL + g.halo_slot, ph + halo_o);
-                    cp4(st + 7 * SPL + g.halo_slot, ph + lo + halo_o);
+                    cp4(st + 2 * (3 * SPL + g.halo_slot), ph + halo_o);
+                    cp4(st + 2 * (3 * SPL + g.halo_slot) + 1, ph + lo + halo_o);
                 }
             }
         }
@@ -223,30 +236,32 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         const float *sk = ring + ri.s * T32_STAGE;
         const float *su = ring + ri.up(k == nz - 1) * T32_STAGE, *sd = ring + ri.dn(k == 0) * T32_STAGE;
         const uint32_t c = ((const uint32_t *)sk)[8 * SPL + threadIdx.x];
+        const float2 *k2 = (const float2 *)sk, *u2 = (const float2 *)su, *d2 = (const float2 *)sd;
         float pc[6], sum[6];
         #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            const float *a = sk + q * SPL;
-            pc[q] = a[s0];
+        for (int p = 0; p < 3; ++p) {
+            const float2 *a = k2 + p * SPL;
+            const float2 cc = a[s0], xe = a[s0 + 1], xw = a[s0 - 1], yn = a[s0 + SX], ys = a[s0 - SX];
+            const float2 zu = u2[p * SPL + s0], zd = d2[p * SPL + s0];
+            pc[2 * p] = cc.x;
+            pc[2 * p + 1] = cc.y;
             // neighbour sums e, w, n, s, u, d (kernels_evol.cu:101-122); z clamped
-            float sm = a[s0 + 1] + a[s0 - 1];
-            sm = sm + a[s0 + SX];
-            sm = sm + a[s0 - SX];
-            sm = sm + su[q * SPL + s0];
-            sum[q] = sm + sd[q * SPL + s0];
+            sum[2 * p] = ((((xe.x + xw.x) + yn.x) + ys.x) + zu.x) + zd.x;
+            sum[2 * p + 1] = ((((xe.y + xw.y) + yn.y) + ys.y) + zu.y) + zd.y;
         }
         float ex = 0.f, ey = 0.f, ez = 0.f;
         df a0{0.f, 0.f};
         if (dep) {
-            const float *fh = sk + 6 * SPL, *fl = sk + 7 * SPL;
-            a0 = df{fh[s0], fl[s0]};
+            const float2 *f2 = k2 + 3 * SPL;
+            const float2 fc = f2[s0], fu = u2[3 * SPL + s0], fd = d2[3 * SPL + s0];
+            const float2 fe = f2[s0 + 1], fw = f2[s0 - 1], fn = f2[s0 + SX], fsth = f2[s0 - SX];
+            a0 = df{fc.x, fc.y};
             df pu, pd;
-            efield_z(neu, k, nz, df{su[6 * SPL + s0], su[7 * SPL + s0]}, df{sd[6 * SPL + s0], sd[7 * SPL + s0]},
-                     pu, pd);
+            efield_z(neu, k, nz, df{fu.x, fu.y}, df{fd.x, fd.y}, pu, pd);
             // -1 * E with E = -(phi_+ - phi_-) / (2h)
-            ex = phi_diff(df{fh[s0 + 1], fl[s0 + 1]}, df{fh[s0 - 1], fl[s0 - 1]}) * inv_2hf;
-            ey = phi_diff(df{fh[s0 + SX], fl[s0 + SX]}, df{fh[s0 - SX], fl[s0 - SX]}) * inv_2hf;
-            ez = phi_diff(pu, pd) * inv_2hf;
+            ex = phi_diff32(df{fe.x, fe.y}, df{fw.x, fw.y}) * inv_2hf;
+            ey = phi_diff32(df{fn.x, fn.y}, df{fsth.x, fsth.y}) * inv_2hf;
+            ez = phi_diff32(pu, pd) * inv_2hf;
         }
         float pn[6], pMZl, pSZl;
         tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
