@@ -139,6 +139,23 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
+    """The slowest rank's timed region (replicas run independently; the job
+    is as fast as its slowest rank).  dist: torch.distributed when N > 1."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    return float(t.item())
+
+
+def replica_rate(cells_per_rank: int, steps: int, ms_max: float, world: int) -> float:
+    """Whole-job cell-steps/s of `world` replicas of `cells_per_rank` cells
+    each advancing `steps` steps within `ms_max` milliseconds (weak scaling)."""
+    return world * cells_per_rank * steps / (ms_max * 1e-3)
+
+
 def make_oracle_film(w, orc, crit_relres=True):
     import oracle
     f = oracle.Film(nx=w.nx, ny=w.ny, nz=w.nz, del_h=w.del_h, del_t=w.del_t, omega=w.omega,
@@ -273,12 +290,8 @@ def run_ours(args):
         ms = ev0.elapsed_time(ev1)
         torch.cuda.synchronize()
     it, rf = film.iters(K)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    ms_max = float(t.item())
-    value = world * w.N * K / (ms_max * 1e-3)
+    ms_max = max_over_ranks(ms, dist, "cuda")
+    value = replica_rate(w.N, K, ms_max, world)
 
     # per-kernel device times (CUDA events on the launch stream)
     kms = film.time_kernels(reps=20, stream=sp)
