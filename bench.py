@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -33,29 +34,53 @@ sys.path.insert(0, ROOT)
 METRIC = "TDGL cell-steps/s incl. PCG, FP32-refined vs FP64 on GB300 at equal P-E error"
 CONFIG_ID = 1
 
-# Algorithmic bytes per cell and launch (compulsory DRAM traffic of each kernel).
-#   tdgl:     read 6 P + phi + code, write 6 P (FP32 also: read the two older
-#             potentials of the quadratic warm start, write the warm start)
-#   setup:    FP64 rhs: read Pm(3) + phi + code + dinv, write r
-#             FP32 first refinement pass (one eps): read x (double-float) + Pm(3), write r
-#   update:   (FP64) read x, p, r, q, dinv, write x, r
-#             (FP32 update pass after the direct solve) read phi (double-float), dx, r,
-#             write phi (double-float), r
-#   spmv:     (FP64) read r, p_old, dinv, code, write p, q
-#   pcg_iter: (FP32, one single-reduction iteration of the persistent solver)
-#             read x, p, r, s, w, dinv, code, write x, p, r, s, w
-#   spec:     (FP32, direct inner solve, two real planes per complex spectrum plane) x-FFT:
-#             read r, write spectra; y-FFT, z-solve, y-FFT: read and write the spectra;
-#             x-FFT: read the spectra, write x -> 5 x (4 + 4) B
-#   spmv32:   (FP32 batch, masked two-kernel PCG) read r, p_old, dinv, code, write p, q
-#   update32: (FP32 batch) read x, p, r, q, dinv, write x, r
-BYTES = {
+# Algorithmic bytes per cell (the compulsory DRAM traffic of the path, the
+# roofline's numerator), with s = 4 (FP32) or 8 (FP64) bytes per stored value
+# and the grain code 4 bytes; per-grain tables are cache-resident:
+#   tdgl:  read 6 P, write 6 P, read phi, read the code, write div P  -> 14 s + 4
+#   pcg:   one inner iteration: the SpMV reads p and the code and writes Ap;
+#          the update reads x, r, Ap, p and writes x, r              -> 10 s + 4
+#          (the direct inner solve is counted as one inner iteration)
+#   ref:   one FP64-accurate refinement pass: read phi, div P, the code,
+#          write r                                                     -> 28 (FP32 path)
+ALG = {"fp32": {"tdgl": 14 * 4 + 4, "pcg": 10 * 4 + 4, "ref": 28},
+       "fp64": {"tdgl": 14 * 8 + 4, "pcg": 10 * 8 + 4, "ref": 0}}
+# The per-kernel algorithmic bytes of the roofline line (by kernel):
+#   tdgl -> ALG tdgl; setup (first refinement pass; FP64: the RHS) and update
+#   (update pass) -> ALG ref (FP64 rhs: read Pm, write b: 3 s + 4 + s);
+#   spec (one direct solve) and pcg_iter / spmv+update -> ALG pcg.
+# Bytes the kernels as designed move per launch (what they read and write,
+# including the double-float potential and the warm start's older
+# potentials), kept beside the algorithmic figure:
+DESIGN_BYTES = {
     "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4 + 2 * 8 + 8, "setup": 8 + 12 + 4, "update": 8 + 4 + 4 + 4 + 8,
              "pcg_iter": 7 * 4 + 5 * 4, "spmv32": 4 * 4 + 2 * 4, "update32": 5 * 4 + 2 * 4, "spec": 40},
     "fp64": {"tdgl": 6 * 8 * 2 + 8 + 4, "setup": 24 + 8 + 4 + 8 + 8, "spmv": 8 * 3 + 4 + 16,
              "update": 5 * 8 + 2 * 8},
 }
 KERNELS = {"fp32": ["tdgl", "setup", "pcg_iter"], "fp64": ["tdgl", "setup", "spmv", "update"]}
+
+
+def alg_bytes(mode: str, kernel: str) -> int:
+    """Algorithmic bytes per cell of one launch of `kernel`."""
+    a = ALG[mode]
+    if kernel == "tdgl":
+        return a["tdgl"]
+    if kernel in ("setup", "update") and mode == "fp32":
+        return a["ref"]
+    if mode == "fp64" and kernel == "setup":
+        return 3 * 8 + 4 + 8
+    if mode == "fp64" and kernel == "spmv":
+        return 8 + 4 + 8                      # the SpMV part of one iteration
+    if mode == "fp64" and kernel == "update":
+        return a["pcg"] - (8 + 4 + 8)         # the update part
+    return a["pcg"]                           # spec, pcg_iter, spmv32 + update32
+
+
+def step_bytes(mode: str, n_iter: float, n_ref: float) -> float:
+    """B_alg = B_tdgl + n_iter B_pcg + n_ref B_ref per cell-step."""
+    a = ALG[mode]
+    return a["tdgl"] + n_iter * a["pcg"] + n_ref * a["ref"]
 
 
 def measured_peaks():
@@ -242,6 +267,82 @@ def run_reference(args):
     return 0
 
 
+def film_kw(cg, fp64: bool, inner=None) -> dict:
+    kw = dict(precision=cg.FP64 if fp64 else cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8,
+              max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000,
+              warm_start=2)
+    if inner is not None:
+        kw["inner_solver"] = inner
+    return kw
+
+
+def timed_repeats(film, Ez, rows, W: int, K: int, R: int, stream, dist=None, clocks=None):
+    """W untimed warm-up steps, then R timed regions of exactly K steps each
+    (the P-E loop continues from region to region), each bracketed by a
+    barrier and a device synchronisation and timed with CUDA events on the
+    launch stream.  Returns the per-region milliseconds."""
+    import torch
+    sp = stream.cuda_stream
+    out = []
+    with torch.cuda.stream(stream):
+        film.run(Ez[:W], rows[:W], stream=sp)
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        for r in range(R):
+            e = Ez[W + r * K:W + (r + 1) * K]
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            film.run(e, rows[:K], stream=sp, sync=False)
+            ev1.record(stream)
+            ev1.synchronize()
+            film.sync()
+            torch.cuda.synchronize()
+            out.append(ev0.elapsed_time(ev1))
+    return out
+
+
+def n_repeats(K: int, W: int, n_sched: int, est_ms_step: float, target_s: float = 1.5, r_min: int = 10) -> int:
+    """Timed regions: at least r_min, enough for ~target_s of timed work (so
+    the clock sampler sees the GPU under load), within the loop's schedule."""
+    want = max(r_min, int(math.ceil(target_s * 1e3 / max(K * est_ms_step, 1e-6))))
+    return max(1, min(want, (n_sched - W) // K))
+
+
+def side_run(cg, w, fp64: bool, inner, K: int, stream, mats=None, name=""):
+    """A short sample of another solver configuration of the same film (the
+    PCG paths): cell-steps/s over K steps after 3 warm-up steps, the PCG
+    iterations per step and the inner solve's kernel time."""
+    import torch
+    mm = w.mats if mats is None else mats
+    f = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, mm, **w.film_kwargs(), **film_kw(cg, fp64, inner))
+    f.set_state(w.P_init)
+    rows = np.arange(3 + K, dtype=np.int32)
+    ms = timed_repeats(f, w.sched.Ez, rows, 3, K, 1, stream)
+    it, rf = f.iters(K)
+    kms = f.time_kernels(reps=5, stream=stream.cuda_stream)
+    mode = "fp64" if fp64 else "fp32"
+    n_iter, n_ref = float(np.mean(it)), float(np.mean(rf))
+    rate = w.N * K / (ms[0] * 1e-3)
+    out = {"value": rate, "unit": "cell-steps/s", "steps": K, "ms_per_step": ms[0] / K,
+           "inner_solver": "direct" if f.inner_solver == cg.INNER_DIRECT else "pcg",
+           "pcg_iters_per_step": n_iter, "refine_passes_per_step": n_ref,
+           "eps_r": [float(v) for v in np.asarray(mm)[:, 7]],
+           "frac_step": step_bytes(mode, n_iter, n_ref) * rate / 1e9 / measured_peaks()[0]}
+    if not fp64 and f.inner_solver != cg.INNER_DIRECT:
+        # kernel_ms[2]: one iteration of the persistent PCG over the film
+        out["pcg_kernel"] = {"kernel": "k_pcg_cg2", "us_per_iter": kms[2] * 1e3,
+                             "bytes_per_cell": ALG["fp32"]["pcg"],
+                             "frac": ALG["fp32"]["pcg"] * w.N / (kms[2] * 1e-3) / 1e9 / measured_peaks()[0]}
+    f.close()
+    torch.cuda.synchronize()
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -259,43 +360,31 @@ def run_ours(args):
     from cmsl_gb300 import workloads as wl
 
     fp64 = args.precision == "fp64"
+    mode = "fp64" if fp64 else "fp32"
     w = wl.config(args.config)
-    kw = dict(precision=cg.FP64 if fp64 else cg.FP32_REFINED, pcg_crit=cg.CRIT_RELRES, tol_rel=1e-8,
-              max_iter=4000, refine_tol=1e-8, max_refine=6, inner_tol=1e-5, inner_max_iter=2000,
-              warm_start=2)
-    film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **kw)
+    film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **film_kw(cg, fp64))
     zchunk = 0 if args.no_autotune else film.autotune()
     film.set_state(w.P_init)
     K, W = args.steps, args.warmup
-    Ez = w.sched.Ez[: W + K]
-    rows = np.arange(W + K, dtype=np.int32)
+    n_sched = w.sched.n_steps
+    rows = np.arange(max(W, K) + 1, dtype=np.int32)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    with torch.cuda.stream(stream):
-        film.run(Ez[:W], rows[:W], stream=sp)
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        clocks = Clocks(local)
-        clocks.start()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        film.run(Ez[W:W + K], rows[:K], stream=sp, sync=False)
-        ev1.record(stream)
-        ev1.synchronize()
-        film.sync()
-        clk = clocks.stop()
-        ms = ev0.elapsed_time(ev1)
-        torch.cuda.synchronize()
+    # a first timed region sizes the repeats
+    probe = timed_repeats(film, w.sched.Ez, rows, W, K, 1, stream, dist)
+    R = args.repeats or n_repeats(K, W + K, n_sched, probe[0] / K)
+    film.set_state(w.P_init)
+    clocks = Clocks(local)
+    ms_all = timed_repeats(film, w.sched.Ez, rows, W, K, R, stream, dist, clocks)
+    clk = clocks.stop()
+    clk["repeats"] = R
+    ms = statistics.median(ms_all)
     it, rf = film.iters(K)
     ms_max = max_over_ranks(ms, dist, "cuda")
     value = replica_rate(w.N, K, ms_max, world)
 
     # per-kernel device times (CUDA events on the launch stream)
-    kms = film.time_kernels(reps=20, stream=sp)
-    mode = "fp64" if fp64 else "fp32"
+    kms = film.time_kernels(reps=50, stream=sp)
     n_iter = float(np.mean(it))
     n_ref = float(np.mean(rf))
     direct = film.inner_solver == cg.INNER_DIRECT
@@ -307,14 +396,21 @@ def run_ours(args):
     top = max(per_step, key=per_step.get)
     ki = names.index(top)
     peak, peak_kind = measured_peaks()
-    achieved = BYTES[mode][top] * w.N / (kms[ki] * 1e-3) / 1e9
+    b_alg = alg_bytes(mode, top)
+    achieved = b_alg * w.N / (kms[ki] * 1e-3) / 1e9
     traffic = ncu_traffic(w.name).get(mode, {}).get(top)
+    b_step = step_bytes(mode, n_iter, n_ref)
     roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind,
-            "bytes_per_cell": BYTES[mode][top],
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "bytes_per_cell": b_alg, "design_bytes_per_cell": DESIGN_BYTES[mode].get(top),
             "traffic": (traffic * w.N) if traffic is not None else None,
             "kernel_ms": {k: float(kms[i]) for i, k in enumerate(names)},
-            "share": {k: per_step[k] / sum(per_step.values()) for k in per_step}}
+            "kernel_frac": {k: alg_bytes(mode, k) * w.N / (kms[i] * 1e-3) / 1e9 / peak for i, k in enumerate(names)},
+            "share": {k: per_step[k] / sum(per_step.values()) for k in per_step},
+            "step_bytes_per_cell": b_step,
+            "frac_step": b_step * value / world / 1e9 / peak,
+            "step_model": "B_tdgl + n_iter B_pcg + n_ref B_ref = %d + %.2f x %d + %.2f x %d" % (
+                ALG[mode]["tdgl"], n_iter, ALG[mode]["pcg"], n_ref, ALG[mode]["ref"])}
     if fp64:
         launches = int(K * 3 + 2 * it.sum())
     elif direct:
@@ -326,7 +422,7 @@ def run_ours(args):
 
     # end to end through the C ABI: host state in, K steps, host rows + state
     # out, the state arrays page-locked and allocated once (as a campaign
-    # reuses them from loop to loop)
+    # reuses them from loop to loop); the median of several calls
     P_in = [cg.pinned_empty(w.N) for _ in range(6)]
     for a, p in zip(P_in, w.P_init):
         a[:] = p
@@ -334,20 +430,43 @@ def run_ours(args):
     film.set_state(P_in)
     film.get_state(out=st_out)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    film.set_state(P_in)
-    film.run(Ez[W:W + K], rows[:K])
-    r = film.rows(0, K)
-    P_out, phi_out = film.get_state(out=st_out)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_t = []
+    for _ in range(args.e2e_repeats):
+        t0 = time.perf_counter()
+        film.set_state(P_in)
+        film.run(w.sched.Ez[W:W + K], rows[:K])
+        film.rows(0, K)
+        film.get_state(out=st_out)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
     esz = 8 if fp64 else 4
     h2d = 6 * w.N * esz + K * 12
     d2h = K * 88 + 6 * w.N * esz + w.N * 8
     e2e = {"value": w.N * K / e2e_s * world, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d // K,
-           "d2h_bytes_per_step": d2h // K,
+           "d2h_bytes_per_step": d2h // K, "repeats": len(e2e_t),
            "note": "per call: host P upload, K steps with host field/row arrays, host rows, P and phi download "
-                   "(state arrays page-locked, allocated once)"}
+                   "(state arrays page-locked, allocated once); median of the calls"}
+    film.close()
+
+    # the PCG paths (the metric's 'incl. PCG'): the same film with the inner
+    # solve forced to the persistent Jacobi-PCG; the film with the reference
+    # deck's three permittivities (which takes the PCG); the FP64 mode
+    # (reference PCG) on both -- the FP32-over-FP64 speed-up at equal inner
+    # algorithm next to the one the direct solve gives
+    pcg = None
+    if rank == 0 and world == 1 and not fp64 and not args.no_pcg:
+        mats3 = np.array(w.mats, copy=True)
+        mats3[:, 7] = [40.0, 30.0, 15.0]      # eps_afe, eps_fe, eps_de of src/inputs/InputParams
+        Ks = max(5, min(K, 20))
+        pcg = {"uni_eps_pcg": side_run(cg, w, False, cg.INNER_PCG, Ks, stream),
+               "three_eps": side_run(cg, w, False, None, Ks, stream, mats=mats3),
+               "fp64_uni_eps": side_run(cg, w, True, None, 3, stream),
+               "fp64_three_eps": side_run(cg, w, True, None, 3, stream, mats=mats3)}
+        pcg["speedup_fp32_over_fp64"] = {
+            "direct_inner_solve": value / pcg["fp64_uni_eps"]["value"],
+            "same_inner_pcg_uni_eps": pcg["uni_eps_pcg"]["value"] / pcg["fp64_uni_eps"]["value"],
+            "same_inner_pcg_three_eps": pcg["three_eps"]["value"] / pcg["fp64_three_eps"]["value"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -364,18 +483,28 @@ def run_ours(args):
             "config": {"workload": w.name, "cells": w.N, "grid": [w.nx, w.ny, w.nz],
                        "precision": "fp64" if fp64 else "fp32-refined (fp64 phi, refine to 1e-8)",
                        "pcg": "||b-A phi|| <= 1e-8 ||b||", "parallelism": "replicas" if world > 1 else "single",
-                       "tile": {"x": 32, "y": 8, "z_chunk": zchunk, "chosen_by": "heuristic" if args.no_autotune else "autotuner (cmsl_film_autotune)"},
-                       "l2": "no flush: per-step state %.0f MB > 129 MB L2" % (film.device_bytes() / 1e6)},
+                       "tile": {"x": 32, "y": 8, "z_chunk": zchunk,
+                                "chosen_by": "heuristic" if args.no_autotune else "autotuner (cmsl_film_autotune)"},
+                       "timing": "%d timed regions of K steps, each bracketed by barrier + synchronize and timed "
+                                 "with CUDA events on the launch stream; value from the median region" % R,
+                       "l2": "no flush: per-step state %.0f MB > 129 MB L2" % (film_bytes(w, fp64) / 1e6)},
+            "timed_regions_ms": {"median": ms, "min": min(ms_all), "max": max(ms_all), "n": len(ms_all)},
             "inner_solver": "direct (in-plane FFT + tridiagonal z, one solve per refinement pass)" if direct
             else ("pcg (Jacobi, reference algorithm)" if fp64 else "pcg (persistent single-reduction Jacobi-PCG)"),
             "pcg_iters_per_step": n_iter, "refine_passes_per_step": n_ref,
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+            "roofline": roof, "pcg_paths": pcg, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches * R,
         }
         print(json.dumps(line))
-    film.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def film_bytes(w, fp64: bool) -> int:
+    """State a step reads and writes: two P sets, the potentials, the code."""
+    s = 8 if fp64 else 4
+    return w.N * (12 * s + 5 * 8 + 4)
 
 
 def run_batch(args):
@@ -438,9 +567,12 @@ def run_batch(args):
     top = max(per_step, key=per_step.get)
     ki = names.index(top)
     peak, peak_kind = measured_peaks()
-    achieved = BYTES["fp32"][top] * cells / (kms[ki] * 1e-3) / 1e9
+    achieved = alg_bytes("fp32", top) * cells / (kms[ki] * 1e-3) / 1e9
+    b_step = step_bytes("fp32", n_it, n_ref)
     roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "bytes_per_cell": BYTES["fp32"][top],
+            "frac": achieved / peak, "peak_source": peak_kind, "bytes_per_cell": alg_bytes("fp32", top),
+            "design_bytes_per_cell": DESIGN_BYTES["fp32"].get(top), "step_bytes_per_cell": b_step,
+            "frac_step": b_step * (cells * K / (ms * 1e-3)) / 1e9 / peak,
             "traffic": None, "kernel_ms": {k: float(kms[i]) for i, k in enumerate(names)},
             "share": {k: per_step[k] / sum(per_step.values()) for k in per_step}}
 
@@ -530,6 +662,9 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="heuristic z chunk instead of the tile autotuner")
+    ap.add_argument("--repeats", type=int, default=0, help="timed regions of K steps (0: enough for ~1.5 s, >= 10)")
+    ap.add_argument("--e2e-repeats", type=int, default=5, help="end-to-end calls (the median is reported)")
+    ap.add_argument("--no-pcg", action="store_true", help="skip the PCG-path samples")
     ap.add_argument("--config", type=int, default=CONFIG_ID, choices=[0, 1, 2, 3, 4],
                     help="benchmark configuration (default 1; 3 = the 64-film batched ensemble)")
     args = ap.parse_args()

@@ -16,7 +16,9 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CUDA_SOURCES = ["engine.cu", "noalloc.cu", "adjoint.cu", "grains.cu"]
 HOST_SOURCES = ["formats.cpp"]
-HEADERS = ["cmsl_dev.cuh", "dfloat.cuh", "kernels.cuh", "pcg_persist.cuh", "spectral.cuh", "engine.h"]
+HEADERS = ["cmsl_dev.cuh", "dfloat.cuh", "kernels.cuh", "pcg_persist.cuh", "spectral.cuh", "stencil32.cuh",
+           "engine.h"]
+OBJDIR = os.path.join(HERE, "_build")
 
 
 def nvcc() -> str:
@@ -70,14 +72,29 @@ def build_cli(verbose: bool = False, force: bool = False) -> str:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
+    """Compiles every translation unit to an object in parallel (one nvcc per
+    source), then links libcmsl_gb.so."""
     srcs = [os.path.join(CSRC, s) for s in CUDA_SOURCES + HOST_SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    deps = srcs + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "cmsl.h")]
+    deps = srcs + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "cmsl.h"),
+                                                             os.path.join(ROOT, "include", "cmsl_io.h")]
     if not force and not _stale(OUT, deps):
         return OUT
+    os.makedirs(OBJDIR, exist_ok=True)
+    common = [nvcc(), ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+    objs, procs = [], []
+    for src in srcs:
+        obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+        objs.append(obj)
+        cmd = common + ["-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((cmd, subprocess.Popen(cmd)))
+    for cmd, p in procs:
+        if p.wait() != 0:
+            raise subprocess.CalledProcessError(p.returncode, cmd)
     tmp = OUT + ".tmp"
-    cmd = [nvcc(), ARCH, "-O3", "-std=c++17", "-lineinfo", "-shared", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
-           "-o", tmp] + srcs + ["-lcudart"]
+    cmd = [nvcc(), ARCH, "-shared", "-o", tmp] + objs + ["-lcudart"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.run(cmd, check=True)

@@ -15,9 +15,12 @@
 // The array exists once per device for as long as the library is loaded.
 // Its device address is looked up once per device, with that device current,
 // on the first call made on that device: make that first call before any
-// stream capture.  Every call shares the array, so calls whose GPU work
-// overlaps (different streams, different host threads on one device) race;
-// serialise them.  Each call re-initialises every part of the array it reads.
+// stream capture.  The looked-up address is kept for the life of the process
+// and does not survive cudaDeviceReset (or any other destruction of the
+// device's primary context): after one, no further call may be made.  Every
+// call shares the array, so calls whose GPU work overlaps (different streams,
+// different host threads on one device) race; serialise them.  Each call
+// re-initialises every part of the array it reads.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -114,6 +117,8 @@ extern "C" cmsl_status cmsl_depol_solve_noalloc(int nx, int ny, int nz, double d
                                                 int32_t *iters_out, int32_t *status_out)
 {
     if (nx < 1 || ny < 1 || nz < 3) return na_fail(CMSL_ERR_ARG, "grid: need nx, ny >= 1 and nz >= 3");
+    // work items pack z0 and z1 into 16-bit fields (the film API's limit too)
+    if (nx > 32767 || ny > 32767 || nz > 32767) return na_fail(CMSL_ERR_ARG, "grid: each side must be <= 32767");
     const long long N = (long long)nx * ny * nz;
     if (N > NA_MAX_CELLS) return na_fail(CMSL_ERR_ARG, "grid larger than the 131072-cell scratch of the no-alloc solve");
     if (!material_dev || !eps_r || !Pmx_dev || !Pmy_dev || !Pmz_dev || !phi_dev)
@@ -196,14 +201,13 @@ extern "C" cmsl_status cmsl_depol_solve_noalloc(int nx, int ny, int nz, double d
     SolveDev S{};
     int bad = 0;
     for (int guard = 0;; ++guard) {
+        // the material check is read on the caller's stream with the first state read
+        if (guard == 0 && (e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return na_fail(CMSL_ERR_CUDA, "reading the material check failed", e);
         if ((e = cudaMemcpyAsync(&S, d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess)
             return na_fail(CMSL_ERR_CUDA, "reading the solver state failed", e);
-        if (guard == 0) {
-            if ((e = cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
-                return na_fail(CMSL_ERR_CUDA, "reading the material check failed", e);
-            if (bad) return na_fail(CMSL_ERR_ARG, "material ids must be 0 (AFE), 1 (FE) or 2 (DE)");
-        }
+        if (guard == 0 && bad) return na_fail(CMSL_ERR_ARG, "material ids must be 0 (AFE), 1 (FE) or 2 (DE)");
         if (!S.active) break;
         if (guard > max_iter + 1) return na_fail(CMSL_ERR_STATE, "PCG loop did not stop");
         k_spmv<double, Exact><<<nit, NT, 0, s>>>(d, F);

@@ -273,13 +273,15 @@ cmsl_status cmsl_film_loop_gradient(cmsl_film *film, int n_steps, const double *
  * buffers).  It runs the FP64 Jacobi-PCG of cmsl_film_depol -- the same
  * kernels and stop test -- with every work buffer in one fixed device array
  * of about 6.3 MB that stays resident on each GPU that loads the library.
- *   - grids up to 131072 cells (nx*ny*nz; nz >= 3); larger grids return
- *     CMSL_ERR_ARG and do nothing;
+ *   - grids up to 131072 cells (nx*ny*nz; nz >= 3) and up to 32767 cells
+ *     along each side; other grids return CMSL_ERR_ARG and do nothing;
  *   - inputs and outputs are device pointers: material id per cell (0 AFE,
  *     1 FE, 2 DE), eps_r per material (host), the new Pm components, and phi
  *     (warm start in, solution out, in place);
  *   - the first call on a device looks up the array's device address with
- *     that device current; make it before any stream capture;
+ *     that device current; make it before any stream capture; the address
+ *     is kept for the life of the process and does not survive
+ *     cudaDeviceReset (no call may follow one);
  *   - all calls share the array: calls whose GPU work overlaps race, so
  *     serialise them; each call clears the state it reads;
  *   - returns after the solve (it reads the loop flags on `stream`). */

@@ -11,5 +11,5 @@ the reference sources are available and is used to pin the restatement.
 """
 from .oracle import (  # noqa: F401
     Film, OracleLib, RefLib, load, load_ref, build, build_ref, MAT_AFE, MAT_FE, MAT_DE,
-    DIRICHLET, NEUMANN, CRIT_REF, CRIT_RELRES,
+    DIRICHLET, NEUMANN, CRIT_REF, CRIT_RELRES, reference_root,
 )

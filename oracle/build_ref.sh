@@ -13,10 +13,10 @@
 # oracle/_ref/ because the rest of those files needs a GPU runtime (cuBLAS,
 # cuRAND, kernel launches) or does not compile as shipped (main.cu:483).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default $CMSL_REFERENCE_ROOT, else /root/reference)
 set -eu
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-/root/reference}
+REF=${1:-${CMSL_REFERENCE_ROOT:-/root/reference}}
 SRC="$REF/HZO_Code_github/src"
 INC="$REF/HZO_Code_github/include"
 OUT="$HERE/_ref"

@@ -114,15 +114,30 @@ class Film:
         return s
 
 
+# Where the reference sources lie: $CMSL_REFERENCE_ROOT, else the checkout
+# this build was made against when it exists; None where neither does (the
+# GPU machine), and everything that needs the sources skips.
+_DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root() -> str | None:
+    """The reference checkout (the directory holding HZO_Code_github), or None."""
+    for r in (os.environ.get("CMSL_REFERENCE_ROOT"), _DEFAULT_REFERENCE_ROOT):
+        if r and os.path.isdir(os.path.join(r, "HZO_Code_github", "src")):
+            return r
+    return None
+
+
 def build() -> str:
     """Builds liboracle.so with the committed Makefile; returns its path."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     return os.path.join(HERE, "liboracle.so")
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
+def build_ref(reference_root: str | None = None) -> str | None:
     """Builds _ref/libcmsl_ref.so from the reference sources when present."""
-    if not os.path.isdir(os.path.join(reference_root, "HZO_Code_github", "src")):
+    reference_root = reference_root or reference_root_or_none()
+    if not reference_root or not os.path.isdir(os.path.join(reference_root, "HZO_Code_github", "src")):
         return None
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), reference_root], check=True,
                    stdout=subprocess.DEVNULL)
@@ -480,7 +495,11 @@ def load(rebuild: bool = False) -> OracleLib:
     return _cache[path]
 
 
-def load_ref(reference_root: str = "/root/reference") -> RefLib | None:
+def reference_root_or_none() -> str | None:
+    return reference_root()
+
+
+def load_ref(reference_root: str | None = None) -> RefLib | None:
     path = os.path.join(HERE, "_ref", "libcmsl_ref.so")
     if not os.path.exists(path):
         if build_ref(reference_root) is None:

@@ -109,3 +109,25 @@ def test_state_out_arrays_checked_without_gpu():
     L = _lib.lib()
     assert L.cmsl_host_alloc(16, None) == 1
     assert L.cmsl_host_free(None) == 0
+
+
+def test_noalloc_argument_checks_without_gpu():
+    """The allocation-free solve rejects grids it cannot tile before any CUDA
+    call: a side above 32767 (the work items pack z ranges into 16 bits),
+    more than 131072 cells, or nz < 3."""
+    import ctypes as C
+    import numpy as np
+    from cmsl_gb300 import _lib
+    L = _lib.lib()
+    eps = (C.c_double * 3)(30.0, 30.0, 30.0)
+    it = np.zeros(1, np.int32)
+    st = np.zeros(1, np.int32)
+    buf = np.zeros(8)
+    p = C.c_void_p(buf.ctypes.data)
+    ip = it.ctypes.data_as(C.POINTER(C.c_int32))
+    sp = st.ctypes.data_as(C.POINTER(C.c_int32))
+    for (nx, ny, nz), msg in (((1, 1, 70000), b"32767"), ((70000, 1, 3), b"32767"), ((1, 40000, 3), b"32767"),
+                              ((128, 128, 16), b"131072"), ((4, 4, 2), b"nz >= 3")):
+        rc = L.cmsl_depol_solve_noalloc(nx, ny, nz, 0.5, 0, 1.0, p, eps, p, p, p, p, 1e-3, 1e-2, 10, 0, None, ip, sp)
+        assert rc == 1, (nx, ny, nz)
+        assert msg in L.cmsl_last_error(), (nx, ny, nz, L.cmsl_last_error())

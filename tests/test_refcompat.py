@@ -33,9 +33,11 @@ def compat():
 
 
 def test_reference_program_links_against_compat_layer(compat, tmp_path):
-    if not os.path.isdir("/root/reference/HZO_Code_github/src"):
+    import oracle
+    rr = oracle.reference_root()
+    if rr is None:
         pytest.skip("reference sources not available")
-    r = subprocess.run(["sh", os.path.join(HERE, "refcompat", "link_reference.sh"), "/root/reference", ROOT,
+    r = subprocess.run(["sh", os.path.join(HERE, "refcompat", "link_reference.sh"), rr, ROOT,
                         str(tmp_path)], capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     assert os.path.exists(tmp_path / "Pfmhzo_gb")

@@ -49,12 +49,15 @@ def _noalloc(torch, _lib, f, Pm, phi_dev, tol_abs, tol_rel):
     return int(it[0]), int(st[0])
 
 
+# (40, 17, 9): two x tiles (one partial) and partial y tiles; (20, 5, 4): one
+# partial tile; (64, 64, 32): the scratch array full (131072 cells).
+@pytest.mark.parametrize("shape", [(40, 17, 9), (20, 5, 4), (64, 64, 32)])
 @pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
-def test_noalloc_matches_film_depol_twice(setup, zbc):
+def test_noalloc_matches_film_depol_twice(setup, zbc, shape):
     torch, cg, _lib = setup
-    f, P1 = random_film(40, 17, 9, seed=51, zbc=zbc, eps_0_nd=3.0)
+    f, P1 = random_film(*shape, seed=51, zbc=zbc, eps_0_nd=3.0)
     f.tol_abs, f.tol_rel = 1e-10, 1e-8
-    _, P2 = random_film(40, 17, 9, seed=52, zbc=zbc, eps_0_nd=3.0)
+    _, P2 = random_film(*shape, seed=52, zbc=zbc, eps_0_nd=3.0)
     phi0 = np.zeros(f.N)
     # existing entry point: two solves in a row, the second warm-started
     with cg.Film.from_oracle_film(f) as g:
@@ -87,3 +90,34 @@ def test_noalloc_rejects_oversize_grid(setup):
         it.ctypes.data_as(C.POINTER(C.c_int32)), st.ctypes.data_as(C.POINTER(C.c_int32)))
     assert rc == 1
     assert b"131072" in _lib.lib().cmsl_last_error()
+
+
+@pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
+def test_noalloc_matches_oracle(setup, zbc):
+    """One solve against the oracle's restatement of Depol_field
+    (depol_varEPS.cu:332-595) directly: same potential to the PCG's
+    dot-product summation order, iteration count within one."""
+    torch, cg, _lib = setup
+    f, P = random_film(40, 17, 9, seed=53, zbc=zbc, eps_0_nd=3.0)
+    f.tol_abs, f.tol_rel = 1e-10, 1e-8
+    phi0 = np.random.default_rng(4).normal(size=f.N) * 0.01
+    want, _, _, info = oracle.load().depol_field(f, P[:3], phi0)
+    phi = torch.as_tensor(phi0.copy(), device="cuda")
+    it, st = _noalloc(torch, _lib, f, P[:3], phi, f.tol_abs, f.tol_rel)
+    got = phi.cpu().numpy()
+    assert st == 0 and info["status"] == 0
+    assert abs(it - info["iters"]) <= 1
+    assert np.abs(got - want).max() <= 1e-10 * np.abs(want).max()
+
+
+def test_noalloc_rejects_bad_material(setup):
+    """A material id outside 0..2 is reported as an argument error (the
+    solve's material check is read on the caller's stream)."""
+    torch, cg, _lib = setup
+    f, P = random_film(20, 5, 4, seed=54)
+    f.grain_mat = np.asarray(f.grain_mat).copy()
+    f.grain_mat[int(np.asarray(f.omega)[0])] = 3      # the grain of cell 0
+    phi = torch.zeros(f.N, dtype=torch.float64, device="cuda")
+    with pytest.raises(cg.CmslError) as e:
+        _noalloc(torch, _lib, f, P[:3], phi, 1e-10, 1e-8)
+    assert e.value.status == 1 and "material" in str(e.value)
