@@ -97,6 +97,8 @@ def lib() -> C.CDLL:
     L.cmsl_batch_autotune.argtypes = [fp, C.POINTER(C.c_int32)]
     L.cmsl_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.cmsl_host_free.argtypes = [C.c_void_p]
+    L.cmsl_film_depol_device.argtypes = [fp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, _ip, _ip]
     L.cmsl_depol_solve_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double,
                                            C.c_void_p, _dp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, _ip, _ip]
@@ -114,7 +116,8 @@ EXPORTS = [
     "cmsl_last_error", "cmsl_version", "cmsl_film_create", "cmsl_film_destroy", "cmsl_film_set_state",
     "cmsl_film_get_state", "cmsl_host_alloc", "cmsl_host_free", "cmsl_film_run", "cmsl_film_sync",
     "cmsl_film_get_rows", "cmsl_film_get_iters",
-    "cmsl_film_tdgl_step", "cmsl_film_depol", "cmsl_film_apply_operator", "cmsl_film_efield",
+    "cmsl_film_tdgl_step", "cmsl_film_depol", "cmsl_film_depol_device", "cmsl_film_apply_operator",
+    "cmsl_film_efield",
     "cmsl_film_diag_inv", "cmsl_film_time_kernels", "cmsl_film_device_bytes", "cmsl_film_inner_solver", "cmsl_film_autotune",
     "cmsl_film_checkpoint_write",
     "cmsl_film_checkpoint_read", "cmsl_film_loop_gradient",

@@ -46,7 +46,8 @@ def build_refcompat(verbose: bool = False, force: bool = False) -> str:
     deps = [src, os.path.join(ROOT, "include", "cmsl.h"), os.path.join(ROOT, "include", "cmsl_io.h")]
     if not force and not _stale(REFCOMPAT, deps):
         return REFCOMPAT
-    cmd = [nvcc(), ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"),
+    cmd = [nvcc(), ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+           "-I" + os.path.join(ROOT, "include"),
            "-c", src, "-o", REFCOMPAT + ".tmp"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

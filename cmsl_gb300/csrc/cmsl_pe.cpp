@@ -175,10 +175,10 @@ int main(int argc, char **argv)
                                  nullptr, &ns, nullptr, nullptr, &nr) != CMSL_OK)
             return die(cmsl_last_error());
         const int pre = deck.do_pre_relax ? 15000 : 0;                          // evolve.cu:171-211
-        std::vector<double> Ez(pre + ns, 0.0), rowE(nr);
-        std::vector<int32_t> row(pre + ns, -1), rowc(nr);
-        cmsl_evolve_schedule(sc.maxEz, sc.delEz, deck.num_steps, 1, single, sc.E0_ref, 100000000, Ez.data() + pre,
-                             row.data() + pre, &ns, rowE.data(), rowc.data(), &nr);
+        std::vector<double> Ez(ns, 0.0), rowE(nr);
+        std::vector<int32_t> row(ns, -1), rowc(nr);
+        cmsl_evolve_schedule(sc.maxEz, sc.delEz, deck.num_steps, 1, single, sc.E0_ref, 100000000, Ez.data(),
+                             row.data(), &ns, rowE.data(), rowc.data(), &nr);
 
         cmsl_film_desc d = {};
         d.nx = nx; d.ny = ny; d.nz = nz; d.del_h = deck.del_h; d.del_t = deck.del_t;
@@ -192,6 +192,24 @@ int main(int argc, char **argv)
         if (cmsl_film_create(&d, &film) != CMSL_OK) return die(cmsl_last_error());
         const double *Pp[6] = {P[0].data(), P[1].data(), P[2].data(), P[3].data(), P[4].data(), P[5].data()};
         cmsl_status st = cmsl_film_set_state(film, Pp, nullptr);
+        if (st == CMSL_OK && pre > 0) {
+            // stage A: pre-relax at E = 0, then the two midplane slices of
+            // evolve.cu:202-210 (Psz of the relaxed state; Psz in the crystal
+            // frame of the state the last pre-relax step started from)
+            std::vector<double> Ez0((size_t)pre, 0.0), S[6], phi((size_t)N), loc((size_t)N);
+            std::vector<int32_t> r0((size_t)pre, -1);
+            double *Sp[6];
+            for (int q = 0; q < 6; ++q) { S[q].resize((size_t)N); Sp[q] = S[q].data(); }
+            if (pre > 1) st = cmsl_film_run(film, pre - 1, Ez0.data(), r0.data(), nullptr);
+            if (st == CMSL_OK) st = cmsl_film_sync(film);
+            if (st == CMSL_OK) st = cmsl_film_get_state(film, Sp, phi.data());
+            if (st == CMSL_OK) st = cmsl_crystal_z(N, omega.data(), TR.data(), Sp[3], Sp[4], Sp[5], loc.data());
+            if (st == CMSL_OK) st = cmsl_film_run(film, 1, Ez0.data(), r0.data(), nullptr);
+            if (st == CMSL_OK) st = cmsl_film_sync(film);
+            if (st == CMSL_OK) st = cmsl_film_get_state(film, Sp, phi.data());
+            if (st == CMSL_OK) st = cmsl_midplane_slice_write("slice_E0_midplane.dat", Sp[5], nx, ny, nz);
+            if (st == CMSL_OK) st = cmsl_midplane_slice_write("slice_E0_midplane_local.dat", loc.data(), nx, ny, nz);
+        }
         if (st == CMSL_OK) st = cmsl_film_run(film, (int)Ez.size(), Ez.data(), row.data(), nullptr);
         if (st == CMSL_OK) st = cmsl_film_sync(film);
         std::vector<double> rows((size_t)nr * CMSL_ROW_WIDTH);
@@ -215,7 +233,8 @@ int main(int argc, char **argv)
                          rowc[r] + pre);
         }
         std::fclose(fo);
-        std::printf("simulation %d: %d steps, %d rows -> %s\n", sim_index, (int)Ez.size(), nr, (outdir + name).c_str());
+        std::printf("simulation %d: %d steps, %d rows -> %s\n", sim_index, pre + (int)Ez.size(), nr,
+                    (outdir + name).c_str());
     }
     return 0;
 }

@@ -1545,6 +1545,85 @@ cmsl_status cmsl_film_depol(cmsl_film *f, int32_t *iters, int32_t *status)
     return CMSL_OK;
 }
 
+// Depol_field over caller device arrays: Pm in, phi (warm start in,
+// solution out) and E out, converted by kernels on `stream`; nothing passes
+// through the host and nothing is allocated.
+cmsl_status cmsl_film_depol_device(cmsl_film *f, const double *Pmx, const double *Pmy, const double *Pmz,
+                                   double *phi, double *Ex, double *Ey, double *Ez, void *stream, int32_t *iters,
+                                   int32_t *status)
+{
+    if (!f || !Pmx || !Pmy || !Pmz || !phi) return fail(CMSL_ERR_ARG, "NULL argument");
+    if (f->n_films != 1) return fail(CMSL_ERR_ARG, "depol_device: single films only");
+    if (!f->any_dep) return fail(CMSL_ERR_STATE, "depol_device: the film has no depolarisation solve");
+    cudaStream_t st = (cudaStream_t)stream;
+    const FilmHost &h = f->fh[0];
+    Ctl c;
+    SolveDev S;
+    CK(cudaMemcpyAsync(&c, f->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double *src[3] = {Pmx, Pmy, Pmz};
+    for (int q = 0; q < 3; ++q) {
+        if (f->precision == CMSL_FP64)
+            k_host_in<double><<<XFER_GRID, XFER_NT, 0, st>>>(src[q], (double *)f->d_P[c.cur][q] + h.off, h.N);
+        else
+            k_host_in<float><<<XFER_GRID, XFER_NT, 0, st>>>(src[q], (float *)f->d_P[c.cur][q] + h.off, h.N);
+    }
+    // the warm start: every potential buffer holds phi (no extrapolation)
+    if (f->precision == CMSL_FP64) {
+        for (int q = 0; q < 2; ++q)
+            CK(cudaMemcpyAsync(f->d_phi[q] + h.off, phi, sizeof(double) * h.N, cudaMemcpyDeviceToDevice, st));
+    } else {
+        float *b0 = (float *)f->d_phi[0];
+        k_phi_in<<<XFER_GRID, XFER_NT, 0, st>>>(phi, b0 + h.off, b0 + f->ncells + h.off, h.N);
+        for (int q = 1; q < 4; ++q) {
+            float *b = (float *)f->d_phi[q];
+            CK(cudaMemcpyAsync(b + h.off, b0 + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(b + f->ncells + h.off, b0 + f->ncells + h.off, sizeof(float) * h.N,
+                               cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    CK(cudaGetLastError());
+    S = SolveDev{};
+    S.phi_cur = 0;
+    S.phi_prev = f->precision == CMSL_FP64 ? 0 : 1;
+    S.phi_prev2 = f->precision == CMSL_FP64 ? 0 : 2;
+    S.phi_prev3 = f->precision == CMSL_FP64 ? 0 : 3;
+    S.outer_active = 1;
+    CK(cudaMemcpyAsync(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice, st));
+    // the solve kernels read the new Pm from set cur^1: point it at set cur
+    Fields<double> F64 = f->fields<double>();
+    Fields<float> F32 = f->fields<float>();
+    for (int q = 0; q < 6; ++q) {
+        F64.P[c.cur ^ 1][q] = F64.P[c.cur][q];
+        F32.P[c.cur ^ 1][q] = F32.P[c.cur][q];
+    }
+    const Dev d = f->dev(0);
+    const unsigned nit = (unsigned)f->items.size();
+    if (f->precision != CMSL_FP64) {
+        k_extrap<<<nit, NT, 0, st>>>(d);
+        CK(cudaGetLastError());
+    }
+    TRY(solve_direct(f, st, d, F64, F32));
+    CK(cudaMemcpyAsync(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (f->precision == CMSL_FP64) {
+        CK(cudaMemcpyAsync(phi, f->d_phi[S.phi_cur] + h.off, sizeof(double) * h.N, cudaMemcpyDeviceToDevice, st));
+    } else {
+        const float *b = (const float *)f->d_phi[S.phi_cur];
+        k_phi_out<<<XFER_GRID, XFER_NT, 0, st>>>(b + h.off, b + f->ncells + h.off, phi, h.N);
+    }
+    if (Ex && Ey && Ez) {
+        if (f->precision == CMSL_FP64) k_efield<<<nit, NT, 0, st>>>(d, Ex - h.off, Ey - h.off, Ez - h.off);
+        else k_efield_df<<<nit, NT, 0, st>>>(d, Ex - h.off, Ey - h.off, Ez - h.off);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    if (iters) { iters[0] = S.total_iters; iters[1] = f->precision != CMSL_FP64 ? S.refine : 0; }
+    if (status) *status = S.status;
+    return CMSL_OK;
+}
+
 cmsl_status cmsl_film_apply_operator(cmsl_film *f, const double *x, double *y)
 {
     if (!f || !x || !y) return fail(CMSL_ERR_ARG, "NULL argument");
@@ -1572,13 +1651,13 @@ cmsl_status cmsl_film_apply_operator(cmsl_film *f, const double *x, double *y)
 cmsl_status cmsl_film_efield(cmsl_film *f, double *Ex, double *Ey, double *Ez)
 {
     if (!f || !Ex || !Ey || !Ez) return fail(CMSL_ERR_ARG, "NULL argument");
-    if (f->precision != CMSL_FP64) return fail(CMSL_ERR_STATE, "efield: FP64 films only");
     CK(cudaDeviceSynchronize());
     const long long N = f->fh[0].N;   // the film's cells (the buffers are padded beyond)
     double *e = nullptr;
     CK(cudaMalloc(&e, sizeof(double) * 3 * N));
     const Dev d = f->dev(0);
-    k_efield<<<(int)f->items.size(), NT>>>(d, e, e + N, e + 2 * N);
+    if (f->precision == CMSL_FP64) k_efield<<<(int)f->items.size(), NT>>>(d, e, e + N, e + 2 * N);
+    else k_efield_df<<<(int)f->items.size(), NT>>>(d, e, e + N, e + 2 * N);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaMemcpy(Ex, e, sizeof(double) * N, cudaMemcpyDeviceToHost);
     if (err == cudaSuccess) err = cudaMemcpy(Ey, e + N, sizeof(double) * N, cudaMemcpyDeviceToHost);

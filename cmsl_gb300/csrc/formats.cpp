@@ -394,6 +394,34 @@ cmsl_status cmsl_vector_field_write(const char *path, const double *Px, const do
     return CMSL_OK;
 }
 
+// write_midplane_slice (generate.cu:67-88): "i j value" lines of the plane
+// k = nz/2, rows j in order, a blank line after each.
+cmsl_status cmsl_midplane_slice_write(const char *path, const double *v, int nx, int ny, int nz)
+{
+    if (!path || !v || nx < 1 || ny < 1 || nz < 1) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    File f(std::fopen(path, "w"));
+    if (!f) return io_fail(CMSL_ERR_IO, std::string("cannot write ") + path);
+    const long long base = (long long)nx * ny * (nz / 2);
+    for (int j = 0; j < ny; ++j) {
+        for (int i = 0; i < nx; ++i) std::fprintf(f.get(), "%d %d %.16e\n", i, j, v[base + i + (long long)nx * j]);
+        std::fprintf(f.get(), "\n");
+    }
+    return std::ferror(f.get()) ? io_fail(CMSL_ERR_IO, std::string("short write ") + path) : CMSL_OK;
+}
+
+// The crystal-frame z component (row 3 of the grain's rotation applied to
+// the lab vector), in the order of kernels_evol.cu:162-167.
+cmsl_status cmsl_crystal_z(long long n, const int32_t *omega, const double *TR, const double *x, const double *y,
+                           const double *z, double *out)
+{
+    if (n < 0 || !omega || !TR || !x || !y || !z || !out) return io_fail(CMSL_ERR_ARG, "bad arguments");
+    for (long long i = 0; i < n; ++i) {
+        const double *t = TR + 9LL * omega[i];
+        out[i] = t[6] * x[i] + t[7] * y[i] + t[8] * z[i];
+    }
+    return CMSL_OK;
+}
+
 // Calc_EfieldMag (depol_varEPS.cu:223-276) on the host: E = -grad(phi), x/y
 // periodic; Dirichlet z with phi = 0 beyond the planes, or the mirrored
 // Neumann neighbours.

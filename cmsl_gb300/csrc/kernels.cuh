@@ -1141,4 +1141,40 @@ static __global__ void k_efield(Dev d, double *Ex, double *Ey, double *Ez)
     }
 }
 
+// E = -grad(phi) of the double-float potential of CMSL_FP32_REFINED films
+// (hi half at the cell, lo half ncells further on): each value is formed as
+// hi + lo in FP64, then differenced as in k_efield.
+static __global__ void k_efield_df(Dev d, double *Ex, double *Ey, double *Ez)
+{
+    const int4 it = d.items[blockIdx.x];
+    const FilmDev *f = d.films + it.x;
+    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
+    const Geom g = make_geom(f, it.y, it.z);
+    if (!g.valid) return;
+    const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+    const int i = g.x0 + lx, j = g.y0 + ly, nx = g.nx, ny = g.ny, nz = g.nz;
+    const float *hi = (const float *)phi_sel(d, d.solve[it.x].phi_cur) + f->off;
+    const float *lo = hi + d.ncells;
+    Ex += f->off; Ey += f->off; Ez += f->off;
+    const double two_h = f->two_h;
+    auto id = [&](int a, int b, int c) { return a + (long long)nx * (b + (long long)ny * c); };
+    auto phi = [&](long long c) { return (double)hi[c] + (double)lo[c]; };
+    for (int k = z0; k < z1; ++k) {
+        const long long o = g.own_pl + (long long)k * g.plane;
+        Ex[o] = __ddiv_rn(-__dsub_rn(phi(id((i + 1) % nx, j, k)), phi(id((i - 1 + nx) % nx, j, k))), two_h);
+        Ey[o] = __ddiv_rn(-__dsub_rn(phi(id(i, (j + 1) % ny, k)), phi(id(i, (j - 1 + ny) % ny, k))), two_h);
+        double pu, pd;
+        if (f->zbc == 0) {
+            pu = (k == nz - 1) ? 0.0 : phi(id(i, j, k + 1));
+            pd = (k == 0) ? 0.0 : phi(id(i, j, k - 1));
+        } else {
+            const int up = (k == 0) ? 1 : (k == nz - 1 ? nz - 2 : k + 1);
+            const int dn = (k == 0) ? 1 : (k == nz - 1 ? nz - 2 : k - 1);
+            pu = phi(id(i, j, up));
+            pd = phi(id(i, j, dn));
+        }
+        Ez[o] = __ddiv_rn(-__dsub_rn(pu, pd), two_h);
+    }
+}
+
 }  // namespace cmsl

@@ -11,6 +11,7 @@
 // (include/globals.h, include/cuda_deps.h, include/types.h); the definitions
 // come from the reference's global.cu.  The precision is FP64 (bit-identical
 // TDGL) unless CMSL_PRECISION=fp32 selects FP32_REFINED.
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -136,13 +137,73 @@ void store_state(cmsl_film *f)
     }
 }
 
+// The film Depol_field solves on, kept between calls: it is rebuilt only
+// when the grid, the materials, the grain map or the rotations change (a
+// content hash of the host arrays, far cheaper than rebuilding the film).
+struct DepolCache {
+    cmsl_film *f = nullptr;
+    std::vector<int32_t> gm;
+    uint64_t key = 0;
+} g_depol;
+
+uint64_t mix(uint64_t h, uint64_t v)
+{
+    h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+    return h;
+}
+
+uint64_t hash_words(uint64_t h, const void *p, size_t bytes)
+{
+    const unsigned char *b = (const unsigned char *)p;
+    size_t i = 0;
+    for (; i + 8 <= bytes; i += 8) {
+        uint64_t v;
+        std::memcpy(&v, b + i, 8);
+        h = mix(h, v);
+    }
+    for (; i < bytes; ++i) h = mix(h, b[i]);
+    return h;
+}
+
+uint64_t depol_key()
+{
+    const size_t N = (size_t)nx * ny * nz;
+    uint64_t h = mix(mix(mix(0x1234, (uint64_t)nx), (uint64_t)ny), (uint64_t)nz);
+    h = mix(mix(mix(h, (uint64_t)ng_total), (uint64_t)dep_flag), (uint64_t)zbc_flag);
+    const double sc[3] = {del_h, del_t, eps_0_nd};
+    h = hash_words(h, sc, sizeof sc);
+    const MaterialNorm *m[3] = {&N_AFE, &N_FE, &N_DE};
+    for (const MaterialNorm *q : m) h = hash_words(h, q, sizeof(MaterialNorm));
+    const char *p = std::getenv("CMSL_PRECISION");
+    h = mix(h, (p && std::string(p) == "fp32") ? 1u : 0u);
+    if (omega) h = hash_words(h, omega, N * sizeof(int));
+    if (grain_mat) h = hash_words(h, grain_mat, (size_t)ng_total * sizeof(int));
+    if (TR_h) h = hash_words(h, TR_h, (size_t)ng_total * 9 * sizeof(double));
+    return h;
+}
+
+cmsl_film *depol_film()
+{
+    const uint64_t key = depol_key();
+    if (!g_depol.f || g_depol.key != key) {
+        if (g_depol.f) cmsl_film_destroy(g_depol.f);
+        g_depol.f = make_film(g_depol.gm);
+        g_depol.key = key;
+    }
+    return g_depol.f;
+}
+
 }  // namespace
 
 void evolve_resources_init(void) {}
 
-// evolve.cu:67-71: frees the host P buffers
+// evolve.cu:67-71: frees the host P buffers (and the film Depol_field keeps)
 void evolve_resources_cleanup(void)
 {
+    if (g_depol.f) {
+        cmsl_film_destroy(g_depol.f);
+        g_depol.f = nullptr;
+    }
     double **h[6] = {&Pmx, &Pmy, &Pmz, &Psx, &Psy, &Psz};
     for (double **p : h) {
         std::free(*p);
@@ -150,18 +211,48 @@ void evolve_resources_cleanup(void)
     }
 }
 
-// depol_varEPS.cu:332-595: one solve on the new Pm, warm-started from phi_dep_d.
+// depol_varEPS.cu:332-595: one solve on the new Pm (Pmx/Pmy/Pmz_d),
+// warm-started from phi_dep_d (allocated and zeroed on first use, as
+// init_phi_linear with g_bot = g_top = 0), writing phi_dep_d and
+// delecX/Y/Z_d in place on the device.  The film is kept between calls.
 void Depol_field(void)
 {
-    std::vector<int32_t> gm;
-    cmsl_film *f = make_film(gm);
-    double *news[6] = {Pmx_d, Pmy_d, Pmz_d, Psx_d, Psy_d, Psz_d};
-    load_state(f, news, true);
+    if (!dep_flag) return;
+    const size_t N = (size_t)nx * ny * nz;
+    if (!phi_dep_initialized || !phi_dep_d) {
+        if (!phi_dep_d) cuda_or_die(cudaMalloc(&phi_dep_d, N * sizeof(double)), "phi alloc");
+        cuda_or_die(cudaMemset(phi_dep_d, 0, N * sizeof(double)), "phi init");
+        phi_dep_initialized = true;
+    }
+    cmsl_film *f = depol_film();
     int32_t it[2] = {0, 0}, st = 0;
-    if (cmsl_film_depol(f, it, &st) != CMSL_OK) die("cmsl_film_depol");
+    if (cmsl_film_depol_device(f, Pmx_d, Pmy_d, Pmz_d, phi_dep_d, delecX_d, delecY_d, delecZ_d, nullptr, it, &st) !=
+        CMSL_OK)
+        die("cmsl_film_depol_device");
     if (st != 0 && st != 3) std::printf("PCG breakdown (status %d)\n", st);
-    store_state(f);
-    cmsl_film_destroy(f);
+}
+
+// The two slice files of the pre-relax stage (evolve.cu:202-210): Psz of
+// the relaxed state, and Psz in the crystal frame of the state the last
+// pre-relax step started from (the kernel's Psz_local output).
+void pre_relax_slices(cmsl_film *f, int pre)
+{
+    const size_t N = (size_t)nx * ny * nz;
+    std::vector<double> P[6], phi(N), loc(N);
+    double *Pp[6];
+    for (int q = 0; q < 6; ++q) { P[q].resize(N); Pp[q] = P[q].data(); }
+    std::vector<double> Ez0((size_t)pre, 0.0);
+    std::vector<int32_t> r0((size_t)pre, -1);
+    if (pre > 1 && cmsl_film_run(f, pre - 1, Ez0.data(), r0.data(), nullptr) != CMSL_OK) die("cmsl_film_run");
+    if (cmsl_film_sync(f) != CMSL_OK) std::printf("PCG ERROR reported during the pre-relax: %s\n", cmsl_last_error());
+    if (cmsl_film_get_state(f, Pp, phi.data()) != CMSL_OK) die("cmsl_film_get_state");
+    if (cmsl_crystal_z((long long)N, omega, TR_h, Pp[3], Pp[4], Pp[5], loc.data()) != CMSL_OK) die("cmsl_crystal_z");
+    if (cmsl_film_run(f, 1, Ez0.data(), r0.data(), nullptr) != CMSL_OK) die("cmsl_film_run");
+    if (cmsl_film_sync(f) != CMSL_OK) std::printf("PCG ERROR reported during the pre-relax: %s\n", cmsl_last_error());
+    if (cmsl_film_get_state(f, Pp, phi.data()) != CMSL_OK) die("cmsl_film_get_state");
+    if (cmsl_midplane_slice_write("slice_E0_midplane.dat", Pp[5], nx, ny, nz) != CMSL_OK ||
+        cmsl_midplane_slice_write("slice_E0_midplane_local.dat", loc.data(), nx, ny, nz) != CMSL_OK)
+        std::fprintf(stderr, "Cannot write the midplane slices: %s\n", cmsl_last_error());
 }
 
 // evolve.cu:73-440: the P-E loop with the sweep file output.
@@ -179,15 +270,16 @@ void Evolve(void)
                              nullptr, nullptr, &nr) != CMSL_OK)
         die("cmsl_evolve_schedule");
     const int pre = do_pre_relax ? 15000 : 0;                             // evolve.cu:171-211
-    std::vector<double> Ez(pre + ns, 0.0), rowE(nr);
-    std::vector<int32_t> row(pre + ns, -1), rowc(nr);
-    cmsl_evolve_schedule(maxEz, delEz, time_to_change, 1, single, E0_ref, 100000000, Ez.data() + pre,
-                         row.data() + pre, &ns, rowE.data(), rowc.data(), &nr);
+    std::vector<double> Ez(ns, 0.0), rowE(nr);
+    std::vector<int32_t> row(ns, -1), rowc(nr);
+    cmsl_evolve_schedule(maxEz, delEz, time_to_change, 1, single, E0_ref, 100000000, Ez.data(), row.data(), &ns,
+                         rowE.data(), rowc.data(), &nr);
 
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, 0);
+    if (pre > 0) pre_relax_slices(f, pre);                                // stage A at E = 0
     if (cmsl_film_run(f, (int)Ez.size(), Ez.data(), row.data(), nullptr) != CMSL_OK) die("cmsl_film_run");
     if (cmsl_film_sync(f) != CMSL_OK) std::printf("PCG ERROR reported during the loop: %s\n", cmsl_last_error());
     cudaEventRecord(b, 0);

@@ -80,6 +80,8 @@ def _bind():
                                                                       _dp, _dp, C.POINTER(_dp), C.POINTER(_dp)]
     L.cmsl_vector_field_write.argtypes = [C.c_char_p, _dp, _dp, _dp, C.c_longlong, C.c_double]
     L.cmsl_efield_host.argtypes = [C.c_int] * 3 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp]
+    L.cmsl_midplane_slice_write.argtypes = [C.c_char_p, _dp, C.c_int, C.c_int, C.c_int]
+    L.cmsl_crystal_z.argtypes = [C.c_longlong, _ip, _dp, _dp, _dp, _dp, _dp]
     _bound = True
     return L
 
@@ -267,3 +269,21 @@ def efield(nx, ny, nz, del_h, zbc, phi):
     E = [np.zeros(phi.size) for _ in range(3)]
     check(L.cmsl_efield_host(nx, ny, nz, float(del_h), int(zbc), _d(phi), _d(E[0]), _d(E[1]), _d(E[2])))
     return E
+
+
+def write_midplane_slice(path: str, v, nx, ny, nz) -> None:
+    """write_midplane_slice (generate.cu:67-88): plane nz/2 as "i j value" lines."""
+    L = _bind()
+    v = np.ascontiguousarray(v, np.float64)
+    check(L.cmsl_midplane_slice_write(path.encode(), _d(v), int(nx), int(ny), int(nz)))
+
+
+def crystal_z(omega, TR, x, y, z):
+    """Crystal-frame z component per cell (kernelCalc_antiferro's *_local)."""
+    L = _bind()
+    om = np.ascontiguousarray(omega, np.int32)
+    tr = np.ascontiguousarray(TR, np.float64)
+    a = [np.ascontiguousarray(v, np.float64) for v in (x, y, z)]
+    out = np.zeros(om.size)
+    check(L.cmsl_crystal_z(om.size, om.ctypes.data_as(_ip), _d(tr), _d(a[0]), _d(a[1]), _d(a[2]), _d(out)))
+    return out

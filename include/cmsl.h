@@ -153,12 +153,26 @@ cmsl_status cmsl_film_get_iters(cmsl_film *film, int n, int32_t *pcg_iters, int3
  *    kernelCalc_antiferro computed from the current phi (Calc_EfieldMag);
  *  - depol: one Depol_field (RHS from the current Pm, warm-started PCG);
  *  - apply_operator: y = A x with the film's operator (apply_A), FP64 or FP32;
- *  - efield: E = -grad(phi) of the current phi (Calc_EfieldMag), FP64 films. */
+ *  - efield: E = -grad(phi) of the current phi (Calc_EfieldMag; FP32-refined
+ *    films difference the double-float potential in FP64). */
 cmsl_status cmsl_film_tdgl_step(cmsl_film *film, double Ez);
 cmsl_status cmsl_film_depol(cmsl_film *film, int32_t *iters, int32_t *status);
 cmsl_status cmsl_film_apply_operator(cmsl_film *film, const double *x, double *y);
 cmsl_status cmsl_film_efield(cmsl_film *film, double *Ex, double *Ey, double *Ez);
 cmsl_status cmsl_film_diag_inv(cmsl_film *film, double *dinv);
+
+/* Depol_field (depol_varEPS.cu:332-595) over the caller's DEVICE arrays, as
+ * the reference's global-state solve sees them: the new Pm (Pmx/Pmy/Pmz_d),
+ * phi_dep_d (warm start in, solution out, in place) and delecX/Y/Z_d (E out;
+ * pass NULLs to skip).  Everything is converted and copied by kernels on
+ * `stream`; nothing goes through the host and nothing is allocated per call,
+ * so a caller keeps one film for its grid and calls this once per step.  The
+ * film's own P state is overwritten (its Pm with the given one).  Single
+ * films with a depolarisation solve; iters[0] PCG iterations, iters[1]
+ * refinement passes (FP32_REFINED). */
+cmsl_status cmsl_film_depol_device(cmsl_film *film, const double *Pmx, const double *Pmy, const double *Pmz,
+                                   double *phi, double *Ex, double *Ey, double *Ez, void *stream,
+                                   int32_t *iters, int32_t *status);
 
 /* Average device time (ms, CUDA events on the launch stream) of each kernel
  * of a step, each launched `reps` times back to back on the current state:

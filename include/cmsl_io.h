@@ -139,6 +139,16 @@ cmsl_status cmsl_checkpoint_read(const char *path, int nx, int ny, int nz, int *
 cmsl_status cmsl_vector_field_write(const char *path, const double *Px, const double *Py, const double *Pz,
                                     long long n, double scale);
 
+/* write_midplane_slice (generate.cu:67-88): the plane k = nz/2 of v as text
+ * lines "i j value" (%.16e), a blank line after each row j. */
+cmsl_status cmsl_midplane_slice_write(const char *path, const double *v, int nx, int ny, int nz);
+
+/* The crystal-frame z component of a lab-frame vector field per cell,
+ * TR[9 omega + 6] x + TR[9 omega + 7] y + TR[9 omega + 8] z in that order
+ * (kernelCalc_antiferro's *_local outputs, kernels_evol.cu:160-175). */
+cmsl_status cmsl_crystal_z(long long n, const int32_t *omega, const double *TR, const double *x, const double *y,
+                           const double *z, double *out);
+
 /* Calc_EfieldMag (depol_varEPS.cu:223-276) on the host: E = -grad(phi). */
 cmsl_status cmsl_efield_host(int nx, int ny, int nz, double del_h, int zbc, const double *phi, double *Ex,
                              double *Ey, double *Ez);

@@ -331,6 +331,7 @@ class RefLib:
         L.ref_read_checkpoint.argtypes = [C.c_char_p, C.POINTER(_dp), C.POINTER(_dp)] + [C.c_int] * 3 + [
             _ip, _ip, _dp, _dp]
         L.ref_write_vector_field.argtypes = [C.c_char_p, _dp, _dp, _dp] + [C.c_int] * 3 + [C.c_double]
+        L.ref_write_midplane_slice.argtypes = [C.c_char_p, _dp] + [C.c_int] * 3
 
     @staticmethod
     def per_voxel(film: Film):
@@ -470,6 +471,11 @@ class RefLib:
         """generate.cu write_vector_field_binary."""
         a = [np.ascontiguousarray(x, np.float64) for x in (Px, Py, Pz)]
         self.lib.ref_write_vector_field(path.encode(), _d(a[0]), _d(a[1]), _d(a[2]), nx, ny, nz, float(p0))
+
+    def write_midplane_slice(self, path: str, v, nx, ny, nz):
+        """generate.cu write_midplane_slice."""
+        v = np.ascontiguousarray(v, np.float64)
+        self.lib.ref_write_midplane_slice(path.encode(), _d(v), nx, ny, nz)
 
     def depol_field(self, film: Film, Pm, phi, tol_abs=1e-3, tol_rel=1e-2, max_iter=4000):
         eps = self.per_voxel(film)[7]

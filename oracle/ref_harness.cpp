@@ -307,4 +307,9 @@ void ref_write_vector_field(const char *fname, double *Px, double *Py, double *P
     write_vector_field_binary(fname, Px, Py, Pz, nx_, ny_, nz_, p0);
 }
 
+void ref_write_midplane_slice(const char *fname, const double *v, int nx_, int ny_, int nz_)
+{
+    write_midplane_slice(fname, v, nx_, ny_, nz_);
+}
+
 }  // extern "C"

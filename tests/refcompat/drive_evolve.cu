@@ -1,6 +1,13 @@
 // Test driver: sets the reference globals from a setup file, calls the
-// reference entry point Evolve() (provided by libcmsl_gb's refcompat object),
-// and writes the final P.  Setup file layout (native endianness):
+// reference entry points (provided by libcmsl_gb's refcompat object) and
+// writes the result.  Modes (argv[4]):
+//   evolve (default)  Evolve(); writes the final P, count and peloop
+//   pre               the same with do_pre_relax = 1 (the slice files land in
+//                     the working directory)
+//   depol             Depol_field() twice on the device arrays: P as the new
+//                     state, then 0.9 P, the second call warm-started from
+//                     the first's phi_dep_d; writes phi and E of both calls
+// Setup file layout (native endianness):
 //   int32  nx ny nz ng dep_flag zbc num_steps
 //   double del_h del_t eps_0_nd maxEz delEz E0_ref P0_ref
 //   double mats[3][8] (AFE, FE, DE: alpha beta gamma g a0 kappa L eps_r)
@@ -27,11 +34,16 @@ extern double *TR_h;
 extern double *Pmx_old_d, *Pmy_old_d, *Pmz_old_d, *Pmx_d, *Pmy_d, *Pmz_d;
 extern double *Psx_old_d, *Psy_old_d, *Psz_old_d, *Psx_d, *Psy_d, *Psz_d;
 extern double *delecX_d, *delecY_d, *delecZ_d;
+extern double *phi_dep_d;
+extern bool phi_dep_initialized;
 void Evolve(void);
+void Depol_field(void);
+void evolve_resources_cleanup(void);
 
 int main(int argc, char **argv)
 {
-    if (argc < 4) { std::fprintf(stderr, "usage: drive_evolve setup.bin out_dir final_P.bin\n"); return 2; }
+    if (argc < 4) { std::fprintf(stderr, "usage: drive_evolve setup.bin out_dir result.bin [evolve|pre|depol]\n"); return 2; }
+    const char *mode = argc > 4 ? argv[4] : "evolve";
     FILE *f = std::fopen(argv[1], "rb");
     if (!f) return 2;
     int iv[7];
@@ -67,6 +79,30 @@ int main(int argc, char **argv)
     }
     double **E[3] = {&delecX_d, &delecY_d, &delecZ_d};
     for (auto e : E) { cudaMalloc(e, N * sizeof(double)); cudaMemset(*e, 0, N * sizeof(double)); }
+    if (std::strcmp(mode, "depol") == 0) {
+        // the new Pm is what Depol_field reads
+        for (int q = 0; q < 6; ++q)
+            cudaMemcpy(*news[q], P.data() + q * N, N * sizeof(double), cudaMemcpyHostToDevice);
+        f = std::fopen(argv[3], "wb");
+        std::vector<double> v(N);
+        for (int call = 0; call < 2; ++call) {
+            if (call == 1)
+                for (int q = 0; q < 3; ++q) {
+                    for (size_t i = 0; i < N; ++i) v[i] = 0.9 * P[q * N + i];
+                    cudaMemcpy(*news[q], v.data(), N * sizeof(double), cudaMemcpyHostToDevice);
+                }
+            Depol_field();
+            double *out[4] = {phi_dep_d, delecX_d, delecY_d, delecZ_d};
+            for (double *o : out) {
+                cudaMemcpy(v.data(), o, N * sizeof(double), cudaMemcpyDeviceToHost);
+                std::fwrite(v.data(), sizeof(double), N, f);
+            }
+        }
+        std::fclose(f);
+        evolve_resources_cleanup();
+        return cudaGetLastError() == cudaSuccess ? 0 : 3;
+    }
+    if (std::strcmp(mode, "pre") == 0) do_pre_relax = 1;
     Evolve();
     for (int q = 0; q < 6; ++q) cudaMemcpy(P.data() + q * N, *olds[q], N * sizeof(double), cudaMemcpyDeviceToHost);
     f = std::fopen(argv[3], "wb");

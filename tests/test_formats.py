@@ -283,6 +283,25 @@ def test_vector_field_bytes_equal_reference(ref, tmp_path):
     assert mine.read_bytes() == theirs.read_bytes()
 
 
+@pytest.mark.parametrize("shape", [(5, 4, 3), (7, 6, 8)])
+def test_midplane_slice_bytes_equal_reference(ref, tmp_path, shape):
+    nx, ny, nz = shape
+    v = np.random.default_rng(11).normal(size=nx * ny * nz) * 1e-3
+    mine, theirs = tmp_path / "m.dat", tmp_path / "t.dat"
+    fm.write_midplane_slice(str(mine), v, nx, ny, nz)
+    ref.write_midplane_slice(str(theirs), v, nx, ny, nz)
+    assert mine.read_bytes() == theirs.read_bytes()
+
+
+def test_crystal_z_equals_reference_local_output(ref):
+    """The crystal-frame z components are kernelCalc_antiferro's Pmz_local /
+    Psz_local outputs (kernels_evol.cu:160-175), bit for bit."""
+    f, P = random_film(9, 7, 5, seed=12)
+    _, loc = ref.tdgl_step(f, P, 0.2)
+    assert np.array_equal(fm.crystal_z(f.omega, f.TR, P[0], P[1], P[2]), loc[2])
+    assert np.array_equal(fm.crystal_z(f.omega, f.TR, P[3], P[4], P[5]), loc[5])
+
+
 @pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
 def test_host_efield_matches_reference_kernel(ref, zbc):
     f, _ = random_film(9, 7, 5, seed=8, zbc=zbc)
