@@ -17,6 +17,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_SOURCES = ["engine.cu", "noalloc.cu", "adjoint.cu", "grains.cu"]
 HOST_SOURCES = ["formats.cpp"]
 HEADERS = ["cmsl_dev.cuh", "dfloat.cuh", "kernels.cuh", "pcg_persist.cuh", "spectral.cuh", "stencil32.cuh",
+           "stencil_tma.cuh", "tma.cuh",
            "engine.h"]
 OBJDIR = os.path.join(HERE, "_build")
 

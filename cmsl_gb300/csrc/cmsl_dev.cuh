@@ -5,19 +5,22 @@
 //     at FilmDev::off (a multiple of 32 cells: 128-byte aligned FP32 rows for
 //     the vectorised passes) and are in the reference's C order
 //     i + nx*(j + ny*k);
-//   * P fields: two ping-pong sets of six SoA arrays (Pmx..Psz) in the
-//     compute type T (double for CMSL_FP64, float for CMSL_FP32_REFINED),
-//     each set one allocation with field q at q * ncells;
+//   * P fields: two ping-pong sets, each one allocation: CMSL_FP64 -- six
+//     SoA double arrays (Pmx..Psz), field q at q * ncells; CMSL_FP32_REFINED
+//     -- three float2 arrays of the pairs (Pmx, Pmy), (Pmz, Psx), (Psy, Psz),
+//     pair j at j * ncells float2 (a stencil point of a pair is one 8-byte
+//     load or one 8-byte tensor-copy element);
 //   * code[c]: grain id (bits 0-23, film-local) | material (bits 24-25) |
 //     interface flag (bit 26) -- replaces the reference's seven per-voxel FP64
 //     parameter arrays, omega and is_interface (kernels_evol.cu:133-146);
 //   * phi: FP64 potentials (two buffers), or five double-float buffers in
-//     FP32_REFINED mode (hi half at the cell, lo half ncells further on) for
-//     the extrapolated warm start; PCG vectors r, p[2], q, dinv, x in T;
+//     FP32_REFINED mode ((hi, lo) float2 per cell) for the extrapolated warm
+//     start; PCG vectors r, p[2], q, dinv, x in T;
 //   * per-grain rotations TR (9 per grain, row major) in T.
 // Work is cut into items (film, x0, y0, z0..z1): one thread block per item,
 // a TX x TY thread tile marching through z0..z1.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -101,6 +104,8 @@ struct CgBuf {
     unsigned int *arrive;       // grid-barrier arrival counter (reset by k_refine32)
     float4 *part;               // [2][grid] per-block partial sums (two double-float pairs), by parity
     int *err;                   // barrier timeout flag
+    unsigned long long spin_limit;   // sleeps of a barrier wait before it gives up
+    int hold_block;             // failure injection: this block never arrives at a barrier (-1: none)
     const int4 *bricks;         // stencil work list: TX x TY x (<= PZ planes) bricks, film by film
     const int *blk_film;        // film of each block of the cooperative grid
     int n_bricks;
@@ -120,12 +125,26 @@ template <class T> struct Fields {
     const T *TR;
 };
 
+// Tensor maps of one film for the tensor-copy (TMA) staging of the FP32
+// stencil passes (films with nx % 32 == 0 and ny % 8 == 0).  Each tensor has
+// maps of three box shapes: the tile body {TX, TY}, one x row {TX, 1} (the
+// y halo rows) and a column strip {16 bytes, TY} (the x halo columns).
+enum { TM_BODY = 0, TM_ROW = 1, TM_COL = 2 };
+struct FilmMaps {            // CUtensorMap carries its own alignment
+    CUtensorMap P[2][3];        // P set s: 4D {nx, ny, nz, 3} of float2 pairs
+    CUtensorMap phi[5][3];      // potential buffer b: 3D {nx, ny, nz} of (hi, lo) float2
+    CUtensorMap code[3];        // 3D uint32
+    CUtensorMap x[3];           // the inner solve's correction dx: 3D float
+    CUtensorMap r;              // 3D float (body)
+    CUtensorMap dinv;           // 3D float (body)
+};
+
 struct Dev {
     const FilmDev *films;
     const int4 *items;
     int n_films, n_items;
     const uint32_t *code;
-    long long ncells;           // cells of all films (double-float phi: lo half offset)
+    long long ncells;           // cells of all films (stride of the FP32 P pairs)
     double *phi[5];
     double *partial;            // [n_items * NPART]
     unsigned int *counter;      // one ticket counter (reset by the last block)
@@ -143,6 +162,8 @@ struct Dev {
     unsigned int *arrive;       // grid-barrier counter of the persistent PCG (or null)
     cudaGraphConditionalHandle h_inner, h_outer;
     cudaGraphConditionalHandle h_steps;   // the graph's step loop (0: one step per launch)
+    const FilmMaps *maps;       // [n_films] tensor maps (TMA stencil passes), or null
+    int *err;                   // device error word (bounded waits that gave up)
 };
 
 }  // namespace cmsl

@@ -37,6 +37,8 @@
 #include <thread>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "engine.h"
 #include "cmsl_io.h"
 
@@ -493,33 +495,69 @@ cmsl_status build_graph(Engine *e)
 // (a GPU writing fresh pageable pages pays a page fault per page).  Without
 // that device attribute uploads are converted on the host too.
 template <class T>
-__global__ void k_host_in(const double *__restrict__ src, T *__restrict__ dst, long long n)
+__global__ void k_host_in(const double *__restrict__ src, T *__restrict__ dst, long long n, int stride)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        dst[i] = (T)src[i];
+        dst[i * stride] = (T)src[i];
 }
-// potential as double-float: hi = (float)x, lo = (float)(x - hi)
-__global__ void k_phi_in(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo, long long n)
+// potential as double-float pairs: hi = (float)x, lo = (float)(x - hi)
+__global__ void k_phi_in(const double *__restrict__ src, float2 *__restrict__ dst, long long n)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double x = src[i];
         const float h = (float)x;
-        hi[i] = h;
-        lo[i] = (float)(x - (double)h);
+        dst[i] = make_float2(h, (float)(x - (double)h));
     }
 }
 template <class T>
-__global__ void k_host_out(const T *__restrict__ src, double *__restrict__ dst, long long n)
+__global__ void k_host_out(const T *__restrict__ src, double *__restrict__ dst, long long n, int stride)
 {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        dst[i] = (double)src[i];
+        dst[i] = (double)src[i * stride];
 }
-__global__ void k_phi_out(const float *__restrict__ hi, const float *__restrict__ lo, double *__restrict__ dst,
-                          long long n)
+__global__ void k_phi_out(const float2 *__restrict__ src, double *__restrict__ dst, long long n)
 {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        dst[i] = (double)hi[i] + (double)lo[i];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = src[i];
+        dst[i] = (double)v.x + (double)v.y;
+    }
 }
+// Per-cell codes of one film on the device (the set-up of main.cu:13-52 and
+// init_conf.cu:68-106 reduced to one word per cell): grain id | material
+// << 24 | interface << 26, the interface flag of build_interface_flag unless
+// the caller gave one; the voxels of each material counted per block and
+// added in integers (exact).  Grain ids were checked on the host.
+__global__ void k_film_code(const int32_t *__restrict__ omega, const int32_t *__restrict__ gmat,
+                            const int32_t *__restrict__ iface, int nx, int ny, int nz, uint32_t *__restrict__ code,
+                            unsigned long long *__restrict__ counts)
+{
+    __shared__ unsigned int s_cnt[3];
+    if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    const long long plane = (long long)nx * ny, n = plane * nz;
+    unsigned int c0 = 0, c1 = 0, c2 = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int g = omega[i], m = gmat[g];
+        int fl = 0;
+        if (iface) {
+            fl = iface[i] != 0;
+        } else {
+            const long long k = i / plane;
+            if (m == CMSL_FE && k > 0 && k < nz - 1)
+                fl = gmat[omega[i + plane]] != CMSL_FE || gmat[omega[i - plane]] != CMSL_FE;
+        }
+        code[i] = (uint32_t)g | ((uint32_t)m << 24) | ((uint32_t)fl << 26);
+        c0 += m == 0;
+        c1 += m == 1;
+        c2 += m == 2;
+    }
+    atomicAdd(&s_cnt[0], c0);
+    atomicAdd(&s_cnt[1], c1);
+    atomicAdd(&s_cnt[2], c2);
+    __syncthreads();
+    if (threadIdx.x < 3) atomicAdd(&counts[threadIdx.x], (unsigned long long)s_cnt[threadIdx.x]);
+}
+
 constexpr int XFER_GRID = 152 * 8, XFER_NT = 256;
 
 // The device address of page-locked host memory at p (null for pageable
@@ -651,23 +689,27 @@ cmsl_status step_direct(Engine *e, cudaStream_t st)
 }
 
 
+// Field q of P set s: FP64 -- its own array; FP32 -- one half of the pair
+// (q & ~1, q | 1), element i at stride 2 (pstride).
 template <class T>
 cmsl_status put_fields(Engine *e, int film, int set, const double *const P[6])
 {
     const FilmHost &h = e->fh[film];
+    const int ps = e->pstride();
     for (int q = 0; q < 6; ++q)
         if (!P[q]) return fail(CMSL_ERR_ARG, "P[%d] is NULL", q);
     if (e->host_direct) {
         for (int q = 0; q < 6; ++q)
-            k_host_in<T><<<XFER_GRID, XFER_NT>>>(P[q], (T *)e->d_P[set][q] + h.off, h.N);
+            k_host_in<T><<<XFER_GRID, XFER_NT>>>(P[q], (T *)e->d_P[set][q] + ps * h.off, h.N, ps);
         CK(cudaGetLastError());
         CK(cudaDeviceSynchronize());
         return CMSL_OK;
     }
-    std::vector<T> tmp((size_t)h.N);
-    for (int q = 0; q < 6; ++q) {
-        for (long long i = 0; i < h.N; ++i) tmp[i] = (T)P[q][i];
-        CK(cudaMemcpy((T *)e->d_P[set][q] + h.off, tmp.data(), h.N * sizeof(T), cudaMemcpyHostToDevice));
+    std::vector<T> tmp((size_t)(ps * h.N));
+    for (int q = 0; q < 6; q += ps) {
+        for (long long i = 0; i < h.N; ++i)
+            for (int u = 0; u < ps; ++u) tmp[ps * i + u] = (T)P[q + u][i];
+        CK(cudaMemcpy((T *)e->d_P[set][q] + ps * h.off, tmp.data(), ps * h.N * sizeof(T), cudaMemcpyHostToDevice));
     }
     return CMSL_OK;
 }
@@ -705,10 +747,11 @@ template <class T>
 cmsl_status get_fields(Engine *e, int film, int set, double *const P[6])
 {
     const FilmHost &h = e->fh[film];
+    const int ps = e->pstride();
     bool rest = false;                  // arrays left for the paths below
     for (int q = 0; q < 6; ++q) {
         double *dv = locked_dst(P[q]);
-        if (dv) k_host_out<T><<<XFER_GRID, XFER_NT>>>((const T *)e->d_P[set][q] + h.off, dv, h.N);
+        if (dv) k_host_out<T><<<XFER_GRID, XFER_NT>>>((const T *)e->d_P[set][q] + ps * h.off, dv, h.N, ps);
         else rest = rest || P[q];
     }
     CK(cudaGetLastError());
@@ -717,28 +760,117 @@ cmsl_status get_fields(Engine *e, int film, int set, double *const P[6])
     double *Pr[6];
     for (int q = 0; q < 6; ++q) Pr[q] = locked_dst(P[q]) ? nullptr : P[q];
     P = Pr;
+    // one DMA copy of each field (FP64) or pair (FP32) into pinned memory,
+    // then the conversion into the caller's arrays on the host cores
+    void *stg = nullptr;
+    std::vector<T> tmp;
     if (e->host_direct) {
-        // one DMA copy into pinned memory, then the conversion into the
-        // caller's arrays on the host cores
-        void *stg = nullptr;
         TRY(pinned_stage(e, &stg));
-        const T *st = (const T *)stg;
-        for (int q = 0; q < 6; ++q) {
-            if (!P[q]) continue;
-            CK(cudaMemcpy((void *)st, (const T *)e->d_P[set][q] + h.off, sizeof(T) * h.N, cudaMemcpyDeviceToHost));
-            double *dst = P[q];
+    } else {
+        tmp.resize((size_t)(ps * h.N));
+        stg = tmp.data();
+    }
+    const T *st = (const T *)stg;
+    for (int q = 0; q < 6; q += ps) {
+        bool want = false;
+        for (int u = 0; u < ps; ++u) want = want || P[q + u];
+        if (!want) continue;
+        CK(cudaMemcpy((void *)st, (const T *)e->d_P[set][q] + ps * h.off, sizeof(T) * ps * h.N,
+                      cudaMemcpyDeviceToHost));
+        for (int u = 0; u < ps; ++u) {
+            double *dst = P[q + u];
+            if (!dst) continue;
             parallel_for(h.N, [&](long long i0, long long i1) {
-                for (long long i = i0; i < i1; ++i) dst[i] = (double)st[i];
+                for (long long i = i0; i < i1; ++i) dst[i] = (double)st[ps * i + u];
             });
         }
-        return CMSL_OK;
     }
-    std::vector<T> tmp((size_t)h.N);
-    for (int q = 0; q < 6; ++q) {
-        if (!P[q]) continue;
-        CK(cudaMemcpy(tmp.data(), (const T *)e->d_P[set][q] + h.off, h.N * sizeof(T), cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < h.N; ++i) P[q][i] = (double)tmp[i];
+    return CMSL_OK;
+}
+
+// Builds every film's codes into d_code (film f at its offset) and the
+// per-material voxel counts of the film tables.
+cmsl_status build_film_codes(Engine *e, const cmsl_film_desc *descs, std::vector<FilmDev> &fds)
+{
+    long long nmax = 0;
+    int gmax = 0;
+    for (const FilmHost &h : e->fh) {
+        nmax = std::max(nmax, h.N);
+        gmax = std::max(gmax, h.ng);
     }
+    int32_t *t = nullptr;
+    unsigned long long *cnt = nullptr;
+    CK(cudaMalloc(&t, sizeof(int32_t) * (size_t)(2 * nmax + gmax)));
+    cudaError_t err = cudaMalloc(&cnt, sizeof(unsigned long long) * 3);
+    for (int fi = 0; fi < e->n_films && err == cudaSuccess; ++fi) {
+        const cmsl_film_desc *dsc = descs + fi;
+        const FilmHost &h = e->fh[fi];
+        int32_t *om = t, *fl = t + nmax, *gm = t + 2 * nmax;
+        unsigned long long c[3] = {0, 0, 0};
+        err = cudaMemcpy(om, dsc->omega, sizeof(int32_t) * h.N, cudaMemcpyHostToDevice);
+        if (err == cudaSuccess) err = cudaMemcpy(gm, dsc->grain_mat, sizeof(int32_t) * h.ng, cudaMemcpyHostToDevice);
+        if (err == cudaSuccess && dsc->is_interface)
+            err = cudaMemcpy(fl, dsc->is_interface, sizeof(int32_t) * h.N, cudaMemcpyHostToDevice);
+        if (err == cudaSuccess) err = cudaMemset(cnt, 0, sizeof(unsigned long long) * 3);
+        if (err == cudaSuccess) {
+            const unsigned blocks = (unsigned)std::min<long long>((h.N + 255) / 256, 152LL * 16);
+            k_film_code<<<blocks, 256>>>(om, gm, dsc->is_interface ? fl : nullptr, h.nx, h.ny, h.nz,
+                                         e->d_code + h.off, cnt);
+            err = cudaGetLastError();
+        }
+        if (err == cudaSuccess) err = cudaMemcpy(c, cnt, sizeof c, cudaMemcpyDeviceToHost);
+        for (int q = 0; q < 3; ++q) fds[fi].n_mat[q] = (double)c[q];
+    }
+    cudaFree(t);
+    if (cnt) cudaFree(cnt);
+    if (err != cudaSuccess) return fail(CMSL_ERR_CUDA, "building the cell codes failed: %s", cudaGetErrorString(err));
+    return CMSL_OK;
+}
+
+// Tensor maps of every film for the tensor-copy staging (FilmMaps): the P
+// sets as 4D {nx, ny, nz, 3} float2-pair tensors, the five potential buffers
+// and the correction dx, the codes, r and D^-1 as 3D tensors, each in the
+// three box shapes the stencil passes copy (tile body, x row, x halo strip).
+cmsl_status make_maps(Engine *e)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (!fn || q != cudaDriverEntryPointSuccess) return fail(CMSL_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const int F = e->n_films;
+    std::vector<FilmMaps> maps((size_t)F);
+    const cuuint64_t cells = (cuuint64_t)e->ncells;
+    for (int fi = 0; fi < F; ++fi) {
+        const FilmHost &h = e->fh[fi];
+        FilmMaps &M = maps[fi];
+        // box shapes: tile body, one x row, a 16-byte x strip
+        auto enc = [&](CUtensorMap *m3, void *base, int esz, int rank, int nq, int n_shapes) -> cmsl_status {
+            const cuuint64_t dims[4] = {(cuuint64_t)h.nx, (cuuint64_t)h.ny, (cuuint64_t)h.nz, (cuuint64_t)nq};
+            const cuuint64_t strides[3] = {(cuuint64_t)h.nx * esz, (cuuint64_t)h.nx * h.ny * esz, cells * esz};
+            const cuuint32_t shapes[3][4] = {{TX, TY, 1, 1}, {TX, 1, 1, 1}, {(cuuint32_t)(16 / esz), TY, 1, 1}};
+            const cuuint32_t unit[4] = {1, 1, 1, 1};
+            for (int sh = 0; sh < n_shapes; ++sh) {
+                const CUresult r = encode(m3 + sh, esz == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32,
+                                          rank, base, dims, strides, shapes[sh], unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                if (r != CUDA_SUCCESS) return fail(CMSL_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+            }
+            return CMSL_OK;
+        };
+        for (int s = 0; s < 2; ++s) TRY(enc(M.P[s], (float2 *)e->d_P[s][0] + h.off, 8, 4, 3, 3));
+        for (int b = 0; b < 5; ++b) TRY(enc(M.phi[b], (float2 *)e->d_phi[b] + h.off, 8, 3, 1, 3));
+        TRY(enc(M.code, (uint32_t *)e->d_code + h.off, 4, 3, 1, 3));
+        TRY(enc(M.x, (float *)e->d_x + h.off, 4, 3, 1, 3));
+        TRY(enc(&M.r, (float *)e->d_r + h.off, 4, 3, 1, 1));
+        TRY(enc(&M.dinv, (float *)e->d_dinv + h.off, 4, 3, 1, 1));
+    }
+    TRY(e->alloc((void **)&e->d_maps, sizeof(FilmMaps) * F));
+    CK(cudaMemcpy(e->d_maps, maps.data(), sizeof(FilmMaps) * F, cudaMemcpyHostToDevice));
     return CMSL_OK;
 }
 
@@ -820,36 +952,19 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         if (n > cg_per * cg_nsm) e->persistent = false;
     }
 
-    // per-cell code (grain id local to the film), interface flags
-    // (main.cu:13-42), material voxel counts, work items, film tables
-    std::vector<uint32_t> code((size_t)e->ncells);
+    // grain ids are checked on the host (before any device work); the
+    // per-cell codes, interface flags and material voxel counts are built on
+    // the device below (build_film_codes); work items, film tables
     std::vector<FilmDev> fds((size_t)n);
     int g_off = 0;
     for (int fi = 0; fi < n; ++fi) {
         const cmsl_film_desc *dsc = descs + fi;
         const FilmHost &h = e->fh[fi];
-        const long long plane = (long long)h.nx * h.ny;
         const std::string who = n > 1 ? "film " + std::to_string(fi) + ": " : "";
-        double nmat[3] = {0, 0, 0};
         for (long long i = 0; i < h.N; ++i) {
             const int gid = dsc->omega[i];
             if (gid < 0 || gid >= h.ng)
                 return fail(CMSL_ERR_ARG, "%scell %lld has grain id %d outside [0,%d)", who.c_str(), i, gid, h.ng);
-            const int mat = dsc->grain_mat[gid];
-            int iface;
-            if (dsc->is_interface) {
-                iface = dsc->is_interface[i] != 0;
-            } else {
-                const long long k = i / plane;
-                iface = 0;
-                if (mat == CMSL_FE && k > 0 && k < h.nz - 1) {
-                    const int mu = dsc->grain_mat[dsc->omega[i + plane]];
-                    const int md = dsc->grain_mat[dsc->omega[i - plane]];
-                    iface = (mu != CMSL_FE || md != CMSL_FE);
-                }
-            }
-            code[h.off + i] = (uint32_t)gid | ((uint32_t)mat << 24) | ((uint32_t)iface << 26);
-            nmat[mat] += 1.0;
         }
         FilmDev &fd = fds[fi];
         fill_film(fd, dsc, e->precision);
@@ -857,7 +972,6 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         fd.off = h.off;
         fd.g_off = g_off;
         g_off += h.ng;
-        for (int q = 0; q < 3; ++q) fd.n_mat[q] = nmat[q];
     }
     e->xy_tiles = xy_tiles;
 
@@ -927,6 +1041,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         const char *hd = getenv("CMSL_HOST_COPY");   // 1: host-side conversion and copies
         e->host_direct = pageable && host_tables && !(hd && atoi(hd) != 0);
     }
+    TRY(e->alloc((void **)&e->d_code, sizeof(uint32_t) * cells));
+    TRY(build_film_codes(e, descs, fds));
     e->fdh = fds;
     TRY(e->alloc((void **)&e->d_films, sizeof(FilmDev) * n));
     e->items_cap = std::max(count_items(e, ZCHUNK_MIN), count_items(e, 0));
@@ -939,14 +1055,16 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         if (hit != g_tuned.end()) zc = hit->second;
         TRY(set_items(e, zc));
     }
-    TRY(e->alloc((void **)&e->d_code, sizeof(uint32_t) * cells));
-    CK(cudaMemcpy(e->d_code, code.data(), sizeof(uint32_t) * cells, cudaMemcpyHostToDevice));
     if (e->precision == CMSL_FP64) TRY(upload_TR<double>(e, descs, n));
     else TRY(upload_TR<float>(e, descs, n));
     for (int s = 0; s < 2; ++s) {
-        // the six fields of a set back to back (field q at q * cells)
+        // FP64: the six fields of a set back to back (field q at q * cells);
+        // FP32: the pairs (Pmx, Pmy), (Pmz, Psx), (Psy, Psz) as float2 arrays
+        // back to back, field q the half q & 1 of pair q / 2 (stride 2)
         TRY(e->alloc(&e->d_P[s][0], 6 * e->esz * cells));
-        for (int q = 1; q < 6; ++q) e->d_P[s][q] = (char *)e->d_P[s][0] + q * e->esz * cells;
+        for (int q = 1; q < 6; ++q)
+            e->d_P[s][q] = e->precision == CMSL_FP64 ? (char *)e->d_P[s][0] + q * e->esz * cells
+                                                      : (void *)((float *)e->d_P[s][0] + (q >> 1) * 2 * cells + (q & 1));
     }
     TRY(e->alloc(&e->d_r, e->esz * cells));
     TRY(e->alloc(&e->d_q, e->esz * cells));
@@ -974,6 +1092,12 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(e->alloc((void **)&B.part, sizeof(float4) * 2 * e->cg_grid));
         TRY(e->alloc((void **)&B.arrive, sizeof(unsigned int) * 2));
         TRY(e->alloc((void **)&B.err, sizeof(int) * 2));
+        // the barrier waits' limit, and a block that withholds its arrivals,
+        // for the host test that makes a barrier run out (CMSL_PCG_SPIN_LIMIT,
+        // CMSL_PCG_HOLD_BLOCK); the kernel then returns and reports the timeout
+        const char *sl = getenv("CMSL_PCG_SPIN_LIMIT"), *hb = getenv("CMSL_PCG_HOLD_BLOCK");
+        B.spin_limit = sl && atoll(sl) > 0 ? (unsigned long long)atoll(sl) : BARRIER_SPIN_LIMIT;
+        B.hold_block = hb ? atoi(hb) : -1;
     }
     if (e->spectral) {
         // per-film plans, tables and block ranges of the three passes
@@ -1054,6 +1178,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(e->alloc((void **)&e->d_phi[4], sizeof(double) * cells));
     }
     TRY(e->alloc((void **)&e->d_counter, sizeof(unsigned int) * 4));
+    TRY(e->alloc((void **)&e->d_err, sizeof(int)));
     TRY(e->alloc((void **)&e->d_solve, sizeof(SolveDev) * n));
     TRY(e->alloc((void **)&e->d_ctl, sizeof(Ctl)));
     TRY(ensure_schedule(e, 16, 16));
@@ -1063,10 +1188,23 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         // depolarised film has one eps
         bool uni = true;
         for (int fi = 0; fi < n; ++fi) uni &= !e->fh[fi].dep || fds[fi].uni_eps != 0;
-        e->refine_fn = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
-        e->refine_smem = uni ? r32_smem<true>() : r32_smem<false>();
-        e->tdgl_fn = (void *)k_tdgl32<T32_NS>;
-        e->tdgl_smem = T32_SMEM;
+        // tensor-copy staging when every film has full tiles (CMSL_NO_TMA=1:
+        // the cp.async ring for all)
+        const char *nt = getenv("CMSL_NO_TMA");
+        e->tma = !(nt && atoi(nt) != 0);
+        for (int fi = 0; fi < n; ++fi) e->tma = e->tma && e->fh[fi].nx % TX == 0 && e->fh[fi].ny % TY == 0;
+        if (e->tma) {
+            TRY(make_maps(e));
+            e->refine_fn = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
+            e->refine_smem = uni ? rt_smem<true>() : rt_smem<false>();
+            e->tdgl_fn = (void *)k_tdgl32t<TT_NS>;
+            e->tdgl_smem = TT_SMEM;
+        } else {
+            e->refine_fn = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
+            e->refine_smem = uni ? r32_smem<true>() : r32_smem<false>();
+            e->tdgl_fn = (void *)k_tdgl32<T32_NS>;
+            e->tdgl_smem = T32_SMEM;
+        }
         e->refine_nt = e->tdgl_nt = NT;
         CK(cudaFuncSetAttribute(e->refine_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem));
         CK(cudaFuncSetAttribute(e->tdgl_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem));
@@ -1099,38 +1237,29 @@ cmsl_status set_state(Engine *e, int film, const double *const P[6], const doubl
         else CK(cudaMemset(dst, 0, sizeof(double) * h.N));
         CK(cudaMemcpy(e->d_phi[1] + h.off, dst, sizeof(double) * h.N, cudaMemcpyDeviceToDevice));
     } else if (e->host_direct) {
-        // double-float: hi half at the cell, lo half ncells further on; the
-        // previous potentials start equal to the given one
-        float *b0 = (float *)e->d_phi[0];
+        // double-float (hi, lo) pairs per cell; the previous potentials
+        // start equal to the given one
+        float2 *b0 = (float2 *)e->d_phi[0] + h.off;
         if (phi) {
-            k_phi_in<<<XFER_GRID, XFER_NT>>>(phi, b0 + h.off, b0 + e->ncells + h.off, h.N);
+            k_phi_in<<<XFER_GRID, XFER_NT>>>(phi, b0, h.N);
             CK(cudaGetLastError());
         } else {
-            CK(cudaMemset(b0 + h.off, 0, sizeof(float) * h.N));
-            CK(cudaMemset(b0 + e->ncells + h.off, 0, sizeof(float) * h.N));
+            CK(cudaMemset(b0, 0, sizeof(float2) * h.N));
         }
-        for (int q = 1; q < 4; ++q) {
-            float *b = (float *)e->d_phi[q];
-            CK(cudaMemcpy(b + h.off, b0 + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToDevice));
-            CK(cudaMemcpy(b + e->ncells + h.off, b0 + e->ncells + h.off, sizeof(float) * h.N,
-                          cudaMemcpyDeviceToDevice));
-        }
+        for (int q = 1; q < 4; ++q)
+            CK(cudaMemcpy((float2 *)e->d_phi[q] + h.off, b0, sizeof(float2) * h.N, cudaMemcpyDeviceToDevice));
         CK(cudaMemset((float *)e->d_x + h.off, 0, sizeof(float) * h.N));
     } else {
-        // double-float: hi half at the cell, lo half ncells further on
-        std::vector<float> hi((size_t)h.N, 0.f), lo((size_t)h.N, 0.f);
+        // double-float (hi, lo) pairs per cell
+        std::vector<float2> hl((size_t)h.N, make_float2(0.f, 0.f));
         if (phi)
             for (long long i = 0; i < h.N; ++i) {
                 const df v = df_from_double(phi[i]);
-                hi[i] = v.h;
-                lo[i] = v.l;
+                hl[i] = make_float2(v.h, v.l);
             }
         // the previous potentials start equal to the given one (no extrapolation on step 1)
-        for (int q = 0; q < 4; ++q) {
-            float *b = (float *)e->d_phi[q];
-            CK(cudaMemcpy(b + h.off, hi.data(), sizeof(float) * h.N, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(b + e->ncells + h.off, lo.data(), sizeof(float) * h.N, cudaMemcpyHostToDevice));
-        }
+        for (int q = 0; q < 4; ++q)
+            CK(cudaMemcpy((float2 *)e->d_phi[q] + h.off, hl.data(), sizeof(float2) * h.N, cudaMemcpyHostToDevice));
         CK(cudaMemset((float *)e->d_x + h.off, 0, sizeof(float) * h.N));
     }
     SolveDev S0{};
@@ -1160,26 +1289,24 @@ cmsl_status get_state(Engine *e, int film, double *const P[6], double *phi)
         if (e->precision == CMSL_FP64) {
             CK(cudaMemcpy(phi, e->d_phi[S.phi_cur] + h.off, sizeof(double) * h.N, cudaMemcpyDeviceToHost));
         } else if (dv) {
-            const float *b = (const float *)e->d_phi[S.phi_cur];
-            k_phi_out<<<XFER_GRID, XFER_NT>>>(b + h.off, b + e->ncells + h.off, dv, h.N);
+            k_phi_out<<<XFER_GRID, XFER_NT>>>((const float2 *)e->d_phi[S.phi_cur] + h.off, dv, h.N);
             CK(cudaGetLastError());
             CK(cudaDeviceSynchronize());
-        } else if (e->host_direct) {
-            const float *b = (const float *)e->d_phi[S.phi_cur];
-            void *stg = nullptr;
-            TRY(pinned_stage(e, &stg));
-            float *hi = (float *)stg, *lo = hi + h.N;
-            CK(cudaMemcpy(hi, b + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(lo, b + e->ncells + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
-            parallel_for(h.N, [&](long long i0, long long i1) {
-                for (long long i = i0; i < i1; ++i) phi[i] = (double)hi[i] + (double)lo[i];
-            });
         } else {
-            std::vector<float> hi((size_t)h.N), lo((size_t)h.N);
-            const float *b = (const float *)e->d_phi[S.phi_cur];
-            CK(cudaMemcpy(hi.data(), b + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(lo.data(), b + e->ncells + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToHost));
-            for (long long i = 0; i < h.N; ++i) phi[i] = (double)hi[i] + (double)lo[i];
+            const float2 *b = (const float2 *)e->d_phi[S.phi_cur] + h.off;
+            void *stg = nullptr;
+            std::vector<float2> tmp;
+            if (e->host_direct) {
+                TRY(pinned_stage(e, &stg));
+            } else {
+                tmp.resize((size_t)h.N);
+                stg = tmp.data();
+            }
+            const float2 *hl = (const float2 *)stg;
+            CK(cudaMemcpy((void *)hl, b, sizeof(float2) * h.N, cudaMemcpyDeviceToHost));
+            parallel_for(h.N, [&](long long i0, long long i1) {
+                for (long long i = i0; i < i1; ++i) phi[i] = (double)hl[i].x + (double)hl[i].y;
+            });
         }
     }
     return CMSL_OK;
@@ -1231,6 +1358,11 @@ cmsl_status sync(Engine *e, int32_t *film_status)
         int err = 0;
         CK(cudaMemcpy(&err, e->cg.err, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) return fail(CMSL_ERR_CUDA, "persistent PCG grid barrier timed out");
+    }
+    if (e->d_err) {
+        int err = 0;
+        CK(cudaMemcpy(&err, e->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err & TMA_ERR_WAIT) return fail(CMSL_ERR_CUDA, "a tensor-copy wait of a stencil pass timed out");
     }
     int first = -1;
     for (int fi = 0; fi < e->n_films; ++fi) {
@@ -1563,25 +1695,22 @@ cmsl_status cmsl_film_depol_device(cmsl_film *f, const double *Pmx, const double
     CK(cudaMemcpyAsync(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     const double *src[3] = {Pmx, Pmy, Pmz};
+    const int ps = f->pstride();
     for (int q = 0; q < 3; ++q) {
         if (f->precision == CMSL_FP64)
-            k_host_in<double><<<XFER_GRID, XFER_NT, 0, st>>>(src[q], (double *)f->d_P[c.cur][q] + h.off, h.N);
+            k_host_in<double><<<XFER_GRID, XFER_NT, 0, st>>>(src[q], (double *)f->d_P[c.cur][q] + h.off, h.N, 1);
         else
-            k_host_in<float><<<XFER_GRID, XFER_NT, 0, st>>>(src[q], (float *)f->d_P[c.cur][q] + h.off, h.N);
+            k_host_in<float><<<XFER_GRID, XFER_NT, 0, st>>>(src[q], (float *)f->d_P[c.cur][q] + ps * h.off, h.N, ps);
     }
     // the warm start: every potential buffer holds phi (no extrapolation)
     if (f->precision == CMSL_FP64) {
         for (int q = 0; q < 2; ++q)
             CK(cudaMemcpyAsync(f->d_phi[q] + h.off, phi, sizeof(double) * h.N, cudaMemcpyDeviceToDevice, st));
     } else {
-        float *b0 = (float *)f->d_phi[0];
-        k_phi_in<<<XFER_GRID, XFER_NT, 0, st>>>(phi, b0 + h.off, b0 + f->ncells + h.off, h.N);
-        for (int q = 1; q < 4; ++q) {
-            float *b = (float *)f->d_phi[q];
-            CK(cudaMemcpyAsync(b + h.off, b0 + h.off, sizeof(float) * h.N, cudaMemcpyDeviceToDevice, st));
-            CK(cudaMemcpyAsync(b + f->ncells + h.off, b0 + f->ncells + h.off, sizeof(float) * h.N,
-                               cudaMemcpyDeviceToDevice, st));
-        }
+        float2 *b0 = (float2 *)f->d_phi[0] + h.off;
+        k_phi_in<<<XFER_GRID, XFER_NT, 0, st>>>(phi, b0, h.N);
+        for (int q = 1; q < 4; ++q)
+            CK(cudaMemcpyAsync((float2 *)f->d_phi[q] + h.off, b0, sizeof(float2) * h.N, cudaMemcpyDeviceToDevice, st));
     }
     CK(cudaGetLastError());
     S = SolveDev{};
@@ -1610,8 +1739,7 @@ cmsl_status cmsl_film_depol_device(cmsl_film *f, const double *Pmx, const double
     if (f->precision == CMSL_FP64) {
         CK(cudaMemcpyAsync(phi, f->d_phi[S.phi_cur] + h.off, sizeof(double) * h.N, cudaMemcpyDeviceToDevice, st));
     } else {
-        const float *b = (const float *)f->d_phi[S.phi_cur];
-        k_phi_out<<<XFER_GRID, XFER_NT, 0, st>>>(b + h.off, b + f->ncells + h.off, phi, h.N);
+        k_phi_out<<<XFER_GRID, XFER_NT, 0, st>>>((const float2 *)f->d_phi[S.phi_cur] + h.off, phi, h.N);
     }
     if (Ex && Ey && Ez) {
         if (f->precision == CMSL_FP64) k_efield<<<nit, NT, 0, st>>>(d, Ex - h.off, Ey - h.off, Ez - h.off);

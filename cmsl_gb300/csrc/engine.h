@@ -10,6 +10,7 @@
 #include "pcg_persist.cuh"
 #include "spectral.cuh"
 #include "stencil32.cuh"
+#include "stencil_tma.cuh"
 
 namespace cmsl_eng {
 
@@ -94,10 +95,17 @@ struct Engine {
     int spec_zt = 0;            // threads per block of the z solve
     size_t spec_smem[3] = {0, 0, 0};
     bool persistent = false;
+    // tensor-copy staging of the FP32 stencil passes (every film's nx % 32 == 0, ny % 8 == 0)
+    bool tma = false;
+    FilmMaps *d_maps = nullptr;
+    int *d_err = nullptr;               // device error word
     CgBuf cg{};
     int cg_grid = 0;
     void *cg_fn = nullptr;
     size_t cg_smem = 0;
+
+    // element stride of one P field in its set: FP32 fields are halves of float2 pairs
+    int pstride() const { return precision == CMSL_FP64 ? 1 : 2; }
 
     ~Engine()
     {
@@ -135,6 +143,8 @@ struct Engine {
         d.wstride = wstride; d.rstride = rstride;
         d.use_cond = use_cond; d.h_inner = hi; d.h_outer = ho;
         d.arrive = cg.arrive;
+        d.maps = d_maps;
+        d.err = d_err;
         return d;
     }
 

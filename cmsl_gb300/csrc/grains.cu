@@ -1,11 +1,15 @@
 // grains.cu -- grain maps on the GPU.
 //
+// The interface flags of a device-resident map (cmsl_interface_flags_gpu,
+// the reference's build_interface_flag), for maps that never leave the GPU.
+//
 // The columnar periodic Voronoi map of cmsl_voronoi_columnar (the stand-in for
 // the reference's genpolycr_layered/voronoi.c, a brute-force nearest-seed
 // search per voxel) computed on the device: one thread per (i, j) column,
 // the seed points staged in shared memory, the distances in explicitly
 // rounded FP64 so the map is identical to the host generator's.  The seeds,
 // centres and orientations come from the same host SplitMix64 stream.
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -55,6 +59,26 @@ __global__ void __launch_bounds__(VB) k_voronoi(int nx, int ny, int nz, int ng, 
         for (int k = 0; k < nz; ++k) omega[c + plane * k] = best;
 }
 
+// build_interface_flag (main.cu:13-42): an FE voxel off the first and last
+// planes is an interface voxel when the voxel above or below it is not FE (a
+// grain id outside [0, ng) counts as not FE); 1 / 0 per voxel.
+__global__ void k_interface(int nx, int ny, int nz, int ng, const int32_t *__restrict__ omega,
+                            const int32_t *__restrict__ gmat, int32_t *__restrict__ flag)
+{
+    const long long plane = (long long)nx * ny, n = plane * nz;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int g = omega[i];
+        const long long k = i / plane;
+        int v = 0;
+        if (g >= 0 && g < ng && gmat[g] == CMSL_FE && k > 0 && k < nz - 1) {
+            const int gu = omega[i + plane], gd = omega[i - plane];
+            const int mu = (gu >= 0 && gu < ng) ? gmat[gu] : -1, md = (gd >= 0 && gd < ng) ? gmat[gd] : -1;
+            v = (mu != CMSL_FE || md != CMSL_FE) ? 1 : 0;
+        }
+        flag[i] = v;
+    }
+}
+
 cmsl_status gfail(cmsl_status s, const char *msg)
 {
     cmsl_internal_set_error(msg);
@@ -84,6 +108,26 @@ extern "C" cmsl_status cmsl_voronoi_columnar_gpu(int nx, int ny, int nz, int ng,
     if (e == cudaSuccess) e = cudaMemcpy(omega, d_om, sizeof(int32_t) * N, cudaMemcpyDeviceToHost);
     cudaFree(d_s);
     cudaFree(d_om);
+    if (e != cudaSuccess) {
+        cmsl_internal_set_error(cudaGetErrorString(e));
+        return CMSL_ERR_CUDA;
+    }
+    return CMSL_OK;
+}
+
+// Interface flags of a grain map held in device memory (a map generated on
+// the GPU stays there): omega_dev[N], grain_mat_dev[n_grains], flags_dev[N],
+// grain ids outside [0, n_grains) count as not FE (never read beyond the table),
+// all device pointers; runs on `stream` and returns without synchronising.
+extern "C" cmsl_status cmsl_interface_flags_gpu(int nx, int ny, int nz, int n_grains, const int32_t *omega_dev,
+                                                const int32_t *grain_mat_dev, int32_t *flags_dev, void *stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || n_grains < 1 || !omega_dev || !grain_mat_dev || !flags_dev)
+        return gfail(CMSL_ERR_ARG, "bad arguments");
+    const long long n = (long long)nx * ny * nz;
+    const unsigned blocks = (unsigned)std::min<long long>((n + VB - 1) / VB, 152LL * 16);
+    k_interface<<<blocks, VB, 0, (cudaStream_t)stream>>>(nx, ny, nz, n_grains, omega_dev, grain_mat_dev, flags_dev);
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         cmsl_internal_set_error(cudaGetErrorString(e));
         return CMSL_ERR_CUDA;

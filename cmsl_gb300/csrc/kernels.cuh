@@ -53,7 +53,7 @@ __device__ __forceinline__ double *phi_sel(const Dev &d, int i)
 }
 
 // Potential storage: FP64 mode keeps doubles; FP32_REFINED keeps double-float
-// pairs (hi half at cell c, lo half at cell ncells + c of the same buffer).
+// (hi, lo) pairs, one float2 per cell.
 template <class T> struct PhiAcc;
 template <> struct PhiAcc<double> {
     using V = double;
@@ -64,10 +64,9 @@ template <> struct PhiAcc<double> {
 };
 template <> struct PhiAcc<float> {
     using V = df;
-    const float *h, *l;
-    __device__ __forceinline__ PhiAcc(const Dev &d, int buf, long long off)
-        : h((const float *)phi_sel(d, buf) + off), l((const float *)phi_sel(d, buf) + d.ncells + off) {}
-    __device__ __forceinline__ V ld(long long o) const { return df{h[o], l[o]}; }
+    const float2 *p;
+    __device__ __forceinline__ PhiAcc(const Dev &d, int buf, long long off) : p((const float2 *)phi_sel(d, buf) + off) {}
+    __device__ __forceinline__ V ld(long long o) const { const float2 v = p[o]; return df{v.x, v.y}; }
     static __device__ __forceinline__ V zero() { return df{0.f, 0.f}; }
 };
 __device__ __forceinline__ float phi_diff(df a, df b)
@@ -758,8 +757,8 @@ __device__ __forceinline__ void step_end(const Dev &d)
 }
 
 // ----------------------------- FP32 refinement: end of a residual pass
-// The potential of CMSL_FP32_REFINED is stored as double-float (hi half at
-// cell c, lo half at cell ncells + c of the same buffer) in five rotating
+// The potential of CMSL_FP32_REFINED is stored as double-float ((hi, lo)
+// pairs, one float2 per cell) in five rotating
 // buffers: the current one, the three before it (extrapolated warm start) and
 // a free one.  A residual pass (k_refine32, stencil32.cuh) forms r = b - A phi
 // in double-float; in the last block this function takes every film's
@@ -1142,8 +1141,8 @@ static __global__ void k_efield(Dev d, double *Ex, double *Ey, double *Ez)
 }
 
 // E = -grad(phi) of the double-float potential of CMSL_FP32_REFINED films
-// (hi half at the cell, lo half ncells further on): each value is formed as
-// hi + lo in FP64, then differenced as in k_efield.
+// ((hi, lo) pairs per cell): each value is formed as hi + lo in FP64, then
+// differenced as in k_efield.
 static __global__ void k_efield_df(Dev d, double *Ex, double *Ey, double *Ez)
 {
     const int4 it = d.items[blockIdx.x];
@@ -1153,12 +1152,11 @@ static __global__ void k_efield_df(Dev d, double *Ex, double *Ey, double *Ez)
     if (!g.valid) return;
     const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
     const int i = g.x0 + lx, j = g.y0 + ly, nx = g.nx, ny = g.ny, nz = g.nz;
-    const float *hi = (const float *)phi_sel(d, d.solve[it.x].phi_cur) + f->off;
-    const float *lo = hi + d.ncells;
+    const float2 *hl = (const float2 *)phi_sel(d, d.solve[it.x].phi_cur) + f->off;
     Ex += f->off; Ey += f->off; Ez += f->off;
     const double two_h = f->two_h;
     auto id = [&](int a, int b, int c) { return a + (long long)nx * (b + (long long)ny * c); };
-    auto phi = [&](long long c) { return (double)hi[c] + (double)lo[c]; };
+    auto phi = [&](long long c) { const float2 v = hl[c]; return (double)v.x + (double)v.y; };
     for (int k = z0; k < z1; ++k) {
         const long long o = g.own_pl + (long long)k * g.plane;
         Ex[o] = __ddiv_rn(-__dsub_rn(phi(id((i + 1) % nx, j, k)), phi(id((i - 1 + nx) % nx, j, k))), two_h);

@@ -38,7 +38,9 @@ __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p)
     return v;
 }
 
-constexpr unsigned long long BARRIER_SPIN_LIMIT = 20000000ull;   // x ~100 ns sleeps
+// Spins of a grid-barrier wait before it gives up (x ~100 ns sleeps): the
+// default of CgBuf::spin_limit (about 1 s).
+constexpr unsigned long long BARRIER_SPIN_LIMIT = 20000000ull;
 
 // Brick geometry of the persistent solver: a block of PBX x PBY threads owns
 // the TX x TY column tile plus its one-cell x/y halo; it stages u = D^-1 r for
@@ -162,11 +164,11 @@ __device__ __forceinline__ bool grid_sync(const CgBuf &B, unsigned int &target)
     target += gridDim.x;
     if (threadIdx.x == 0) {
         __threadfence();
-        atomicAdd(B.arrive, 1u);
+        if ((int)blockIdx.x != B.hold_block) atomicAdd(B.arrive, 1u);
         int ok = 1;
         unsigned long long spins = 0;
         while (ld_acquire(B.arrive) < target) {
-            if (++spins > BARRIER_SPIN_LIMIT) { ok = 0; atomicExch(B.err, 1); break; }
+            if (++spins > B.spin_limit) { ok = 0; atomicExch(B.err, 1); break; }
             __nanosleep(32);
         }
         s_ok2 = ok;
@@ -387,11 +389,11 @@ __device__ __forceinline__ bool grid_allreduce_films(const CgBuf &B, int n_films
         const float h0 = (float)blk[0], h1 = (float)blk[1];
         __stcg(part + blockIdx.x, make_float4(h0, (float)(blk[0] - (double)h0), h1, (float)(blk[1] - (double)h1)));
         __threadfence();
-        atomicAdd(B.arrive, 1u);
+        if ((int)blockIdx.x != B.hold_block) atomicAdd(B.arrive, 1u);
         int ok = 1;
         unsigned long long spins = 0;
         while (ld_acquire(B.arrive) < target) {
-            if (++spins > BARRIER_SPIN_LIMIT) { ok = 0; atomicExch(B.err, 1); break; }
+            if (++spins > B.spin_limit) { ok = 0; atomicExch(B.err, 1); break; }
             __nanosleep(64);
         }
         s_ok = ok;
@@ -449,11 +451,11 @@ __device__ __forceinline__ bool grid_allreduce_all(const CgBuf &B, int parity, u
         const float h0 = (float)blk[0], h1 = (float)blk[1];
         __stcg(part + blockIdx.x, make_float4(h0, (float)(blk[0] - (double)h0), h1, (float)(blk[1] - (double)h1)));
         __threadfence();
-        atomicAdd(B.arrive, 1u);
+        if ((int)blockIdx.x != B.hold_block) atomicAdd(B.arrive, 1u);
         int ok = 1;
         unsigned long long spins = 0;
         while (ld_acquire(B.arrive) < target) {
-            if (++spins > BARRIER_SPIN_LIMIT) { ok = 0; atomicExch(B.err, 1); break; }
+            if (++spins > B.spin_limit) { ok = 0; atomicExch(B.err, 1); break; }
             __nanosleep(64);
         }
         s_ok = ok;

@@ -8,10 +8,16 @@
 // the ring as well, so a thread carries no plane-to-plane state beyond its
 // partial sums, several blocks share an SM, and each plane costs one barrier.
 //
-// Each thread owns one cell of the tile and copies it (4 bytes per field)
-// and at most one x/y halo cell.  (Pair tiles -- two x-adjacent cells per
-// thread with 8-byte copies -- execute a third fewer instructions but halve
-// the warps an SM holds within the same shared memory, and measured slower.)
+// FP32 storage (CMSL_FP32_REFINED): P is kept as three float2 arrays per set,
+// the pairs (Pmx, Pmy), (Pmz, Psx), (Psy, Psz) (pair j at j * ncells float2
+// of the set's allocation), and every double-float potential interleaves its
+// (hi, lo) halves per cell; a stencil point of a pair is one 8-byte copy and
+// one 8-byte shared load.
+//
+// Each thread owns one cell of the tile and copies it and at most one x/y
+// halo cell.  (Pair tiles -- two x-adjacent cells per thread -- execute a
+// third fewer instructions but halve the warps an SM holds within the same
+// shared memory, and measured slower.)
 //
 // Ring protocol (identical in both kernels): planes zlo = max(z0-1, 0) ..
 // zhi = min(z1, nz-1) are staged, plane p in stage (p - zlo) % NS, one
@@ -53,6 +59,16 @@ __device__ __forceinline__ int phi_free(const SolveDev *S)
 {
     return 10 - S->phi_cur - S->phi_prev - S->phi_prev2 - S->phi_prev3;
 }
+
+// The (hi, lo) pairs of double-float potential buffer i.
+__device__ __forceinline__ float2 *phi2_sel(const Dev &d, int i) { return (float2 *)phi_sel(d, i); }
+__device__ __forceinline__ df ld_df(const float2 *p)
+{
+    const float2 v = *p;
+    return df{v.x, v.y};
+}
+// The three P pairs of FP32 set s (pair j at j * ncells).
+__device__ __forceinline__ float2 *pairs32(const Fields<float> &F, int s) { return (float2 *)F.P[s][0]; }
 
 // Stage bookkeeping of the ring: s is the stage of the plane being computed.
 template <int NS> struct RingIdx {
@@ -178,16 +194,17 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
     const float inv_2hf = f->inv_2hf;
     const long long off = f->off, lo = d.ncells, fs = d.ncells;
     const SolveDev *S = d.solve + it.x;
-    const float *ph = (const float *)phi_sel(d, S->phi_cur) + off;
-    const float *qh = (const float *)phi_sel(d, S->phi_prev) + off;
-    const float *uh = (const float *)phi_sel(d, S->phi_prev2) + off;
-    const float *vh = (const float *)phi_sel(d, S->phi_prev3) + off;
-    float *nh = (float *)phi_sel(d, phi_free(S)) + off;
+    const float2 *ph = phi2_sel(d, S->phi_cur) + off;
+    const float2 *qh = phi2_sel(d, S->phi_prev) + off;
+    const float2 *uh = phi2_sel(d, S->phi_prev2) + off;
+    const float2 *vh = phi2_sel(d, S->phi_prev3) + off;
+    float2 *nh = phi2_sel(d, phi_free(S)) + off;
     const uint32_t *code = d.code + off;
     const float4 *TR4 = (const float4 *)(F.TR + (long long)TR32 * f->g_off);
-    const float *Po = (cur ? F.P[1][0] : F.P[0][0]) + off;   // the six fields of a set at q * fs
-    float *Pn = (cur ? F.P[0][0] : F.P[1][0]) + off;
+    const float2 *Po = pairs32(F, cur) + off;   // the three pairs of a set at j * fs
+    float2 *Pn = pairs32(F, cur ^ 1) + off;
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
+    (void)lo;
 
     // copies of plane p (planes are issued in order, p = zlo, zlo + 1, ...)
     long long own_o = g.own_pl + (long long)zlo * g.plane, halo_o = g.halo_pl + (long long)zlo * g.plane;
@@ -195,20 +212,14 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         if (p <= zhi) {
             if (g.valid) {
                 #pragma unroll
-                for (int q = 0; q < 6; ++q) cp4(st + 2 * ((q >> 1) * SPL + g.own_slot) + (q & 1), Po + q * fs + own_o);
-                if (dep) {
-                    cp4(st + 2 * (3 * SPL + g.own_slot), ph + own_o);
-                    cp4(st + 2 * (3 * SPL + g.own_slot) + 1, ph + lo + own_o);
-                }
+                for (int j = 0; j < 3; ++j) cp8(st + 2 * (j * SPL + g.own_slot), Po + j * fs + own_o);
+                if (dep) cp8(st + 2 * (3 * SPL + g.own_slot), ph + own_o);
                 cp4(st + 8 * SPL + threadIdx.x, code + own_o);
             }
             if (g.halo) {
                 #pragma unroll
-                for (int q = 0; q < 6; ++q) cp4(st + 2 * ((q >> 1) * SPL + g.halo_slot) + (q & 1), Po + q * fs + halo_o);
-                if (dep) {
-                    cp4(st + 2 * (3 * SPL + g.halo_slot), ph + halo_o);
-                    cp4(st + 2 * (3 * SPL + g.halo_slot) + 1, ph + lo + halo_o);
-                }
+                for (int j = 0; j < 3; ++j) cp8(st + 2 * (j * SPL + g.halo_slot), Po + j * fs + halo_o);
+                if (dep) cp8(st + 2 * (3 * SPL + g.halo_slot), ph + halo_o);
             }
         }
         cp_commit();
@@ -230,9 +241,9 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         if (!g.valid) continue;
         // older potentials for the warm start (consumed after the step's arithmetic)
         df wq{0.f, 0.f}, wu{0.f, 0.f}, wv{0.f, 0.f};
-        if (dep && warm >= 1) wq = df{qh[o], qh[lo + o]};
-        if (dep && warm >= 2) wu = df{uh[o], uh[lo + o]};
-        if (dep && warm >= 3) wv = df{vh[o], vh[lo + o]};
+        if (dep && warm >= 1) wq = ld_df(qh + o);
+        if (dep && warm >= 2) wu = ld_df(uh + o);
+        if (dep && warm >= 3) wv = ld_df(vh + o);
         const float *sk = ring + ri.s * T32_STAGE;
         const float *su = ring + ri.up(k == nz - 1) * T32_STAGE, *sd = ring + ri.dn(k == 0) * T32_STAGE;
         const uint32_t c = ((const uint32_t *)sk)[8 * SPL + threadIdx.x];
@@ -267,12 +278,11 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
         tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
                     pMZl, pSZl);
         #pragma unroll
-        for (int q = 0; q < 6; ++q) Pn[q * fs + o] = pn[q];
+        for (int j = 0; j < 3; ++j) Pn[j * fs + o] = make_float2(pn[2 * j], pn[2 * j + 1]);
         if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
         if (dep) {
             const df w = extrap_phi(warm, a0, wq, wu, wv);
-            nh[o] = w.h;
-            nh[lo + o] = w.l;
+            nh[o] = make_float2(w.h, w.l);
         }
     }
     cp_wait<0>();
@@ -293,18 +303,16 @@ static __global__ void __launch_bounds__(NT) k_extrap(Dev d)
     const Geom g = make_geom(f, it.y, it.z);
     if (!f->dep_flag || !g.valid) return;
     const SolveDev *S = d.solve + it.x;
-    const long long off = f->off, lo = d.ncells;
-    const float *ph = (const float *)phi_sel(d, S->phi_cur) + off;
-    const float *qh = (const float *)phi_sel(d, S->phi_prev) + off;
-    const float *uh = (const float *)phi_sel(d, S->phi_prev2) + off;
-    const float *vh = (const float *)phi_sel(d, S->phi_prev3) + off;
-    float *nh = (float *)phi_sel(d, phi_free(S)) + off;
+    const long long off = f->off;
+    const float2 *ph = phi2_sel(d, S->phi_cur) + off;
+    const float2 *qh = phi2_sel(d, S->phi_prev) + off;
+    const float2 *uh = phi2_sel(d, S->phi_prev2) + off;
+    const float2 *vh = phi2_sel(d, S->phi_prev3) + off;
+    float2 *nh = phi2_sel(d, phi_free(S)) + off;
     for (int k = z0; k < z1; ++k) {
         const long long o = g.own_pl + (long long)k * g.plane;
-        const df w = extrap_phi(f->warm, df{ph[o], ph[lo + o]}, df{qh[o], qh[lo + o]}, df{uh[o], uh[lo + o]},
-                                df{vh[o], vh[lo + o]});
-        nh[o] = w.h;
-        nh[lo + o] = w.l;
+        const df w = extrap_phi(f->warm, ld_df(ph + o), ld_df(qh + o), ld_df(uh + o), ld_df(vh + o));
+        nh[o] = make_float2(w.h, w.l);
     }
 }
 
@@ -448,8 +456,11 @@ __device__ __forceinline__ void refine_partials(const Dev &d, float (&acc)[3], d
     block_partial32<3>(d, acc, sRed);
 }
 
+// Stage layout (floats): x = phi (+ dx) as one (hi, lo) float2 plane, dx,
+// the (Pmx, Pmy) pair plane, Pmz (own), then the general-eps code and D^-1.
+// The update pass keeps the old r of the own cell in the Pmz slot.
 template <bool UNI> struct R32Lay {
-    static constexpr int FH = 0, FL = SPL, DX = 2 * SPL, PX = 3 * SPL, PY = 4 * SPL, PZ = 5 * SPL;
+    static constexpr int FX = 0, DX = 2 * SPL, PA = 3 * SPL, PZ = 5 * SPL;
     static constexpr int CODE = 5 * SPL + NT, DINV = 6 * SPL + NT;   // general eps only
     static constexpr int STAGE = UNI ? 5 * SPL + NT : 6 * SPL + 2 * NT;
 };
@@ -484,11 +495,12 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
     const bool apply = S->refine > 0;                   // later pass: x = phi + dx; first: the warm start
     const bool upd = UNI && apply && S->upd && f->upd_ok;   // r <- r - A dx (after the direct solve, one eps)
     const int cur = d.ctl->cur, fr = phi_free(S);
-    const long long off = f->off, lo = d.ncells, fs = d.ncells;
-    const float *xh = (const float *)phi_sel(d, apply ? S->phi_cur : fr) + off;
-    float *nh = (float *)phi_sel(d, fr) + off;
+    const long long off = f->off, fs = d.ncells;
+    const float2 *xh = phi2_sel(d, apply ? S->phi_cur : fr) + off;
+    float2 *nh = phi2_sel(d, fr) + off;
     const float *dx = F.x + off;
-    const float *Pm = (cur ? F.P[0][0] : F.P[1][0]) + off;   // the new Pm: x, y, z at 0, fs, 2 fs
+    const float2 *PA = pairs32(F, cur ^ 1) + off;            // the new (Pmx, Pmy)
+    const float *PZ = (const float *)(PA + fs);              // the new Pmz: .x of the (Pmz, Psx) pairs
     const uint32_t *code = d.code + off;
     const float *dinv = F.dinv + off;
     float *r = F.r + off;
@@ -502,31 +514,26 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
             if (upd) {
                 // update pass: dx with its halo; phi and the old r of the own cell
                 if (g.valid) {
-                    cp4(st + L::FH + so, xh + own_o);
-                    cp4(st + L::FL + so, xh + lo + own_o);
+                    cp8(st + L::FX + 2 * so, xh + own_o);
                     cp4(st + L::DX + so, dx + own_o);
-                    cp4(st + L::PX + so, r + own_o);
+                    cp4(st + L::PZ + threadIdx.x, r + own_o);
                 }
                 if (g.halo) cp4(st + L::DX + sh, dx + halo_o);
             } else {
                 if (g.valid) {
-                    cp4(st + L::FH + so, xh + own_o);
-                    cp4(st + L::FL + so, xh + lo + own_o);
+                    cp8(st + L::FX + 2 * so, xh + own_o);
                     if (apply) cp4(st + L::DX + so, dx + own_o);
-                    cp4(st + L::PX + so, Pm + own_o);
-                    cp4(st + L::PY + so, Pm + fs + own_o);
-                    cp4(st + L::PZ + threadIdx.x, Pm + 2 * fs + own_o);
+                    cp8(st + L::PA + 2 * so, PA + own_o);
+                    cp4(st + L::PZ + threadIdx.x, PZ + 2 * own_o);
                     if (!UNI) {
                         cp4(st + L::CODE + so, code + own_o);
                         cp4(st + L::DINV + threadIdx.x, dinv + own_o);
                     }
                 }
                 if (g.halo) {
-                    cp4(st + L::FH + sh, xh + halo_o);
-                    cp4(st + L::FL + sh, xh + lo + halo_o);
+                    cp8(st + L::FX + 2 * sh, xh + halo_o);
                     if (apply) cp4(st + L::DX + sh, dx + halo_o);
-                    cp4(st + L::PX + sh, Pm + halo_o);
-                    cp4(st + L::PY + sh, Pm + fs + halo_o);
+                    cp8(st + L::PA + 2 * sh, PA + halo_o);
                     if (!UNI) cp4(st + L::CODE + sh, code + halo_o);
                 }
             }
@@ -551,9 +558,12 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
         const float *su = ring + ri.up(k == nz - 1) * L::STAGE, *sd = ring + ri.dn(k == 0) * L::STAGE;
         auto D = [&](const float *st, int s) { return st[L::DX + s]; };
         auto X = [&](const float *st, int s) {        // x = phi (+ dx on later passes)
-            const df p{st[L::FH + s], st[L::FL + s]};
+            const float2 v = ((const float2 *)(st + L::FX))[s];
+            const df p{v.x, v.y};
             return apply ? df_add_f(p, D(st, s)) : p;
         };
+        auto PAx = [&](const float *st, int s) { return ((const float2 *)(st + L::PA))[s].x; };
+        auto PAy = [&](const float *st, int s) { return ((const float2 *)(st + L::PA))[s].y; };
         auto M = [&](const float *st, int s) { return UNI ? 0 : code_mat(((const uint32_t *)st)[L::CODE + s]); };
         RCell c;
         c.xc = X(sk, s0);
@@ -565,19 +575,16 @@ __global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
         } else {
             c.xe = X(sk, s0 + 1); c.xw = X(sk, s0 - 1); c.xn = X(sk, s0 + SX); c.xs = X(sk, s0 - SX);
             c.xu = X(su, s0); c.xd = X(sd, s0);
-            c.pxe = sk[L::PX + s0 + 1]; c.pxw = sk[L::PX + s0 - 1];
-            c.pyn = sk[L::PY + s0 + SX]; c.pys = sk[L::PY + s0 - SX];
+            c.pxe = PAx(sk, s0 + 1); c.pxw = PAx(sk, s0 - 1);
+            c.pyn = PAy(sk, s0 + SX); c.pys = PAy(sk, s0 - SX);
             c.pzu = su[L::PZ + tz]; c.pzd = sd[L::PZ + tz];
         }
         // identity rows: the Dirichlet planes, or the Neumann pin
         const bool ident = rc.neu ? (long long)k * g.plane == pin : (k == 0 || k == nz - 1);
         float rv;
-        refine_cell<UNI>(rc, k, ident, upd, c, upd ? sk[L::PX + s0] : 0.f, UNI ? 0.f : sk[L::DINV + tz], rv, acc);
+        refine_cell<UNI>(rc, k, ident, upd, c, upd ? sk[L::PZ + tz] : 0.f, UNI ? 0.f : sk[L::DINV + tz], rv, acc);
         r[o] = rv;
-        if (apply) {
-            nh[o] = c.xc.h;
-            nh[lo + o] = c.xc.l;
-        }
+        if (apply) nh[o] = make_float2(c.xc.h, c.xc.l);
     }
     cp_wait<0>();
     refine_partials(d, acc, sRed);

@@ -74,6 +74,7 @@ def _bind():
                                        _dp, _ip, C.POINTER(C.c_int), _dp, _ip, C.POINTER(C.c_int)]
     L.cmsl_voronoi_columnar.argtypes = [C.c_int] * 4 + [C.c_uint64, _ip, _dp, _dp]
     L.cmsl_voronoi_columnar_gpu.argtypes = [C.c_int] * 4 + [C.c_uint64, _ip, _dp, _dp]
+    L.cmsl_interface_flags_gpu.argtypes = [C.c_int] * 4 + [C.c_void_p] * 4
     L.cmsl_checkpoint_write.argtypes = [C.c_char_p] + [C.c_int] * 5 + [C.c_double, C.c_double, C.POINTER(_dp),
                                                                        C.POINTER(_dp)]
     L.cmsl_checkpoint_read.argtypes = [C.c_char_p] + [C.c_int] * 3 + [C.POINTER(C.c_int), C.POINTER(C.c_int),

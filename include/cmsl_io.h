@@ -104,6 +104,13 @@ cmsl_status cmsl_assign_materials(int nx, int ny, int nz, int n_grains, const in
 cmsl_status cmsl_interface_flags(int nx, int ny, int nz, const int32_t *omega, const int32_t *grain_mat,
                                  int32_t *flag);
 
+/* build_interface_flag (main.cu:13-52) on DEVICE arrays (omega[N],
+ * grain_mat[n_grains], flags[N]), e.g. a grain map generated on the GPU;
+ * grain ids outside [0, n_grains) count as not FE; runs on `stream` without
+ * synchronising. */
+cmsl_status cmsl_interface_flags_gpu(int nx, int ny, int nz, int n_grains, const int32_t *omega_dev,
+                                     const int32_t *grain_mat_dev, int32_t *flags_dev, void *stream);
+
 /* The field schedule of Evolve (evolve.cu:123-409): Ez[s] per step and
  * row[s] (output row index or -1); row_E/row_count per row.  n_periods = 1 is
  * the reference's peloop < 2.  Pass NULL arrays to query the sizes. */

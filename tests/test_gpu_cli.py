@@ -139,3 +139,47 @@ def test_gpu_voronoi_equals_host(cli, dims):
     a = fm.voronoi_columnar(nx, ny, nz, ng, seed)
     b = fm.voronoi_columnar(nx, ny, nz, ng, seed, device=True)
     assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+@pytest.mark.parametrize("shape", [(24, 20, 8), (64, 48, 12), (7, 5, 3)])
+def test_interface_flags_on_device_match_reference_algorithm(cli, shape):
+    """build_interface_flag (main.cu:13-52) on device arrays, bitwise against
+    the oracle's restatement, on layered maps with FE / AFE / DE grains and
+    a map with grain ids outside the table (counted as not FE)."""
+    import torch
+    import oracle
+    from tests.films import voronoi_columnar
+    nx, ny, nz = shape
+    rng = np.random.default_rng(sum(shape))
+    ng = 9
+    om = voronoi_columnar(nx, ny, nz, ng, rng)
+    kk = np.repeat(np.arange(nz), nx * ny)
+    om = np.where(kk % 3 == 1, (om + 4) % ng, om).astype(np.int32)      # z interfaces between grains
+    gm = rng.choice([0, 1, 2], size=ng, p=[0.3, 0.5, 0.2]).astype(np.int32)
+    gm[0] = 1
+    want = oracle.load().interface_flags(nx, ny, nz, om, gm)
+    dev = torch.device("cuda", 0)
+    d_om = torch.as_tensor(om, device=dev)
+    d_gm = torch.as_tensor(gm, device=dev)
+    d_fl = torch.full((om.size,), -7, dtype=torch.int32, device=dev)
+    L = fm._bind()
+    torch.cuda.synchronize()
+    fm.check(L.cmsl_interface_flags_gpu(nx, ny, nz, ng, d_om.data_ptr(), d_gm.data_ptr(), d_fl.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert np.array_equal(d_fl.cpu().numpy(), want)
+    # ids outside [0, ng): never read beyond the table, counted as not FE
+    om2 = om.copy()
+    om2[nx * ny * (nz // 2)] = ng + 5
+    om2[nx * ny * (nz // 2) + 1] = -1
+    d_om2 = torch.as_tensor(om2, device=dev)
+    fm.check(L.cmsl_interface_flags_gpu(nx, ny, nz, ng, d_om2.data_ptr(), d_gm.data_ptr(), d_fl.data_ptr(), None))
+    torch.cuda.synchronize()
+    got = d_fl.cpu().numpy()
+    gmx = np.concatenate([gm, [-1]])
+    mat = np.where((om2 >= 0) & (om2 < ng), gmx[np.clip(om2, 0, ng)], -1)
+    exp = np.zeros(om2.size, np.int32)
+    plane = nx * ny
+    for i in range(plane, om2.size - plane):
+        if mat[i] == 1:
+            exp[i] = int(mat[i + plane] != 1 or mat[i - plane] != 1)
+    assert np.array_equal(got, exp)
