@@ -13,7 +13,10 @@
 
 namespace cmsl {
 
-constexpr unsigned TMA_SPIN_LIMIT = 1u << 22;
+// A wait gives up after TMA_SPIN_LIMIT tries of at most TMA_SUSPEND_NS each
+// (about one second).
+constexpr unsigned TMA_SPIN_LIMIT = 1u << 20;
+constexpr unsigned TMA_SUSPEND_NS = 1000;
 constexpr int TMA_ERR_WAIT = 1;          // bit in the device error word: a tensor-copy wait gave up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -49,11 +52,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     asm volatile(
         "{\n"
         ".reg .pred p;\n"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         "selp.u32 %0, 1, 0, p;\n"
         "}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "n"(TMA_SUSPEND_NS)
         : "memory");
     return ok != 0;
 }
