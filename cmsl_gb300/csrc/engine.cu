@@ -1180,6 +1180,16 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     TRY(e->alloc((void **)&e->d_counter, sizeof(unsigned int) * 4));
     TRY(e->alloc((void **)&e->d_err, sizeof(int)));
     TRY(e->alloc((void **)&e->d_solve, sizeof(SolveDev) * n));
+    {
+        // every film's potential rotation valid from creation on (set_state
+        // sets the same): FP32_REFINED buffers 0..3 in use, 4 free
+        std::vector<SolveDev> S0((size_t)n);
+        for (SolveDev &x : S0) {
+            x = SolveDev{};
+            if (e->precision != CMSL_FP64) { x.phi_prev = 1; x.phi_prev2 = 2; x.phi_prev3 = 3; }
+        }
+        CK(cudaMemcpy(e->d_solve, S0.data(), sizeof(SolveDev) * n, cudaMemcpyHostToDevice));
+    }
     TRY(e->alloc((void **)&e->d_ctl, sizeof(Ctl)));
     TRY(ensure_schedule(e, 16, 16));
 

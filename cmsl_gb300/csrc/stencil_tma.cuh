@@ -54,6 +54,15 @@ __device__ __forceinline__ NbOff nb_off(int esz)
     return o;
 }
 
+// Map sets by buffer index, clamped as phi_sel clamps its pointers (any
+// index outside 0..4 selects buffer 4), so a stale or unset solver slot can
+// never select memory outside the film's table.
+__device__ __forceinline__ const CUtensorMap *phi_maps(const FilmMaps *M, int i)
+{
+    return M->phi[(i >= 0 && i < 5) ? i : 4];
+}
+__device__ __forceinline__ const CUtensorMap *p_maps(const FilmMaps *M, int set) { return M->P[set & 1]; }
+
 // Appends the five boxes of one field region (base: byte offset in the
 // stage) for tile (x0, y0); q is the 4D map's field index or -1 (3D map).
 struct OpBuilder {
@@ -173,8 +182,8 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
     R.tx = (uint32_t)(3 * REG2 + (dep ? REG2 : 0) + BODY1);
     if (threadIdx.x == 0) {
         OpBuilder b{ops, 0, x0, y0, nx, ny};
-        for (int j = 0; j < 3; ++j) b.region(M->P[cur], j * REG2, j, 8);
-        if (dep) b.region(M->phi[pcur], TT_PHI, -1, 8);
+        for (int j = 0; j < 3; ++j) b.region(p_maps(M, cur), j * REG2, j, 8);
+        if (dep) b.region(phi_maps(M, pcur), TT_PHI, -1, 8);
         b.body(M->code, TT_CODE - 4 * TR_BODY, -1, 4);
     }
     __syncthreads();
@@ -303,14 +312,14 @@ __global__ void __launch_bounds__(NT, 4) k_refine32t(Dev d, Fields<float> F)
     if (threadIdx.x == 0) {
         OpBuilder b{ops, 0, x0, y0, nx, ny};
         if (upd) {
-            b.body(M->phi[xb], RT_X, -1, 8);
+            b.body(phi_maps(M, xb), RT_X, -1, 8);
             b.region(M->x, RT_DX, -1, 4);
             b.add(&M->r, RT_PZ, x0, y0, -1);
         } else {
-            b.region(M->phi[xb], RT_X, -1, 8);
+            b.region(phi_maps(M, xb), RT_X, -1, 8);
             if (apply) b.region(M->x, RT_DX, -1, 4);
-            b.region(M->P[cur ^ 1], RT_PA, 0, 8);
-            b.add(&M->P[cur ^ 1][TM_BODY], RT_PZ, x0, y0, 1);
+            b.region(p_maps(M, cur ^ 1), RT_PA, 0, 8);
+            b.add(&p_maps(M, cur ^ 1)[TM_BODY], RT_PZ, x0, y0, 1);
             if (!UNI) {
                 b.region(M->code, RT_CODE, -1, 4);
                 b.add(&M->dinv, RT_DINV, x0, y0, -1);

@@ -122,3 +122,41 @@ def test_autograd_function_landau_coefficients(gpu):
         tm[i] -= h
         fd[i] = (fit.loss(tp) - fit.loss(tm)) / (2 * h)
     assert (np.abs(g - fd) <= 1e-3 * np.abs(fd) + 1e-6 * np.abs(fd).max()).all(), (g, fd)
+
+
+def test_adjoint_matches_oracle_finite_differences(gpu):
+    """An FP64 reference gradient independent of this library: central
+    differences of the loss computed entirely by the oracle (the CPU FP64
+    restatement of the reference kernels and Depol_field PCG, solved to
+    1e-13), against the adjoint on the GPU.  Same tolerance as the GPU
+    finite differences above."""
+    f, P, Ez, rows = _problem(n=30, seed=62)
+    orc = oracle.load()
+    mats0 = np.array(f.mats, np.float64)
+
+    def oloss(mats, target):
+        f2 = dataclasses.replace(f, mats=np.asarray(mats, np.float64))
+        _, _, _, st, _, rc = orc.run(f2, P, np.zeros(f.N), Ez, rows)
+        assert rc == 0
+        d = st[:, 0] - target
+        return float(np.mean(d * d))
+
+    pert = mats0.copy()
+    pert[:, [0, 1, 2, 5]] *= 1.03
+    f2 = dataclasses.replace(f, mats=pert)
+    _, _, _, st, _, rc = orc.run(f2, P, np.zeros(f.N), Ez, rows)
+    assert rc == 0
+    target = st[:, 0].copy()
+    L, g = _grad(gpu, f, P, Ez, rows, target, K=10)
+    assert L == pytest.approx(oloss(mats0, target), rel=1e-9, abs=0.0)
+    fd = np.zeros((3, 5))
+    for m in range(3):
+        for p, col in enumerate(COLS):
+            h = 1e-5 * max(abs(mats0[m, col]), 1.0)
+            mp, mm = mats0.copy(), mats0.copy()
+            mp[m, col] += h
+            mm[m, col] -= h
+            fd[m, p] = (oloss(mp, target) - oloss(mm, target)) / (2 * h)
+    scale = np.abs(fd).max()
+    assert scale > 0
+    assert (np.abs(g - fd) <= 1e-3 * np.abs(fd) + 1e-6 * scale).all(), (g, fd)

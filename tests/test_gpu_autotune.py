@@ -55,3 +55,34 @@ def test_batch_autotune(gpu):
              enumerate([(32, 16, 6), (24, 20, 12)])]
     with gpu.Batch.from_oracle_films(films) as b:
         assert b.autotune() in (4, 8, 12)
+
+
+@pytest.mark.parametrize("inner", ["direct", "pcg"])
+def test_autotune_before_any_state_on_tensor_copy_films(gpu, inner):
+    """A film with full 32 x 8 tiles takes the tensor-copy (TMA) stencil
+    passes; autotuning it straight after creation, before any set_state, runs
+    those passes on the creation-time solver slots.  The run that follows
+    matches the oracle (FP32-refined against FP64 solved to 1e-12)."""
+    from cmsl_gb300 import workloads as wl
+    w = wl.hzo_film("tma_64x32x10", 64, 32, 10, 7, 9, 0.4, E_amp_MVcm=4.0, steps_per_period=400)
+    mats = np.array(w.mats, copy=True)
+    if inner == "pcg":
+        mats[:, 7] = [40.0, 30.0, 15.0]
+    orc = oracle.load()
+    f = oracle.Film(nx=w.nx, ny=w.ny, nz=w.nz, del_h=w.del_h, del_t=w.del_t, omega=w.omega,
+                    grain_mat=w.grain_mat, TR=w.TR, mats=mats,
+                    is_interface=orc.interface_flags(w.nx, w.ny, w.nz, w.omega, w.grain_mat),
+                    dep_flag=1, eps_0_nd=w.eps_0_nd)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    n = 8
+    Ez = w.sched.Ez[:n] * 40.0
+    Pw, _, _, _, _, rc = orc.run(f, w.P_init, np.zeros(w.N), Ez)
+    assert rc == 0
+    with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED) as g:
+        assert g.inner_solver == (gpu.INNER_DIRECT if inner == "direct" else gpu.INNER_PCG)
+        assert g.autotune() in (4, 8, 10)
+        g.set_state(w.P_init)
+        g.run(Ez)
+        Pg, _ = g.get_state()
+    err = max(np.abs(a - b).max() / np.abs(b).max() for a, b in zip(Pg, Pw))
+    assert err <= 2e-5
