@@ -363,7 +363,9 @@ def run_ours(args):
     mode = "fp64" if fp64 else "fp32"
     w = wl.config(args.config)
     film = cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, w.mats, **w.film_kwargs(), **film_kw(cg, fp64))
-    zchunk = 0 if args.no_autotune else film.autotune()
+    if not args.no_autotune:
+        film.autotune()
+    tile_cfg = film.tile_config()
     film.set_state(w.P_init)
     K, W = args.steps, args.warmup
     n_sched = w.sched.n_steps
@@ -483,8 +485,8 @@ def run_ours(args):
             "config": {"workload": w.name, "cells": w.N, "grid": [w.nx, w.ny, w.nz],
                        "precision": "fp64" if fp64 else "fp32-refined (fp64 phi, refine to 1e-8)",
                        "pcg": "||b-A phi|| <= 1e-8 ||b||", "parallelism": "replicas" if world > 1 else "single",
-                       "tile": {"x": 32, "y": 8, "z_chunk": zchunk,
-                                "chosen_by": "heuristic" if args.no_autotune else "autotuner (cmsl_film_autotune)"},
+                       "tile": dict(tile_cfg, chosen_by="heuristic" if args.no_autotune
+                                    else "autotuner (cmsl_film_autotune)"),
                        "timing": "%d timed regions of K steps, each bracketed by barrier + synchronize and timed "
                                  "with CUDA events on the launch stream; value from the median region" % R,
                        "l2": "no flush: per-step state %.0f MB > 129 MB L2" % (film_bytes(w, fp64) / 1e6)},
@@ -531,7 +533,9 @@ def run_batch(args):
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     b = cg.Batch(descs)
-    zchunk = 0 if args.no_autotune else b.autotune()
+    if not args.no_autotune:
+        b.autotune()
+    b_tile = b.tile_config()
     for i, w in enumerate(ws):
         b.set_state(i, w.P_init)
     with torch.cuda.stream(stream):
@@ -634,7 +638,8 @@ def run_batch(args):
         "config": {"workload": "c3_ensemble64", "films": len(ws), "cells": cells,
                    "precision": "fp32-refined (fp64 phi, refine to 1e-8)", "pcg": "||b-A phi|| <= 1e-8 ||b|| per film",
                    "parallelism": "single", "l2": "no flush: batch state > 129 MB L2",
-                   "tile": {"x": 32, "y": 8, "z_chunk": zchunk, "chosen_by": "heuristic" if args.no_autotune else "autotuner (cmsl_batch_autotune)"}},
+                   "tile": dict(b_tile, chosen_by="heuristic" if args.no_autotune
+                                else "autotuner (cmsl_batch_autotune)")},
         "sequential": {"value": seq, "unit": "cell-steps/s", "ms_per_step": seq_ms / K,
                        "speedup_batch_over_sequential": value / seq},
         "pcg_iters_per_step_max_film": n_it, "refine_passes_per_step_max_film": n_ref,

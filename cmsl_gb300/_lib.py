@@ -80,6 +80,7 @@ def lib() -> C.CDLL:
     L.cmsl_film_device_bytes.argtypes = [fp, C.POINTER(C.c_size_t)]
     L.cmsl_film_inner_solver.argtypes = [fp, C.POINTER(C.c_int)]
     L.cmsl_film_autotune.argtypes = [fp, C.POINTER(C.c_int32)]
+    L.cmsl_film_tile_config.argtypes = [fp, C.POINTER(C.c_int32)]
     L.cmsl_film_checkpoint_write.argtypes = [fp, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double]
     L.cmsl_film_checkpoint_read.argtypes = [fp, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp, _dp]
     L.cmsl_film_loop_gradient.argtypes = [fp, C.c_int, _dp, _ip, _dp, C.c_int, C.c_int, _dp, _dp]
@@ -95,6 +96,7 @@ def lib() -> C.CDLL:
     L.cmsl_batch_device_bytes.argtypes = [fp, C.POINTER(C.c_size_t)]
     L.cmsl_batch_inner_solver.argtypes = [fp, C.POINTER(C.c_int)]
     L.cmsl_batch_autotune.argtypes = [fp, C.POINTER(C.c_int32)]
+    L.cmsl_batch_tile_config.argtypes = [fp, C.POINTER(C.c_int32)]
     L.cmsl_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
     L.cmsl_host_free.argtypes = [C.c_void_p]
     L.cmsl_film_depol_device.argtypes = [fp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -119,11 +121,12 @@ EXPORTS = [
     "cmsl_film_tdgl_step", "cmsl_film_depol", "cmsl_film_depol_device", "cmsl_film_apply_operator",
     "cmsl_film_efield",
     "cmsl_film_diag_inv", "cmsl_film_time_kernels", "cmsl_film_device_bytes", "cmsl_film_inner_solver", "cmsl_film_autotune",
+    "cmsl_film_tile_config",
     "cmsl_film_checkpoint_write",
     "cmsl_film_checkpoint_read", "cmsl_film_loop_gradient",
     "cmsl_batch_create",
     "cmsl_batch_destroy", "cmsl_batch_set_state", "cmsl_batch_get_state", "cmsl_batch_run", "cmsl_batch_sync",
     "cmsl_batch_get_rows", "cmsl_batch_get_iters", "cmsl_batch_time_kernels", "cmsl_batch_device_bytes",
-    "cmsl_batch_inner_solver", "cmsl_batch_autotune",
+    "cmsl_batch_inner_solver", "cmsl_batch_autotune", "cmsl_batch_tile_config",
     "cmsl_depol_solve_noalloc",
 ]

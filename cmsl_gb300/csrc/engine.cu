@@ -142,8 +142,13 @@ cmsl_status set_items(Engine *e, int zc)
     return CMSL_OK;
 }
 
-// Tile shapes tuned in this process, by film-shape class.
-std::map<std::string, int> g_tuned;
+// Tile shapes tuned in this process, by film-shape class: the z chunk and
+// the staging of the TDGL and of the residual passes.
+struct Tuned {
+    int zchunk;
+    bool tma_tdgl, tma_refine;
+};
+std::map<std::string, Tuned> g_tuned;
 std::mutex g_tuned_mu;
 
 std::string shape_key(const Engine *e)
@@ -1052,7 +1057,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         int zc = 0;
         std::lock_guard<std::mutex> lk(g_tuned_mu);
         const auto hit = g_tuned.find(shape_key(e));
-        if (hit != g_tuned.end()) zc = hit->second;
+        if (hit != g_tuned.end()) zc = hit->second.zchunk;
         TRY(set_items(e, zc));
     }
     if (e->precision == CMSL_FP64) TRY(upload_TR<double>(e, descs, n));
@@ -1203,21 +1208,28 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         const char *nt = getenv("CMSL_NO_TMA");
         e->tma = !(nt && atoi(nt) != 0);
         for (int fi = 0; fi < n; ++fi) e->tma = e->tma && e->fh[fi].nx % TX == 0 && e->fh[fi].ny % TY == 0;
+        e->refine_fn_c = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
+        e->refine_smem_c = uni ? r32_smem<true>() : r32_smem<false>();
+        e->tdgl_fn_c = (void *)k_tdgl32<T32_NS>;
+        e->tdgl_smem_c = T32_SMEM;
+        CK(cudaFuncSetAttribute(e->refine_fn_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem_c));
+        CK(cudaFuncSetAttribute(e->tdgl_fn_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem_c));
         if (e->tma) {
             TRY(make_maps(e));
-            e->refine_fn = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
-            e->refine_smem = uni ? rt_smem<true>() : rt_smem<false>();
-            e->tdgl_fn = (void *)k_tdgl32t<TT_NS>;
-            e->tdgl_smem = TT_SMEM;
-        } else {
-            e->refine_fn = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
-            e->refine_smem = uni ? r32_smem<true>() : r32_smem<false>();
-            e->tdgl_fn = (void *)k_tdgl32<T32_NS>;
-            e->tdgl_smem = T32_SMEM;
+            e->refine_fn_t = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
+            e->refine_smem_t = uni ? rt_smem<true>() : rt_smem<false>();
+            e->tdgl_fn_t = (void *)k_tdgl32t<TT_NS>;
+            e->tdgl_smem_t = TT_SMEM;
+            CK(cudaFuncSetAttribute(e->refine_fn_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem_t));
+            CK(cudaFuncSetAttribute(e->tdgl_fn_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem_t));
         }
         e->refine_nt = e->tdgl_nt = NT;
-        CK(cudaFuncSetAttribute(e->refine_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem));
-        CK(cudaFuncSetAttribute(e->tdgl_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem));
+        e->stage(true, true);
+        {
+            std::lock_guard<std::mutex> lk(g_tuned_mu);
+            const auto hit = g_tuned.find(shape_key(e));
+            if (hit != g_tuned.end()) e->stage(hit->second.tma_tdgl, hit->second.tma_refine);
+        }
     }
     const Dev d = e->dev(0);
     if (e->precision == CMSL_FP64) k_dinv<double><<<(int)e->items.size(), NT>>>(d, (double *)e->d_dinv);
@@ -1535,25 +1547,48 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
     std::vector<int> cands;
     for (int c = ZCHUNK_MIN; c < maxnz; c *= 2) cands.push_back(c);
     cands.push_back(maxnz);
-    int best = 0;
+    // per z chunk: both stagings of the TDGL and of the residual passes where
+    // the tensor copies apply (the two kernels are independent, so each takes
+    // its faster staging)
+    Tuned best{0, e->tma_tdgl, e->tma_refine};
     double best_ms = 0.0;
     for (int c : cands) {
         TRY(set_items(e, c));
-        double ms[4] = {0, 0, 0, 0};
-        TRY(time_kernels(e, 5, nullptr, ms));
-        double t = ms[0] + ms[1];                          // TDGL step + first pass (FP32) / set-up (FP64)
-        if (e->precision == CMSL_FP64) t += ms[2] + ms[3];
-        else if (e->spectral) t += ms[3];                  // update pass
-        else if (!e->persistent) t += ms[2] + ms[3];       // two-kernel PCG
-        if (best == 0 || t < best_ms) { best = c; best_ms = t; }
+        double tt[2] = {0.0, 0.0}, tr[2] = {0.0, 0.0}, rest = 0.0;
+        const int nst = e->tma ? 2 : 1;
+        for (int v = 0; v < nst; ++v) {
+            if (e->precision != CMSL_FP64) e->stage(v == 0, v == 0);
+            double ms[4] = {0, 0, 0, 0};
+            TRY(time_kernels(e, 5, nullptr, ms));
+            tt[v] = ms[0];                                  // TDGL step
+            tr[v] = ms[1];                                  // first pass (FP32) / set-up (FP64)
+            if (e->precision == CMSL_FP64) rest = ms[2] + ms[3];
+            else if (e->spectral) tr[v] += ms[3];           // update pass
+            else if (!e->persistent) rest = ms[2] + ms[3];  // two-kernel PCG
+        }
+        const int vt = (nst == 2 && tt[1] < tt[0]) ? 1 : 0, vr = (nst == 2 && tr[1] < tr[0]) ? 1 : 0;
+        const double t = tt[vt] + tr[vr] + rest;
+        if (best.zchunk == 0 || t < best_ms) {
+            best = Tuned{c, e->tma && vt == 0, e->tma && vr == 0};
+            best_ms = t;
+        }
     }
-    TRY(set_items(e, best));
+    TRY(set_items(e, best.zchunk));
+    if (e->precision != CMSL_FP64) e->stage(best.tma_tdgl, best.tma_refine);
     {
         std::lock_guard<std::mutex> lk(g_tuned_mu);
         g_tuned[shape_key(e)] = best;
     }
-    if (zchunk) *zchunk = best;
+    if (zchunk) *zchunk = best.zchunk;
     return CMSL_OK;
+}
+
+void tile_config(const Engine *e, int32_t cfg[4])
+{
+    cfg[0] = TX;
+    cfg[1] = TY;
+    cfg[2] = e->zchunk;
+    cfg[3] = (e->tma_tdgl ? 1 : 0) | (e->tma_refine ? 2 : 0);
 }
 
 size_t device_bytes(const Engine *e)
@@ -1876,6 +1911,13 @@ cmsl_status cmsl_film_autotune(cmsl_film *f, int32_t *zchunk)
     return autotune(f, zchunk);
 }
 
+cmsl_status cmsl_film_tile_config(cmsl_film *f, int32_t cfg[4])
+{
+    if (!f || !cfg) return fail(CMSL_ERR_ARG, "NULL argument");
+    tile_config(f, cfg);
+    return CMSL_OK;
+}
+
 cmsl_status cmsl_film_device_bytes(cmsl_film *f, size_t *bytes)
 {
     if (!f || !bytes) return fail(CMSL_ERR_ARG, "NULL argument");
@@ -1958,6 +2000,13 @@ cmsl_status cmsl_batch_autotune(cmsl_batch *b, int32_t *zchunk)
 {
     if (!b) return fail(CMSL_ERR_ARG, "NULL batch");
     return autotune(b, zchunk);
+}
+
+cmsl_status cmsl_batch_tile_config(cmsl_batch *b, int32_t cfg[4])
+{
+    if (!b || !cfg) return fail(CMSL_ERR_ARG, "NULL argument");
+    tile_config(b, cfg);
+    return CMSL_OK;
 }
 
 cmsl_status cmsl_batch_device_bytes(cmsl_batch *b, size_t *bytes)

@@ -95,8 +95,24 @@ struct Engine {
     int spec_zt = 0;            // threads per block of the z solve
     size_t spec_smem[3] = {0, 0, 0};
     bool persistent = false;
-    // tensor-copy staging of the FP32 stencil passes (every film's nx % 32 == 0, ny % 8 == 0)
+    // tensor-copy staging of the FP32 stencil passes (every film's nx % 32 == 0, ny % 8 == 0);
+    // the TDGL and the residual passes each take the tensor-copy or the
+    // cp.async ring, whichever the autotuner measured faster (tensor copies
+    // until tuned)
     bool tma = false;
+    bool tma_tdgl = false, tma_refine = false;
+    void *tdgl_fn_t = nullptr, *tdgl_fn_c = nullptr, *refine_fn_t = nullptr, *refine_fn_c = nullptr;
+    size_t tdgl_smem_t = 0, tdgl_smem_c = 0, refine_smem_t = 0, refine_smem_c = 0;
+    void stage(bool tdgl_tma, bool refine_tma)
+    {
+        tma_tdgl = tma && tdgl_tma;
+        tma_refine = tma && refine_tma;
+        tdgl_fn = tma_tdgl ? tdgl_fn_t : tdgl_fn_c;
+        tdgl_smem = tma_tdgl ? tdgl_smem_t : tdgl_smem_c;
+        refine_fn = tma_refine ? refine_fn_t : refine_fn_c;
+        refine_smem = tma_refine ? refine_smem_t : refine_smem_c;
+        graph_valid = false;
+    }
     FilmMaps *d_maps = nullptr;
     int *d_err = nullptr;               // device error word
     CgBuf cg{};

@@ -3,9 +3,9 @@
 // pass (k_refine32t).
 //
 // Same work items and arithmetic as stencil32.cuh, but a plane of every field
-// is brought into the ring by cp.async.bulk.tensor copies that one warp
-// issues (one lane per box) and that complete on the stage's mbarrier; no
-// thread computes a copy address.  A field of a plane lands as five boxes:
+// is brought into the ring by cp.async.bulk.tensor copies that the first
+// lane of each warp issues (a few boxes each) and that complete on the
+// stage's mbarrier; no thread computes a per-cell copy address.  A field of a plane lands as five boxes:
 //
 //   [S row: TX][tile: TY x TX][N row: TX][W strip: TY x 16 B][E strip: TY x 16 B]
 //
@@ -20,7 +20,7 @@
 // plane p in stage (p - zlo) % NS, whose barrier completes phase
 // (p - zlo) / NS when the plane has landed.  Before computing plane k every
 // thread waits for plane k+1, the block syncs (retiring every read of plane
-// k-2) and warp 0 issues plane k+NS-2 into that stage.
+// k-2) and the warps' first lanes issue plane k+NS-2 into that stage.
 #pragma once
 #include "stencil32.cuh"
 #include "tma.cuh"
@@ -102,10 +102,9 @@ template <int NS, int MAXOPS> struct TmaRing {
     __device__ __forceinline__ int st(int p) const { return (p - zlo) % NS; }
     __device__ __forceinline__ void issue(int p) const
     {
-        if (p <= zhi && threadIdx.x < 32) {
+        if (p <= zhi) {
             const int s = st(p);
-            fence_proxy_async_smem();
-            tma_issue_plane(ops, n_ops, base + (uint32_t)(s * stage_bytes), p, &bar[s], tx, threadIdx.x);
+            tma_issue_plane(ops, n_ops, base + (uint32_t)(s * stage_bytes), p, &bar[s], tx);
         }
     }
     __device__ __forceinline__ void wait(int p, int *err) const
@@ -198,15 +197,22 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
     for (int q = 0; q < 7; ++q) acc[q] = 0.f;
     RingIdx<NS> ri{z0 - zlo};
     long long o = (long long)(x0 + lx) + (long long)nx * (y0 + ly) + (long long)z0 * plane;
+    const long long plane_step = plane;
+    float2 oq{0.f, 0.f}, ou{0.f, 0.f};
+    auto ld_old = [&](long long oo) {
+        if (dep && warm >= 1) oq = qh[oo];
+        if (dep && warm >= 2) ou = uh[oo];
+    };
+    ld_old(o);
     for (int k = z0; k < z1; ++k, o += plane, ri.next()) {
         R.wait(k + 1, d.err);
         __syncthreads();
         R.issue(k + NS - 2);
-        // older potentials for the warm start (consumed after the step's arithmetic)
-        df wq{0.f, 0.f}, wu{0.f, 0.f}, wv{0.f, 0.f};
-        if (dep && warm >= 1) wq = ld_df(qh + o);
-        if (dep && warm >= 2) wu = ld_df(uh + o);
-        if (dep && warm >= 3) wv = ld_df(vh + o);
+        // older potentials for the warm start, loaded one plane ahead (the
+        // cubic start's third one in place), consumed after the step's arithmetic
+        const df wq{oq.x, oq.y}, wu{ou.x, ou.y};
+        const df wv = (dep && warm >= 3) ? ld_df(vh + o) : df{0.f, 0.f};
+        if (k + 1 < z1) ld_old(o + plane_step);
         const unsigned char *sk = R.stage(ri.s);
         const unsigned char *su = R.stage(ri.up(k == nz - 1)), *sd = R.stage(ri.dn(k == 0));
         const uint32_t c = ((const uint32_t *)(sk + TT_CODE))[threadIdx.x];

@@ -1,9 +1,9 @@
 // tma.cuh -- Blackwell tensor-memory-access staging: mbarrier-completed
 // cp.async.bulk.tensor copies of 2.5D stencil tiles into shared memory.
 //
-// One warp issues a plane's copies (one lane per box), each copy counts its
-// bytes on the stage's mbarrier, and every thread waits on that barrier's
-// phase before reading the stage.  Waits are bounded: after TMA_SPIN_LIMIT
+// The first lanes of the block's warps issue a plane's copies (a few boxes
+// each), each copy counts its bytes on the stage's mbarrier, and every
+// thread waits on that barrier's phase before reading the stage.  Waits are bounded: after TMA_SPIN_LIMIT
 // unsuccessful tries the wait records an error in the device error word and
 // returns, so a kernel never spins forever.
 #pragma once
@@ -107,15 +107,21 @@ struct TmaOp {
     int pad;
 };
 
-// Issues the `n` copies of plane z into the stage at byte address `stage`
-// from the lanes of one warp (lane i: copies i, i + 32, ...).  Lane 0 first
-// arms the stage's barrier with the stage's byte count.
+// Issues the `n` copies of plane z into the stage at byte address `stage`,
+// spread over the first lane of every warp of the block (warp w: copies w,
+// w + nw, ...), so no warp carries the whole plane's issue work.  Thread 0
+// arms the stage's barrier with the stage's byte count (copies that complete
+// before the arming only take the barrier's byte count below zero; the phase
+// cannot complete before the arrival).  Every issuing lane first orders the
+// block's earlier generic reads of the stage before its async-proxy writes.
 __device__ __forceinline__ void tma_issue_plane(const TmaOp *ops, int n, uint32_t stage, int z, uint64_t *bar,
-                                                uint32_t bytes, int lane)
+                                                uint32_t bytes)
 {
-    if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
+    if ((threadIdx.x & 31) != 0) return;
+    const int w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    if (w == 0) mbar_arrive_expect_tx(bar, bytes);
+    if (w < n) fence_proxy_async_smem();
+    for (int i = w; i < n; i += nw) {
         const TmaOp o = ops[i];
         if (o.q < 0) tma_load_3d(stage + o.dst, o.map, o.x, o.y, z, bar);
         else tma_load_4d(stage + o.dst, o.map, o.x, o.y, z, o.q, bar);

@@ -100,6 +100,14 @@ def _oracle_kw(f):
                 pcg_crit=f.crit)
 
 
+def _tile_config(fn, h):
+    cfg = (C.c_int32 * 4)()
+    check(fn(h, cfg))
+    return {"x": int(cfg[0]), "y": int(cfg[1]), "z_chunk": int(cfg[2]),
+            "tdgl_staging": "tensor copies" if cfg[3] & 1 else "cp.async ring",
+            "residual_staging": "tensor copies" if cfg[3] & 2 else "cp.async ring"}
+
+
 class Film:
     """One film on the GPU.
 
@@ -259,11 +267,16 @@ class Film:
         return v.value
 
     def autotune(self):
-        """Times the stencil passes for several work-item z chunks, keeps the
-        fastest and returns it (cmsl_film_autotune)."""
+        """Times the stencil passes for several work-item z chunks (and both
+        stagings where tensor copies apply), keeps the fastest and returns
+        the z chunk (cmsl_film_autotune)."""
         v = C.c_int32()
         check(lib().cmsl_film_autotune(self._h, C.byref(v)))
         return int(v.value)
+
+    def tile_config(self):
+        """The stencil passes' tile, z chunk and staging (cmsl_film_tile_config)."""
+        return _tile_config(lib().cmsl_film_tile_config, self._h)
 
 
 class Batch:
@@ -383,6 +396,10 @@ class Batch:
         v = C.c_int32()
         check(lib().cmsl_batch_autotune(self._h, C.byref(v)))
         return int(v.value)
+
+    def tile_config(self):
+        """The stencil passes' tile, z chunk and staging (cmsl_batch_tile_config)."""
+        return _tile_config(lib().cmsl_batch_tile_config, self._h)
 
     def device_bytes(self):
         b = C.c_size_t()

@@ -188,12 +188,20 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, doub
 cmsl_status cmsl_film_inner_solver(cmsl_film *film, int *solver);
 
 /* Tile-shape autotuner: times the stencil passes of this film for work-item z
- * chunks 4, 8, 16, ... up to nz on the device, keeps the fastest (reported in
- * *zchunk, may be NULL) and remembers it for films of the same shape class
- * created later in the process.  Leaves the state (P, phi) as it is; results
- * of later steps equal the untuned ones up to the order of the row sums.
- * CMSL_ZCHUNK=<n> in the environment fixes the chunk of untuned handles. */
+ * chunks 4, 8, 16, ... up to nz on the device -- and, for CMSL_FP32_REFINED
+ * films with full 32 x 8 tiles, both stagings of the TDGL and of the
+ * residual passes (tensor copies or the cp.async ring) -- keeps the fastest
+ * (the z chunk in *zchunk, may be NULL) and remembers it for films of the same
+ * shape class created later in the process.  Leaves the state (P, phi) as it
+ * is; results of later steps equal the untuned ones up to the order of the
+ * row sums.  CMSL_ZCHUNK=<n> fixes the chunk of untuned handles,
+ * CMSL_NO_TMA=1 the cp.async staging. */
 cmsl_status cmsl_film_autotune(cmsl_film *film, int32_t *zchunk);
+
+/* The stencil-pass configuration in use: cfg[0] tile x, cfg[1] tile y,
+ * cfg[2] z chunk (0: the per-film heuristic), cfg[3] staging bits (1: the
+ * TDGL by tensor copies, 2: the residual passes by tensor copies). */
+cmsl_status cmsl_film_tile_config(cmsl_film *film, int32_t cfg[4]);
 
 /* Bytes of device memory the film holds. */
 cmsl_status cmsl_film_device_bytes(cmsl_film *film, size_t *bytes);
@@ -246,6 +254,7 @@ cmsl_status cmsl_batch_inner_solver(cmsl_batch *batch, int *solver);
 /* The batch's tile-shape autotuner, as cmsl_film_autotune (one z chunk for
  * all films of the batch). */
 cmsl_status cmsl_batch_autotune(cmsl_batch *batch, int32_t *zchunk);
+cmsl_status cmsl_batch_tile_config(cmsl_batch *batch, int32_t cfg[4]);
 
 /* Restart files in the reference's checkpoint layout (generate.cu:90-264;
  * cmsl_io.h cmsl_checkpoint_write/read).  write: P and E = -grad(phi) of the
