@@ -146,7 +146,7 @@ cmsl_status set_items(Engine *e, int zc)
 // the staging of the TDGL and of the residual passes.
 struct Tuned {
     int zchunk;
-    bool tma_tdgl, tma_refine;
+    int stg_tdgl, stg_refine;
 };
 std::map<std::string, Tuned> g_tuned;
 std::mutex g_tuned_mu;
@@ -1208,27 +1208,55 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         const char *nt = getenv("CMSL_NO_TMA");
         e->tma = !(nt && atoi(nt) != 0);
         for (int fi = 0; fi < n; ++fi) e->tma = e->tma && e->fh[fi].nx % TX == 0 && e->fh[fi].ny % TY == 0;
-        e->refine_fn_c = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
-        e->refine_smem_c = uni ? r32_smem<true>() : r32_smem<false>();
-        e->tdgl_fn_c = (void *)k_tdgl32<T32_NS>;
-        e->tdgl_smem_c = T32_SMEM;
-        CK(cudaFuncSetAttribute(e->refine_fn_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem_c));
-        CK(cudaFuncSetAttribute(e->tdgl_fn_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem_c));
+        e->refine_fns[STG_CP] = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
+        e->refine_smems[STG_CP] = uni ? r32_smem<true>() : r32_smem<false>();
+        e->tdgl_fns[STG_CP] = (void *)k_tdgl32<T32_NS>;
+        e->tdgl_smems[STG_CP] = T32_SMEM;
         if (e->tma) {
             TRY(make_maps(e));
-            e->refine_fn_t = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
-            e->refine_smem_t = uni ? rt_smem<true>() : rt_smem<false>();
-            e->tdgl_fn_t = (void *)k_tdgl32t<TT_NS>;
-            e->tdgl_smem_t = TT_SMEM;
-            CK(cudaFuncSetAttribute(e->refine_fn_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->refine_smem_t));
-            CK(cudaFuncSetAttribute(e->tdgl_fn_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_smem_t));
+            e->refine_fns[STG_TMA] = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
+            e->refine_smems[STG_TMA] = uni ? rt_smem<true>() : rt_smem<false>();
+            e->tdgl_fns[STG_TMA] = (void *)k_tdgl32t<TT_NS>;
+            e->tdgl_smems[STG_TMA] = TT_SMEM;
+            e->refine_fns[STG_FLOW] = uni ? (void *)k_refine32f<true, RF_NS> : (void *)k_refine32f<false, RF_NS>;
+            e->refine_smems[STG_FLOW] = (size_t)RF_NS * (uni ? rt_stage<true>() : rt_stage<false>()) + 128;
+            // CMSL_TF_VARIANT: 0 rotation loaded per plane, 4 blocks per SM;
+            // 1 rotation kept per grain, 3 blocks per SM and a 5-plane ring;
+            // 2 rotation kept per grain, 4 blocks per SM; 3 rotation loaded
+            // per plane, 3 blocks per SM and a 5-plane ring
+            const char *tv = getenv("CMSL_TF_VARIANT");
+            const int tfv = tv ? atoi(tv) : 0;
+            if (tfv == 1 || tfv == 3) {
+                e->tdgl_fns[STG_FLOW] = tfv == 1 ? (void *)k_tdgl32f<5, true, 3> : (void *)k_tdgl32f<5, false, 3>;
+                e->tdgl_smems[STG_FLOW] = (size_t)5 * TT_STAGE + 128;
+            } else {
+                e->tdgl_fns[STG_FLOW] = tfv == 2 ? (void *)k_tdgl32f<TF_NS, true, 4> : (void *)k_tdgl32f<TF_NS, false, 4>;
+                e->tdgl_smems[STG_FLOW] = (size_t)TF_NS * TT_STAGE + 128;
+            }
+        }
+        for (int v = 0; v < (e->tma ? N_STG : 1); ++v) {
+            CK(cudaFuncSetAttribute(e->refine_fns[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)e->refine_smems[v]));
+            CK(cudaFuncSetAttribute(e->tdgl_fns[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)e->tdgl_smems[v]));
         }
         e->refine_nt = e->tdgl_nt = NT;
-        e->stage(true, true);
-        {
+        // CMSL_STAGING=<tdgl><residual> (digits 0 cp.async ring, 1 tensor
+        // copies, 2 warp-flow tensor copies) fixes the staging of films with
+        // full tiles; the autotuner then keeps it
+        int st_t = STG_TMA, st_r = STG_TMA;
+        const char *sg = getenv("CMSL_STAGING");
+        e->staging_fixed = false;
+        if (sg && strlen(sg) == 2 && sg[0] >= '0' && sg[0] < '0' + N_STG && sg[1] >= '0' && sg[1] < '0' + N_STG) {
+            st_t = sg[0] - '0';
+            st_r = sg[1] - '0';
+            e->staging_fixed = true;
+        }
+        e->stage(st_t, st_r);
+        if (!e->staging_fixed) {
             std::lock_guard<std::mutex> lk(g_tuned_mu);
             const auto hit = g_tuned.find(shape_key(e));
-            if (hit != g_tuned.end()) e->stage(hit->second.tma_tdgl, hit->second.tma_refine);
+            if (hit != g_tuned.end()) e->stage(hit->second.stg_tdgl, hit->second.stg_refine);
         }
     }
     const Dev d = e->dev(0);
@@ -1547,17 +1575,18 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
     std::vector<int> cands;
     for (int c = ZCHUNK_MIN; c < maxnz; c *= 2) cands.push_back(c);
     cands.push_back(maxnz);
-    // per z chunk: both stagings of the TDGL and of the residual passes where
+    // per z chunk: every staging of the TDGL and of the residual passes where
     // the tensor copies apply (the two kernels are independent, so each takes
-    // its faster staging)
-    Tuned best{0, e->tma_tdgl, e->tma_refine};
+    // its fastest staging; a staging fixed by CMSL_STAGING is kept)
+    Tuned best{0, e->stg_tdgl, e->stg_refine};
     double best_ms = 0.0;
+    const bool tune_stg = e->precision != CMSL_FP64 && e->tma && !e->staging_fixed;
+    const int nst = tune_stg ? N_STG : 1;
     for (int c : cands) {
         TRY(set_items(e, c));
-        double tt[2] = {0.0, 0.0}, tr[2] = {0.0, 0.0}, rest = 0.0;
-        const int nst = e->tma ? 2 : 1;
+        double tt[N_STG] = {0.0, 0.0, 0.0}, tr[N_STG] = {0.0, 0.0, 0.0}, rest = 0.0;
         for (int v = 0; v < nst; ++v) {
-            if (e->precision != CMSL_FP64) e->stage(v == 0, v == 0);
+            if (tune_stg) e->stage(v, v);
             double ms[4] = {0, 0, 0, 0};
             TRY(time_kernels(e, 5, nullptr, ms));
             tt[v] = ms[0];                                  // TDGL step
@@ -1566,16 +1595,20 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
             else if (e->spectral) tr[v] += ms[3];           // update pass
             else if (!e->persistent) rest = ms[2] + ms[3];  // two-kernel PCG
         }
-        const int vt = (nst == 2 && tt[1] < tt[0]) ? 1 : 0, vr = (nst == 2 && tr[1] < tr[0]) ? 1 : 0;
+        int vt = 0, vr = 0;
+        for (int v = 1; v < nst; ++v) {
+            if (tt[v] < tt[vt]) vt = v;
+            if (tr[v] < tr[vr]) vr = v;
+        }
         const double t = tt[vt] + tr[vr] + rest;
         if (best.zchunk == 0 || t < best_ms) {
-            best = Tuned{c, e->tma && vt == 0, e->tma && vr == 0};
+            best = tune_stg ? Tuned{c, vt, vr} : Tuned{c, e->stg_tdgl, e->stg_refine};
             best_ms = t;
         }
     }
     TRY(set_items(e, best.zchunk));
-    if (e->precision != CMSL_FP64) e->stage(best.tma_tdgl, best.tma_refine);
-    {
+    if (e->precision != CMSL_FP64) e->stage(best.stg_tdgl, best.stg_refine);
+    if (!e->staging_fixed) {
         std::lock_guard<std::mutex> lk(g_tuned_mu);
         g_tuned[shape_key(e)] = best;
     }
@@ -1588,7 +1621,7 @@ void tile_config(const Engine *e, int32_t cfg[4])
     cfg[0] = TX;
     cfg[1] = TY;
     cfg[2] = e->zchunk;
-    cfg[3] = (e->tma_tdgl ? 1 : 0) | (e->tma_refine ? 2 : 0);
+    cfg[3] = e->stg_tdgl | (e->stg_refine << 2);
 }
 
 size_t device_bytes(const Engine *e)

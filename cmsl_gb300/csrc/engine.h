@@ -33,6 +33,9 @@ cmsl_status fail(cmsl_status s, const char *fmt, ...);
         if (s_ != CMSL_OK) return s_;        \
     } while (0)
 
+// Staging of the FP32 stencil passes (Engine::stage).
+enum { STG_CP = 0, STG_TMA = 1, STG_FLOW = 2, N_STG = 3 };
+
 // Host view of one film of a handle.
 struct FilmHost {
     int nx, ny, nz, ng, dep, zbc;
@@ -95,22 +98,25 @@ struct Engine {
     int spec_zt = 0;            // threads per block of the z solve
     size_t spec_smem[3] = {0, 0, 0};
     bool persistent = false;
-    // tensor-copy staging of the FP32 stencil passes (every film's nx % 32 == 0, ny % 8 == 0);
-    // the TDGL and the residual passes each take the tensor-copy or the
-    // cp.async ring, whichever the autotuner measured faster (tensor copies
-    // until tuned)
+    // staging of the FP32 stencil passes: STG_CP the cp.async ring (any
+    // film), STG_TMA tensor copies with a block barrier per plane, STG_FLOW
+    // tensor copies with per-stage full/empty barriers and no block barrier
+    // (the tensor copies need every film's nx % 32 == 0, ny % 8 == 0).  The
+    // TDGL and the residual passes each take the staging the autotuner
+    // measured fastest (STG_TMA until tuned)
     bool tma = false;
-    bool tma_tdgl = false, tma_refine = false;
-    void *tdgl_fn_t = nullptr, *tdgl_fn_c = nullptr, *refine_fn_t = nullptr, *refine_fn_c = nullptr;
-    size_t tdgl_smem_t = 0, tdgl_smem_c = 0, refine_smem_t = 0, refine_smem_c = 0;
-    void stage(bool tdgl_tma, bool refine_tma)
+    int stg_tdgl = 0, stg_refine = 0;
+    bool staging_fixed = false;         // CMSL_STAGING set the staging: the autotuner keeps it
+    void *tdgl_fns[3] = {nullptr, nullptr, nullptr}, *refine_fns[3] = {nullptr, nullptr, nullptr};
+    size_t tdgl_smems[3] = {0, 0, 0}, refine_smems[3] = {0, 0, 0};
+    void stage(int tdgl_stg, int refine_stg)
     {
-        tma_tdgl = tma && tdgl_tma;
-        tma_refine = tma && refine_tma;
-        tdgl_fn = tma_tdgl ? tdgl_fn_t : tdgl_fn_c;
-        tdgl_smem = tma_tdgl ? tdgl_smem_t : tdgl_smem_c;
-        refine_fn = tma_refine ? refine_fn_t : refine_fn_c;
-        refine_smem = tma_refine ? refine_smem_t : refine_smem_c;
+        stg_tdgl = tma ? tdgl_stg : 0;
+        stg_refine = tma ? refine_stg : 0;
+        tdgl_fn = tdgl_fns[stg_tdgl];
+        tdgl_smem = tdgl_smems[stg_tdgl];
+        refine_fn = refine_fns[stg_refine];
+        refine_smem = refine_smems[stg_refine];
         graph_valid = false;
     }
     FilmMaps *d_maps = nullptr;

@@ -100,12 +100,11 @@ __device__ __forceinline__ void load_coef4(const FilmDev *f, float4 (*sC)[3])
 
 // One cell: P^{n+1} (pn) from P^n (pc), the 6-neighbour sums, -E (ex, ey, ez)
 // and -Ez_applied (mEz); pMZl, pSZl (crystal frame) for the sweep rows.
-__device__ __forceinline__ void tdgl_cell32(const float4 *K, const float4 *tr, const float (&pc)[6],
-                                            const float (&sum)[6], float ex, float ey, float ez, float mEz,
-                                            float (&pn)[6], float &pMZl, float &pSZl)
+// The grain's rotation t (row major) given.
+__device__ __forceinline__ void tdgl_cell32t(const float4 *K, const float (&t)[9], const float (&pc)[6],
+                                             const float (&sum)[6], float ex, float ey, float ez, float mEz,
+                                             float (&pn)[6], float &pMZl, float &pSZl)
 {
-    const float4 t0 = __ldg(tr), t1 = __ldg(tr + 1), t2 = __ldg(tr + 2);
-    const float t[9] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x};
     const float4 ka = K[0], kb = K[1], kc = K[2];
     const float relax = ka.x, A = ka.y, LdT = ka.z, ag = ka.w, ags = kb.x, b4 = kb.y, b12 = kb.z, g6 = kb.w;
     const float a02 = kc.x;
@@ -138,6 +137,23 @@ __device__ __forceinline__ void tdgl_cell32(const float4 *K, const float4 *tr, c
     // explicit Euler with the 6-neighbour Laplacian (kernels_evol.cu:223-229)
     #pragma unroll
     for (int q = 0; q < 6; ++q) pn[q] = pc[q] * relax + A * sum[q] - LdT * b[q];
+}
+
+__device__ __forceinline__ void load_tr32(const float4 *tr, float (&t)[9])
+{
+    const float4 t0 = __ldg(tr), t1 = __ldg(tr + 1), t2 = __ldg(tr + 2);
+    t[0] = t0.x; t[1] = t0.y; t[2] = t0.z; t[3] = t0.w;
+    t[4] = t1.x; t[5] = t1.y; t[6] = t1.z; t[7] = t1.w; t[8] = t2.x;
+}
+
+// The rotation loaded from the grain's entry tr.
+__device__ __forceinline__ void tdgl_cell32(const float4 *K, const float4 *tr, const float (&pc)[6],
+                                            const float (&sum)[6], float ex, float ey, float ez, float mEz,
+                                            float (&pn)[6], float &pMZl, float &pSZl)
+{
+    float t[9];
+    load_tr32(tr, t);
+    tdgl_cell32t(K, t, pc, sum, ex, ey, ez, mEz, pn, pMZl, pSZl);
 }
 
 // z neighbours of the potential for E (depol_varEPS.cu:246-273): zero beyond

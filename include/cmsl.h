@@ -199,8 +199,10 @@ cmsl_status cmsl_film_inner_solver(cmsl_film *film, int *solver);
 cmsl_status cmsl_film_autotune(cmsl_film *film, int32_t *zchunk);
 
 /* The stencil-pass configuration in use: cfg[0] tile x, cfg[1] tile y,
- * cfg[2] z chunk (0: the per-film heuristic), cfg[3] staging bits (1: the
- * TDGL by tensor copies, 2: the residual passes by tensor copies). */
+ * cfg[2] z chunk (0: the per-film heuristic), cfg[3] the stagings: bits 0-1
+ * the TDGL's, bits 2-3 the residual passes' (0 the cp.async ring, 1 tensor
+ * copies with a block barrier per plane, 2 tensor copies with per-stage
+ * full/empty barriers). */
 cmsl_status cmsl_film_tile_config(cmsl_film *film, int32_t cfg[4]);
 
 /* Bytes of device memory the film holds. */
