@@ -436,14 +436,22 @@ cmsl_status build_graph(Engine *e)
                     CK(cudaGraphKernelNodeSetAttribute(*out, cudaLaunchAttributeCooperative, &av));
                     return CMSL_OK;
                 }
-                struct Node { void *fn; int grid, block; void **args; size_t smem; } seq[] = {
+                struct Node { void *fn; int grid, block; void **args; size_t smem; };
+                const Node rows[] = {
                     {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
                     {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
                     {(void *)k_spec_z, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
                     {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
                     {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
+                const Node cols[] = {
+                    {(void *)k_spec_x<true, true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
+                    {(void *)k_spec_yzy, e->spec_grid[3], SPEC_NT, a_s, e->spec_smem[3]},
+                    {(void *)k_spec_x<false, true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
+                const Node *seq = e->spec_col ? cols : rows;
+                const int nseq = e->spec_col ? 3 : 5;
                 const cudaGraphNode_t *prev = dep;
-                for (const Node &q : seq) {
+                for (int qi = 0; qi < nseq; ++qi) {
+                    const Node &q = seq[qi];
                     TRY(add_kernel(gs, out, prev, prev ? 1 : 0, q.fn, q.grid, q.block, q.args, q.smem));
                     prev = out;
                 }
@@ -620,6 +628,13 @@ cmsl_status launch_tdgl32(Engine *e, cudaStream_t st, const Dev &d, const Fields
 cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<float> &F32)
 {
     const SpecDev &sp = e->spec;
+    if (e->spec_col) {
+        k_spec_x<true, true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
+        k_spec_yzy<<<e->spec_grid[3], SPEC_NT, e->spec_smem[3], st>>>(d, sp);
+        k_spec_x<false, true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
+        CK(cudaGetLastError());
+        return CMSL_OK;
+    }
     k_spec_x<true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
     k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
     k_spec_z<<<e->spec_grid[2], e->spec_zt, e->spec_smem[2], st>>>(d, sp);
@@ -1108,7 +1123,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         // per-film plans, tables and block ranges of the three passes
         const int zt = spec_zthreads(spec_mmax);
         std::vector<SpecFilm> sf((size_t)n);
-        std::vector<int> bxf, byf, bzf;
+        std::vector<int> bxf, byf, bzf, bqf;
+        size_t smq = 0;
         std::vector<float2> tw;
         std::vector<float> lam;
         long long coff = 0;
@@ -1127,7 +1143,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             const FilmHost &h = e->fh[fi];
             SpecFilm &P = sf[fi];
             P.nx = h.nx; P.ny = h.ny; P.nz = h.nz; P.off = h.off;
-            P.bx0 = (int)bxf.size(); P.by0 = (int)byf.size(); P.bz0 = (int)bzf.size();
+            P.bx0 = (int)bxf.size(); P.by0 = (int)byf.size(); P.bz0 = (int)bzf.size(); P.bq0 = (int)bqf.size();
             if (!h.dep) continue;                                    // no solve, no blocks
             P.M = h.nz - 2;
             P.Mp = (P.M + 1) / 2;
@@ -1146,6 +1162,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             bxf.insert(bxf.end(), (size_t)gx, fi);
             byf.insert(byf.end(), (size_t)gy, fi);
             bzf.insert(bzf.end(), (size_t)gz, fi);
+            bqf.insert(bqf.end(), (size_t)(h.nx / 2 + 1), fi);                  // mirror pairs of columns
+            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp, P.M, SPEC_NT));
             smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * h.nx) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }
@@ -1160,6 +1178,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(upload(bxf.data(), sizeof(int) * bxf.size(), &p)); sp.bx_film = (const int *)p;
         TRY(upload(byf.data(), sizeof(int) * byf.size(), &p)); sp.by_film = (const int *)p;
         TRY(upload(bzf.data(), sizeof(int) * bzf.size(), &p)); sp.bz_film = (const int *)p;
+        TRY(upload(bqf.data(), sizeof(int) * bqf.size(), &p)); sp.bq_film = (const int *)p;
         TRY(upload(tw.data(), sizeof(float2) * tw.size(), &p)); sp.tw = (const float2 *)p;
         TRY(upload(lam.data(), sizeof(float) * lam.size(), &p)); sp.lam = (const float *)p;
         TRY(e->alloc((void **)&sp.C, sizeof(float2) * (size_t)coff));
@@ -1174,6 +1193,24 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));
         CK(cudaFuncSetAttribute(k_spec_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[2]));
+        // the column layout when every film's column pairs fit one block
+        // (CMSL_SPEC_ROWS=1 keeps the row layout)
+        {
+            int dev = 0, optin = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+            const char *rl = getenv("CMSL_SPEC_ROWS");
+            e->spec_col = smq <= (size_t)optin && !(rl && atoi(rl) != 0);
+            e->spec_grid[3] = (int)bqf.size();
+            e->spec_smem[3] = smq;
+            if (e->spec_col) {
+                CK(cudaFuncSetAttribute(k_spec_x<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)e->spec_smem[0]));
+                CK(cudaFuncSetAttribute(k_spec_x<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)e->spec_smem[0]));
+                CK(cudaFuncSetAttribute(k_spec_yzy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smq));
+            }
+        }
     }
     TRY(e->alloc((void **)&e->d_phi[0], sizeof(double) * cells));
     TRY(e->alloc((void **)&e->d_phi[1], sizeof(double) * cells));

@@ -24,6 +24,16 @@
 // (y); twiddles exp(-2 pi i t / n) and eigenvalues come from host tables
 // computed in double.  The z solve keeps the Thomas elimination in shared
 // memory, so each spectrum value is read and written once per sweep.
+//
+// Two layouts of the spectra.  Row layout ([Mp][ny][nx], five launches): x
+// transforms, y transforms, z solve, y transforms, x transforms.  Column
+// layout ([Mp][nx][ny], three launches, films whose column pairs fit one
+// block's shared memory): the x transforms store (and the last ones load)
+// through shared memory transposed, and one block per mirror pair of
+// columns {kx, nx - kx} holds both columns of every packed plane, so it runs
+// the y transforms, the z solve of all modes (kx, ky) with their mirrors
+// (nx - kx, ny - ky), and the y transforms back, with contiguous column reads
+// and writes (k_spec_yzy).
 #pragma once
 #include "kernels.cuh"
 
@@ -48,6 +58,7 @@ struct SpecFilm {
     int twx, twy, lamx, lamy;   // offsets into the twiddle / eigenvalue tables
     float scale;                // h^2 / (eps nx ny)
     int bx0, by0, bz0;          // first block of the film in the x, y and z grids
+    int bq0;                    // first block of the film in the column-pair grid (column layout)
 };
 
 struct SpecDev {
@@ -56,6 +67,7 @@ struct SpecDev {
     const float2 *tw;           // exp(-2 pi i t / n) per film and axis
     const float *lam;           // 2 - 2 cos(2 pi t / n) per film and axis
     const int *bx_film, *by_film, *bz_film;   // film of every block of the three grids
+    const int *bq_film;         // film of every block of the column-pair grid (column layout)
 };
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -309,8 +321,20 @@ __device__ __forceinline__ void spec_finish(const Dev &d)
 // from the FP32 residual r (interior planes 2j and 2j+1, i.e. z planes 2j+1
 // and 2j+2, as real and imaginary parts) into the spectra; otherwise from the
 // spectra into the real correction x (and x = 0 on the Dirichlet planes).
-// Shared memory: two padded tiles of rb rows and the twiddles.
-template <bool IN_REAL>
+// COL: the spectra in the column layout, stored (IN_REAL) or loaded through a
+// shared-memory tile transposed, so that a warp touches runs of consecutive
+// y.  Shared memory: two padded tiles of rb rows and the twiddles.
+__device__ __forceinline__ int fft_pow2_passes(int lgn)
+{
+    int n = 0;
+    for (int lgNs = 0; lgNs < lgn; ++n) {
+        const int rem = lgn - lgNs;
+        lgNs += (rem >= 4 && (rem & 3) != 1) ? 4 : rem >= 3 ? 3 : rem;
+    }
+    return n;
+}
+
+template <bool IN_REAL, bool COL = false>
 __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
@@ -331,17 +355,34 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
     const int tile = spec_pad(rb * nx) + 1;
     float2 *a = sm2, *b = sm2 + tile, *tw = sm2 + 2 * tile;
     for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twx + t);
+    // spectrum value (row r0 + sq, x element e) in the column layout
+    auto col_at = [&](int sq, int e) -> long long {
+        const int rw = r0 + sq, j = rw / ny;
+        return ((long long)j * nx + e) * ny + (rw - j * ny);
+    };
+    if (COL && !IN_REAL) {
+        // transposed load: consecutive threads take consecutive rows of one column
+        const int total = nr * nx;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int e = t / nr, sq = t - e * nr;
+            a[spec_pad(sq * nx + e)] = Cf[col_at(sq, e)];
+        }
+        __syncthreads();
+    }
     // row r0 + sq is (j, y) = packed plane j, in-plane row y; its residual
     // rows in r are z planes 2j+1 and 2j+2
     auto ld = [&](int sq, int e) -> float2 {
-        if (!IN_REAL) return Cf[(long long)(r0 + sq) * nx + e];
+        if (!IN_REAL) return COL ? a[spec_pad(sq * nx + e)] : Cf[(long long)(r0 + sq) * nx + e];
         const int rw = r0 + sq, j = rw / ny;
         const long long o = (long long)(2 * j + 1) * plane + (long long)(rw - j * ny) * nx + e;
         return make_float2(rr[o], 2 * j + 1 < M ? rr[o + plane] : 0.f);
     };
+    // the tile that receives the transform in the column layout's store
+    float2 *res = (ax.lg >= 0 && (fft_pow2_passes(ax.lg) & 1) == 0) ? a : b;
     auto st = [&](int sq, int e, float2 v) {
         if (IN_REAL) {
-            Cf[(long long)(r0 + sq) * nx + e] = v;
+            if (COL) res[spec_pad(sq * nx + e)] = v;
+            else Cf[(long long)(r0 + sq) * nx + e] = v;
             return;
         }
         // the transform of conj(W) is conj(x_2j + i x_2j+1) (scale folded into the z solve)
@@ -357,10 +398,21 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
         fft_pow2<false>(a, b, nr, ax.lg, 1, nx, tw, ld, st);
     } else {
         const int total = nr * nx;
-        for (int t = threadIdx.x; t < total; t += blockDim.x) a[spec_pad(t)] = ld(t / nx, t - (t / nx) * nx);
+        if (!(COL && !IN_REAL))
+            for (int t = threadIdx.x; t < total; t += blockDim.x) a[spec_pad(t)] = ld(t / nx, t - (t / nx) * nx);
         __syncthreads();
-        const float2 *res = fft_mixed<false>(a, b, nr, ax, 1, nx, tw);
-        for (int t = threadIdx.x; t < total; t += blockDim.x) st(t / nx, t - (t / nx) * nx, res[spec_pad(t)]);
+        res = fft_mixed<false>(a, b, nr, ax, 1, nx, tw);
+        if (!(COL && IN_REAL))
+            for (int t = threadIdx.x; t < total; t += blockDim.x) st(t / nx, t - (t / nx) * nx, res[spec_pad(t)]);
+    }
+    if (COL && IN_REAL) {
+        // transposed store: consecutive threads write consecutive rows of one column
+        __syncthreads();
+        const int total = nr * nx;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int e = t / nr, sq = t - e * nr;
+            Cf[col_at(sq, e)] = res[spec_pad(sq * nx + e)];
+        }
     }
     if (!IN_REAL) spec_finish(d);
 }
@@ -482,6 +534,128 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
         const float2 u = make_float2(dd.x - c * v.x, dd.y - c * v.y);
         put(j, u, v);
         xn = u;
+    }
+}
+
+
+// Column layout: the y transforms, the z solve and the y transforms back of
+// one mirror pair of columns {kx, kx2 = (nx - kx) mod nx} of every packed
+// plane of a film (one block; kx = kx2 for kx = 0 and, for even nx, nx/2).
+// Sequence s = j * ncol + c of the shared tiles is column c (0: kx, 1: kx2)
+// of packed plane j, its ny values contiguous (padded every 16).  Modes
+// (kx, ky) pair with (kx2, (ny - ky) mod ny); a self-mirror column pairs ky
+// with ny - ky inside itself, one thread per pair (ky <= ny - ky).  The
+// elimination runs in place: the pair's slots at plane j take the eliminated
+// right-hand sides of interior planes 2j and 2j+1 (for a mode that is its
+// own mirror both are real and share its one slot), then the conjugates of
+// the packed solutions, whose forward y transforms go back to the spectra.
+// Shared memory: two tiles, the y twiddles, c' of every interior plane for
+// each thread.
+__host__ __device__ inline size_t spec_yzy_bytes(int ny, int Mp, int M, int nt)
+{
+    return sizeof(float2) * (2 * (size_t)(spec_pad(2 * Mp * ny) + 1) + ny) + sizeof(float) * (size_t)M * nt;
+}
+
+static __global__ void __launch_bounds__(SPEC_NT, 1) k_spec_yzy(Dev d, SpecDev sp)
+{
+    extern __shared__ float2 sm2[];
+    const int f = __ldg(sp.bq_film + blockIdx.x);
+    if (!spec_run(d, f)) return;
+    const SpecFilm &P = sp.films[f];
+    const int nx = P.nx, ny = P.ny, M = P.M, Mp = P.Mp;
+    const int kx = blockIdx.x - P.bq0, kx2 = kx == 0 ? 0 : nx - kx;
+    const int ncol = kx == kx2 ? 1 : 2, nseq = ncol * Mp;
+    const int tile = spec_pad(2 * Mp * ny) + 1;
+    float2 *A = sm2, *B = sm2 + tile, *tw = sm2 + 2 * tile;
+    float *cps = (float *)(tw + ny);
+    const SpecAxis ay = P.ay;
+    float2 *Cf = sp.C + P.coff;
+    auto gcol = [&](int sq) {                    // first value of sequence sq in the spectra
+        const int j = sq / ncol, c = sq - j * ncol;
+        return Cf + ((long long)j * nx + (c ? kx2 : kx)) * ny;
+    };
+    for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twy + t);
+    __syncthreads();
+    // forward y transforms: spectra -> tile R
+    float2 *R;
+    if (ay.lg >= 0) {
+        R = (fft_pow2_passes(ay.lg) & 1) == 0 ? A : B;
+        auto ld = [&](int sq, int e) { return gcol(sq)[e]; };
+        auto st = [&](int sq, int e, float2 v) { R[spec_pad(sq * ny + e)] = v; };
+        fft_pow2<false>(A, B, nseq, ay.lg, 1, ny, tw, ld, st);
+    } else {
+        for (int t = threadIdx.x; t < nseq * ny; t += blockDim.x) A[spec_pad(t)] = gcol(t / ny)[t - (t / ny) * ny];
+        __syncthreads();
+        R = fft_mixed<false>(A, B, nseq, ay, 1, ny, tw);
+    }
+    __syncthreads();
+    // z solve, one thread per mode pair (as k_spec_z)
+    const int npair = ncol == 2 ? ny : ny / 2 + 1;
+    const float s = 0.5f * P.scale;
+    const float lx = __ldg(sp.lam + P.lamx + kx);
+    for (int ky = threadIdx.x; ky < npair; ky += blockDim.x) {
+        const int ky2 = ky == 0 ? 0 : ny - ky;
+        const bool self = ncol == 1 && ky == ky2;
+        float *cp = cps + threadIdx.x;
+        auto slot_a = [&](int j) { return &R[spec_pad((j * ncol) * ny + ky)]; };
+        auto slot_b = [&](int j) { return &R[spec_pad((j * ncol + ncol - 1) * ny + ky2)]; };
+        const float dg = lx + __ldg(sp.lam + P.lamy + ky) + 2.f;
+        float c_prev = 0.f;
+        float2 d_prev = make_float2(0.f, 0.f);
+        auto sweep = [&](int k, float2 rk) {     // forward elimination (sub/super-diagonal -1)
+            const float inv = 1.f / (dg + c_prev);
+            d_prev = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
+            c_prev = -inv;
+            cp[(size_t)k * blockDim.x] = c_prev;
+            return d_prev;
+        };
+        for (int j = 0; j < Mp; ++j) {
+            const float2 a = *slot_a(j), b = *slot_b(j);       // Z(m), Z(-m)
+            const float2 d0 = sweep(2 * j, make_float2(a.x + b.x, a.y - b.y));
+            float2 d1 = make_float2(0.f, 0.f);
+            if (2 * j + 1 < M) d1 = sweep(2 * j + 1, make_float2(a.y + b.y, b.x - a.x));
+            if (self) {
+                *slot_a(j) = make_float2(d0.x, d1.x);
+            } else {
+                *slot_a(j) = d0;
+                *slot_b(j) = d1;
+            }
+        }
+        // back substitution, two planes at a time; the slots take the
+        // conjugates of W(m) = X_2j + i X_2j+1 and W(-m) = conj X_2j + i conj X_2j+1
+        float2 xn = make_float2(0.f, 0.f);
+        for (int j = Mp - 1; j >= 0; --j) {
+            float2 d0, d1;
+            if (self) {
+                const float2 q = *slot_a(j);
+                d0 = make_float2(q.x, 0.f);
+                d1 = make_float2(q.y, 0.f);
+            } else {
+                d0 = *slot_a(j);
+                d1 = *slot_b(j);
+            }
+            float2 v = make_float2(0.f, 0.f);
+            if (2 * j + 1 < M) {
+                const float c = cp[(size_t)(2 * j + 1) * blockDim.x];
+                v = make_float2(d1.x - c * xn.x, d1.y - c * xn.y);
+            }
+            const float c = cp[(size_t)(2 * j) * blockDim.x];
+            const float2 u = make_float2(d0.x - c * v.x, d0.y - c * v.y);
+            *slot_a(j) = make_float2(u.x - v.y, -(u.y + v.x));
+            if (!self) *slot_b(j) = make_float2(u.x + v.y, u.y - v.x);
+            xn = u;
+        }
+    }
+    __syncthreads();
+    // y transforms of the conjugated solutions: tile R -> spectra
+    if (ay.lg >= 0) {
+        float2 *other = R == A ? B : A;
+        auto ld = [&](int sq, int e) { return R[spec_pad(sq * ny + e)]; };
+        auto st = [&](int sq, int e, float2 v) { gcol(sq)[e] = v; };
+        fft_pow2<false>(R, other, nseq, ay.lg, 1, ny, tw, ld, st);
+    } else {
+        const float2 *res = fft_mixed<false>(R, R == A ? B : A, nseq, ay, 1, ny, tw);
+        for (int t = threadIdx.x; t < nseq * ny; t += blockDim.x) gcol(t / ny)[t - (t / ny) * ny] = res[spec_pad(t)];
     }
 }
 
