@@ -1255,21 +1255,6 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             e->refine_smems[STG_TMA] = uni ? rt_smem<true>() : rt_smem<false>();
             e->tdgl_fns[STG_TMA] = (void *)k_tdgl32t<TT_NS>;
             e->tdgl_smems[STG_TMA] = TT_SMEM;
-            e->refine_fns[STG_FLOW] = uni ? (void *)k_refine32f<true, RF_NS> : (void *)k_refine32f<false, RF_NS>;
-            e->refine_smems[STG_FLOW] = (size_t)RF_NS * (uni ? rt_stage<true>() : rt_stage<false>()) + 128;
-            // CMSL_TF_VARIANT: 0 rotation loaded per plane, 4 blocks per SM;
-            // 1 rotation kept per grain, 3 blocks per SM and a 5-plane ring;
-            // 2 rotation kept per grain, 4 blocks per SM; 3 rotation loaded
-            // per plane, 3 blocks per SM and a 5-plane ring
-            const char *tv = getenv("CMSL_TF_VARIANT");
-            const int tfv = tv ? atoi(tv) : 0;
-            if (tfv == 1 || tfv == 3) {
-                e->tdgl_fns[STG_FLOW] = tfv == 1 ? (void *)k_tdgl32f<5, true, 3> : (void *)k_tdgl32f<5, false, 3>;
-                e->tdgl_smems[STG_FLOW] = (size_t)5 * TT_STAGE + 128;
-            } else {
-                e->tdgl_fns[STG_FLOW] = tfv == 2 ? (void *)k_tdgl32f<TF_NS, true, 4> : (void *)k_tdgl32f<TF_NS, false, 4>;
-                e->tdgl_smems[STG_FLOW] = (size_t)TF_NS * TT_STAGE + 128;
-            }
         }
         for (int v = 0; v < (e->tma ? N_STG : 1); ++v) {
             CK(cudaFuncSetAttribute(e->refine_fns[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1279,8 +1264,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         }
         e->refine_nt = e->tdgl_nt = NT;
         // CMSL_STAGING=<tdgl><residual> (digits 0 cp.async ring, 1 tensor
-        // copies, 2 warp-flow tensor copies) fixes the staging of films with
-        // full tiles; the autotuner then keeps it
+        // copies) fixes the staging of films with full tiles; the autotuner
+        // then keeps it
         int st_t = STG_TMA, st_r = STG_TMA;
         const char *sg = getenv("CMSL_STAGING");
         e->staging_fixed = false;
@@ -1621,7 +1606,7 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
     const int nst = tune_stg ? N_STG : 1;
     for (int c : cands) {
         TRY(set_items(e, c));
-        double tt[N_STG] = {0.0, 0.0, 0.0}, tr[N_STG] = {0.0, 0.0, 0.0}, rest = 0.0;
+        double tt[N_STG] = {0.0, 0.0}, tr[N_STG] = {0.0, 0.0}, rest = 0.0;
         for (int v = 0; v < nst; ++v) {
             if (tune_stg) e->stage(v, v);
             double ms[4] = {0, 0, 0, 0};

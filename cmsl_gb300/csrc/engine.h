@@ -34,7 +34,7 @@ cmsl_status fail(cmsl_status s, const char *fmt, ...);
     } while (0)
 
 // Staging of the FP32 stencil passes (Engine::stage).
-enum { STG_CP = 0, STG_TMA = 1, STG_FLOW = 2, N_STG = 3 };
+enum { STG_CP = 0, STG_TMA = 1, N_STG = 2 };
 
 // Host view of one film of a handle.
 struct FilmHost {
@@ -100,16 +100,14 @@ struct Engine {
     bool spec_col = false;      // column layout: x, fused y-z-y, x (three launches per solve)
     bool persistent = false;
     // staging of the FP32 stencil passes: STG_CP the cp.async ring (any
-    // film), STG_TMA tensor copies with a block barrier per plane, STG_FLOW
-    // tensor copies with per-stage full/empty barriers and no block barrier
-    // (the tensor copies need every film's nx % 32 == 0, ny % 8 == 0).  The
-    // TDGL and the residual passes each take the staging the autotuner
-    // measured fastest (STG_TMA until tuned)
+    // film), STG_TMA tensor copies (every film's nx % 32 == 0, ny % 8 == 0).
+    // The TDGL and the residual passes each take the staging the autotuner
+    // measured faster (STG_TMA until tuned)
     bool tma = false;
     int stg_tdgl = 0, stg_refine = 0;
     bool staging_fixed = false;         // CMSL_STAGING set the staging: the autotuner keeps it
-    void *tdgl_fns[3] = {nullptr, nullptr, nullptr}, *refine_fns[3] = {nullptr, nullptr, nullptr};
-    size_t tdgl_smems[3] = {0, 0, 0}, refine_smems[3] = {0, 0, 0};
+    void *tdgl_fns[2] = {nullptr, nullptr}, *refine_fns[2] = {nullptr, nullptr};
+    size_t tdgl_smems[2] = {0, 0}, refine_smems[2] = {0, 0};
     void stage(int tdgl_stg, int refine_stg)
     {
         stg_tdgl = tma ? tdgl_stg : 0;

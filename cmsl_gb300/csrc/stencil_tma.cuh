@@ -390,326 +390,4 @@ __global__ void __launch_bounds__(NT, 4) k_refine32t(Dev d, Fields<float> F)
 }
 
 
-// ------------------------------------------------ warp-flow tensor-copy ring
-// The stage layout and copies of TmaRing without a block barrier per plane:
-// full[s] completes when the plane staged in s has landed, empty[s] when all
-// NT/32 warps have released it.  A warp releases plane k-1 once it has read
-// plane k's neighbourhood (computing k+1 reads k, k+1 and k+2), and the first
-// lane of one warp per plane -- warp (k - z0) % (NT/32), so the issue work and
-// the wait for the slowest warp rotate over the warps -- waits until every
-// warp has released plane k-1 and issues plane k-1+NS into that stage.  Plane
-// p is first read when computing p-1, so NS-3 planes are in flight while a
-// warp computes, and a fast warp runs at most NS-3 planes ahead of the
-// slowest.  Every issued plane is waited for by every thread before the item
-// ends, so no copy is in flight when the block exits.
-template <int NS> struct TmaFlow {
-    uint32_t base;                // shared address of stage 0
-    const unsigned char *ptr;     // generic address of stage 0
-    uint64_t *full, *empty;
-    const TmaOp *ops;
-    int n_ops, zlo, zhi, stage_bytes;
-    uint32_t tx;                  // bytes per plane
-    __device__ __forceinline__ int st(int p) const { return (p - zlo) % NS; }
-    __device__ __forceinline__ uint32_t par(int p) const { return (uint32_t)((p - zlo) / NS) & 1u; }
-    // one thread: plane p into its stage once the plane before it there is released
-    __device__ __forceinline__ void produce(int p, int *err) const
-    {
-        if (p > zhi) return;
-        const int s = st(p);
-        if (p - NS >= zlo) mbar_wait(&empty[s], par(p - NS), err);
-        tma_issue_all(ops, n_ops, base + (uint32_t)(s * stage_bytes), p, &full[s], tx);
-    }
-    __device__ __forceinline__ void wait(int p, int *err) const
-    {
-        if (p <= zhi) mbar_wait(&full[st(p)], par(p), err);
-    }
-    // first lane of a warp, after the warp's last read of plane p
-    __device__ __forceinline__ void release(int p) const
-    {
-        if (p >= zlo && p <= zhi) mbar_arrive(&empty[st(p)]);
-    }
-    __device__ __forceinline__ const unsigned char *stage(int s) const { return ptr + s * stage_bytes; }
-};
-
-// The barriers initialised (thread 0); the caller issues the first planes
-// from thread 0 and syncs the block before any thread waits.
-template <int NS>
-__device__ __forceinline__ TmaFlow<NS> flow_setup(unsigned char *dyn, uint64_t *full, uint64_t *empty,
-                                                  const TmaOp *ops, int zlo, int zhi, int stage_bytes)
-{
-    TmaFlow<NS> r;
-    const uint32_t raw = smem_u32(dyn);
-    r.base = (raw + 127u) & ~127u;
-    r.ptr = dyn + (r.base - raw);
-    r.full = full;
-    r.empty = empty;
-    r.ops = ops;
-    r.zlo = zlo;
-    r.zhi = zhi;
-    r.stage_bytes = stage_bytes;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < NS; ++s) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], NT / 32);
-        }
-        fence_barrier_init();
-    }
-    return r;
-}
-
-// This warp has read plane k's neighbourhood: release plane k-1, and the
-// rotating producer issues plane k-1+NS (planes up to zlo+NS-1 come from the
-// prologue).
-template <int NS>
-__device__ __forceinline__ void flow_advance(const TmaFlow<NS> &R, int k, int z0, int *err)
-{
-    __syncwarp();
-    if ((threadIdx.x & 31) != 0) return;
-    R.release(k - 1);
-    if (k - 1 >= R.zlo && (int)(threadIdx.x >> 5) == (k - z0) % (NT / 32)) R.produce(k - 1 + NS, err);
-}
-
-// ------------------------------------------------ TDGL step, warp flow
-// k_tdgl32t with the warp-flow ring.  TRC: the grain rotation is kept in
-// registers while the cell's grain id is unchanged from the plane below
-// (columnar grains: loaded once per item); MINB resident blocks per SM.
-constexpr int TF_NS = 4;
-
-template <int NS, bool TRC, int MINB>
-__global__ void __launch_bounds__(NT, MINB) k_tdgl32f(Dev d, Fields<float> F)
-{
-    static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
-    extern __shared__ unsigned char smem_tf[];
-    __shared__ __align__(8) uint64_t full[NS], empty[NS];
-    __shared__ TmaOp ops[TT_OPS];
-    __shared__ float4 sC[6][3];
-    __shared__ double sRed[NT / 32][7];
-    __shared__ double sTot[7];
-    const int4 it = d.items[blockIdx.x];
-    const FilmDev *f = d.films + it.x;
-    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    load_coef4(f, sC);
-    const int nx = f->nx, ny = f->ny, nz = f->nz, x0 = it.y, y0 = it.z;
-    const int cur = d.ctl->cur, rs = d.ctl->run_step;
-    const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
-    const int row = d.rows[(long long)it.x * d.wstride + rs];
-    const int dep = f->dep_flag, warm = f->warm;
-    const bool neu = f->zbc != 0;
-    const float inv_2hf = f->inv_2hf;
-    const long long off = f->off, fs = d.ncells, plane = (long long)nx * ny;
-    const SolveDev *S = d.solve + it.x;
-    const int pcur = S->phi_cur;
-    const float2 *qh = phi2_sel(d, S->phi_prev) + off;
-    const float2 *uh = phi2_sel(d, S->phi_prev2) + off;
-    const float2 *vh = phi2_sel(d, S->phi_prev3) + off;
-    float2 *nh = phi2_sel(d, phi_free(S)) + off;
-    const float4 *TR4 = (const float4 *)(F.TR + (long long)TR32 * f->g_off);
-    float2 *Pn = pairs32(F, cur ^ 1) + off;
-    const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
-    const FilmMaps *M = d.maps + it.x;
-
-    auto R = flow_setup<NS>(smem_tf, full, empty, ops, zlo, zhi, TT_STAGE);
-    R.n_ops = 3 * 5 + (dep ? 5 : 0) + 1;
-    R.tx = (uint32_t)(3 * REG2 + (dep ? REG2 : 0) + BODY1);
-    if (threadIdx.x == 0) {
-        OpBuilder b{ops, 0, x0, y0, nx, ny};
-        for (int j = 0; j < 3; ++j) b.region(p_maps(M, cur), j * REG2, j, 8);
-        if (dep) b.region(phi_maps(M, pcur), TT_PHI, -1, 8);
-        b.body(M->code, TT_CODE - 4 * TR_BODY, -1, 4);
-        for (int p = zlo; p <= min(zlo + NS - 1, zhi); ++p) R.produce(p, d.err);
-    }
-    __syncthreads();
-    for (int p = zlo; p <= z0; ++p) R.wait(p, d.err);
-
-    const NbOff o2 = nb_off(8);
-    const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
-    float acc[7];
-    #pragma unroll
-    for (int q = 0; q < 7; ++q) acc[q] = 0.f;
-    RingIdx<NS> ri{z0 - zlo};
-    long long o = (long long)(x0 + lx) + (long long)nx * (y0 + ly) + (long long)z0 * plane;
-    float2 oq{0.f, 0.f}, ou{0.f, 0.f};
-    auto ld_old = [&](long long oo) {
-        if (dep && warm >= 1) oq = qh[oo];
-        if (dep && warm >= 2) ou = uh[oo];
-    };
-    ld_old(o);
-    int gid = -1;
-    float t[9];
-    for (int k = z0; k < z1; ++k, o += plane, ri.next()) {
-        R.wait(k + 1, d.err);
-        const df wq{oq.x, oq.y}, wu{ou.x, ou.y};
-        const df wv = (dep && warm >= 3) ? ld_df(vh + o) : df{0.f, 0.f};
-        if (k + 1 < z1) ld_old(o + plane);
-        const unsigned char *sk = R.stage(ri.s);
-        const unsigned char *su = R.stage(ri.up(k == nz - 1)), *sd = R.stage(ri.dn(k == 0));
-        const uint32_t c = ((const uint32_t *)(sk + TT_CODE))[threadIdx.x];
-        if (!TRC || code_gid(c) != gid) {
-            gid = code_gid(c);
-            load_tr32(TR4 + 3LL * gid, t);
-        }
-        float pc[6], sum[6];
-        #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const float2 *a = (const float2 *)(sk + j * REG2);
-            const float2 cc = a[o2.c], xe = a[o2.e], xw = a[o2.w], yn = a[o2.n], ys = a[o2.s];
-            const float2 zu = ((const float2 *)(su + j * REG2))[o2.c], zd = ((const float2 *)(sd + j * REG2))[o2.c];
-            pc[2 * j] = cc.x;
-            pc[2 * j + 1] = cc.y;
-            // neighbour sums e, w, n, s, u, d (kernels_evol.cu:101-122); z clamped
-            sum[2 * j] = ((((xe.x + xw.x) + yn.x) + ys.x) + zu.x) + zd.x;
-            sum[2 * j + 1] = ((((xe.y + xw.y) + yn.y) + ys.y) + zu.y) + zd.y;
-        }
-        float ex = 0.f, ey = 0.f, ez = 0.f;
-        df a0{0.f, 0.f};
-        if (dep) {
-            const float2 *f2 = (const float2 *)(sk + TT_PHI);
-            const float2 fc = f2[o2.c], fe = f2[o2.e], fw = f2[o2.w], fn = f2[o2.n], fsth = f2[o2.s];
-            const float2 fu = ((const float2 *)(su + TT_PHI))[o2.c], fd = ((const float2 *)(sd + TT_PHI))[o2.c];
-            a0 = df{fc.x, fc.y};
-            df pu, pd;
-            efield_z(neu, k, nz, df{fu.x, fu.y}, df{fd.x, fd.y}, pu, pd);
-            // -1 * E with E = -(phi_+ - phi_-) / (2h)
-            ex = phi_diff32(df{fe.x, fe.y}, df{fw.x, fw.y}) * inv_2hf;
-            ey = phi_diff32(df{fn.x, fn.y}, df{fsth.x, fsth.y}) * inv_2hf;
-            ez = phi_diff32(pu, pd) * inv_2hf;
-        }
-        // this warp's reads of the ring for plane k are done
-        flow_advance(R, k, z0, d.err);
-        float pn[6], pMZl, pSZl;
-        tdgl_cell32t(sC[code_mat(c) * 2 + code_iface(c)], t, pc, sum, ex, ey, ez, mEz, pn, pMZl, pSZl);
-        #pragma unroll
-        for (int j = 0; j < 3; ++j) Pn[j * fs + o] = make_float2(pn[2 * j], pn[2 * j + 1]);
-        if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
-        if (dep) {
-            const df w = extrap_phi(warm, a0, wq, wu, wv);
-            nh[o] = make_float2(w.h, w.l);
-        }
-    }
-
-    if (row >= 0) block_partial32<7>(d, acc, sRed);
-    if (!ticket_last(d.counter)) return;
-    tdgl_finish<true>(d, rs, sRed, sTot);
-}
-
-// ------------------------------------------------- residual pass, warp flow
-// k_refine32t with the warp-flow ring.
-constexpr int RF_NS = 5;
-
-template <bool UNI, int NS>
-__global__ void __launch_bounds__(NT, 4) k_refine32f(Dev d, Fields<float> F)
-{
-    static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
-    constexpr int STAGE = rt_stage<UNI>();
-    extern __shared__ unsigned char smem_rf[];
-    __shared__ __align__(8) uint64_t full[NS], empty[NS];
-    __shared__ TmaOp ops[RT_OPS];
-    __shared__ double sRed[NT / 32][3];
-    __shared__ double sTot[3];
-    const int4 it = d.items[blockIdx.x];
-    const FilmDev *f = d.films + it.x;
-    const SolveDev *S = d.solve + it.x;
-    const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    const int nx = f->nx, ny = f->ny, nz = f->nz, x0 = it.y, y0 = it.z;
-    const long long plane = (long long)nx * ny;
-    // film constants in registers (the stores below might alias the film table)
-    RConst rc;
-    rc.cb = df{f->cb_h, f->cb_l};
-    rc.cu = df{f->cf_h[0], f->cf_l[0]};
-    rc.dinv_u = f->dinv_uni;
-    rc.nz = nz;
-    rc.neu = f->zbc != 0;
-    rc.ref = f->ref_id;
-    rc.cf_h = f->cf_h;
-    rc.cf_l = f->cf_l;
-    const bool run = f->dep_flag != 0 && (d.force || S->outer_active);
-    const bool apply = S->refine > 0;                   // later pass: x = phi + dx; first: the warm start
-    const bool upd = UNI && apply && S->upd && f->upd_ok;   // r <- r - A dx (after the direct solve, one eps)
-    const int cur = d.ctl->cur, fr = phi_free(S), xb = apply ? S->phi_cur : fr;
-    const long long off = f->off;
-    float2 *nh = phi2_sel(d, fr) + off;
-    float *r = F.r + off;
-    const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
-    const FilmMaps *M = d.maps + it.x;
-
-    auto R = flow_setup<NS>(smem_rf, full, empty, ops, zlo, run ? zhi : -1, STAGE);
-    R.n_ops = upd ? 7 : 5 + (apply ? 5 : 0) + 5 + 1 + (UNI ? 0 : 6);
-    R.tx = (uint32_t)(upd ? BODY2 + REG1 + BODY1
-                          : REG2 + (apply ? REG1 : 0) + REG2 + BODY2 + (UNI ? 0 : REG1 + BODY1));
-    if (threadIdx.x == 0) {
-        OpBuilder b{ops, 0, x0, y0, nx, ny};
-        if (upd) {
-            b.body(phi_maps(M, xb), RT_X, -1, 8);
-            b.region(M->x, RT_DX, -1, 4);
-            b.add(&M->r, RT_PZ, x0, y0, -1);
-        } else {
-            b.region(phi_maps(M, xb), RT_X, -1, 8);
-            if (apply) b.region(M->x, RT_DX, -1, 4);
-            b.region(p_maps(M, cur ^ 1), RT_PA, 0, 8);
-            b.add(&p_maps(M, cur ^ 1)[TM_BODY], RT_PZ, x0, y0, 1);
-            if (!UNI) {
-                b.region(M->code, RT_CODE, -1, 4);
-                b.add(&M->dinv, RT_DINV, x0, y0, -1);
-            }
-        }
-        for (int p = zlo; p <= min(zlo + NS - 1, R.zhi); ++p) R.produce(p, d.err);
-    }
-    __syncthreads();
-
-    const NbOff o2 = nb_off(8), o1 = nb_off(4);
-    const int lx = threadIdx.x % TX, ly = threadIdx.x / TX, tz = threadIdx.x;
-    const long long own_pl = (long long)(x0 + lx) + (long long)nx * (y0 + ly);
-    const long long pin = rc.neu ? rc.ref - own_pl : -1;   // the pinned cell's plane offset in this column
-    float acc[3] = {0.f, 0.f, 0.f};
-    if (run) {
-        for (int p = zlo; p <= z0; ++p) R.wait(p, d.err);
-        RingIdx<NS> ri{z0 - zlo};
-        long long o = own_pl + (long long)z0 * plane;
-        for (int k = z0; k < z1; ++k, o += plane, ri.next()) {
-            R.wait(k + 1, d.err);
-            const unsigned char *sk = R.stage(ri.s);
-            const unsigned char *su = R.stage(ri.up(k == nz - 1)), *sd = R.stage(ri.dn(k == 0));
-            auto D = [&](const unsigned char *st, int s) { return ((const float *)(st + RT_DX))[s]; };
-            auto X = [&](const unsigned char *st, int s2, int s1) {   // x = phi (+ dx on later passes)
-                const float2 v = ((const float2 *)(st + RT_X))[s2];
-                const df p{v.x, v.y};
-                return apply ? df_add_f(p, D(st, s1)) : p;
-            };
-            auto PA = [&](const unsigned char *st, int s) { return ((const float2 *)(st + RT_PA))[s]; };
-            auto M_ = [&](const unsigned char *st, int s) {
-                return UNI ? 0 : code_mat(((const uint32_t *)(st + RT_CODE))[s]);
-            };
-            RCell c;
-            c.xc = X(sk, o2.c, o1.c);
-            c.mc = M_(sk, o1.c); c.me = M_(sk, o1.e); c.mw = M_(sk, o1.w); c.mn = M_(sk, o1.n); c.ms = M_(sk, o1.s);
-            c.mu = M_(su, o1.c); c.md = M_(sd, o1.c);
-            if (upd) {
-                c.dc = D(sk, o1.c); c.de = D(sk, o1.e); c.dw = D(sk, o1.w); c.dn = D(sk, o1.n);
-                c.ds = D(sk, o1.s); c.du = D(su, o1.c); c.dd = D(sd, o1.c);
-            } else {
-                c.xe = X(sk, o2.e, o1.e); c.xw = X(sk, o2.w, o1.w); c.xn = X(sk, o2.n, o1.n);
-                c.xs = X(sk, o2.s, o1.s);
-                c.xu = X(su, o2.c, o1.c); c.xd = X(sd, o2.c, o1.c);
-                c.pxe = PA(sk, o2.e).x; c.pxw = PA(sk, o2.w).x;
-                c.pyn = PA(sk, o2.n).y; c.pys = PA(sk, o2.s).y;
-                c.pzu = ((const float2 *)(su + RT_PZ))[tz].x;
-                c.pzd = ((const float2 *)(sd + RT_PZ))[tz].x;
-            }
-            const float r_old = upd ? ((const float *)(sk + RT_PZ))[tz] : 0.f;
-            const float dv = UNI ? 0.f : ((const float *)(sk + RT_DINV))[tz];
-            // this warp's reads of the ring for plane k are done
-            flow_advance(R, k, z0, d.err);
-            // identity rows: the Dirichlet planes, or the Neumann pin
-            const bool ident = rc.neu ? (long long)k * plane == pin : (k == 0 || k == nz - 1);
-            float rv;
-            refine_cell<UNI>(rc, k, ident, upd, c, r_old, dv, rv, acc);
-            r[o] = rv;
-            if (apply) nh[o] = make_float2(c.xc.h, c.xc.l);
-        }
-    }
-    refine_partials(d, acc, sRed);
-    if (!ticket_last(d.counter)) return;
-    refine_finish(d, sRed, sTot);
-}
-
 }  // namespace cmsl

@@ -46,12 +46,6 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
-// One arrival (release semantics at block scope), no byte count.
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;
@@ -112,19 +106,6 @@ struct TmaOp {
     int x, y, q;    // q < 0: a 3D map
     int pad;
 };
-
-// All `n` copies of plane z from one thread (the producer of a warp-flow ring).
-__device__ __forceinline__ void tma_issue_all(const TmaOp *ops, int n, uint32_t stage, int z, uint64_t *bar,
-                                              uint32_t bytes)
-{
-    fence_proxy_async_smem();
-    mbar_arrive_expect_tx(bar, bytes);
-    for (int i = 0; i < n; ++i) {
-        const TmaOp o = ops[i];
-        if (o.q < 0) tma_load_3d(stage + o.dst, o.map, o.x, o.y, z, bar);
-        else tma_load_4d(stage + o.dst, o.map, o.x, o.y, z, o.q, bar);
-    }
-}
 
 // Issues the `n` copies of plane z into the stage at byte address `stage`,
 // spread over the first lane of every warp of the block (warp w: copies w,

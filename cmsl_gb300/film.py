@@ -103,9 +103,9 @@ def _oracle_kw(f):
 def _tile_config(fn, h):
     cfg = (C.c_int32 * 4)()
     check(fn(h, cfg))
-    names = ("cp.async ring", "tensor copies", "tensor copies, warp flow")
+    names = ("cp.async ring", "tensor copies")
     return {"x": int(cfg[0]), "y": int(cfg[1]), "z_chunk": int(cfg[2]),
-            "tdgl_staging": names[cfg[3] & 3], "residual_staging": names[(cfg[3] >> 2) & 3]}
+            "tdgl_staging": names[cfg[3] & 1], "residual_staging": names[(cfg[3] >> 2) & 1]}
 
 
 class Film:

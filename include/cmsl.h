@@ -201,8 +201,7 @@ cmsl_status cmsl_film_autotune(cmsl_film *film, int32_t *zchunk);
 /* The stencil-pass configuration in use: cfg[0] tile x, cfg[1] tile y,
  * cfg[2] z chunk (0: the per-film heuristic), cfg[3] the stagings: bits 0-1
  * the TDGL's, bits 2-3 the residual passes' (0 the cp.async ring, 1 tensor
- * copies with a block barrier per plane, 2 tensor copies with per-stage
- * full/empty barriers). */
+ * copies). */
 cmsl_status cmsl_film_tile_config(cmsl_film *film, int32_t cfg[4]);
 
 /* Bytes of device memory the film holds. */

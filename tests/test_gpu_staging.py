@@ -1,11 +1,10 @@
-"""The three stagings of the FP32 stencil passes on films with full 32 x 8
-tiles -- the cp.async ring (0), tensor copies with a block barrier per plane
-(1), tensor copies with per-stage full/empty barriers and no block barrier
-(2) -- each fixed through CMSL_STAGING at film creation, advance a film like
-the FP64 oracle solved to 1e-12 (max |P| error <= 2e-5 of max |P|, as the
-other FP32-refined parity tests).  Both residual kernels are covered: one
-permittivity (direct inner solve) and three (persistent PCG), Dirichlet and
-Neumann z boundaries, and every variant of the warp-flow TDGL."""
+"""The two stagings of the FP32 stencil passes on films with full 32 x 8
+tiles -- the cp.async ring (0) and tensor copies (1) -- in every combination
+for the TDGL and the residual passes, each fixed through CMSL_STAGING at film
+creation, advance a film like the FP64 oracle solved to 1e-12 (max |P| error
+<= 2e-5 of max |P|, as the other FP32-refined parity tests).  Both residual
+kernels are covered: one permittivity (direct inner solve) and three
+(persistent PCG), Dirichlet and Neumann z boundaries."""
 import numpy as np
 import pytest
 
@@ -39,11 +38,10 @@ def _oracle_film(orc, w, mats, zbc):
     return f
 
 
-@pytest.mark.parametrize("staging,variant", [("00", "0"), ("11", "0"), ("22", "0"), ("22", "1"),
-                                             ("22", "2"), ("22", "3"), ("21", "1"), ("12", "0")])
+@pytest.mark.parametrize("staging", ["00", "11", "01", "10"])
 @pytest.mark.parametrize("eps", ["one", "three"])
 @pytest.mark.parametrize("zbc", [oracle.DIRICHLET, oracle.NEUMANN])
-def test_staging_matches_oracle(gpu, orc, staging, variant, eps, zbc, monkeypatch):
+def test_staging_matches_oracle(gpu, orc, staging, eps, zbc, monkeypatch):
     from cmsl_gb300 import workloads as wl
     w = wl.hzo_film("stg_64x32x13", 64, 32, 13, 9, 21, 0.4, E_amp_MVcm=4.0, steps_per_period=400)
     mats = np.array(w.mats, copy=True)
@@ -57,10 +55,9 @@ def test_staging_matches_oracle(gpu, orc, staging, variant, eps, zbc, monkeypatc
     Pw, _, _, _, _, rc = orc.run(f, P0, np.zeros(w.N), Ez)
     assert rc == 0
     monkeypatch.setenv("CMSL_STAGING", staging)
-    monkeypatch.setenv("CMSL_TF_VARIANT", variant)
     with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED) as g:
         cfg = g.tile_config()
-        names = ("cp.async ring", "tensor copies", "tensor copies, warp flow")
+        names = ("cp.async ring", "tensor copies")
         assert cfg["tdgl_staging"] == names[int(staging[0])]
         assert cfg["residual_staging"] == names[int(staging[1])]
         g.set_state(P0)
