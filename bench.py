@@ -252,6 +252,7 @@ def run_reference(args):
     # each step is a bounded sample: the full film, one time step
     cpu_port_rate(w, max(1, min(args.warmup, 1)), 60.0)
     rate, done, secs = cpu_port_rate(w, args.steps, 150.0)
+    gpu_ref = reference_gpu(w) if not args.no_ref_gpu else None
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-steps/s", "n_gpus": args.gpus,
         "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(done, 1),
@@ -262,9 +263,36 @@ def run_reference(args):
                          "sample": "%d full time steps of %s (%d cells) from its initial state" %
                                    (done, w.name, w.N)},
         "e2e": {"value": rate, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_fp64_gpu": gpu_ref,
     }
     print(json.dumps(line))
     return 0
+
+
+def reference_gpu(w):
+    """The reference program's own FP64 GPU path (Pfmhzo.exe: its CUDA TDGL
+    kernel and cuBLAS Jacobi-PCG) on a film of this workload's grid and grain
+    count, built from the staged sources (oracle/ref_gpu.sh) and timed by the
+    Evolve loop's own CUDA events; None when the sources are not staged."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        from oracle import ref_gpu_time as rg
+        if not rg.build_reference():
+            return {"unavailable": "reference program sources not staged or its build failed"}
+        amp = float(w.extra.get("Emax", 0.0)) * w.E0_ref          # V/m
+        a = argparse.Namespace(nx=w.nx, ny=w.ny, nz=w.nz, grains=int(len(w.grain_mat)), seed=1,
+                               Eap=amp, delEap=amp / 10.0, num_steps=4, timeout=600.0, only_reference=True)
+        out = rg.measure(a)
+        r = out["reference_fp64"]
+        return {"value": r["cell_steps_per_s"], "unit": "cell-steps/s", "steps": r["steps"], "seconds": r["seconds"],
+                "grid": out["grid"], "grains": out["grains"],
+                "note": "Pfmhzo.exe (reference CUDA kernels + cuBLAS PCG, its own stop test rz <= 1e-6 or "
+                        "rz/rz0 <= 1e-4), one staircase P-E loop of the reference deck on a columnar Voronoi map of "
+                        "this grid, 40 % AFE, eps 30; Kernel execution time of its Evolve"}
+    except Exception as exc:       # reported, never fatal to the CPU baseline
+        return {"unavailable": "%s: %s" % (type(exc).__name__, str(exc)[:300])}
 
 
 def film_kw(cg, fp64: bool, inner=None) -> dict:
@@ -670,6 +698,8 @@ def main():
     ap.add_argument("--repeats", type=int, default=0, help="timed regions of K steps (0: enough for ~1.5 s, >= 10)")
     ap.add_argument("--e2e-repeats", type=int, default=5, help="end-to-end calls (the median is reported)")
     ap.add_argument("--no-pcg", action="store_true", help="skip the PCG-path samples")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="reference arm: skip the reference program's FP64 GPU path")
     ap.add_argument("--config", type=int, default=CONFIG_ID, choices=[0, 1, 2, 3, 4],
                     help="benchmark configuration (default 1; 3 = the 64-film batched ensemble)")
     args = ap.parse_args()

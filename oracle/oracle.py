@@ -144,6 +144,18 @@ def build_ref(reference_root: str | None = None) -> str | None:
     return os.path.join(HERE, "_ref", "libcmsl_ref.so")
 
 
+def stage_ref_gpu(reference_root: str | None = None) -> bool:
+    """Copies the reference program's sources (three mechanical fixes for
+    CUDA 13) into baseline/_ref/hzo for building on a GPU machine
+    (oracle/ref_gpu.sh stage); False when the sources are absent."""
+    reference_root = reference_root or reference_root_or_none()
+    if not reference_root:
+        return False
+    subprocess.run(["sh", os.path.join(HERE, "ref_gpu.sh"), "stage", reference_root], check=True,
+                   stdout=subprocess.DEVNULL)
+    return True
+
+
 class OracleLib:
     def __init__(self, path: str):
         self.lib = L = C.CDLL(path)

@@ -118,15 +118,32 @@ def main(argv=None):
     ap.add_argument("--delEap", type=float, default=3.0e7, help="field step of the staircase, V/m")
     ap.add_argument("--num-steps", type=int, default=2, help="time steps per field level")
     ap.add_argument("--timeout", type=float, default=1200.0)
+    ap.add_argument("--only-reference", action="store_true", help="time Pfmhzo.exe alone")
     args = ap.parse_args(argv)
+    print(json.dumps(measure(args)))
+
+
+def build_reference(timeout: float = 600.0) -> bool:
+    """Builds Pfmhzo.exe (and Pfmhzo_gb when the library is built) from the
+    staged sources; False when they are not staged or the build fails."""
+    if not os.path.exists(os.path.join(REF_DIR, "src", "evolve.cu")):
+        return False
+    r = subprocess.run(["sh", os.path.join(HERE, "ref_gpu.sh"), "build"], capture_output=True, text=True,
+                       timeout=timeout)
+    return r.returncode == 0 and os.path.exists(os.path.join(REF_DIR, "Pfmhzo.exe"))
+
+
+def measure(args) -> dict:
     ref, gb = os.path.join(REF_DIR, "Pfmhzo.exe"), os.path.join(REF_DIR, "Pfmhzo_gb")
-    for x in (ref, gb):
+    runs = [("reference_fp64", ref, {})]
+    if not getattr(args, "only_reference", False):
+        runs += [("cmsl_fp64", gb, {"CMSL_PRECISION": "fp64"}), ("cmsl_fp32_refined", gb, {"CMSL_PRECISION": "fp32"})]
+    for _, x, _ in runs:
         if not os.path.exists(x):
             raise SystemExit("%s missing: run oracle/ref_gpu.sh stage (where the reference is) and build" % x)
     N = args.nx * args.ny * args.nz
     out = {"grid": [args.nx, args.ny, args.nz], "cells": N, "grains": args.grains}
-    for name, exe, env in (("reference_fp64", ref, {}), ("cmsl_fp64", gb, {"CMSL_PRECISION": "fp64"}),
-                           ("cmsl_fp32_refined", gb, {"CMSL_PRECISION": "fp32"})):
+    for name, exe, env in runs:
         with tempfile.TemporaryDirectory() as root:
             steps = make_tree(root, args.nx, args.ny, args.nz, args.grains, args.seed, args.Eap, args.delEap,
                               args.num_steps)
@@ -135,8 +152,8 @@ def main(argv=None):
     out["solve"] = ("the reference's PCG stop test (rz <= 1e-6 or rz/rz0 <= 1e-4, global.cu) for the FP64 runs; "
                     "the FP32-refined run refines to ||b - A phi|| <= 1e-8 ||b||")
     out["speedup_vs_reference_fp64"] = {k: out[k]["cell_steps_per_s"] / out["reference_fp64"]["cell_steps_per_s"]
-                                        for k in ("cmsl_fp64", "cmsl_fp32_refined")}
-    print(json.dumps(out))
+                                        for k in ("cmsl_fp64", "cmsl_fp32_refined") if k in out}
+    return out
 
 
 if __name__ == "__main__":
