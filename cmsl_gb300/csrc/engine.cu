@@ -445,7 +445,7 @@ cmsl_status build_graph(Engine *e)
                     {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
                 const Node cols[] = {
                     {(void *)k_spec_x<true, true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
-                    {(void *)k_spec_yzy, e->spec_grid[3], SPEC_NT, a_s, e->spec_smem[3]},
+                    {(void *)k_spec_yzy, e->spec_grid[3], SPEC_YZY_NT, a_s, e->spec_smem[3]},
                     {(void *)k_spec_x<false, true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
                 const Node *seq = e->spec_col ? cols : rows;
                 const int nseq = e->spec_col ? 3 : 5;
@@ -630,7 +630,7 @@ cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<f
     const SpecDev &sp = e->spec;
     if (e->spec_col) {
         k_spec_x<true, true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
-        k_spec_yzy<<<e->spec_grid[3], SPEC_NT, e->spec_smem[3], st>>>(d, sp);
+        k_spec_yzy<<<e->spec_grid[3], SPEC_YZY_NT, e->spec_smem[3], st>>>(d, sp);
         k_spec_x<false, true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
         CK(cudaGetLastError());
         return CMSL_OK;
@@ -1163,8 +1163,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             byf.insert(byf.end(), (size_t)gy, fi);
             bzf.insert(bzf.end(), (size_t)gz, fi);
             bqf.insert(bqf.end(), (size_t)(h.nx / 2 + 1), fi);                  // mirror pairs of columns
-            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp, P.M, SPEC_NT));
-            smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * h.nx) + 1) + h.nx));   // two tiles + twiddles
+            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp, P.M, SPEC_YZY_NT));
+            smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * spec_x_pitch(h.nx, true)) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }
         SpecDev &sp = e->spec;
@@ -1247,14 +1247,22 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         for (int fi = 0; fi < n; ++fi) e->tma = e->tma && e->fh[fi].nx % TX == 0 && e->fh[fi].ny % TY == 0;
         e->refine_fns[STG_CP] = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
         e->refine_smems[STG_CP] = uni ? r32_smem<true>() : r32_smem<false>();
-        e->tdgl_fns[STG_CP] = (void *)k_tdgl32<T32_NS>;
-        e->tdgl_smems[STG_CP] = T32_SMEM;
+        // experiment: CMSL_TDGL_VARIANT 1 rotation kept per grain (4 blocks/SM),
+        // 2 rotation kept per grain (3 blocks/SM), 3 a 5-plane ring (3 blocks/SM)
+        const char *tv = getenv("CMSL_TDGL_VARIANT");
+        const int tdv = tv ? atoi(tv) : 0;
+        e->tdgl_fns[STG_CP] = tdv == 1 ? (void *)k_tdgl32<T32_NS, true, 4>
+                            : tdv == 2 ? (void *)k_tdgl32<T32_NS, true, 3>
+                            : tdv == 3 ? (void *)k_tdgl32<5, false, 3> : (void *)k_tdgl32<T32_NS>;
+        e->tdgl_smems[STG_CP] = tdv == 3 ? sizeof(float) * 5 * T32_STAGE : T32_SMEM;
         if (e->tma) {
             TRY(make_maps(e));
             e->refine_fns[STG_TMA] = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
             e->refine_smems[STG_TMA] = uni ? rt_smem<true>() : rt_smem<false>();
-            e->tdgl_fns[STG_TMA] = (void *)k_tdgl32t<TT_NS>;
-            e->tdgl_smems[STG_TMA] = TT_SMEM;
+            e->tdgl_fns[STG_TMA] = tdv == 1 ? (void *)k_tdgl32t<TT_NS, true, 4>
+                                 : tdv == 2 ? (void *)k_tdgl32t<TT_NS, true, 3>
+                                 : tdv == 3 ? (void *)k_tdgl32t<5, false, 3> : (void *)k_tdgl32t<TT_NS>;
+            e->tdgl_smems[STG_TMA] = tdv == 3 ? (size_t)5 * TT_STAGE + 128 : TT_SMEM;
         }
         for (int v = 0; v < (e->tma ? N_STG : 1); ++v) {
             CK(cudaFuncSetAttribute(e->refine_fns[v], cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -324,6 +324,8 @@ __device__ __forceinline__ void spec_finish(const Dev &d)
 // COL: the spectra in the column layout, stored (IN_REAL) or loaded through a
 // shared-memory tile transposed, so that a warp touches runs of consecutive
 // y.  Shared memory: two padded tiles of rb rows and the twiddles.
+__host__ __device__ inline int spec_x_pitch(int nx, bool col) { return col ? nx + 1 : nx; }
+
 __device__ __forceinline__ int fft_pow2_passes(int lgn)
 {
     int n = 0;
@@ -352,7 +354,11 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
     float2 *Cf = sp.C + P.coff;
     const SpecAxis ax = P.ax;
     const int M = P.M, Mp = P.Mp;
-    const int tile = spec_pad(rb * nx) + 1;
+    // row pitch of the tiles: nx, or nx + 1 in the column layout, whose
+    // transposed copies read a column of the tile (an odd pitch in 8-byte
+    // words spreads its rows over the banks)
+    const int pitch = spec_x_pitch(nx, COL);
+    const int tile = spec_pad(rb * pitch) + 1;
     float2 *a = sm2, *b = sm2 + tile, *tw = sm2 + 2 * tile;
     for (int t = threadIdx.x; t < nx; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twx + t);
     // spectrum value (row r0 + sq, x element e) in the column layout
@@ -365,14 +371,14 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
         const int total = nr * nx;
         for (int t = threadIdx.x; t < total; t += blockDim.x) {
             const int e = t / nr, sq = t - e * nr;
-            a[spec_pad(sq * nx + e)] = Cf[col_at(sq, e)];
+            a[spec_pad(sq * pitch + e)] = Cf[col_at(sq, e)];
         }
         __syncthreads();
     }
     // row r0 + sq is (j, y) = packed plane j, in-plane row y; its residual
     // rows in r are z planes 2j+1 and 2j+2
     auto ld = [&](int sq, int e) -> float2 {
-        if (!IN_REAL) return COL ? a[spec_pad(sq * nx + e)] : Cf[(long long)(r0 + sq) * nx + e];
+        if (!IN_REAL) return COL ? a[spec_pad(sq * pitch + e)] : Cf[(long long)(r0 + sq) * nx + e];
         const int rw = r0 + sq, j = rw / ny;
         const long long o = (long long)(2 * j + 1) * plane + (long long)(rw - j * ny) * nx + e;
         return make_float2(rr[o], 2 * j + 1 < M ? rr[o + plane] : 0.f);
@@ -381,7 +387,7 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
     float2 *res = (ax.lg >= 0 && (fft_pow2_passes(ax.lg) & 1) == 0) ? a : b;
     auto st = [&](int sq, int e, float2 v) {
         if (IN_REAL) {
-            if (COL) res[spec_pad(sq * nx + e)] = v;
+            if (COL) res[spec_pad(sq * pitch + e)] = v;
             else Cf[(long long)(r0 + sq) * nx + e] = v;
             return;
         }
@@ -395,15 +401,21 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
     };
     if (ax.lg >= 0) {
         __syncthreads();                                                 // twiddles
-        fft_pow2<false>(a, b, nr, ax.lg, 1, nx, tw, ld, st);
+        fft_pow2<false>(a, b, nr, ax.lg, 1, pitch, tw, ld, st);
     } else {
         const int total = nr * nx;
         if (!(COL && !IN_REAL))
-            for (int t = threadIdx.x; t < total; t += blockDim.x) a[spec_pad(t)] = ld(t / nx, t - (t / nx) * nx);
+            for (int t = threadIdx.x; t < total; t += blockDim.x) {
+                const int sq = t / nx, e = t - sq * nx;
+                a[spec_pad(sq * pitch + e)] = ld(sq, e);
+            }
         __syncthreads();
-        res = fft_mixed<false>(a, b, nr, ax, 1, nx, tw);
+        res = fft_mixed<false>(a, b, nr, ax, 1, pitch, tw);
         if (!(COL && IN_REAL))
-            for (int t = threadIdx.x; t < total; t += blockDim.x) st(t / nx, t - (t / nx) * nx, res[spec_pad(t)]);
+            for (int t = threadIdx.x; t < total; t += blockDim.x) {
+                const int sq = t / nx, e = t - sq * nx;
+                st(sq, e, res[spec_pad(sq * pitch + e)]);
+            }
     }
     if (COL && IN_REAL) {
         // transposed store: consecutive threads write consecutive rows of one column
@@ -411,7 +423,7 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
         const int total = nr * nx;
         for (int t = threadIdx.x; t < total; t += blockDim.x) {
             const int e = t / nr, sq = t - e * nr;
-            Cf[col_at(sq, e)] = res[spec_pad(sq * nx + e)];
+            Cf[col_at(sq, e)] = res[spec_pad(sq * pitch + e)];
         }
     }
     if (!IN_REAL) spec_finish(d);
@@ -556,7 +568,9 @@ __host__ __device__ inline size_t spec_yzy_bytes(int ny, int Mp, int M, int nt)
     return sizeof(float2) * (2 * (size_t)(spec_pad(2 * Mp * ny) + 1) + ny) + sizeof(float) * (size_t)M * nt;
 }
 
-static __global__ void __launch_bounds__(SPEC_NT, 1) k_spec_yzy(Dev d, SpecDev sp)
+constexpr int SPEC_YZY_NT = 512;
+
+static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
     const int f = __ldg(sp.bq_film + blockIdx.x);
