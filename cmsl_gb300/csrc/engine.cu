@@ -179,8 +179,8 @@ SpecAxis spec_plan(int n)
 }
 
 // Shared memory of the z solve per thread: the staged / eliminated plane
-// pairs (16 bytes each) and c' per plane (4 bytes).
-size_t spec_zbytes(int M) { return (size_t)16 * ((M + 1) / 2) + (size_t)4 * M; }
+// pairs (16 bytes each).
+size_t spec_zbytes(int M) { return (size_t)16 * ((M + 1) / 2); }
 
 // Threads per block of the z solve: its shared memory stays within 96 KB;
 // 0 if M is too large.
@@ -1125,6 +1125,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         std::vector<SpecFilm> sf((size_t)n);
         std::vector<int> bxf, byf, bzf, bqf;
         size_t smq = 0;
+        long long ioff = 0;
         std::vector<float2> tw;
         std::vector<float> lam;
         long long coff = 0;
@@ -1151,6 +1152,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             P.ay = spec_plan(h.ny);
             P.coff = coff;
             coff += (long long)P.Mp * h.nx * h.ny;
+            P.ioff = ioff;
+            ioff += (long long)P.M * h.nx * h.ny;
             const double eps = descs[fi].mats[0].eps_r;              // harm(eps, eps) = eps on every face
             P.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
             tables(h.nx, &P.twx, &P.lamx);
@@ -1163,9 +1166,39 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             byf.insert(byf.end(), (size_t)gy, fi);
             bzf.insert(bzf.end(), (size_t)gz, fi);
             bqf.insert(bqf.end(), (size_t)(h.nx / 2 + 1), fi);                  // mirror pairs of columns
-            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp, P.M, SPEC_YZY_NT));
+            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp));
             smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * spec_x_pitch(h.nx, true)) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
+        }
+        // the column layout when every film's column pairs fit one block
+        // (CMSL_SPEC_ROWS=1 keeps the row layout)
+        {
+            int dev = 0, optin = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+            const char *rl = getenv("CMSL_SPEC_ROWS");
+            e->spec_col = smq <= (size_t)optin && !(rl && atoi(rl) != 0);
+        }
+        // Thomas pivots of every film, mode and interior plane, in double:
+        // dg = lam_x + lam_y + 2, inv_k = 1 / (dg - c'_{k-1}) with c'_k = -inv_k
+        std::vector<float> piv((size_t)std::max<long long>(ioff, 1));
+        for (int fi = 0; fi < n; ++fi) {
+            const FilmHost &h = e->fh[fi];
+            const SpecFilm &P = sf[fi];
+            if (!h.dep) continue;
+            const long long modes = (long long)h.nx * h.ny;
+            for (int ky = 0; ky < h.ny; ++ky)
+                for (int kx = 0; kx < h.nx; ++kx) {
+                    const double sx = std::sin(M_PI * kx / h.nx), sy = std::sin(M_PI * ky / h.ny);
+                    const double dg = 4.0 * sx * sx + 4.0 * sy * sy + 2.0;
+                    const long long mode = e->spec_col ? (long long)kx * h.ny + ky : (long long)ky * h.nx + kx;
+                    double c = 0.0;
+                    for (int k = 0; k < P.M; ++k) {
+                        const double inv = 1.0 / (dg + c);
+                        piv[(size_t)(P.ioff + k * modes + mode)] = (float)inv;
+                        c = -inv;
+                    }
+                }
         }
         SpecDev &sp = e->spec;
         auto upload = [&](const void *src, size_t bytes, void **dst) -> cmsl_status {
@@ -1181,6 +1214,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(upload(bqf.data(), sizeof(int) * bqf.size(), &p)); sp.bq_film = (const int *)p;
         TRY(upload(tw.data(), sizeof(float2) * tw.size(), &p)); sp.tw = (const float2 *)p;
         TRY(upload(lam.data(), sizeof(float) * lam.size(), &p)); sp.lam = (const float *)p;
+        TRY(upload(piv.data(), sizeof(float) * piv.size(), &p)); sp.piv = (const float *)p;
         TRY(e->alloc((void **)&sp.C, sizeof(float2) * (size_t)coff));
         e->spec_zt = zt;
         e->spec_grid[0] = (int)bxf.size();
@@ -1193,14 +1227,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));
         CK(cudaFuncSetAttribute(k_spec_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[2]));
-        // the column layout when every film's column pairs fit one block
-        // (CMSL_SPEC_ROWS=1 keeps the row layout)
         {
-            int dev = 0, optin = 0;
-            CK(cudaGetDevice(&dev));
-            CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-            const char *rl = getenv("CMSL_SPEC_ROWS");
-            e->spec_col = smq <= (size_t)optin && !(rl && atoi(rl) != 0);
             e->spec_grid[3] = (int)bqf.size();
             e->spec_smem[3] = smq;
             if (e->spec_col) {

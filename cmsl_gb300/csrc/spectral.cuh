@@ -59,6 +59,7 @@ struct SpecFilm {
     float scale;                // h^2 / (eps nx ny)
     int bx0, by0, bz0;          // first block of the film in the x, y and z grids
     int bq0;                    // first block of the film in the column-pair grid (column layout)
+    long long ioff;             // first pivot of the film in SpecDev::piv
 };
 
 struct SpecDev {
@@ -68,6 +69,11 @@ struct SpecDev {
     const float *lam;           // 2 - 2 cos(2 pi t / n) per film and axis
     const int *bx_film, *by_film, *bz_film;   // film of every block of the three grids
     const int *bq_film;         // film of every block of the column-pair grid (column layout)
+    // Thomas pivots 1 / (dg - c'_{k-1}) of every interior plane k and mode,
+    // [k][mode] per film (mode kx * ny + ky in the column layout, ky * nx + kx
+    // in the row layout), computed on the host in double: the z solves run
+    // without divisions on their serial chain
+    const float *piv;
 };
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -485,7 +491,8 @@ __host__ __device__ inline long long spec_canon_count(int nx, int ny)
 // solution is the conjugate).  The thread's packed spectra at m and -m for
 // every plane pair are first copied into shared memory at once (cp.async),
 // then eliminated there: [Mp][blockDim] float4 (Z(m), Z(-m)), overwritten by
-// the eliminated right-hand sides (d'_2j, d'_2j+1), and [M][blockDim] of c'.
+// the eliminated right-hand sides (d'_2j, d'_2j+1); the pivots come from
+// SpecDev::piv.
 // Writes the conjugates of the packed scaled solutions, so that the next
 // forward transforms invert.
 static __global__ void k_spec_z(Dev d, SpecDev sp)
@@ -496,29 +503,25 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
     const SpecFilm &P = sp.films[f];
     const int M = P.M, Mp = P.Mp, T = blockDim.x, tx = threadIdx.x;
     float4 *dp = (float4 *)sm2;
-    float *cps = (float *)(dp + (size_t)Mp * T);
     int x, y;
     if (!spec_canon_mode((long long)(blockIdx.x - P.bz0) * T + tx, P.nx, P.ny, x, y)) return;
     const long long modes = (long long)P.nx * P.ny;
     const long long m = (long long)y * P.nx + x;
     const long long mm = (long long)(y == 0 ? 0 : P.ny - y) * P.nx + (x == 0 ? 0 : P.nx - x);
     float2 *Ca = sp.C + P.coff + m, *Cb = sp.C + P.coff + mm;
+    const float *pv = sp.piv + P.ioff + m;          // pivot of plane k at pv[k * modes]
     for (int j = 0; j < Mp; ++j) {
         float2 *s = (float2 *)(dp + (size_t)j * T + tx);
         cp8(s, Ca + j * modes);
         cp8(s + 1, Cb + j * modes);
     }
     cp_commit();
-    const float dg = __ldg(sp.lam + P.lamx + x) + __ldg(sp.lam + P.lamy + y) + 2.f;
     const float s = 0.5f * P.scale;
     cp_wait<0>();
-    float c_prev = 0.f;
     float2 d_prev = make_float2(0.f, 0.f);
     auto sweep = [&](int k, float2 rk) {             // forward elimination (sub/super-diagonal -1)
-        const float inv = 1.f / (dg + c_prev);
+        const float inv = __ldg(pv + k * modes);
         d_prev = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
-        c_prev = -inv;
-        cps[k * T + tx] = c_prev;
         return d_prev;
     };
     for (int j = 0; j < Mp; ++j) {
@@ -528,8 +531,9 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
         if (2 * j + 1 < M) d1 = sweep(2 * j + 1, make_float2(ab.y + ab.w, ab.z - ab.x));   // (Z(m) - conj Z(-m)) / i
         dp[(size_t)j * T + tx] = make_float4(d0.x, d0.y, d1.x, d1.y);
     }
-    // back substitution, two planes at a time; store conj of the packed pair
-    // W(m) = X_2j + i X_2j+1 and W(-m) = conj X_2j + i conj X_2j+1
+    // back substitution (x_k = d'_k + pivot_k x_{k+1}), two planes at a time;
+    // store conj of the packed pair W(m) = X_2j + i X_2j+1 and
+    // W(-m) = conj X_2j + i conj X_2j+1
     auto put = [&](int j, float2 p0, float2 p1) {
         Ca[j * modes] = make_float2(p0.x - p1.y, -(p0.y + p1.x));
         Cb[j * modes] = make_float2(p0.x + p1.y, p0.y - p1.x);
@@ -539,11 +543,11 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
         const float4 dd = dp[(size_t)j * T + tx];
         float2 v = make_float2(0.f, 0.f);
         if (2 * j + 1 < M) {
-            const float c = cps[(2 * j + 1) * T + tx];
-            v = make_float2(dd.z - c * xn.x, dd.w - c * xn.y);
+            const float c = __ldg(pv + (2 * j + 1) * modes);
+            v = make_float2(dd.z + c * xn.x, dd.w + c * xn.y);
         }
-        const float c = cps[2 * j * T + tx];
-        const float2 u = make_float2(dd.x - c * v.x, dd.y - c * v.y);
+        const float c = __ldg(pv + 2 * j * modes);
+        const float2 u = make_float2(dd.x + c * v.x, dd.y + c * v.y);
         put(j, u, v);
         xn = u;
     }
@@ -561,11 +565,11 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
 // right-hand sides of interior planes 2j and 2j+1 (for a mode that is its
 // own mirror both are real and share its one slot), then the conjugates of
 // the packed solutions, whose forward y transforms go back to the spectra.
-// Shared memory: two tiles, the y twiddles, c' of every interior plane for
-// each thread.
-__host__ __device__ inline size_t spec_yzy_bytes(int ny, int Mp, int M, int nt)
+// Shared memory: two tiles and the y twiddles; the pivots come from
+// SpecDev::piv.
+__host__ __device__ inline size_t spec_yzy_bytes(int ny, int Mp)
 {
-    return sizeof(float2) * (2 * (size_t)(spec_pad(2 * Mp * ny) + 1) + ny) + sizeof(float) * (size_t)M * nt;
+    return sizeof(float2) * (2 * (size_t)(spec_pad(2 * Mp * ny) + 1) + ny);
 }
 
 constexpr int SPEC_YZY_NT = 512;
@@ -581,8 +585,8 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
     const int ncol = kx == kx2 ? 1 : 2, nseq = ncol * Mp;
     const int tile = spec_pad(2 * Mp * ny) + 1;
     float2 *A = sm2, *B = sm2 + tile, *tw = sm2 + 2 * tile;
-    float *cps = (float *)(tw + ny);
     const SpecAxis ay = P.ay;
+    const long long modes = (long long)nx * ny;
     float2 *Cf = sp.C + P.coff;
     auto gcol = [&](int sq) {                    // first value of sequence sq in the spectra
         const int j = sq / ncol, c = sq - j * ncol;
@@ -606,21 +610,16 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
     // z solve, one thread per mode pair (as k_spec_z)
     const int npair = ncol == 2 ? ny : ny / 2 + 1;
     const float s = 0.5f * P.scale;
-    const float lx = __ldg(sp.lam + P.lamx + kx);
     for (int ky = threadIdx.x; ky < npair; ky += blockDim.x) {
         const int ky2 = ky == 0 ? 0 : ny - ky;
         const bool self = ncol == 1 && ky == ky2;
-        float *cp = cps + threadIdx.x;
+        const float *pv = sp.piv + P.ioff + (long long)kx * ny + ky;   // pivot of plane k at pv[k * modes]
         auto slot_a = [&](int j) { return &R[spec_pad((j * ncol) * ny + ky)]; };
         auto slot_b = [&](int j) { return &R[spec_pad((j * ncol + ncol - 1) * ny + ky2)]; };
-        const float dg = lx + __ldg(sp.lam + P.lamy + ky) + 2.f;
-        float c_prev = 0.f;
         float2 d_prev = make_float2(0.f, 0.f);
         auto sweep = [&](int k, float2 rk) {     // forward elimination (sub/super-diagonal -1)
-            const float inv = 1.f / (dg + c_prev);
+            const float inv = __ldg(pv + k * modes);
             d_prev = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
-            c_prev = -inv;
-            cp[(size_t)k * blockDim.x] = c_prev;
             return d_prev;
         };
         for (int j = 0; j < Mp; ++j) {
@@ -635,8 +634,9 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
                 *slot_b(j) = d1;
             }
         }
-        // back substitution, two planes at a time; the slots take the
-        // conjugates of W(m) = X_2j + i X_2j+1 and W(-m) = conj X_2j + i conj X_2j+1
+        // back substitution (x_k = d'_k + pivot_k x_{k+1}), two planes at a
+        // time; the slots take the conjugates of W(m) = X_2j + i X_2j+1 and
+        // W(-m) = conj X_2j + i conj X_2j+1
         float2 xn = make_float2(0.f, 0.f);
         for (int j = Mp - 1; j >= 0; --j) {
             float2 d0, d1;
@@ -650,11 +650,11 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
             }
             float2 v = make_float2(0.f, 0.f);
             if (2 * j + 1 < M) {
-                const float c = cp[(size_t)(2 * j + 1) * blockDim.x];
-                v = make_float2(d1.x - c * xn.x, d1.y - c * xn.y);
+                const float c = __ldg(pv + (2 * j + 1) * modes);
+                v = make_float2(d1.x + c * xn.x, d1.y + c * xn.y);
             }
-            const float c = cp[(size_t)(2 * j) * blockDim.x];
-            const float2 u = make_float2(d0.x - c * v.x, d0.y - c * v.y);
+            const float c = __ldg(pv + 2 * j * modes);
+            const float2 u = make_float2(d0.x + c * v.x, d0.y + c * v.y);
             *slot_a(j) = make_float2(u.x - v.y, -(u.y + v.x));
             if (!self) *slot_b(j) = make_float2(u.x + v.y, u.y - v.x);
             xn = u;
