@@ -179,8 +179,8 @@ SpecAxis spec_plan(int n)
 }
 
 // Shared memory of the z solve per thread: the staged / eliminated plane
-// pairs (16 bytes each).
-size_t spec_zbytes(int M) { return (size_t)16 * ((M + 1) / 2); }
+// pairs (16 bytes each) and the pivots (4 bytes per plane).
+size_t spec_zbytes(int M) { return (size_t)16 * ((M + 1) / 2) + (size_t)4 * M; }
 
 // Threads per block of the z solve: its shared memory stays within 96 KB;
 // 0 if M is too large.
@@ -1166,7 +1166,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             byf.insert(byf.end(), (size_t)gy, fi);
             bzf.insert(bzf.end(), (size_t)gz, fi);
             bqf.insert(bqf.end(), (size_t)(h.nx / 2 + 1), fi);                  // mirror pairs of columns
-            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp));
+            smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp, P.M));
             smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * spec_x_pitch(h.nx, true)) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }

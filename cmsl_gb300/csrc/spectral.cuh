@@ -491,8 +491,8 @@ __host__ __device__ inline long long spec_canon_count(int nx, int ny)
 // solution is the conjugate).  The thread's packed spectra at m and -m for
 // every plane pair are first copied into shared memory at once (cp.async),
 // then eliminated there: [Mp][blockDim] float4 (Z(m), Z(-m)), overwritten by
-// the eliminated right-hand sides (d'_2j, d'_2j+1); the pivots come from
-// SpecDev::piv.
+// the eliminated right-hand sides (d'_2j, d'_2j+1), and [M][blockDim] of
+// the mode's pivots (SpecDev::piv) staged with them.
 // Writes the conjugates of the packed scaled solutions, so that the next
 // forward transforms invert.
 static __global__ void k_spec_z(Dev d, SpecDev sp)
@@ -509,7 +509,11 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
     const long long m = (long long)y * P.nx + x;
     const long long mm = (long long)(y == 0 ? 0 : P.ny - y) * P.nx + (x == 0 ? 0 : P.nx - x);
     float2 *Ca = sp.C + P.coff + m, *Cb = sp.C + P.coff + mm;
-    const float *pv = sp.piv + P.ioff + m;          // pivot of plane k at pv[k * modes]
+    float *pvs = (float *)(dp + (size_t)Mp * T) + tx;   // this thread's pivots, plane k at pvs[k * T]
+    {
+        const float *pv = sp.piv + P.ioff + m;          // pivot of plane k at pv[k * modes]
+        for (int k = 0; k < M; ++k) cp4(pvs + (size_t)k * T, pv + k * modes);
+    }
     for (int j = 0; j < Mp; ++j) {
         float2 *s = (float2 *)(dp + (size_t)j * T + tx);
         cp8(s, Ca + j * modes);
@@ -520,7 +524,7 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
     cp_wait<0>();
     float2 d_prev = make_float2(0.f, 0.f);
     auto sweep = [&](int k, float2 rk) {             // forward elimination (sub/super-diagonal -1)
-        const float inv = __ldg(pv + k * modes);
+        const float inv = pvs[(size_t)k * T];
         d_prev = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
         return d_prev;
     };
@@ -543,10 +547,10 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
         const float4 dd = dp[(size_t)j * T + tx];
         float2 v = make_float2(0.f, 0.f);
         if (2 * j + 1 < M) {
-            const float c = __ldg(pv + (2 * j + 1) * modes);
+            const float c = pvs[(size_t)(2 * j + 1) * T];
             v = make_float2(dd.z + c * xn.x, dd.w + c * xn.y);
         }
-        const float c = __ldg(pv + 2 * j * modes);
+        const float c = pvs[(size_t)(2 * j) * T];
         const float2 u = make_float2(dd.x + c * v.x, dd.y + c * v.y);
         put(j, u, v);
         xn = u;
@@ -565,11 +569,11 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
 // right-hand sides of interior planes 2j and 2j+1 (for a mode that is its
 // own mirror both are real and share its one slot), then the conjugates of
 // the packed solutions, whose forward y transforms go back to the spectra.
-// Shared memory: two tiles and the y twiddles; the pivots come from
-// SpecDev::piv.
-__host__ __device__ inline size_t spec_yzy_bytes(int ny, int Mp)
+// Shared memory: two tiles, the y twiddles and the column's pivots
+// (SpecDev::piv).
+__host__ __device__ inline size_t spec_yzy_bytes(int ny, int Mp, int M)
 {
-    return sizeof(float2) * (2 * (size_t)(spec_pad(2 * Mp * ny) + 1) + ny);
+    return sizeof(float2) * (2 * (size_t)(spec_pad(2 * Mp * ny) + 1) + ny) + sizeof(float) * (size_t)M * ny;
 }
 
 constexpr int SPEC_YZY_NT = 512;
@@ -592,6 +596,14 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
         const int j = sq / ncol, c = sq - j * ncol;
         return Cf + ((long long)j * nx + (c ? kx2 : kx)) * ny;
     };
+    // the pivots of column kx (its mirror column's are the same: lam(nx - kx) =
+    // lam(kx), lam(ny - ky) = lam(ky)), staged while the transforms run
+    float *pvs = (float *)(tw + ny);
+    for (int t = threadIdx.x; t < M * ny; t += blockDim.x) {
+        const int k = t / ny, ky = t - k * ny;
+        cp4(pvs + t, sp.piv + P.ioff + k * modes + (long long)kx * ny + ky);
+    }
+    cp_commit();
     for (int t = threadIdx.x; t < ny; t += blockDim.x) tw[t] = __ldg(sp.tw + P.twy + t);
     __syncthreads();
     // forward y transforms: spectra -> tile R
@@ -607,18 +619,20 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
         R = fft_mixed<false>(A, B, nseq, ay, 1, ny, tw);
     }
     __syncthreads();
+    cp_wait<0>();
+    __syncthreads();
     // z solve, one thread per mode pair (as k_spec_z)
     const int npair = ncol == 2 ? ny : ny / 2 + 1;
     const float s = 0.5f * P.scale;
     for (int ky = threadIdx.x; ky < npair; ky += blockDim.x) {
         const int ky2 = ky == 0 ? 0 : ny - ky;
         const bool self = ncol == 1 && ky == ky2;
-        const float *pv = sp.piv + P.ioff + (long long)kx * ny + ky;   // pivot of plane k at pv[k * modes]
+        const float *pv = pvs + ky;              // pivot of plane k at pv[k * ny]
         auto slot_a = [&](int j) { return &R[spec_pad((j * ncol) * ny + ky)]; };
         auto slot_b = [&](int j) { return &R[spec_pad((j * ncol + ncol - 1) * ny + ky2)]; };
         float2 d_prev = make_float2(0.f, 0.f);
         auto sweep = [&](int k, float2 rk) {     // forward elimination (sub/super-diagonal -1)
-            const float inv = __ldg(pv + k * modes);
+            const float inv = pv[k * ny];
             d_prev = make_float2((rk.x * s + d_prev.x) * inv, (rk.y * s + d_prev.y) * inv);
             return d_prev;
         };
@@ -650,10 +664,10 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
             }
             float2 v = make_float2(0.f, 0.f);
             if (2 * j + 1 < M) {
-                const float c = __ldg(pv + (2 * j + 1) * modes);
+                const float c = pv[(2 * j + 1) * ny];
                 v = make_float2(d1.x + c * xn.x, d1.y + c * xn.y);
             }
-            const float c = __ldg(pv + 2 * j * modes);
+            const float c = pv[2 * j * ny];
             const float2 u = make_float2(d0.x + c * v.x, d0.y + c * v.y);
             *slot_a(j) = make_float2(u.x - v.y, -(u.y + v.x));
             if (!self) *slot_b(j) = make_float2(u.x + v.y, u.y - v.x);

@@ -187,8 +187,8 @@ constexpr int T32_NS = 4;
 constexpr int T32_STAGE = 8 * SPL + NT;      // floats
 constexpr size_t T32_SMEM = sizeof(float) * T32_NS * T32_STAGE;
 
-template <int NS>
-__global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
+template <int NS, bool TRC = false, int MINB = 4>
+__global__ void __launch_bounds__(NT, MINB) k_tdgl32(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
     extern __shared__ float4 smem_t32[];
@@ -248,6 +248,8 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
     #pragma unroll
     for (int q = 0; q < 7; ++q) acc[q] = 0.f;
     const int s0 = g.own_slot;
+    int gid = -1;
+    float t[9];
     RingIdx<NS> ri{z0 - zlo};
     long long o = g.own_pl + (long long)z0 * g.plane;
     for (int k = z0; k < z1; ++k, o += g.plane, ri.next()) {
@@ -291,8 +293,11 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32(Dev d, Fields<float> F)
             ez = phi_diff32(pu, pd) * inv_2hf;
         }
         float pn[6], pMZl, pSZl;
-        tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
-                    pMZl, pSZl);
+        if (!TRC || code_gid(c) != gid) {
+            gid = code_gid(c);
+            load_tr32(TR4 + 3LL * gid, t);
+        }
+        tdgl_cell32t(sC[code_mat(c) * 2 + code_iface(c)], t, pc, sum, ex, ey, ez, mEz, pn, pMZl, pSZl);
         #pragma unroll
         for (int j = 0; j < 3; ++j) Pn[j * fs + o] = make_float2(pn[2 * j], pn[2 * j + 1]);
         if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);

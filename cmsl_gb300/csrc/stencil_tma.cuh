@@ -143,8 +143,8 @@ constexpr int TT_PHI = 3 * REG2, TT_CODE = 4 * REG2, TT_STAGE = 4 * REG2 + BODY1
 constexpr size_t TT_SMEM = (size_t)TT_NS * TT_STAGE + 128;
 constexpr int TT_OPS = 3 * 5 + 5 + 1;
 
-template <int NS>
-__global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
+template <int NS, bool TRC = false, int MINB = 4>
+__global__ void __launch_bounds__(NT, MINB) k_tdgl32t(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
     extern __shared__ unsigned char smem_tt[];
@@ -195,6 +195,8 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
     float acc[7];
     #pragma unroll
     for (int q = 0; q < 7; ++q) acc[q] = 0.f;
+    int gid = -1;
+    float t[9];
     RingIdx<NS> ri{z0 - zlo};
     long long o = (long long)(x0 + lx) + (long long)nx * (y0 + ly) + (long long)z0 * plane;
     const long long plane_step = plane;
@@ -243,8 +245,11 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
             ez = phi_diff32(pu, pd) * inv_2hf;
         }
         float pn[6], pMZl, pSZl;
-        tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
-                    pMZl, pSZl);
+        if (!TRC || code_gid(c) != gid) {
+            gid = code_gid(c);
+            load_tr32(TR4 + 3LL * gid, t);
+        }
+        tdgl_cell32t(sC[code_mat(c) * 2 + code_iface(c)], t, pc, sum, ex, ey, ez, mEz, pn, pMZl, pSZl);
         #pragma unroll
         for (int j = 0; j < 3; ++j) Pn[j * fs + o] = make_float2(pn[2 * j], pn[2 * j + 1]);
         if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
