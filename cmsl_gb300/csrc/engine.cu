@@ -1170,14 +1170,16 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * spec_x_pitch(h.nx, true)) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }
-        // the column layout when every film's column pairs fit one block
-        // (CMSL_SPEC_ROWS=1 keeps the row layout)
+        // the row layout; CMSL_SPEC_COLS=1 selects the column layout for films
+        // whose column pairs fit one block (three launches instead of five,
+        // 3-5 us less kernel time per solve, but no shorter a step: measured
+        // equal at 256x256x32 and 1-2 us longer at 64x64x16 and 128x128x16)
         {
             int dev = 0, optin = 0;
             CK(cudaGetDevice(&dev));
             CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-            const char *rl = getenv("CMSL_SPEC_ROWS");
-            e->spec_col = smq <= (size_t)optin && !(rl && atoi(rl) != 0);
+            const char *cl = getenv("CMSL_SPEC_COLS");
+            e->spec_col = smq <= (size_t)optin && cl && atoi(cl) != 0;
         }
         // Thomas pivots of every film, mode and interior plane, in double:
         // dg = lam_x + lam_y + 2, inv_k = 1 / (dg - c'_{k-1}) with c'_k = -inv_k

@@ -25,10 +25,10 @@
 // computed in double.  The z solve keeps the Thomas elimination in shared
 // memory, so each spectrum value is read and written once per sweep.
 //
-// Two layouts of the spectra.  Row layout ([Mp][ny][nx], five launches): x
-// transforms, y transforms, z solve, y transforms, x transforms.  Column
-// layout ([Mp][nx][ny], three launches, films whose column pairs fit one
-// block's shared memory): the x transforms store (and the last ones load)
+// Two layouts of the spectra.  Row layout ([Mp][ny][nx], five launches, the
+// default): x transforms, y transforms, z solve, y transforms, x transforms.
+// Column layout ([Mp][nx][ny], three launches, films whose column pairs fit
+// one block's shared memory, selected by CMSL_SPEC_COLS=1): the x transforms store (and the last ones load)
 // through shared memory transposed, and one block per mirror pair of
 // columns {kx, nx - kx} holds both columns of every packed plane, so it runs
 // the y transforms, the z solve of all modes (kx, ky) with their mirrors

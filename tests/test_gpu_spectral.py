@@ -36,10 +36,10 @@ def _uniform(shape, seed, eps=30.0):
 @pytest.mark.parametrize("layout", ["columns", "rows"])
 @pytest.mark.parametrize("shape", [(32, 24, 8), (48, 36, 10), (64, 16, 5), (96, 12, 7), (8, 9, 3), (27, 32, 12)])
 def test_direct_solve_run_vs_oracle(gpu, shape, layout, monkeypatch):
-    """Both layouts of the spectra: columns (x transforms, one block per
-    mirror pair of columns for y, z and y, x transforms) and rows (five
-    passes, CMSL_SPEC_ROWS=1)."""
-    monkeypatch.setenv("CMSL_SPEC_ROWS", "1" if layout == "rows" else "0")
+    """Both layouts of the spectra: rows (five passes, the default) and
+    columns (x transforms, one block per mirror pair of columns for y, z and
+    y, x transforms; CMSL_SPEC_COLS=1)."""
+    monkeypatch.setenv("CMSL_SPEC_COLS", "1" if layout == "columns" else "0")
     f, P = _uniform(shape, seed=sum(shape))
     n = 16
     Ez = np.linspace(0.0, 0.35, n)
