@@ -490,13 +490,18 @@ def run_ours(args):
         mats3[:, 7] = [40.0, 30.0, 15.0]      # eps_afe, eps_fe, eps_de of src/inputs/InputParams
         Ks = max(5, min(K, 20))
         pcg = {"uni_eps_pcg": side_run(cg, w, False, cg.INNER_PCG, Ks, stream),
-               "three_eps": side_run(cg, w, False, None, Ks, stream, mats=mats3),
+               "three_eps_pcg": side_run(cg, w, False, cg.INNER_PCG, Ks, stream, mats=mats3),
+               "three_eps_preconditioned": side_run(cg, w, False, None, Ks, stream, mats=mats3),
                "fp64_uni_eps": side_run(cg, w, True, None, 3, stream),
                "fp64_three_eps": side_run(cg, w, True, None, 3, stream, mats=mats3)}
+        pcg["three_eps_preconditioned"]["note"] = (
+            "the direct solve with the middle of the film's permittivity range preconditions the double-float "
+            "refinement (the film's grains use eps 40 and 30)")
         pcg["speedup_fp32_over_fp64"] = {
             "direct_inner_solve": value / pcg["fp64_uni_eps"]["value"],
             "same_inner_pcg_uni_eps": pcg["uni_eps_pcg"]["value"] / pcg["fp64_uni_eps"]["value"],
-            "same_inner_pcg_three_eps": pcg["three_eps"]["value"] / pcg["fp64_three_eps"]["value"]}
+            "same_inner_pcg_three_eps": pcg["three_eps_pcg"]["value"] / pcg["fp64_three_eps"]["value"],
+            "three_eps_preconditioned": pcg["three_eps_preconditioned"]["value"] / pcg["fp64_three_eps"]["value"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -211,6 +211,50 @@ template <class T> void fill_coef(Coef<T> &c, const cmsl_material &mt, int iface
     c.a02 = (T)(2.0 * mt.a0);
 }
 
+// Permittivities of the materials a film's grains use: the reference value
+// of its direct solve (the middle of their range, which minimises the
+// spectral radius of I - M^-1 A for M = eps_ref times the Laplacian, the
+// discrete operator's face permittivities lying between the smallest and the
+// largest) and the ratio largest / smallest.
+double spec_eps_ref(const cmsl_film_desc &d, double *kappa)
+{
+    bool used[3] = {false, false, false};
+    for (int g = 0; g < d.n_grains; ++g)
+        if (d.grain_mat[g] >= 0 && d.grain_mat[g] <= 2) used[d.grain_mat[g]] = true;
+    double lo = 0.0, hi = 0.0;
+    bool any = false;
+    for (int m = 0; m < 3; ++m) {
+        if (!used[m]) continue;
+        const double e = d.mats[m].eps_r;
+        lo = any ? std::min(lo, e) : e;
+        hi = any ? std::max(hi, e) : e;
+        any = true;
+    }
+    if (!any || !(lo > 0.0)) {
+        if (kappa) *kappa = 1.0;
+        return d.mats[0].eps_r;
+    }
+    if (kappa) *kappa = hi / lo;
+    return 0.5 * (lo + hi);
+}
+
+// Several permittivities with the direct solve: the solve is a
+// preconditioner (M = eps_ref times the Laplacian) of the double-float
+// refinement, which then contracts the residual by (kappa - 1) / (kappa + 1)
+// per pass; CMSL_INNER_AUTO takes it up to this ratio of permittivities.
+constexpr double SPEC_PRECOND_KAPPA = 4.0;
+
+// Refinement passes such a film may take: enough for the contraction
+// (kappa - 1) / (kappa + 1) to reach the refinement target from a zero
+// start, plus a margin.
+int spec_precond_refine_cap(double kappa, double refine_tol)
+{
+    const double rho = (kappa - 1.0) / (kappa + 1.0);
+    const double tol = refine_tol > 0.0 ? std::min(refine_tol, 1e-2) : 1e-8;
+    const double n = rho > 0.0 ? std::ceil(std::log(tol) / std::log(rho)) : 1.0;
+    return (int)std::min(500.0, std::max(16.0, n + 8.0));
+}
+
 // The film-constant table of one film (set-up of main.cu:261-359 and
 // depol_varEPS.cu:126-180 reduced to per-material constants).
 void fill_film(FilmDev &fd, const cmsl_film_desc *dsc, int precision)
@@ -935,26 +979,30 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         all_uni &= descs[i].mats[0].eps_r == descs[i].mats[1].eps_r && descs[i].mats[1].eps_r == descs[i].mats[2].eps_r;
     }
     // direct (spectral) inner solve: every film with a depolarisation solve
-    // has the Dirichlet z boundary, one eps and 2^a 3^b sides
+    // has the Dirichlet z boundary and 2^a 3^b sides; with one eps it is the
+    // exact inverse, with several a preconditioner of the refinement
     int spec_mmax = 1;
     {
-        bool want = false, forced = false, ok = e->precision != CMSL_FP64, anydep = false;
+        bool want = false, forced = false, ok = e->precision != CMSL_FP64, anydep = false, ok_auto = true;
         for (int i = 0; i < n; ++i) {
             const cmsl_film_desc &d = descs[i];
             forced |= d.inner_solver == CMSL_INNER_DIRECT;
             want |= d.inner_solver != CMSL_INNER_PCG;
             if (!d.dep_flag) continue;
             anydep = true;
-            const bool uni = d.mats[0].eps_r == d.mats[1].eps_r && d.mats[1].eps_r == d.mats[2].eps_r;
-            ok &= d.zbc == CMSL_DIRICHLET && uni && d.nz >= 3 && spec_radix_ok(d.nx) && spec_radix_ok(d.ny);
+            double kappa = 1.0;
+            spec_eps_ref(d, &kappa);
+            // several permittivities: the solve preconditions the refinement
+            // (AUTO up to SPEC_PRECOND_KAPPA, any ratio when DIRECT is asked for)
+            ok_auto &= kappa <= SPEC_PRECOND_KAPPA;
+            ok &= d.zbc == CMSL_DIRICHLET && d.nz >= 3 && spec_radix_ok(d.nx) && spec_radix_ok(d.ny);
             spec_mmax = std::max(spec_mmax, d.nz - 2);
         }
         ok &= anydep && spec_zthreads(spec_mmax) > 0;
         if (forced && !ok)
             return fail(CMSL_ERR_ARG, "inner_solver DIRECT needs FP32_REFINED films whose depolarisation solves have "
-                                      "the Dirichlet z boundary, one eps for all materials and nx, ny of the form "
-                                      "2^a 3^b <= 4096");
-        e->spectral = ok && want;
+                                      "the Dirichlet z boundary and nx, ny of the form 2^a 3^b <= 4096");
+        e->spectral = ok && want && (forced || ok_auto);
     }
     int cg_per = 0, cg_nsm = 0;
     e->persistent = e->precision != CMSL_FP64 && !e->spectral && all_dirichlet && n <= CG_MAX_FILMS &&
@@ -988,7 +1036,15 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         }
         FilmDev &fd = fds[fi];
         fill_film(fd, dsc, e->precision);
-        fd.upd_ok = e->spectral ? 1 : 0;
+        // the FP32 update pass r <- r - A dx follows an exact (one-eps) direct solve only
+        fd.upd_ok = e->spectral && fd.uni_eps ? 1 : 0;
+        if (e->spectral && !fd.uni_eps && fd.dep_flag) {
+            double kappa = 1.0;
+            spec_eps_ref(*dsc, &kappa);
+            const int cap = spec_precond_refine_cap(kappa, dsc->refine_tol);
+            fd.max_refine = std::max(fd.max_refine, cap);
+            e->max_refine_cap = std::max(e->max_refine_cap, cap);
+        }
         fd.off = h.off;
         fd.g_off = g_off;
         g_off += h.ng;
@@ -1154,7 +1210,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             coff += (long long)P.Mp * h.nx * h.ny;
             P.ioff = ioff;
             ioff += (long long)P.M * h.nx * h.ny;
-            const double eps = descs[fi].mats[0].eps_r;              // harm(eps, eps) = eps on every face
+            // harm(eps, eps) = eps on every face; several eps: the reference value
+            const double eps = spec_eps_ref(descs[fi], nullptr);
             P.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
             tables(h.nx, &P.twx, &P.lamx);
             tables(h.ny, &P.twy, &P.lamy);

@@ -92,10 +92,17 @@ typedef struct {
 } cmsl_film_desc;
 
 /* The direct inner solve applies to FP32_REFINED films (or batches) whose
- * depolarisation solves have the Dirichlet z boundary, one permittivity for
- * all materials and nx, ny of the form 2^a 3^b (<= 4096): an in-plane FFT, a
- * tridiagonal solve along z per mode and the inverse FFT (exact for that
- * operator up to FP32 rounding). */
+ * depolarisation solves have the Dirichlet z boundary and nx, ny of the form
+ * 2^a 3^b (<= 4096): an in-plane FFT, a tridiagonal solve along z per mode and
+ * the inverse FFT.  With one permittivity for all materials it is exact for
+ * the operator up to FP32 rounding.  With several it solves with one
+ * reference permittivity (the middle of the range the film's grains use) and
+ * preconditions the double-float refinement, whose residual applies the true
+ * operator: each pass contracts the residual by (kappa - 1) / (kappa + 1),
+ * kappa the ratio of the largest to the smallest permittivity, and such a
+ * film may take more refinement passes than max_refine (enough to reach
+ * refine_tol from a zero potential).  CMSL_INNER_AUTO takes it for kappa <= 4
+ * and the PCG otherwise. */
 typedef enum { CMSL_INNER_AUTO = 0, CMSL_INNER_PCG = 1, CMSL_INNER_DIRECT = 2 } cmsl_inner_solver;
 
 typedef struct cmsl_film cmsl_film;

@@ -78,7 +78,8 @@ def test_autotune_before_any_state_on_tensor_copy_films(gpu, inner):
     Ez = w.sched.Ez[:n] * 40.0
     Pw, _, _, _, _, rc = orc.run(f, w.P_init, np.zeros(w.N), Ez)
     assert rc == 0
-    with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED) as g:
+    with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED,
+                                   inner_solver=gpu.INNER_DIRECT if inner == "direct" else gpu.INNER_PCG) as g:
         assert g.inner_solver == (gpu.INNER_DIRECT if inner == "direct" else gpu.INNER_PCG)
         assert g.autotune() in (4, 8, 10)
         cfg = g.tile_config()

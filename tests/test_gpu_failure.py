@@ -42,10 +42,10 @@ def _env(**kw):
 
 def test_pcg_barrier_timeout_is_reported_and_context_survives(gpu):
     cg = gpu
-    # three permittivities (40 / 30 / 15): the FP32 inner solve is the persistent PCG
+    # three permittivities (40 / 30 / 15), the inner solve forced to the persistent PCG
     f, P = random_film(64, 32, 8, seed=71, eps_0_nd=3.0, p_scale=0.2)
     Ez = np.full(3, 0.1)
-    kw = dict(precision=cg.FP32_REFINED, refine_tol=1e-8, max_refine=4, inner_tol=1e-5)
+    kw = dict(precision=cg.FP32_REFINED, refine_tol=1e-8, max_refine=4, inner_tol=1e-5, inner_solver=cg.INNER_PCG)
     old = _env(CMSL_PCG_HOLD_BLOCK="1", CMSL_PCG_SPIN_LIMIT="2000")
     try:
         g = cg.Film.from_oracle_film(f, **kw)

@@ -100,9 +100,16 @@ def test_direct_solve_selection(gpu):
         assert g.inner_solver == gpu.INNER_PCG
     with pytest.raises(gpu.CmslError):
         gpu.Film.from_oracle_film(f, inner_solver=gpu.INNER_DIRECT, **kw)
-    f2, _ = random_film(32, 24, 6, seed=5)          # three permittivities
-    with gpu.Film.from_oracle_film(f2, **kw) as g:
+    f2, _ = random_film(32, 24, 6, seed=5)          # three permittivities, 40 / 30 / 15
+    with gpu.Film.from_oracle_film(f2, **kw) as g:   # ratio 2.7: the solve preconditions the refinement
+        assert g.inner_solver == gpu.INNER_DIRECT
+    mats = MATS_DEFAULT.copy()
+    mats[:, 7] = [100.0, 30.0, 15.0]                 # ratio 6.7: AUTO takes the PCG, DIRECT may be asked for
+    f4, _ = random_film(32, 24, 6, seed=5, mats=mats)
+    with gpu.Film.from_oracle_film(f4, **kw) as g:
         assert g.inner_solver == gpu.INNER_PCG
+    with gpu.Film.from_oracle_film(f4, inner_solver=gpu.INNER_DIRECT, **kw) as g:
+        assert g.inner_solver == gpu.INNER_DIRECT
     f3, _ = _uniform((32, 24, 6), seed=6)
     with gpu.Film.from_oracle_film(f3) as g:          # FP64: the reference's PCG
         assert g.inner_solver == gpu.INNER_PCG
@@ -147,3 +154,47 @@ def test_direct_solve_batch(gpu):
                 Ps, _ = g.get_state()
             for a, w in zip(Pg, Ps):
                 assert np.abs(a - w).max() <= 2e-5 * max(np.abs(w).max(), 1e-30), i
+
+
+@pytest.mark.parametrize("eps", [(40.0, 30.0, 15.0), (40.0, 30.0, 30.0), (100.0, 30.0, 15.0)])
+@pytest.mark.parametrize("shape", [(32, 24, 8), (48, 36, 10), (27, 32, 12)])
+def test_preconditioned_refinement_several_eps(gpu, shape, eps):
+    """Several permittivities with the direct solve: the solve with one
+    reference eps (the middle of the film's range) preconditions the
+    double-float refinement, whose residual pass applies the true operator
+    (harmonic face eps).  Against the FP64 oracle solved to 1e-12 with the
+    tolerances of the other FP32-refined tests; the potential meets the
+    refinement target in FP64; the passes per step stay near
+    log(1e-4 ... 1e-8) / log((kappa - 1) / (kappa + 1))."""
+    mats = MATS_DEFAULT.copy()
+    mats[:, 7] = eps
+    f, P = random_film(*shape, seed=sum(shape) + int(eps[0]), eps_0_nd=4.0, mats=mats, p_scale=0.2, layered=True)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, 1e-12, 20000
+    n = 10
+    Ez = np.linspace(0.0, 0.35, n)
+    rows = np.arange(n, dtype=np.int32)
+    orc = oracle.load()
+    Pw, _, phiw, statw, _, rc = orc.run(f, P, np.zeros(f.N), Ez, rows)
+    assert rc == 0
+    kw = dict(precision=gpu.FP32_REFINED, refine_tol=1e-8, inner_tol=1e-5, max_refine=6,
+              inner_solver=gpu.INNER_DIRECT)
+    with gpu.Film.from_oracle_film(f, **kw) as g:
+        assert g.inner_solver == gpu.INNER_DIRECT
+        g.set_state(P)
+        g.run(Ez, rows)
+        Pg, phig = g.get_state()
+        rg = g.rows()
+        it, rf = g.iters()
+    for a, b in zip(Pg, Pw):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+    assert np.abs(phig - phiw).max() <= 1e-4 * np.abs(phiw).max()
+    assert np.abs(rg[:, :10] - statw[:, :10]).max() <= 1e-5
+    used = sorted(set(float(mats[m, 7]) for m in np.unique(f.grain_mat)))
+    kappa = used[-1] / used[0]
+    rho = (kappa - 1.0) / (kappa + 1.0)
+    bound = 3 + (int(np.ceil(np.log(1e-8) / np.log(rho))) if rho > 0 else 0)
+    assert (rf >= 2).all() and (rf <= bound).all(), (rf, bound)
+    b = -orc.divergence(f, Pg[0], Pg[1], Pg[2])
+    k = np.repeat(np.arange(f.nz), f.nx * f.ny)
+    b[(k == 0) | (k == f.nz - 1)] = 0.0
+    assert np.linalg.norm(b - orc.apply_A(f, phig)) <= 1.5e-8 * np.linalg.norm(b)
