@@ -67,6 +67,8 @@ struct FilmDev {
     float inv_h2f, inv_2hf, eps0f;
     float dinv_uni;             // Jacobi D^-1 of non-identity rows when every material has one eps
     int uni_eps;                // all materials share eps_r
+    float cheb_delta;           // direct solve preconditioning several eps: (kappa - 1) / (kappa + 1),
+                                // the half-width of M^-1 A's spectrum around 1 (0: exact solve)
     int upd_ok;                 // FP32_REFINED: the inner solve leaves r intact (direct solve), so a
                                 // later refinement pass may update r instead of recomputing it
     double n_mat[3];            // voxels per material (sum of the reference's masks)
@@ -95,6 +97,8 @@ struct SolveDev {               // per film, lives in device memory
     int inner_max;              // inner iteration cap of the current pass
     int upd;                    // the next refinement pass updates r <- r - A dx (FP32) instead of
                                 // forming b - A phi in double-float
+    double cheb_rho;            // Chebyshev recurrence of the preconditioned refinement (rho_k)
+    float cheb_w, cheb_m;       // the next direct solve's increment: dx <- w M^-1 r + m dx
 };
 
 // Extra vectors of the single-reduction FP32 PCG (FP32_REFINED mode).

@@ -240,15 +240,18 @@ double spec_eps_ref(const cmsl_film_desc &d, double *kappa)
 
 // Several permittivities with the direct solve: the solve is a
 // preconditioner (M = eps_ref times the Laplacian) of the double-float
-// refinement, which then contracts the residual by (kappa - 1) / (kappa + 1)
-// per pass; CMSL_INNER_AUTO takes it up to this ratio of permittivities.
-constexpr double SPEC_PRECOND_KAPPA = 4.0;
+// refinement, whose increments follow the Chebyshev semi-iteration for M^-1
+// A's spectrum [1 - delta, 1 + delta], delta = (kappa - 1) / (kappa + 1):
+// the residual contracts by about (sqrt(kappa) - 1) / (sqrt(kappa) + 1) per
+// pass; CMSL_INNER_AUTO takes it up to this ratio of permittivities.
+constexpr double SPEC_PRECOND_KAPPA = 16.0;
 
-// Refinement passes such a film may take: enough for the contraction
-// (kappa - 1) / (kappa + 1) to reach the refinement target from a zero
-// start, plus a margin.
+// Refinement passes such a film may take: enough for the plain (fixed-step)
+// contraction (kappa - 1) / (kappa + 1) to reach the refinement target from
+// a zero start, plus a margin -- a safe bound for the Chebyshev iteration.
 int spec_precond_refine_cap(double kappa, double refine_tol)
 {
+    // twice the Chebyshev estimate, and never fewer than plain Richardson's passes would need
     const double rho = (kappa - 1.0) / (kappa + 1.0);
     const double tol = refine_tol > 0.0 ? std::min(refine_tol, 1e-2) : 1e-8;
     const double n = rho > 0.0 ? std::ceil(std::log(tol) / std::log(rho)) : 1.0;
@@ -1038,9 +1041,11 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         fill_film(fd, dsc, e->precision);
         // the FP32 update pass r <- r - A dx follows an exact (one-eps) direct solve only
         fd.upd_ok = e->spectral && fd.uni_eps ? 1 : 0;
+        fd.cheb_delta = 0.f;
         if (e->spectral && !fd.uni_eps && fd.dep_flag) {
             double kappa = 1.0;
             spec_eps_ref(*dsc, &kappa);
+            fd.cheb_delta = (float)((kappa - 1.0) / (kappa + 1.0));
             const int cap = spec_precond_refine_cap(kappa, dsc->refine_tol);
             fd.max_refine = std::max(fd.max_refine, cap);
             e->max_refine_cap = std::max(e->max_refine_cap, cap);

@@ -799,6 +799,24 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
             // times the stencil's cancellation) then stays far below the
             // refinement target; never two update passes in a row
             S->upd = !was_upd && ff->upd_ok && sTot[0] <= 1e-8 * bb;
+            // the next direct solve's increment (Chebyshev semi-iteration for a
+            // direct solve preconditioning several eps, M^-1 A's spectrum in
+            // [1 - delta, 1 + delta]): solve 0 of a step dx = M^-1 r, then
+            // rho_k = 1 / (2 / delta - rho_{k-1}), dx_k = (2 rho_k / delta) M^-1 r
+            // + rho_k rho_{k-1} dx_{k-1}
+            {
+                const double dl = ff->cheb_delta;
+                if (dl <= 0.0 || S->refine == 1) {
+                    S->cheb_rho = dl;
+                    S->cheb_w = 1.f;
+                    S->cheb_m = 0.f;
+                } else {
+                    const double rp = S->cheb_rho, rk = 1.0 / (2.0 / dl - rp);
+                    S->cheb_rho = rk;
+                    S->cheb_w = (float)(2.0 * rk / dl);
+                    S->cheb_m = (float)(rk * rp);
+                }
+            }
             S->iters = 0;
             S->rz = S->rz0 = sTot[2];
             if (conv || !isfinite(sTot[0])) {

@@ -391,6 +391,11 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
     };
     // the tile that receives the transform in the column layout's store
     float2 *res = (ax.lg >= 0 && (fft_pow2_passes(ax.lg) & 1) == 0) ? a : b;
+    // the increment of this solve: w M^-1 r + m (the previous increment), from
+    // the film's Chebyshev recurrence (w = 1, m = 0 for an exact solve)
+    const SolveDev *Sf = d.solve + f;
+    const float cw = IN_REAL ? 1.f : (d.force || Sf->cheb_w == 0.f ? 1.f : Sf->cheb_w);
+    const float cm = IN_REAL || d.force ? 0.f : Sf->cheb_m;
     auto st = [&](int sq, int e, float2 v) {
         if (IN_REAL) {
             if (COL) res[spec_pad(sq * pitch + e)] = v;
@@ -400,8 +405,13 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
         // the transform of conj(W) is conj(x_2j + i x_2j+1) (scale folded into the z solve)
         const int rw = r0 + sq, j = rw / ny;
         const long long yx = (long long)(rw - j * ny) * nx + e, o = (long long)(2 * j + 1) * plane + yx;
-        xx[o] = v.x;
-        if (2 * j + 1 < M) xx[o + plane] = -v.y;
+        if (cm != 0.f) {
+            xx[o] = cw * v.x + cm * xx[o];
+            if (2 * j + 1 < M) xx[o + plane] = cw * -v.y + cm * xx[o + plane];
+        } else {
+            xx[o] = cw * v.x;
+            if (2 * j + 1 < M) xx[o + plane] = cw * -v.y;
+        }
         if (j == 0) xx[yx] = 0.f;                                        // first Dirichlet plane
         if (j == Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;      // last one
     };

@@ -98,11 +98,13 @@ typedef struct {
  * the operator up to FP32 rounding.  With several it solves with one
  * reference permittivity (the middle of the range the film's grains use) and
  * preconditions the double-float refinement, whose residual applies the true
- * operator: each pass contracts the residual by (kappa - 1) / (kappa + 1),
- * kappa the ratio of the largest to the smallest permittivity, and such a
- * film may take more refinement passes than max_refine (enough to reach
- * refine_tol from a zero potential).  CMSL_INNER_AUTO takes it for kappa <= 4
- * and the PCG otherwise. */
+ * operator; the refinement's increments follow the Chebyshev semi-iteration
+ * for the preconditioned spectrum [2 e_min, 2 e_max] / (e_min + e_max), so
+ * each pass contracts the residual by about (sqrt(kappa) - 1) / (sqrt(kappa)
+ * + 1), kappa = e_max / e_min, and such a film may take more refinement
+ * passes than max_refine (enough for (kappa - 1) / (kappa + 1) per pass to
+ * reach refine_tol from a zero potential).  CMSL_INNER_AUTO takes it for
+ * kappa <= 16 and the PCG otherwise. */
 typedef enum { CMSL_INNER_AUTO = 0, CMSL_INNER_PCG = 1, CMSL_INNER_DIRECT = 2 } cmsl_inner_solver;
 
 typedef struct cmsl_film cmsl_film;
