@@ -32,6 +32,17 @@ constexpr int NT = TX * TY;
 constexpr int SX = TX + 2;
 constexpr int SY = TY + 2;
 constexpr int SPL = SX * SY;        // smem cells of one staged plane
+
+// Tiles of the FP32 stencil passes (TDGL and residual passes, cp.async ring):
+// TX x TYc columns, one thread per column; the tile autotuner picks TYc among
+// TILE_YS (the tensor-copy staging and every other item kernel use TY).
+template <int TYc> struct TileShape {
+    static constexpr int SYt = TYc + 2;
+    static constexpr int SPLt = SX * SYt;   // smem cells of one staged plane
+    static constexpr int NTt = TX * TYc;    // threads per block
+    static constexpr int MINB = 1024 / NTt; // resident blocks per SM the kernels are built for
+};
+constexpr int TILE_YS[3] = {4, 8, 16};
 constexpr int NPART = 8;            // doubles of partial sums per item
 
 constexpr uint32_t GID_MASK = 0x00ffffffu;
@@ -55,6 +66,7 @@ struct FilmDev {
     long long off;              // first cell of the film
     int g_off;                  // first grain of the film in TR
     int item_begin, item_end;
+    int sitem_begin, sitem_end; // the film's range of the FP32 stencil passes' items (Dev::sitems)
     int pb_begin, pb_end;       // persistent PCG: the film's block range of the cooperative grid
     int brick_begin, brick_end; // persistent PCG: the film's stencil bricks
     int dep_flag;
@@ -147,6 +159,8 @@ struct Dev {
     const FilmDev *films;
     const int4 *items;
     int n_films, n_items;
+    const int4 *sitems;         // items of the FP32 stencil passes (tile height of the autotuner's choice)
+    int n_sitems;
     const uint32_t *code;
     long long ncells;           // cells of all films (stride of the FP32 P pairs)
     double *phi[5];

@@ -107,13 +107,13 @@ int film_zchunk(const Engine *e, int fi, int zc)
     return zc > 0 ? std::min(zc, nz) : pick_zchunk(e->xy_tiles, nz);
 }
 
-size_t count_items(const Engine *e, int zc)
+size_t count_items(const Engine *e, int zc, int ty = TY)
 {
     size_t n = 0;
     for (int fi = 0; fi < e->n_films; ++fi) {
         const FilmHost &h = e->fh[fi];
         const int c = film_zchunk(e, fi, zc);
-        n += (size_t)((h.nx + TX - 1) / TX) * ((h.ny + TY - 1) / TY) * ((h.nz + c - 1) / c);
+        n += (size_t)((h.nx + TX - 1) / TX) * ((h.ny + ty - 1) / ty) * ((h.nz + c - 1) / c);
     }
     return n;
 }
@@ -122,21 +122,29 @@ size_t count_items(const Engine *e, int zc)
 // next run).
 cmsl_status set_items(Engine *e, int zc)
 {
-    if (count_items(e, zc) > e->items_cap) return fail(CMSL_ERR_ARG, "z chunk %d: too many work items", zc);
-    e->items.clear();
-    for (int fi = 0; fi < e->n_films; ++fi) {
-        const FilmHost &h = e->fh[fi];
-        const int c = film_zchunk(e, fi, zc);
-        FilmDev &fd = e->fdh[fi];
-        fd.item_begin = (int)e->items.size();
-        for (int y0 = 0; y0 < h.ny; y0 += TY)
-            for (int x0 = 0; x0 < h.nx; x0 += TX)
-                for (int z0 = 0; z0 < h.nz; z0 += c)
-                    e->items.push_back(make_int4(fi, x0, y0, z0 | (std::min(h.nz, z0 + c) << 16)));
-        fd.item_end = (int)e->items.size();
+    if (count_items(e, zc) > e->items_cap || count_items(e, zc, e->stile_ty) > e->sitems_cap)
+        return fail(CMSL_ERR_ARG, "z chunk %d: too many work items", zc);
+    // the item kernels' list (TX x TY tiles) and the FP32 stencil passes'
+    // list (TX x stile_ty tiles); the same z chunk
+    for (int list = 0; list < 2; ++list) {
+        std::vector<int4> &v = list ? e->sitems : e->items;
+        const int ty = list ? e->stile_ty : TY;
+        v.clear();
+        for (int fi = 0; fi < e->n_films; ++fi) {
+            const FilmHost &h = e->fh[fi];
+            const int c = film_zchunk(e, fi, zc);
+            FilmDev &fd = e->fdh[fi];
+            (list ? fd.sitem_begin : fd.item_begin) = (int)v.size();
+            for (int y0 = 0; y0 < h.ny; y0 += ty)
+                for (int x0 = 0; x0 < h.nx; x0 += TX)
+                    for (int z0 = 0; z0 < h.nz; z0 += c)
+                        v.push_back(make_int4(fi, x0, y0, z0 | (std::min(h.nz, z0 + c) << 16)));
+            (list ? fd.sitem_end : fd.item_end) = (int)v.size();
+        }
     }
     CK(cudaMemcpy(e->d_films, e->fdh.data(), sizeof(FilmDev) * e->fdh.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_items, e->items.data(), sizeof(int4) * e->items.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_sitems, e->sitems.data(), sizeof(int4) * e->sitems.size(), cudaMemcpyHostToDevice));
     e->zchunk = zc;
     e->graph_valid = false;
     return CMSL_OK;
@@ -147,6 +155,7 @@ cmsl_status set_items(Engine *e, int zc)
 struct Tuned {
     int zchunk;
     int stg_tdgl, stg_refine;
+    int tile_y;                 // tile height of the FP32 stencil passes
 };
 std::map<std::string, Tuned> g_tuned;
 std::mutex g_tuned_mu;
@@ -439,6 +448,7 @@ cmsl_status build_graph(Engine *e)
         return d;
     };
     const int nit = (int)e->items.size();
+    const int nsit = (int)e->sitems.size();        // the FP32 stencil passes' blocks
     KArgs a;
     a.F64 = e->fields<double>();
     a.F32 = e->fields<float>();
@@ -452,7 +462,7 @@ cmsl_status build_graph(Engine *e)
     void *args32[] = {&a.d, &a.F32};
     void *args_d[] = {&a.d};
     if (fp64) TRY(add_kernel(g, &n_tdgl, nullptr, 0, (void *)k_tdgl<double, Exact>, nit, NT, args64));
-    else TRY(add_kernel(g, &n_tdgl, nullptr, 0, e->tdgl_fn, nit, e->tdgl_nt, args32, e->tdgl_smem));
+    else TRY(add_kernel(g, &n_tdgl, nullptr, 0, e->tdgl_fn, nsit, e->tdgl_nt, args32, e->tdgl_smem));
     cudaGraphNode_t last = n_tdgl;
     if (e->any_dep) {
         if (fp64) {
@@ -508,7 +518,7 @@ cmsl_status build_graph(Engine *e)
             cudaGraph_t body;
             if (e->persistent) CK(cudaGraphConditionalHandleCreate(&h_inner, g, 0, cudaGraphCondAssignDefault));
             a.d = dev(h_inner, h_outer);
-            TRY(add_kernel(g, &n_r1, &last, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_kernel(g, &n_r1, &last, 1, e->refine_fn, nsit, e->refine_nt, args32, e->refine_smem));
             if (e->persistent) {
                 cudaGraph_t solve1;
                 cudaGraphNode_t n_c1;
@@ -519,12 +529,12 @@ cmsl_status build_graph(Engine *e)
             }
             // the pass that leaves no film active ends the step (no k_step_end node)
             a.d.step_end = 1;
-            TRY(add_kernel(g, &n_r2, &n_s1, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_kernel(g, &n_r2, &n_s1, 1, e->refine_fn, nsit, e->refine_nt, args32, e->refine_smem));
             TRY(add_while(g, &n_solve, &n_r2, 1, h_outer, &body));
             a.d = dev(0, h_outer);
             a.d.step_end = 1;
             TRY(add_solve(body, nullptr, &n_sb));
-            TRY(add_kernel(body, &n_rb, &n_sb, 1, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_kernel(body, &n_rb, &n_sb, 1, e->refine_fn, nsit, e->refine_nt, args32, e->refine_smem));
             last = nullptr;
         } else {
             // the inner loop's handle belongs to the outer body graph it lives in
@@ -533,7 +543,7 @@ cmsl_status build_graph(Engine *e)
             TRY(add_while(g, &n_solve, &last, 1, h_outer, &outer));
             CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0, cudaGraphCondAssignDefault));
             a.d = dev(h_inner, h_outer);
-            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nit, e->refine_nt, args32, e->refine_smem));
+            TRY(add_kernel(outer, &n_ref, nullptr, 0, e->refine_fn, nsit, e->refine_nt, args32, e->refine_smem));
             TRY(add_while(outer, &n_in, &n_ref, 1, h_inner, &inner));
             TRY(add_kernel(inner, &n_sp, nullptr, 0, (void *)k_spmv<float, Fast>, nit, NT, args32));
             TRY(add_kernel(inner, &n_up, &n_sp, 1, (void *)k_update<float, Fast, true>, nit, NT, args32));
@@ -657,7 +667,7 @@ cmsl_status launch_refine(Engine *e, cudaStream_t st, const Dev &d, const Fields
     Dev dd = d;
     Fields<float> ff = F32;
     void *args[] = {&dd, &ff};
-    CK(cudaLaunchKernel(e->refine_fn, dim3((unsigned)e->items.size()), dim3(e->refine_nt), args, e->refine_smem, st));
+    CK(cudaLaunchKernel(e->refine_fn, dim3((unsigned)e->sitems.size()), dim3(e->refine_nt), args, e->refine_smem, st));
     return CMSL_OK;
 }
 
@@ -667,7 +677,7 @@ cmsl_status launch_tdgl32(Engine *e, cudaStream_t st, const Dev &d, const Fields
     Dev dd = d;
     Fields<float> ff = F32;
     void *args[] = {&dd, &ff};
-    CK(cudaLaunchKernel(e->tdgl_fn, dim3((unsigned)e->items.size()), dim3(e->tdgl_nt), args, e->tdgl_smem, st));
+    CK(cudaLaunchKernel(e->tdgl_fn, dim3((unsigned)e->sitems.size()), dim3(e->tdgl_nt), args, e->tdgl_smem, st));
     return CMSL_OK;
 }
 
@@ -1127,13 +1137,24 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     e->fdh = fds;
     TRY(e->alloc((void **)&e->d_films, sizeof(FilmDev) * n));
     e->items_cap = std::max(count_items(e, ZCHUNK_MIN), count_items(e, 0));
+    e->sitems_cap = std::max(count_items(e, ZCHUNK_MIN, TILE_YS[0]), count_items(e, 0, TILE_YS[0]));
     TRY(e->alloc((void **)&e->d_items, sizeof(int4) * e->items_cap));
-    TRY(e->alloc((void **)&e->d_partial, sizeof(double) * NPART * e->items_cap));
+    TRY(e->alloc((void **)&e->d_sitems, sizeof(int4) * e->sitems_cap));
+    TRY(e->alloc((void **)&e->d_partial, sizeof(double) * NPART * std::max(e->items_cap, e->sitems_cap)));
     {
+        // tile height of the FP32 stencil passes: CMSL_TILE_Y (4, 8 or 16)
+        // fixes it; else a tuned handle of the same shape class, else TY
         int zc = 0;
+        const char *tyv = getenv("CMSL_TILE_Y");
+        const int ty_env = tyv ? atoi(tyv) : 0;
+        e->tile_fixed = e->precision != CMSL_FP64 && (ty_env == 4 || ty_env == 8 || ty_env == 16);
+        e->stile_ty = e->tile_fixed ? ty_env : TY;
         std::lock_guard<std::mutex> lk(g_tuned_mu);
         const auto hit = g_tuned.find(shape_key(e));
-        if (hit != g_tuned.end()) zc = hit->second.zchunk;
+        if (hit != g_tuned.end()) {
+            zc = hit->second.zchunk;
+            if (!e->tile_fixed && e->precision != CMSL_FP64) e->stile_ty = hit->second.tile_y;
+        }
         TRY(set_items(e, zc));
     }
     if (e->precision == CMSL_FP64) TRY(upload_TR<double>(e, descs, n));
@@ -1336,32 +1357,35 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         const char *nt = getenv("CMSL_NO_TMA");
         e->tma = !(nt && atoi(nt) != 0);
         for (int fi = 0; fi < n; ++fi) e->tma = e->tma && e->fh[fi].nx % TX == 0 && e->fh[fi].ny % TY == 0;
-        e->refine_fns[STG_CP] = uni ? (void *)k_refine32<true, R32_NS> : (void *)k_refine32<false, R32_NS>;
-        e->refine_smems[STG_CP] = uni ? r32_smem<true>() : r32_smem<false>();
-        // experiment: CMSL_TDGL_VARIANT 1 rotation kept per grain (4 blocks/SM),
-        // 2 rotation kept per grain (3 blocks/SM), 3 a 5-plane ring (3 blocks/SM)
-        const char *tv = getenv("CMSL_TDGL_VARIANT");
-        const int tdv = tv ? atoi(tv) : 0;
-        e->tdgl_fns[STG_CP] = tdv == 1 ? (void *)k_tdgl32<T32_NS, true, 4>
-                            : tdv == 2 ? (void *)k_tdgl32<T32_NS, true, 3>
-                            : tdv == 3 ? (void *)k_tdgl32<5, false, 3> : (void *)k_tdgl32<T32_NS>;
-        e->tdgl_smems[STG_CP] = tdv == 3 ? sizeof(float) * 5 * T32_STAGE : T32_SMEM;
+        // the cp.async ring at every tile height, the tensor copies at TY rows
+        e->refine_cp[0] = uni ? (void *)k_refine32<true, R32_NS, 4> : (void *)k_refine32<false, R32_NS, 4>;
+        e->refine_cp[1] = uni ? (void *)k_refine32<true, R32_NS, 8> : (void *)k_refine32<false, R32_NS, 8>;
+        e->refine_cp[2] = uni ? (void *)k_refine32<true, R32_NS, 16> : (void *)k_refine32<false, R32_NS, 16>;
+        e->refine_cp_smem[0] = uni ? r32_smem<true, 4>() : r32_smem<false, 4>();
+        e->refine_cp_smem[1] = uni ? r32_smem<true, 8>() : r32_smem<false, 8>();
+        e->refine_cp_smem[2] = uni ? r32_smem<true, 16>() : r32_smem<false, 16>();
+        e->tdgl_cp[0] = (void *)k_tdgl32<T32_NS, 4>;
+        e->tdgl_cp[1] = (void *)k_tdgl32<T32_NS, 8>;
+        e->tdgl_cp[2] = (void *)k_tdgl32<T32_NS, 16>;
+        e->tdgl_cp_smem[0] = t32_smem<4>();
+        e->tdgl_cp_smem[1] = t32_smem<8>();
+        e->tdgl_cp_smem[2] = t32_smem<16>();
+        for (int v = 0; v < 3; ++v) {
+            CK(cudaFuncSetAttribute(e->refine_cp[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)e->refine_cp_smem[v]));
+            CK(cudaFuncSetAttribute(e->tdgl_cp[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)e->tdgl_cp_smem[v]));
+        }
         if (e->tma) {
             TRY(make_maps(e));
-            e->refine_fns[STG_TMA] = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
-            e->refine_smems[STG_TMA] = uni ? rt_smem<true>() : rt_smem<false>();
-            e->tdgl_fns[STG_TMA] = tdv == 1 ? (void *)k_tdgl32t<TT_NS, true, 4>
-                                 : tdv == 2 ? (void *)k_tdgl32t<TT_NS, true, 3>
-                                 : tdv == 3 ? (void *)k_tdgl32t<5, false, 3> : (void *)k_tdgl32t<TT_NS>;
-            e->tdgl_smems[STG_TMA] = tdv == 3 ? (size_t)5 * TT_STAGE + 128 : TT_SMEM;
+            e->refine_tma = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
+            e->refine_tma_smem = uni ? rt_smem<true>() : rt_smem<false>();
+            e->tdgl_tma = (void *)k_tdgl32t<TT_NS>;
+            e->tdgl_tma_smem = TT_SMEM;
+            CK(cudaFuncSetAttribute(e->refine_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)e->refine_tma_smem));
+            CK(cudaFuncSetAttribute(e->tdgl_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->tdgl_tma_smem));
         }
-        for (int v = 0; v < (e->tma ? N_STG : 1); ++v) {
-            CK(cudaFuncSetAttribute(e->refine_fns[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)e->refine_smems[v]));
-            CK(cudaFuncSetAttribute(e->tdgl_fns[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)e->tdgl_smems[v]));
-        }
-        e->refine_nt = e->tdgl_nt = NT;
         // CMSL_STAGING=<tdgl><residual> (digits 0 cp.async ring, 1 tensor
         // copies) fixes the staging of films with full tiles; the autotuner
         // then keeps it
@@ -1696,40 +1720,53 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
     std::vector<int> cands;
     for (int c = ZCHUNK_MIN; c < maxnz; c *= 2) cands.push_back(c);
     cands.push_back(maxnz);
-    // per z chunk: every staging of the TDGL and of the residual passes where
-    // the tensor copies apply (the two kernels are independent, so each takes
-    // its fastest staging; a staging fixed by CMSL_STAGING is kept)
-    Tuned best{0, e->stg_tdgl, e->stg_refine};
+    // per tile height (FP32; 4, 8 and 16 rows unless CMSL_TILE_Y fixed one)
+    // and z chunk: every staging of the TDGL and of the residual passes where
+    // the tensor copies apply (8-row tiles of films with full tiles; the two
+    // kernels are independent, so each takes its fastest staging; a staging
+    // fixed by CMSL_STAGING is kept)
+    const bool fp32 = e->precision != CMSL_FP64;
+    std::vector<int> tys;
+    if (!fp32 || e->tile_fixed) tys.push_back(e->stile_ty);
+    else tys.assign(TILE_YS, TILE_YS + 3);
+    Tuned best{0, e->stg_tdgl, e->stg_refine, e->stile_ty};
     double best_ms = 0.0;
-    const bool tune_stg = e->precision != CMSL_FP64 && e->tma && !e->staging_fixed;
-    const int nst = tune_stg ? N_STG : 1;
-    for (int c : cands) {
-        TRY(set_items(e, c));
-        double tt[N_STG] = {0.0, 0.0}, tr[N_STG] = {0.0, 0.0}, rest = 0.0;
-        for (int v = 0; v < nst; ++v) {
-            if (tune_stg) e->stage(v, v);
-            double ms[4] = {0, 0, 0, 0};
-            TRY(time_kernels(e, 5, nullptr, ms));
-            tt[v] = ms[0];                                  // TDGL step
-            tr[v] = ms[1];                                  // first pass (FP32) / set-up (FP64)
-            if (e->precision == CMSL_FP64) rest = ms[2] + ms[3];
-            else if (e->spectral) tr[v] += ms[3];           // update pass
-            else if (!e->persistent) rest = ms[2] + ms[3];  // two-kernel PCG
-        }
-        int vt = 0, vr = 0;
-        for (int v = 1; v < nst; ++v) {
-            if (tt[v] < tt[vt]) vt = v;
-            if (tr[v] < tr[vr]) vr = v;
-        }
-        const double t = tt[vt] + tr[vr] + rest;
-        if (best.zchunk == 0 || t < best_ms) {
-            best = tune_stg ? Tuned{c, vt, vr} : Tuned{c, e->stg_tdgl, e->stg_refine};
-            best_ms = t;
+    for (int ty : tys) {
+        if (fp32 && e->staging_fixed && (e->stg_tdgl || e->stg_refine) && ty != TY) continue;
+        e->stile_ty = ty;
+        const bool tune_stg = fp32 && e->tma && !e->staging_fixed && ty == TY;
+        const int nst = tune_stg ? N_STG : 1;
+        const int fixed_t = e->stg_tdgl, fixed_r = e->stg_refine;
+        for (int c : cands) {
+            TRY(set_items(e, c));
+            double tt[N_STG] = {0.0, 0.0}, tr[N_STG] = {0.0, 0.0}, rest = 0.0;
+            for (int v = 0; v < nst; ++v) {
+                if (tune_stg) e->stage(v, v);
+                else if (fp32) e->stage(e->staging_fixed ? fixed_t : STG_CP, e->staging_fixed ? fixed_r : STG_CP);
+                double ms[4] = {0, 0, 0, 0};
+                TRY(time_kernels(e, 5, nullptr, ms));
+                tt[v] = ms[0];                                  // TDGL step
+                tr[v] = ms[1];                                  // first pass (FP32) / set-up (FP64)
+                if (!fp32) rest = ms[2] + ms[3];
+                else if (e->spectral) tr[v] += ms[3];           // update pass
+                else if (!e->persistent) rest = ms[2] + ms[3];  // two-kernel PCG
+            }
+            int vt = 0, vr = 0;
+            for (int v = 1; v < nst; ++v) {
+                if (tt[v] < tt[vt]) vt = v;
+                if (tr[v] < tr[vr]) vr = v;
+            }
+            const double t = tt[vt] + tr[vr] + rest;
+            if (best.zchunk == 0 || t < best_ms) {
+                best = tune_stg ? Tuned{c, vt, vr, ty} : Tuned{c, e->stg_tdgl, e->stg_refine, ty};
+                best_ms = t;
+            }
         }
     }
+    e->stile_ty = best.tile_y;
     TRY(set_items(e, best.zchunk));
-    if (e->precision != CMSL_FP64) e->stage(best.stg_tdgl, best.stg_refine);
-    if (!e->staging_fixed) {
+    if (fp32) e->stage(best.stg_tdgl, best.stg_refine);
+    if (!e->staging_fixed && !e->tile_fixed) {
         std::lock_guard<std::mutex> lk(g_tuned_mu);
         g_tuned[shape_key(e)] = best;
     }
@@ -1740,7 +1777,7 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
 void tile_config(const Engine *e, int32_t cfg[4])
 {
     cfg[0] = TX;
-    cfg[1] = TY;
+    cfg[1] = e->precision != CMSL_FP64 ? e->stile_ty : TY;
     cfg[2] = e->zchunk;
     cfg[3] = e->stg_tdgl | (e->stg_refine << 2);
 }

@@ -54,6 +54,9 @@ struct Engine {
     std::vector<FilmDev> fdh;           // host copy of the film tables
     std::vector<int4> items;
     size_t items_cap = 0;               // items the device arrays hold
+    std::vector<int4> sitems;           // items of the FP32 stencil passes (tile height stile_ty)
+    size_t sitems_cap = 0;
+    int stile_ty = TY;
     long long xy_tiles = 0;             // column tiles of all films
     int zchunk = 0;                     // z chunk of the items (0: per-film heuristic)
     // device buffers
@@ -61,6 +64,7 @@ struct Engine {
     size_t bytes = 0;
     FilmDev *d_films = nullptr;
     int4 *d_items = nullptr;
+    int4 *d_sitems = nullptr;
     uint32_t *d_code = nullptr;
     void *d_TR = nullptr;
     double *d_phi[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -103,19 +107,29 @@ struct Engine {
     // film), STG_TMA tensor copies (every film's nx % 32 == 0, ny % 8 == 0).
     // The TDGL and the residual passes each take the staging the autotuner
     // measured faster (STG_TMA until tuned)
+    // The cp.async ring has a kernel per tile height (TILE_YS: 4, 8, 16 rows
+    // of 32 columns); the tensor copies run 8-row tiles only.
     bool tma = false;
     int stg_tdgl = 0, stg_refine = 0;
     bool staging_fixed = false;         // CMSL_STAGING set the staging: the autotuner keeps it
-    void *tdgl_fns[2] = {nullptr, nullptr}, *refine_fns[2] = {nullptr, nullptr};
-    size_t tdgl_smems[2] = {0, 0}, refine_smems[2] = {0, 0};
+    bool tile_fixed = false;            // CMSL_TILE_Y set the tile height: the autotuner keeps it
+    void *tdgl_cp[3] = {nullptr, nullptr, nullptr}, *refine_cp[3] = {nullptr, nullptr, nullptr};
+    size_t tdgl_cp_smem[3] = {0, 0, 0}, refine_cp_smem[3] = {0, 0, 0};
+    void *tdgl_tma = nullptr, *refine_tma = nullptr;
+    size_t tdgl_tma_smem = 0, refine_tma_smem = 0;
+    static int ty_index(int ty) { return ty == 4 ? 0 : ty == 16 ? 2 : 1; }
+    // Stagings for the current tile height (tensor copies only with TY rows).
     void stage(int tdgl_stg, int refine_stg)
     {
-        stg_tdgl = tma ? tdgl_stg : 0;
-        stg_refine = tma ? refine_stg : 0;
-        tdgl_fn = tdgl_fns[stg_tdgl];
-        tdgl_smem = tdgl_smems[stg_tdgl];
-        refine_fn = refine_fns[stg_refine];
-        refine_smem = refine_smems[stg_refine];
+        const bool t_ok = tma && stile_ty == TY;
+        stg_tdgl = t_ok ? tdgl_stg : 0;
+        stg_refine = t_ok ? refine_stg : 0;
+        const int yi = ty_index(stile_ty);
+        tdgl_fn = stg_tdgl ? tdgl_tma : tdgl_cp[yi];
+        tdgl_smem = stg_tdgl ? tdgl_tma_smem : tdgl_cp_smem[yi];
+        refine_fn = stg_refine ? refine_tma : refine_cp[yi];
+        refine_smem = stg_refine ? refine_tma_smem : refine_cp_smem[yi];
+        tdgl_nt = refine_nt = TX * stile_ty;
         graph_valid = false;
     }
     FilmMaps *d_maps = nullptr;
@@ -156,6 +170,7 @@ struct Engine {
     {
         Dev d{};
         d.films = d_films; d.items = d_items; d.n_films = n_films; d.n_items = (int)items.size();
+        d.sitems = d_sitems; d.n_sitems = (int)sitems.size();
         d.code = d_code; d.ncells = ncells;
         for (int q = 0; q < 5; ++q) d.phi[q] = d_phi[q];
         d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;

@@ -102,6 +102,7 @@ struct Geom {
     long long own_pl, halo_pl, plane;
 };
 
+template <int TYc = TY>
 __device__ __forceinline__ Geom make_geom(const FilmDev *f, int x0, int y0)
 {
     Geom g;
@@ -109,7 +110,7 @@ __device__ __forceinline__ Geom make_geom(const FilmDev *f, int x0, int y0)
     g.plane = (long long)g.nx * g.ny;
     const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
     g.wx = min(TX, g.nx - x0);
-    g.wy = min(TY, g.ny - y0);
+    g.wy = min(TYc, g.ny - y0);
     g.valid = lx < g.wx && ly < g.wy;
     g.own_slot = (ly + 1) * SX + lx + 1;
     g.own_pl = (long long)(x0 + lx) + (long long)g.nx * (y0 + ly);
@@ -223,8 +224,9 @@ __device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], do
     __syncthreads();
 }
 
-// In the last block: film f's totals of the block_partial32 pairs (item
-// order: thread-strided, warp tree, then warps in order), valid in thread 0.
+// In the last block: film f's totals of the block_partial32 pairs of its
+// stencil items (Dev::sitems; item order: thread-strided, warp tree, then
+// warps in order), valid in thread 0.
 template <int NV>
 __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, double (*sm)[NV],
                                              double (&out)[NV])
@@ -235,7 +237,7 @@ __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, dou
     df v[NV];
     #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = df{0.f, 0.f};
-    for (int it = f->item_begin + (int)threadIdx.x; it < f->item_end; it += (int)blockDim.x) {
+    for (int it = f->sitem_begin + (int)threadIdx.x; it < f->sitem_end; it += (int)blockDim.x) {
         #pragma unroll
         for (int i = 0; i < NV; ++i) {
             const float2 p = __ldcg((const float2 *)(d.partial + (long long)it * NPART + i));

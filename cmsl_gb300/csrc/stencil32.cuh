@@ -15,7 +15,9 @@
 // one 8-byte shared load.
 //
 // Each thread owns one cell of the tile and copies it and at most one x/y
-// halo cell.  (Pair tiles -- two x-adjacent cells per thread -- execute a
+// halo cell.  The tile is TX x TYc columns (TYc 4, 8 or 16: 128, 256 or 512
+// threads), the autotuner's choice; the blocks take the stencil item list
+// (Dev::sitems) of that tile height.  (Pair tiles -- two x-adjacent cells per thread -- execute a
 // third fewer instructions but halve the warps an SM holds within the same
 // shared memory, and measured slower.)
 //
@@ -184,23 +186,28 @@ constexpr int T32_NS = 4;
 // Stage layout (own + halo slots): P as three float2 planes (P0, P1), (P2, P3),
 // (P4, P5), the potential as one (hi, lo) float2 plane, then the code (own):
 // a stencil point of a pair is one 8-byte shared load.
-constexpr int T32_STAGE = 8 * SPL + NT;      // floats
-constexpr size_t T32_SMEM = sizeof(float) * T32_NS * T32_STAGE;
+template <int TYc> __host__ __device__ constexpr int t32_stage()      // floats
+{
+    return 8 * TileShape<TYc>::SPLt + TileShape<TYc>::NTt;
+}
+template <int TYc> constexpr size_t t32_smem() { return sizeof(float) * T32_NS * t32_stage<TYc>(); }
 
-template <int NS, bool TRC = false, int MINB = 4>
-__global__ void __launch_bounds__(NT, MINB) k_tdgl32(Dev d, Fields<float> F)
+// TYc: the tile height (TX x TYc threads, one column each).
+template <int NS, int TYc = TY>
+__global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_tdgl32(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
+    constexpr int SPL = TileShape<TYc>::SPLt, NT = TileShape<TYc>::NTt, T32_STAGE = t32_stage<TYc>();
     extern __shared__ float4 smem_t32[];
     float *ring = (float *)smem_t32;
     __shared__ float4 sC[6][3];
     __shared__ double sRed[NT / 32][7];
     __shared__ double sTot[7];
-    const int4 it = d.items[blockIdx.x];
+    const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
     load_coef4(f, sC);
-    const Geom g = make_geom(f, it.y, it.z);
+    const Geom g = make_geom<TYc>(f, it.y, it.z);
     const int cur = d.ctl->cur, rs = d.ctl->run_step;
     const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
     const int row = d.rows[(long long)it.x * d.wstride + rs];
@@ -248,8 +255,6 @@ __global__ void __launch_bounds__(NT, MINB) k_tdgl32(Dev d, Fields<float> F)
     #pragma unroll
     for (int q = 0; q < 7; ++q) acc[q] = 0.f;
     const int s0 = g.own_slot;
-    int gid = -1;
-    float t[9];
     RingIdx<NS> ri{z0 - zlo};
     long long o = g.own_pl + (long long)z0 * g.plane;
     for (int k = z0; k < z1; ++k, o += g.plane, ri.next()) {
@@ -293,11 +298,8 @@ __global__ void __launch_bounds__(NT, MINB) k_tdgl32(Dev d, Fields<float> F)
             ez = phi_diff32(pu, pd) * inv_2hf;
         }
         float pn[6], pMZl, pSZl;
-        if (!TRC || code_gid(c) != gid) {
-            gid = code_gid(c);
-            load_tr32(TR4 + 3LL * gid, t);
-        }
-        tdgl_cell32t(sC[code_mat(c) * 2 + code_iface(c)], t, pc, sum, ex, ey, ez, mEz, pn, pMZl, pSZl);
+        tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
+                    pMZl, pSZl);
         #pragma unroll
         for (int j = 0; j < 3; ++j) Pn[j * fs + o] = make_float2(pn[2 * j], pn[2 * j + 1]);
         if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
@@ -480,27 +482,32 @@ __device__ __forceinline__ void refine_partials(const Dev &d, float (&acc)[3], d
 // Stage layout (floats): x = phi (+ dx) as one (hi, lo) float2 plane, dx,
 // the (Pmx, Pmy) pair plane, Pmz (own), then the general-eps code and D^-1.
 // The update pass keeps the old r of the own cell in the Pmz slot.
-template <bool UNI> struct R32Lay {
+template <bool UNI, int TYc = TY> struct R32Lay {
+    static constexpr int SPL = TileShape<TYc>::SPLt, NT = TileShape<TYc>::NTt;
     static constexpr int FX = 0, DX = 2 * SPL, PA = 3 * SPL, PZ = 5 * SPL;
     static constexpr int CODE = 5 * SPL + NT, DINV = 6 * SPL + NT;   // general eps only
     static constexpr int STAGE = UNI ? 5 * SPL + NT : 6 * SPL + 2 * NT;
 };
-template <bool UNI> constexpr size_t r32_smem() { return sizeof(float) * R32_NS * R32Lay<UNI>::STAGE; }
+template <bool UNI, int TYc = TY> constexpr size_t r32_smem()
+{
+    return sizeof(float) * R32_NS * R32Lay<UNI, TYc>::STAGE;
+}
 
-template <bool UNI, int NS>
-__global__ void __launch_bounds__(NT, 4) k_refine32(Dev d, Fields<float> F)
+template <bool UNI, int NS, int TYc = TY>
+__global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_refine32(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
-    using L = R32Lay<UNI>;
+    using L = R32Lay<UNI, TYc>;
+    constexpr int NT = TileShape<TYc>::NTt;
     extern __shared__ float4 smem_r32[];
     float *ring = (float *)smem_r32;
     __shared__ double sRed[NT / 32][3];
     __shared__ double sTot[3];
-    const int4 it = d.items[blockIdx.x];
+    const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const SolveDev *S = d.solve + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
-    const Geom g = make_geom(f, it.y, it.z);
+    const Geom g = make_geom<TYc>(f, it.y, it.z);
     const int nz = g.nz;
     // film constants in registers (the stores below might alias the film table)
     RConst rc;

@@ -2,7 +2,8 @@
 // (TMA) staging: the TDGL step (k_tdgl32t) and the double-float residual
 // pass (k_refine32t).
 //
-// Same work items and arithmetic as stencil32.cuh, but a plane of every field
+// Same work items (the stencil list, Dev::sitems, with the tile height TY)
+// and arithmetic as stencil32.cuh, but a plane of every field
 // is brought into the ring by cp.async.bulk.tensor copies that the first
 // lane of each warp issues (a few boxes each) and that complete on the
 // stage's mbarrier; no thread computes a per-cell copy address.  A field of a plane lands as five boxes:
@@ -143,8 +144,8 @@ constexpr int TT_PHI = 3 * REG2, TT_CODE = 4 * REG2, TT_STAGE = 4 * REG2 + BODY1
 constexpr size_t TT_SMEM = (size_t)TT_NS * TT_STAGE + 128;
 constexpr int TT_OPS = 3 * 5 + 5 + 1;
 
-template <int NS, bool TRC = false, int MINB = 4>
-__global__ void __launch_bounds__(NT, MINB) k_tdgl32t(Dev d, Fields<float> F)
+template <int NS>
+__global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
     extern __shared__ unsigned char smem_tt[];
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(NT, MINB) k_tdgl32t(Dev d, Fields<float> F)
     __shared__ float4 sC[6][3];
     __shared__ double sRed[NT / 32][7];
     __shared__ double sTot[7];
-    const int4 it = d.items[blockIdx.x];
+    const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
     load_coef4(f, sC);
@@ -245,11 +246,8 @@ __global__ void __launch_bounds__(NT, MINB) k_tdgl32t(Dev d, Fields<float> F)
             ez = phi_diff32(pu, pd) * inv_2hf;
         }
         float pn[6], pMZl, pSZl;
-        if (!TRC || code_gid(c) != gid) {
-            gid = code_gid(c);
-            load_tr32(TR4 + 3LL * gid, t);
-        }
-        tdgl_cell32t(sC[code_mat(c) * 2 + code_iface(c)], t, pc, sum, ex, ey, ez, mEz, pn, pMZl, pSZl);
+        tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
+                    pMZl, pSZl);
         #pragma unroll
         for (int j = 0; j < 3; ++j) Pn[j * fs + o] = make_float2(pn[2 * j], pn[2 * j + 1]);
         if (row >= 0) row_acc(acc, code_mat(c), pn, pMZl, pSZl);
@@ -288,7 +286,7 @@ __global__ void __launch_bounds__(NT, 4) k_refine32t(Dev d, Fields<float> F)
     __shared__ TmaOp ops[RT_OPS];
     __shared__ double sRed[NT / 32][3];
     __shared__ double sTot[3];
-    const int4 it = d.items[blockIdx.x];
+    const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const SolveDev *S = d.solve + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;

@@ -83,7 +83,7 @@ def test_autotune_before_any_state_on_tensor_copy_films(gpu, inner):
         assert g.inner_solver == (gpu.INNER_DIRECT if inner == "direct" else gpu.INNER_PCG)
         assert g.autotune() in (4, 8, 10)
         cfg = g.tile_config()
-        assert cfg["x"] == 32 and cfg["y"] == 8 and cfg["z_chunk"] in (4, 8, 10)
+        assert cfg["x"] == 32 and cfg["y"] in (4, 8, 16) and cfg["z_chunk"] in (4, 8, 10)
         g.set_state(w.P_init)
         g.run(Ez)
         Pg, _ = g.get_state()

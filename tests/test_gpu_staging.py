@@ -66,3 +66,34 @@ def test_staging_matches_oracle(gpu, orc, staging, eps, zbc, monkeypatch):
         g.sync()
     err = max(np.abs(a - b).max() / np.abs(b).max() for a, b in zip(Pg, Pw))
     assert err <= 2e-5
+
+
+@pytest.mark.parametrize("tile_y", [4, 8, 16])
+@pytest.mark.parametrize("eps", ["one", "three"])
+@pytest.mark.parametrize("shape", [(64, 32, 13), (40, 20, 9)])
+def test_tile_height_matches_oracle(gpu, orc, tile_y, eps, shape, monkeypatch):
+    """The FP32 stencil passes with tiles of 32 x 4, 32 x 8 and 32 x 16
+    columns (CMSL_TILE_Y; the autotuner's choices), on a film of full tiles
+    and one with partial tiles in x and y, against the FP64 oracle (same
+    tolerance as above)."""
+    from cmsl_gb300 import workloads as wl
+    w = wl.hzo_film("tile_%dx%dx%d" % shape, *shape, 9, 23, 0.4, E_amp_MVcm=4.0, steps_per_period=400)
+    mats = np.array(w.mats, copy=True)
+    if eps == "three":
+        mats[:, 7] = [50.0, 30.0, 15.0]
+    f = _oracle_film(orc, w, mats, oracle.DIRICHLET)
+    n = 6
+    Ez = w.sched.Ez[:n] * 40.0
+    rng = np.random.default_rng(6)
+    P0 = [p + rng.normal(scale=0.05, size=w.N) for p in w.P_init]
+    Pw, _, _, _, _, rc = orc.run(f, P0, np.zeros(w.N), Ez)
+    assert rc == 0
+    monkeypatch.setenv("CMSL_TILE_Y", str(tile_y))
+    with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED) as g:
+        cfg = g.tile_config()
+        assert cfg["x"] == 32 and cfg["y"] == tile_y
+        g.set_state(P0)
+        g.run(Ez)
+        Pg, _ = g.get_state()
+    err = max(np.abs(a - b).max() / np.abs(b).max() for a, b in zip(Pg, Pw))
+    assert err <= 2e-5
