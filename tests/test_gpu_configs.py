@@ -172,3 +172,35 @@ def test_config_segment_fp32_refined(cg, orc, cfg):
     assert _rel(Pg, Pw) <= FP32_P_REL
     assert _rel([phig], [phiw]) <= FP32_PHI_REL
     assert np.abs(rg[:, :10] - statw[:, :10]).max() <= FP32_ROWS_ABS
+
+
+@pytest.mark.parametrize("cfg", [4, 1])
+def test_config_segment_deck_permittivities(cg, orc, cfg):
+    """The configuration's film with the reference deck's permittivities
+    (AFE 50, FE 30, DE 15, src/inputs/InputParams:34-36): the FP32-refined
+    run takes the direct solve as the refinement's preconditioner (Chebyshev
+    increments); 20 steps against the FP64 oracle with the same tolerances."""
+    from cmsl_gb300 import workloads as wl
+    w = wl.config(cfg)
+    mats = np.array(w.mats, copy=True)
+    mats[:, 7] = [50.0, 30.0, 15.0]
+    f = oracle.Film(nx=w.nx, ny=w.ny, nz=w.nz, del_h=w.del_h, del_t=w.del_t, omega=w.omega,
+                    grain_mat=w.grain_mat, TR=w.TR, mats=mats,
+                    is_interface=orc.interface_flags(w.nx, w.ny, w.nz, w.omega, w.grain_mat),
+                    dep_flag=1, eps_0_nd=w.eps_0_nd)
+    f.crit, f.tol_rel, f.max_iter = oracle.CRIT_RELRES, TOL, 20000
+    n = 20
+    rows = np.arange(n, dtype=np.int32)
+    Pw, _, phiw, statw, _, rc = orc.run(f, w.P_init, np.zeros(w.N), w.sched.Ez[:n], rows)
+    assert rc == 0
+    kw = dict(pcg_crit=cg.CRIT_RELRES, tol_rel=TOL, max_iter=20000, precision=cg.FP32_REFINED, refine_tol=TOL,
+              max_refine=6, inner_tol=1e-5, inner_max_iter=2000, warm_start=2)
+    with cg.Film(w.nx, w.ny, w.nz, w.omega, w.grain_mat, w.TR, mats, **w.film_kwargs(), **kw) as g:
+        assert g.inner_solver == cg.INNER_DIRECT
+        g.set_state(w.P_init)
+        g.run(w.sched.Ez[:n], rows)
+        Pg, phig = g.get_state()
+        rg = g.rows(0, n)
+    assert _rel(Pg, Pw) <= FP32_P_REL
+    assert _rel([phig], [phiw]) <= FP32_PHI_REL
+    assert np.abs(rg[:, :10] - statw[:, :10]).max() <= FP32_ROWS_ABS
