@@ -48,12 +48,15 @@ ALG = {"fp32": {"tdgl": 14 * 4 + 4, "pcg": 10 * 4 + 4, "ref": 28},
 # The per-kernel algorithmic bytes of the roofline line (by kernel):
 #   tdgl -> ALG tdgl; setup (first refinement pass; FP64: the RHS) and update
 #   (update pass) -> ALG ref (FP64 rhs: read Pm, write b: 3 s + 4 + s);
-#   spec (one direct solve) and pcg_iter / spmv+update -> ALG pcg.
+#   spec (one direct solve) and pcg_iter / spmv+update -> ALG pcg;
+#   tdgl_check (the TDGL step that also forms the previous step's deferred
+#   check, one refinement pass's work) -> ALG tdgl + ALG ref.
 # Bytes the kernels as designed move per launch (what they read and write,
 # including the double-float potential and the warm start's older
 # potentials), kept beside the algorithmic figure:
 DESIGN_BYTES = {
-    "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4 + 2 * 8 + 8, "setup": 8 + 12 + 4, "update": 8 + 4 + 4 + 4 + 8,
+    "fp32": {"tdgl": 6 * 4 * 2 + 8 + 4 + 2 * 8 + 8, "tdgl_check": 6 * 4 * 2 + 8 + 4 + 2 * 8 + 8 + 4 + 4 + 8,
+             "setup": 8 + 12 + 4, "update": 8 + 4 + 4 + 4 + 8,
              "pcg_iter": 7 * 4 + 5 * 4, "spmv32": 4 * 4 + 2 * 4, "update32": 5 * 4 + 2 * 4, "spec": 40},
     "fp64": {"tdgl": 6 * 8 * 2 + 8 + 4, "setup": 24 + 8 + 4 + 8 + 8, "spmv": 8 * 3 + 4 + 16,
              "update": 5 * 8 + 2 * 8},
@@ -66,6 +69,8 @@ def alg_bytes(mode: str, kernel: str) -> int:
     a = ALG[mode]
     if kernel == "tdgl":
         return a["tdgl"]
+    if kernel == "tdgl_check":
+        return a["tdgl"] + a["ref"]
     if kernel in ("setup", "update") and mode == "fp32":
         return a["ref"]
     if mode == "fp64" and kernel == "setup":
@@ -418,9 +423,13 @@ def run_ours(args):
     n_iter = float(np.mean(it))
     n_ref = float(np.mean(rf))
     direct = film.inner_solver == cg.INNER_DIRECT
-    # direct solve: one full pass per step, the later ones (almost always) update passes
-    names = ["tdgl", "setup", "spec", "update"] if direct else KERNELS[mode]
-    count = {"tdgl": 1.0, "setup": 1.0 if direct else n_ref, "spmv": n_iter,
+    # direct solve: one full pass per step, the later ones (almost always)
+    # update passes -- or, deferred (time_kernels reports no update pass), the
+    # check formed inside the next TDGL step
+    deferred = direct and kms[3] == 0.0
+    names = (["tdgl_check", "setup", "spec"] if deferred else
+             ["tdgl", "setup", "spec", "update"] if direct else KERNELS[mode])
+    count = {"tdgl": 1.0, "tdgl_check": 1.0, "setup": 1.0 if direct else n_ref, "spmv": n_iter,
              "update": max(n_ref - 1.0, 0.0) if direct else n_iter, "pcg_iter": n_iter, "spec": n_iter}
     per_step = {k: kms[i] * count[k] for i, k in enumerate(names)}
     top = max(per_step, key=per_step.get)
@@ -443,6 +452,11 @@ def run_ours(args):
                 ALG[mode]["tdgl"], n_iter, ALG[mode]["pcg"], n_ref, ALG[mode]["ref"])}
     if fp64:
         launches = int(K * 3 + 2 * it.sum())
+    elif deferred:
+        # TDGL (with the previous step's check), the passes but that check,
+        # five per direct solve; after the step loop the last check's pass and
+        # the kernel that opens it
+        launches = int(K + (rf - 1).sum() + 5 * it.sum() + 2)
     elif direct:
         # TDGL, the refinement passes (the last one ends the step), five per direct solve
         launches = int(K + rf.sum() + 5 * it.sum())
@@ -592,13 +606,15 @@ def run_batch(args):
     # inner solve: the direct spectral solve (ms[2] = one solve of every
     # film), or the persistent PCG (ms[2] = one iteration over every film)
     direct = b.inner_solver == cg.INNER_DIRECT
+    deferred = direct and kms[3] == 0.0
     persistent = not direct and len(ws) <= 128 and os.environ.get("CMSL_PCG_TWO_KERNEL", "0") in ("", "0")
-    names = (["tdgl", "setup", "spec", "update"] if direct else
+    names = (["tdgl_check", "setup", "spec"] if deferred else ["tdgl", "setup", "spec", "update"] if direct else
              ["tdgl", "setup", "pcg_iter"] if persistent else ["tdgl", "setup", "spmv32", "update32"])
     # the loops run while any film is active: per step, the most demanding film
     n_ref = float(np.mean(rfs.max(axis=0)))
     n_it = float(np.mean(its.max(axis=0)))
-    count = {"tdgl": 1.0, "setup": 1.0 if direct else n_ref, "update": max(n_ref - 1.0, 0.0), "spmv32": n_it,
+    count = {"tdgl": 1.0, "tdgl_check": 1.0, "setup": 1.0 if direct else n_ref, "update": max(n_ref - 1.0, 0.0),
+             "spmv32": n_it,
              "update32": n_it, "pcg_iter": n_it, "spec": n_it}
     per_step = {k: kms[i] * count[k] for i, k in enumerate(names)}
     top = max(per_step, key=per_step.get)
@@ -684,7 +700,8 @@ def run_batch(args):
                          if direct else "persistent PCG (one cooperative launch per refinement pass)" if persistent
                          else "two-kernel PCG"),
         "clocks": clk,
-        "gpu_launches": (int(K + K * n_ref + 5 * K * n_it) if direct else
+        "gpu_launches": (int(K + K * (n_ref - 1) + 5 * K * n_it + 2) if deferred else
+                         int(K + K * n_ref + 5 * K * n_it) if direct else
                          int(K * 2 + 2 * K * n_ref) if persistent else int(K * 2 + K * n_ref + 2 * K * n_it)),
     }
     print(json.dumps(line))

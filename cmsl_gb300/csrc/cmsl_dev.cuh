@@ -83,6 +83,8 @@ struct FilmDev {
                                 // the half-width of M^-1 A's spectrum around 1 (0: exact solve)
     int upd_ok;                 // FP32_REFINED: the inner solve leaves r intact (direct solve), so a
                                 // later refinement pass may update r instead of recomputing it
+    int defer_ok;               // the check after a step's one direct solve may run inside the next
+                                // TDGL step (upd_ok, warm start at most quadratic)
     double n_mat[3];            // voxels per material (sum of the reference's masks)
     Coef<double> coef[6];       // index mat*2 + iface
     Coef<float> coef32[6];
@@ -111,6 +113,8 @@ struct SolveDev {               // per film, lives in device memory
                                 // forming b - A phi in double-float
     double cheb_rho;            // Chebyshev recurrence of the preconditioned refinement (rho_k)
     float cheb_w, cheb_m;       // the next direct solve's increment: dx <- w M^-1 r + m dx
+    int pending;                // the step ended on its direct solve: the potential is phi_cur (the
+                                // warm start) + dx, its check r <- r - A dx still to come (next TDGL)
 };
 
 // Extra vectors of the single-reduction FP32 PCG (FP32_REFINED mode).
@@ -132,6 +136,7 @@ struct Ctl {
     int cur;                    // which P set is "old"
     int run_step;               // step index within the current run (waveform index)
     int stop;                   // run_step at which the step loop of a graph launch ends
+    int redo;                   // a TDGL step found a pending check failed and reopened the step before
 };
 
 template <class T> struct Fields {
@@ -177,6 +182,7 @@ struct Dev {
     int use_cond;
     int force;                  // run the PCG kernels whatever the flags (kernel timing)
     int step_end;               // a residual pass that leaves no film active also ends the step
+    int defer;                  // films with defer_ok end a step on its direct solve (SolveDev::pending)
     unsigned int *arrive;       // grid-barrier counter of the persistent PCG (or null)
     cudaGraphConditionalHandle h_inner, h_outer;
     cudaGraphConditionalHandle h_steps;   // the graph's step loop (0: one step per launch)

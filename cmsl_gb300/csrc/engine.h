@@ -117,6 +117,12 @@ struct Engine {
     size_t tdgl_cp_smem[3] = {0, 0, 0}, refine_cp_smem[3] = {0, 0, 0};
     void *tdgl_tma = nullptr, *refine_tma = nullptr;
     size_t tdgl_tma_smem = 0, refine_tma_smem = 0;
+    // deferred checks: a step of films with defer_ok ends on its direct
+    // solve and the next TDGL step (the cp.async ring kernels below) forms
+    // the check the update pass formed (CMSL_DEFER=0: the update pass)
+    bool defer = false;
+    void *tdgl_def[3] = {nullptr, nullptr, nullptr};
+    size_t tdgl_def_smem[3] = {0, 0, 0};
     static int ty_index(int ty) { return ty == 4 ? 0 : ty == 16 ? 2 : 1; }
     // Stagings for the current tile height (tensor copies only with TY rows).
     void stage(int tdgl_stg, int refine_stg)
@@ -125,8 +131,9 @@ struct Engine {
         stg_tdgl = t_ok ? tdgl_stg : 0;
         stg_refine = t_ok ? refine_stg : 0;
         const int yi = ty_index(stile_ty);
-        tdgl_fn = stg_tdgl ? tdgl_tma : tdgl_cp[yi];
-        tdgl_smem = stg_tdgl ? tdgl_tma_smem : tdgl_cp_smem[yi];
+        if (defer) stg_tdgl = 0;
+        tdgl_fn = defer ? tdgl_def[yi] : stg_tdgl ? tdgl_tma : tdgl_cp[yi];
+        tdgl_smem = defer ? tdgl_def_smem[yi] : stg_tdgl ? tdgl_tma_smem : tdgl_cp_smem[yi];
         refine_fn = stg_refine ? refine_tma : refine_cp[yi];
         refine_smem = stg_refine ? refine_tma_smem : refine_cp_smem[yi];
         tdgl_nt = refine_nt = TX * stile_ty;

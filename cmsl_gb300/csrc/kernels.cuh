@@ -225,8 +225,11 @@ __device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], do
 }
 
 // In the last block: film f's totals of the block_partial32 pairs of its
-// stencil items (Dev::sitems; item order: thread-strided, warp tree, then
-// warps in order), valid in thread 0.
+// stencil items (Dev::sitems; item order: thread-strided two items a round,
+// warp tree, then warps in order), valid in thread 0.  The last block runs
+// alone at the end of its grid, so the sum is laid out for latency: every
+// load of a round is issued before its sums, and the values' warp trees
+// interleave.
 template <int NV>
 __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, double (*sm)[NV],
                                              double (&out)[NV])
@@ -237,16 +240,28 @@ __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, dou
     df v[NV];
     #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = df{0.f, 0.f};
-    for (int it = f->sitem_begin + (int)threadIdx.x; it < f->sitem_end; it += (int)blockDim.x) {
+    const int b1 = f->sitem_end, stride = (int)blockDim.x;
+    auto part = [&](int it, int i) { return __ldcg((const float2 *)(d.partial + (long long)it * NPART + i)); };
+    int it = f->sitem_begin + (int)threadIdx.x;
+    for (; it + stride < b1; it += 2 * stride) {
+        float2 p[NV], q[NV];
         #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            const float2 p = __ldcg((const float2 *)(d.partial + (long long)it * NPART + i));
+            p[i] = part(it, i);
+            q[i] = part(it + stride, i);
+        }
+        #pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] = df_add_acc(v[i], df_add_acc(df{p[i].x, p[i].y}, df{q[i].x, q[i].y}));
+    }
+    if (it < b1) {
+        #pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const float2 p = part(it, i);
             v[i] = df_add_acc(v[i], df{p.x, p.y});
         }
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    constexpr int UNR = NV > 4 ? 1 : NV;          // seven TDGL totals: one at a time (registers)
-    #pragma unroll UNR
+    #pragma unroll
     for (int i = 0; i < NV; ++i) {
         #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -553,6 +568,51 @@ __global__ void __launch_bounds__(NT) k_tdgl(Dev d, Fields<T> F)
 // sums (evolve.cu:256-357 scaled as in :391-400), and the per-step reset of
 // the solver state.
 // DF: the partials are block_partial32 pairs (FP32 kernel).
+// Film fi's sweep row frow from the totals of its seven row sums (one thread).
+template <int NV>
+__device__ __forceinline__ void row_write(const Dev &d, int fi, int frow, const double (&sTot)[NV])
+{
+    const FilmDev *ff = d.films + fi;
+    double *R = d.rowbuf + ((long long)fi * d.rstride + frow) * 11;
+    const double N = (double)ff->nx * ff->ny * ff->nz;
+    R[0] = sTot[0] * ff->inv_N;
+    R[1] = sTot[1] * ff->inv_N;
+    R[2] = sTot[2] * ff->inv_N;
+    R[3] = sTot[3] * ff->inv_N;
+    const double nFE = ff->n_mat[1], nAFE = ff->n_mat[0], nDE = ff->n_mat[2];
+    R[4] = nFE > 0.0 ? sTot[4] / nFE : 0.0;
+    R[5] = nFE > 0.0 ? nFE / N : 0.0;
+    R[6] = nAFE > 0.0 ? sTot[5] / nAFE : 0.0;
+    R[7] = nAFE > 0.0 ? nAFE / N : 0.0;
+    R[8] = nDE > 0.0 ? sTot[6] / nDE : 0.0;
+    R[9] = nDE > 0.0 ? nDE / N : 0.0;
+    R[10] = (double)(d.ctl->step + 1);
+}
+
+// Film fi's solver state at the start of a step (one thread).
+__device__ __forceinline__ void step_reset(const Dev &d, int fi)
+{
+    SolveDev *S = d.solve + fi;
+    S->outer_active = d.films[fi].dep_flag ? 1 : 0;
+    S->active = 0;
+    S->status = 0;
+    S->refine = 0;
+    S->upd = 0;
+    S->total_iters = 0;
+    S->iters = 0;
+}
+
+// Reopens the step that step_end ended last (one thread): the counters and
+// the P sets as they were before it, so that the residual pass that ends the
+// step again advances them once more.
+__device__ __forceinline__ void step_reopen(const Dev &d)
+{
+    d.ctl->step -= 1;
+    d.ctl->run_step -= 1;
+    d.ctl->cur ^= 1;
+    d.ctl->redo = 1;
+}
+
 template <bool DF>
 __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)[7], double (&sTot)[7])
 {
@@ -562,33 +622,9 @@ __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)
         if (frow >= 0) {
             if (DF) film_total32<7>(d, ff, sRed, sTot);
             else film_total<7>(d, ff, sRed, sTot);
-            if (threadIdx.x == 0) {
-                double *R = d.rowbuf + ((long long)fi * d.rstride + frow) * 11;
-                const double N = (double)ff->nx * ff->ny * ff->nz;
-                R[0] = sTot[0] * ff->inv_N;
-                R[1] = sTot[1] * ff->inv_N;
-                R[2] = sTot[2] * ff->inv_N;
-                R[3] = sTot[3] * ff->inv_N;
-                const double nFE = ff->n_mat[1], nAFE = ff->n_mat[0], nDE = ff->n_mat[2];
-                R[4] = nFE > 0.0 ? sTot[4] / nFE : 0.0;
-                R[5] = nFE > 0.0 ? nFE / N : 0.0;
-                R[6] = nAFE > 0.0 ? sTot[5] / nAFE : 0.0;
-                R[7] = nAFE > 0.0 ? nAFE / N : 0.0;
-                R[8] = nDE > 0.0 ? sTot[6] / nDE : 0.0;
-                R[9] = nDE > 0.0 ? nDE / N : 0.0;
-                R[10] = (double)(d.ctl->step + 1);
-            }
+            if (threadIdx.x == 0) row_write(d, fi, frow, sTot);
         }
-        if (threadIdx.x == 0) {
-            SolveDev *S = d.solve + fi;
-            S->outer_active = ff->dep_flag ? 1 : 0;
-            S->active = 0;
-            S->status = 0;
-            S->refine = 0;
-            S->upd = 0;
-            S->total_iters = 0;
-            S->iters = 0;
-        }
+        if (threadIdx.x == 0) step_reset(d, fi);
     }
     if (threadIdx.x == 0) {
         step_begin(d, rs);
@@ -747,7 +783,7 @@ __device__ __forceinline__ void step_end(const Dev &d)
         SolveDev *S = d.solve + fi;
         const long long w = (long long)fi * d.wstride + d.ctl->run_step;
         d.iters_log[w] = S->total_iters;
-        d.refine_log[w] = S->refine;
+        d.refine_log[w] = S->refine + (S->pending ? 1 : 0);   // a deferred check counts as a pass
         if (S->status != 0 && S->status != 3 && S->sticky == 0) S->sticky = S->status;
     }
     __syncthreads();
@@ -785,7 +821,8 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
             const double bb = was_upd ? S->bb : sTot[1];
             const int c0 = S->phi_cur, p0 = S->phi_prev, q0 = S->phi_prev2, r0 = S->phi_prev3;
             const int fr = 10 - c0 - p0 - q0 - r0;
-            if (S->refine == 0) {            // keep phi_n .. phi_{n-2} for the next step's extrapolation
+            const bool first = S->refine == 0;
+            if (first) {                     // keep phi_n .. phi_{n-2} for the next step's extrapolation
                 S->phi_prev3 = q0;
                 S->phi_prev2 = p0;
                 S->phi_prev = c0;
@@ -839,6 +876,13 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
                 want = fmax(want, ff->inner_tol2);
                 S->inner_tol2 = fmin(want, 1e-4);
                 S->inner_max = ff->inner_max;
+                // the step's first pass before an exact direct solve: the step
+                // ends on that solve, and the next TDGL step forms the check
+                // the update pass would have formed (SolveDev::pending)
+                if (d.defer && ff->defer_ok && first && S->upd && S->active) {
+                    S->pending = 1;
+                    S->outer_active = 0;
+                }
             }
             any_outer |= S->outer_active;
             any_inner |= S->active;
@@ -1054,6 +1098,30 @@ __global__ void __launch_bounds__(NT) k_update(Dev d, Fields<T> F)
 static __global__ void k_step_end(Dev d)
 {
     step_end(d);
+}
+
+// After the last step of a run (one thread): every film whose last step
+// ended on its direct solve gets its check as an update pass.  That step is
+// reopened, so that the residual pass that ends it again leaves the counters
+// where the run left them; h_open (the IF node over those passes) is set
+// when there is such a film.
+static __global__ void k_defer_open(Dev d, cudaGraphConditionalHandle h_open)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int any = 0;
+    for (int fi = 0; fi < d.n_films; ++fi) {
+        SolveDev *S = d.solve + fi;
+        if (!S->pending) continue;
+        S->pending = 0;
+        S->outer_active = 1;
+        S->active = 0;
+        S->refine = 1;
+        S->upd = 1;
+        any = 1;
+    }
+    if (any) step_reopen(d);
+    else d.ctl->redo = 0;
+    set_cond(d, h_open, any);
 }
 
 // ----------------------------------------------------------- utilities

@@ -306,10 +306,14 @@ __device__ __forceinline__ bool spec_run(const Dev &d, int f)
 
 // The inverse transform closes the solve: its last block marks every active
 // film's inner solve done (one "iteration").
+// Under deferred checks (Dev::defer, the solve node of a step) a step whose
+// films all end on this solve ends here.
 __device__ __forceinline__ void spec_finish(const Dev &d)
 {
     if (!ticket_last(d.counter)) return;
+    __shared__ int s_out;
     if (threadIdx.x == 0) {
+        int out = 0;
         if (!d.force)
             for (int f = 0; f < d.n_films; ++f) {
                 SolveDev *S = d.solve + f;
@@ -318,9 +322,13 @@ __device__ __forceinline__ void spec_finish(const Dev &d)
                     S->total_iters += 1;
                     S->active = 0;
                 }
+                out |= S->outer_active;
             }
         *d.counter = 0u;
+        s_out = out;
     }
+    __syncthreads();
+    if (d.defer && d.step_end && !d.force && !s_out) step_end(d);
 }
 
 // x transforms of rows (j, y) of the packed planes, j = 0 .. Mp-1.  IN_REAL:

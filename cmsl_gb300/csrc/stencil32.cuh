@@ -81,6 +81,48 @@ template <int NS> struct RingIdx {
     __device__ __forceinline__ void next() { s = s + 1 == NS ? 0 : s + 1; }
 };
 
+// The neighbourhood of one cell as a residual pass sees it.
+struct RCell {
+    df xc, xe, xw, xn, xs, xu, xd;          // x = phi + dx (z neighbours as loaded, k+1 / k-1 clamped)
+    float dc, de, dw, dn, ds, du, dd;        // pending correction (update passes)
+    float pxe, pxw, pyn, pys, pzu, pzd;      // Pm for the divergence (z clamped)
+    int mc, me, mw, mn, ms, mu, md;          // materials (general eps only)
+};
+
+// Film constants of a residual pass, held in registers.
+struct RConst {
+    df cb, cu;                  // eps_0_nd / (2h); eps / h^2 on every face (one eps)
+    float dinv_u;               // Jacobi weight of the non-identity rows (one eps)
+    int nz;
+    bool neu;                   // Neumann z boundary (mirrored end rows, one pinned cell)
+    long long ref;              // the pinned cell (film-local)
+    const float *cf_h, *cf_l;   // general eps: face coefficient tables (through the film table)
+};
+
+// z neighbours of the operator (depol_varEPS.cu:86-99), given the loaded
+// k+1 and k-1 values (clamped at the ends).
+template <class V>
+__device__ __forceinline__ void zpick(const RConst &rc, int k, V up, V dn, V &u, V &dd)
+{
+    if (!rc.neu || (k > 0 && k < rc.nz - 1)) { u = up; dd = dn; }
+    else if (k == 0) { u = up; dd = up; }
+    else { u = dn; dd = dn; }
+}
+
+// -A dx of one non-identity row in FP32 (dx: the pending correction).
+template <bool UNI>
+__device__ __forceinline__ float minus_adx(const RConst &rc, int k, const RCell &c)
+{
+    float du, ddn;
+    zpick<float>(rc, k, c.du, c.dd, du, ddn);
+    if (UNI) return rc.cu.h * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
+    int mu, md;
+    zpick<int>(rc, k, c.mu, c.md, mu, md);
+    const float *ch = rc.cf_h + c.mc * 3;
+    return ch[c.me] * (c.de - c.dc) - ch[c.mw] * (c.dc - c.dw) + ch[c.mn] * (c.dn - c.dc) -
+           ch[c.ms] * (c.dc - c.ds) + ch[mu] * (du - c.dc) - ch[md] * (c.dc - ddn);
+}
+
 // ------------------------------------------------------------ TDGL step
 // kernelCalc_antiferro (kernels_evol.cu:47-231) with E_dep of the current
 // potential (depol_varEPS.cu:223-276) and the sweep-row sums
@@ -171,7 +213,8 @@ __device__ __forceinline__ void efield_z(bool neumann, int k, int nz, df fu, df 
     }
 }
 
-__device__ __forceinline__ void row_acc(float (&acc)[7], int mat, const float (&pn)[6], float pMZl, float pSZl)
+template <int NV>
+__device__ __forceinline__ void row_acc(float (&acc)[NV], int mat, const float (&pn)[6], float pMZl, float pSZl)
 {
     acc[0] += pn[2];
     acc[1] += pn[5];
@@ -184,25 +227,51 @@ __device__ __forceinline__ void row_acc(float (&acc)[7], int mat, const float (&
 
 constexpr int T32_NS = 4;
 // Stage layout (own + halo slots): P as three float2 planes (P0, P1), (P2, P3),
-// (P4, P5), the potential as one (hi, lo) float2 plane, then the code (own):
-// a stencil point of a pair is one 8-byte shared load.
-template <int TYc> __host__ __device__ constexpr int t32_stage()      // floats
+// (P4, P5), the potential as one (hi, lo) float2 plane, then the code (own),
+// and with DEF the pending correction dx (own + halo): a stencil point of a
+// pair is one 8-byte shared load.
+template <int TYc, bool DEF = false> __host__ __device__ constexpr int t32_stage()      // floats
 {
-    return 8 * TileShape<TYc>::SPLt + TileShape<TYc>::NTt;
+    return 8 * TileShape<TYc>::SPLt + TileShape<TYc>::NTt + (DEF ? TileShape<TYc>::SPLt : 0);
 }
-template <int TYc> constexpr size_t t32_smem() { return sizeof(float) * T32_NS * t32_stage<TYc>(); }
+template <int TYc, bool DEF = false> constexpr size_t t32_smem()
+{
+    return sizeof(float) * T32_NS * t32_stage<TYc, DEF>();
+}
+
+template <int NV>
+__device__ __forceinline__ void tdgl_finish_def(const Dev &d, int rs, double (*sRed)[NV], double (&sTot)[NV]);
 
 // TYc: the tile height (TX x TYc threads, one column each).
-template <int NS, int TYc = TY>
-__global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_tdgl32(Dev d, Fields<float> F)
+// DEF: a film whose previous step ended on its direct solve (SolveDev::pending;
+// every depolarised film under kernel timing) has the potential x0 + dx -- the
+// warm start in phi_cur plus the pending correction dx.  The step takes E
+// from x0 + dx, writes x0 + dx to the free buffer (where the update pass
+// would have put it), extrapolates the next warm start into the third-oldest
+// potential's buffer (a warm start of at most quadratic order never reads
+// it), and forms the check the update pass would have formed: r <- r - A dx
+// in FP32 (r.r in the eighth partial sum).  The last block decides whether
+// the previous step stands (tdgl_finish_def).
+// The check's values raise the registers a thread needs: the DEF kernels are
+// built for three quarters of the blocks per SM (80 registers at 32 x 8
+// tiles, where the 64 of four blocks spilled and ran 15 % slower).
+template <int TYc, bool DEF> constexpr int tdgl32_minb()
+{
+    return DEF && TYc < 16 ? TileShape<TYc>::MINB * 3 / 4 : TileShape<TYc>::MINB;
+}
+
+template <int NS, int TYc = TY, bool DEF = false>
+__global__ void __launch_bounds__(TileShape<TYc>::NTt, tdgl32_minb<TYc, DEF>()) k_tdgl32(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
-    constexpr int SPL = TileShape<TYc>::SPLt, NT = TileShape<TYc>::NTt, T32_STAGE = t32_stage<TYc>();
+    constexpr int SPL = TileShape<TYc>::SPLt, NT = TileShape<TYc>::NTt, T32_STAGE = t32_stage<TYc, DEF>();
+    constexpr int NV = DEF ? 8 : 7;         // row sums (+ the check's r.r)
+    constexpr int DXO = 8 * SPL + NT;       // DEF: the dx plane of a stage
     extern __shared__ float4 smem_t32[];
     float *ring = (float *)smem_t32;
     __shared__ float4 sC[6][3];
-    __shared__ double sRed[NT / 32][7];
-    __shared__ double sTot[7];
+    __shared__ double sRed[NT / 32][NV];
+    __shared__ double sTot[NV];
     const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const int z0 = it.w & 0xffff, z1 = it.w >> 16;
@@ -217,17 +286,26 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
     const float inv_2hf = f->inv_2hf;
     const long long off = f->off, lo = d.ncells, fs = d.ncells;
     const SolveDev *S = d.solve + it.x;
+    const bool pend = DEF && dep && (d.force || S->pending != 0);
     const float2 *ph = phi2_sel(d, S->phi_cur) + off;
     const float2 *qh = phi2_sel(d, S->phi_prev) + off;
     const float2 *uh = phi2_sel(d, S->phi_prev2) + off;
     const float2 *vh = phi2_sel(d, S->phi_prev3) + off;
-    float2 *nh = phi2_sel(d, phi_free(S)) + off;
+    float2 *nh = phi2_sel(d, pend ? S->phi_prev3 : phi_free(S)) + off;
+    float2 *xh = phi2_sel(d, phi_free(S)) + off;     // DEF: the checked potential x0 + dx
+    const float *dxg = F.x + off, *rg = F.r + off;
     const uint32_t *code = d.code + off;
     const float4 *TR4 = (const float4 *)(F.TR + (long long)TR32 * f->g_off);
     const float2 *Po = pairs32(F, cur) + off;   // the three pairs of a set at j * fs
     float2 *Pn = pairs32(F, cur ^ 1) + off;
     const int zlo = max(z0 - 1, 0), zhi = min(z1, nz - 1);
     (void)lo;
+    // the check's operator (one eps) and identity rows, as the update pass has them
+    RConst rc;
+    rc.cu = df{f->cf_h[0], f->cf_l[0]};
+    rc.nz = nz;
+    rc.neu = neu;
+    const long long pin = neu ? (long long)f->ref_id - g.own_pl : -1;
 
     // copies of plane p (planes are issued in order, p = zlo, zlo + 1, ...)
     long long own_o = g.own_pl + (long long)zlo * g.plane, halo_o = g.halo_pl + (long long)zlo * g.plane;
@@ -238,11 +316,13 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
                 for (int j = 0; j < 3; ++j) cp8(st + 2 * (j * SPL + g.own_slot), Po + j * fs + own_o);
                 if (dep) cp8(st + 2 * (3 * SPL + g.own_slot), ph + own_o);
                 cp4(st + 8 * SPL + threadIdx.x, code + own_o);
+                if (pend) cp4(st + DXO + g.own_slot, dxg + own_o);
             }
             if (g.halo) {
                 #pragma unroll
                 for (int j = 0; j < 3; ++j) cp8(st + 2 * (j * SPL + g.halo_slot), Po + j * fs + halo_o);
                 if (dep) cp8(st + 2 * (3 * SPL + g.halo_slot), ph + halo_o);
+                if (pend) cp4(st + DXO + g.halo_slot, dxg + halo_o);
             }
         }
         cp_commit();
@@ -251,9 +331,9 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
     };
     for (int p = zlo; p <= z0 + NS - 3; ++p) issue(p, ring + (p - zlo) * T32_STAGE);
 
-    float acc[7];
+    float acc[NV];
     #pragma unroll
-    for (int q = 0; q < 7; ++q) acc[q] = 0.f;
+    for (int q = 0; q < NV; ++q) acc[q] = 0.f;
     const int s0 = g.own_slot;
     RingIdx<NS> ri{z0 - zlo};
     long long o = g.own_pl + (long long)z0 * g.plane;
@@ -267,6 +347,7 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
         if (dep && warm >= 1) wq = ld_df(qh + o);
         if (dep && warm >= 2) wu = ld_df(uh + o);
         if (dep && warm >= 3) wv = ld_df(vh + o);
+        const float rold = pend ? rg[o] : 0.f;          // DEF: r of the step's first pass
         const float *sk = ring + ri.s * T32_STAGE;
         const float *su = ring + ri.up(k == nz - 1) * T32_STAGE, *sd = ring + ri.dn(k == 0) * T32_STAGE;
         const uint32_t c = ((const uint32_t *)sk)[8 * SPL + threadIdx.x];
@@ -285,6 +366,7 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
         }
         float ex = 0.f, ey = 0.f, ez = 0.f;
         df a0{0.f, 0.f};
+        float chk = 0.f;                                // DEF: the check's r, formed here
         if (dep) {
             const float2 *f2 = k2 + 3 * SPL;
             const float2 fc = f2[s0], fu = u2[3 * SPL + s0], fd = d2[3 * SPL + s0];
@@ -293,9 +375,30 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
             df pu, pd;
             efield_z(neu, k, nz, df{fu.x, fu.y}, df{fd.x, fd.y}, pu, pd);
             // -1 * E with E = -(phi_+ - phi_-) / (2h)
-            ex = phi_diff32(df{fe.x, fe.y}, df{fw.x, fw.y}) * inv_2hf;
-            ey = phi_diff32(df{fn.x, fn.y}, df{fsth.x, fsth.y}) * inv_2hf;
-            ez = phi_diff32(pu, pd) * inv_2hf;
+            ex = phi_diff32(df{fe.x, fe.y}, df{fw.x, fw.y});
+            ey = phi_diff32(df{fn.x, fn.y}, df{fsth.x, fsth.y});
+            ez = phi_diff32(pu, pd);
+            if (pend) {
+                // phi = x0 + dx: the differences of dx added, the own value
+                // resolved and stored; the update pass's r <- r - A dx
+                // (identity rows: x - g with g = 0)
+                RCell cd;
+                const float *dk = sk + DXO;
+                cd.dc = dk[s0]; cd.de = dk[s0 + 1]; cd.dw = dk[s0 - 1]; cd.dn = dk[s0 + SX]; cd.ds = dk[s0 - SX];
+                cd.du = su[DXO + s0]; cd.dd = sd[DXO + s0];
+                df du{cd.du, 0.f}, dd{cd.dd, 0.f};
+                efield_z(neu, k, nz, du, dd, du, dd);
+                ex += cd.de - cd.dw;
+                ey += cd.dn - cd.ds;
+                ez += du.h - dd.h;
+                a0 = df_add_f(a0, cd.dc);
+                xh[o] = make_float2(a0.h, a0.l);
+                const bool ident = neu ? (long long)k * g.plane == pin : (k == 0 || k == nz - 1);
+                chk = ident ? -(a0.h + a0.l) : rold + minus_adx<true>(rc, k, cd);
+            }
+            ex *= inv_2hf;
+            ey *= inv_2hf;
+            ez *= inv_2hf;
         }
         float pn[6], pMZl, pSZl;
         tdgl_cell32(sC[code_mat(c) * 2 + code_iface(c)], TR4 + 3LL * code_gid(c), pc, sum, ex, ey, ez, mEz, pn,
@@ -307,12 +410,85 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_t
             const df w = extrap_phi(warm, a0, wq, wu, wv);
             nh[o] = make_float2(w.h, w.l);
         }
+        if (pend) acc[NV - 1] = fmaf(chk, chk, acc[NV - 1]);
     }
     cp_wait<0>();
 
-    if (row >= 0) block_partial32<7>(d, acc, sRed);
+    if (row >= 0 || pend) block_partial32<NV>(d, acc, sRed);
     if (!ticket_last(d.counter)) return;
-    tdgl_finish<true>(d, rs, sRed, sTot);
+    if constexpr (DEF) tdgl_finish_def<NV>(d, rs, sRed, sTot);
+    else tdgl_finish<true>(d, rs, sRed, sTot);
+}
+
+// Last block of a TDGL step that may carry deferred checks: every pending
+// film's r.r of its check decides whether its previous step stands (the
+// update pass's test, ||r|| <= refine_tol ||b||).  If every check passes,
+// the checked potentials become current and the step begins as
+// tdgl_finish<true> begins it.  If one fails, the previous step is reopened:
+// the step counters and the P sets roll back, the failed films are set up
+// for the update pass that the step's next residual pass then is, the films
+// whose checks passed stay pending (the repeated step checks them again, to
+// the same result), and the step loop runs this step again after that pass
+// has ended the previous one.
+template <int NV>
+__device__ __forceinline__ void tdgl_finish_def(const Dev &d, int rs, double (*sRed)[NV], double (&sTot)[NV])
+{
+    static_assert(NV == 8, "seven row sums and the check's r.r");
+    if (d.force) {              // kernel timing: the state stays as it is
+        if (threadIdx.x == 0) *d.counter = 0u;
+        return;
+    }
+    __shared__ int s_fail;
+    if (threadIdx.x == 0) s_fail = 0;
+    for (int fi = 0; fi < d.n_films; ++fi) {
+        const FilmDev *ff = d.films + fi;
+        SolveDev *S = d.solve + fi;
+        const int frow = d.rows[(long long)fi * d.wstride + rs];
+        const bool pend = ff->dep_flag != 0 && uniform_flag(&S->pending);
+        if (frow < 0 && !pend) continue;
+        film_total32<NV>(d, ff, sRed, sTot);
+        if (threadIdx.x == 0) {
+            if (frow >= 0) row_write(d, fi, frow, sTot);
+            if (pend) {
+                const double rr = sTot[NV - 1];
+                S->rr64 = rr;
+                if (!(rr <= ff->refine_tol2 * S->bb || rr == 0.0)) s_fail = 1;   // NaN fails too
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    if (!s_fail) {
+        for (int fi = 0; fi < d.n_films; ++fi) {
+            SolveDev *S = d.solve + fi;
+            if (S->pending) {
+                // this launch wrote x0 + dx to the free buffer; the warm start
+                // buffer (x0) takes the third-oldest slot, which held the next
+                // warm start and now becomes the free one
+                const int fr = phi_free(S);
+                S->phi_prev3 = S->phi_cur;
+                S->phi_cur = fr;
+                S->pending = 0;
+            }
+            step_reset(d, fi);
+        }
+        step_begin(d, rs);
+    } else {
+        for (int fi = 0; fi < d.n_films; ++fi) {
+            const FilmDev *ff = d.films + fi;
+            SolveDev *S = d.solve + fi;
+            if (S->pending && !(S->rr64 <= ff->refine_tol2 * S->bb || S->rr64 == 0.0)) {
+                S->pending = 0;
+                S->outer_active = 1;
+                S->active = 0;
+                S->refine = 1;
+                S->upd = 1;
+            }
+        }
+        step_reopen(d);
+        set_cond(d, d.h_steps, 1);
+    }
+    *d.counter = 0u;
 }
 
 // Warm start alone (own cells): the free buffer of every depolarised film
@@ -385,48 +561,6 @@ __device__ __forceinline__ df div3(float a, float b, float c, float e, float g, 
     const df s2 = two_sum(s.h, z.h);
     l += s2.l + z.l;
     return fast_two_sum(s2.h, l);
-}
-
-// The neighbourhood of one cell as a residual pass sees it.
-struct RCell {
-    df xc, xe, xw, xn, xs, xu, xd;          // x = phi + dx (z neighbours as loaded, k+1 / k-1 clamped)
-    float dc, de, dw, dn, ds, du, dd;        // pending correction (update passes)
-    float pxe, pxw, pyn, pys, pzu, pzd;      // Pm for the divergence (z clamped)
-    int mc, me, mw, mn, ms, mu, md;          // materials (general eps only)
-};
-
-// Film constants of a residual pass, held in registers.
-struct RConst {
-    df cb, cu;                  // eps_0_nd / (2h); eps / h^2 on every face (one eps)
-    float dinv_u;               // Jacobi weight of the non-identity rows (one eps)
-    int nz;
-    bool neu;                   // Neumann z boundary (mirrored end rows, one pinned cell)
-    long long ref;              // the pinned cell (film-local)
-    const float *cf_h, *cf_l;   // general eps: face coefficient tables (through the film table)
-};
-
-// z neighbours of the operator (depol_varEPS.cu:86-99), given the loaded
-// k+1 and k-1 values (clamped at the ends).
-template <class V>
-__device__ __forceinline__ void zpick(const RConst &rc, int k, V up, V dn, V &u, V &dd)
-{
-    if (!rc.neu || (k > 0 && k < rc.nz - 1)) { u = up; dd = dn; }
-    else if (k == 0) { u = up; dd = up; }
-    else { u = dn; dd = dn; }
-}
-
-// -A dx of one non-identity row in FP32 (dx: the pending correction).
-template <bool UNI>
-__device__ __forceinline__ float minus_adx(const RConst &rc, int k, const RCell &c)
-{
-    float du, ddn;
-    zpick<float>(rc, k, c.du, c.dd, du, ddn);
-    if (UNI) return rc.cu.h * ((c.de + c.dw) + (c.dn + c.ds) + (du + ddn) - 6.f * c.dc);
-    int mu, md;
-    zpick<int>(rc, k, c.mu, c.md, mu, md);
-    const float *ch = rc.cf_h + c.mc * 3;
-    return ch[c.me] * (c.de - c.dc) - ch[c.mw] * (c.dc - c.dw) + ch[c.mn] * (c.dn - c.dc) -
-           ch[c.ms] * (c.dc - c.ds) + ch[mu] * (du - c.dc) - ch[md] * (c.dc - ddn);
 }
 
 // r (FP32 value of b - A x, double-float arithmetic) and b.h of one non-identity row.

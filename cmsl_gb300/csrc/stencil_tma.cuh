@@ -196,8 +196,6 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
     float acc[7];
     #pragma unroll
     for (int q = 0; q < 7; ++q) acc[q] = 0.f;
-    int gid = -1;
-    float t[9];
     RingIdx<NS> ri{z0 - zlo};
     long long o = (long long)(x0 + lx) + (long long)nx * (y0 + ly) + (long long)z0 * plane;
     const long long plane_step = plane;

