@@ -1797,10 +1797,59 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
 
 cmsl_status autotune_items(Engine *e, int32_t *zchunk);
 
-// Tile-shape autotuner: times the stencil passes (TDGL step and the
-// item-based solve kernels: the FP32 first and update passes, the FP64 PCG
-// kernels) for z chunks 4, 8, 16, ... up to the thickest film, keeps the
-// fastest, and remembers it for handles of the same film-shape class.
+// One FP32 step's stencil kernels launched back to back in force mode, as a
+// step runs them: the TDGL step, a step's first residual pass, the direct
+// inner solve and, unless the next TDGL step forms its check, the update
+// pass (the persistent PCG's launch does not depend on the tiles and is left
+// out).  Kernels that follow each other find part of their input in L2, so
+// the autotuner compares tiles on this sequence rather than on kernels timed
+// alone.  The solver state is restored afterwards; *ms is per sequence.
+cmsl_status time_sequence(Engine *e, int reps, double *ms)
+{
+    CK(cudaDeviceSynchronize());
+    const size_t F = (size_t)e->n_films;
+    Dev d = e->dev(0);
+    d.force = 1;
+    Dev d1 = d, d2 = d;
+    d1.force_pass = 1;
+    d2.force_pass = 2;
+    const Fields<float> F32 = e->fields<float>();
+    std::vector<double> e0(F, 0.0);
+    std::vector<int> rowm1(F, -1);
+    CK(cudaMemcpy2D(e->d_wave, sizeof(double) * e->wstride, e0.data(), sizeof(double), sizeof(double), F,
+                    cudaMemcpyHostToDevice));
+    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, rowm1.data(), sizeof(int), sizeof(int), F,
+                    cudaMemcpyHostToDevice));
+    CK(cudaMemset(&e->d_ctl->run_step, 0, sizeof(int)));
+    std::vector<SolveDev> S(F);
+    CK(cudaMemcpy(S.data(), e->d_solve, sizeof(SolveDev) * F, cudaMemcpyDeviceToHost));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    for (int r = -1; r < reps; ++r) {
+        if (r == 0) CK(cudaEventRecord(a, nullptr));
+        TRY(launch_tdgl32(e, nullptr, d, F32));
+        TRY(launch_refine(e, nullptr, d1, F32));
+        if (e->spectral) TRY(spec_launch(e, nullptr, d, F32));
+        if (e->spectral && !e->defer) TRY(launch_refine(e, nullptr, d2, F32));
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(b, nullptr));
+    CK(cudaEventSynchronize(b));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, a, b));
+    *ms = (double)t / reps;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    CK(cudaMemcpy(e->d_solve, S.data(), sizeof(SolveDev) * F, cudaMemcpyHostToDevice));
+    return CMSL_OK;
+}
+
+// Tile-shape autotuner: times the stencil passes (FP32: one step's kernel
+// sequence, time_sequence; FP64: the TDGL step and the PCG kernels) for
+// z chunks 4, 8, 16, ... up to the thickest film, tile heights and stagings,
+// keeps the fastest, and remembers it for handles of the same film-shape
+// class.
 cmsl_status autotune(Engine *e, int32_t *zchunk)
 {
     // the FP64 PCG kernels update the potential in place when timed: keep a copy
@@ -1848,28 +1897,30 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
         const int fixed_t = e->stg_tdgl, fixed_r = e->stg_refine;
         for (int c : cands) {
             TRY(set_items(e, c));
-            double tt[N_STG] = {0.0, 0.0}, tr[N_STG] = {0.0, 0.0}, rest = 0.0;
-            for (int v = 0; v < nst; ++v) {
-                if (tune_stg) e->stage(v, v);
-                else if (fp32) e->stage(e->staging_fixed ? fixed_t : STG_CP, e->staging_fixed ? fixed_r : STG_CP);
+            if (!fp32) {
                 double ms[4] = {0, 0, 0, 0};
                 TRY(time_kernels(e, 5, nullptr, ms));
-                tt[v] = ms[0];                                  // TDGL step
-                tr[v] = ms[1];                                  // first pass (FP32) / set-up (FP64)
-                if (!fp32) rest = ms[2] + ms[3];
-                else if (e->spectral) tr[v] += ms[3];           // update pass
-                else if (!e->persistent) rest = ms[2] + ms[3];  // two-kernel PCG
+                const double t = ms[0] + ms[1] + ms[2] + ms[3];
+                if (best.zchunk == 0 || t < best_ms) {
+                    best = Tuned{c, e->stg_tdgl, e->stg_refine, ty};
+                    best_ms = t;
+                }
+                continue;
             }
-            int vt = 0, vr = 0;
-            for (int v = 1; v < nst; ++v) {
-                if (tt[v] < tt[vt]) vt = v;
-                if (tr[v] < tr[vr]) vr = v;
-            }
-            const double t = tt[vt] + tr[vr] + rest;
-            if (best.zchunk == 0 || t < best_ms) {
-                best = tune_stg ? Tuned{c, vt, vr, ty} : Tuned{c, e->stg_tdgl, e->stg_refine, ty};
-                best_ms = t;
-            }
+            // every staging pair of the TDGL and the residual passes (the
+            // TDGL that forms deferred checks has the cp.async ring only)
+            for (int vt = 0; vt < nst; ++vt)
+                for (int vr = 0; vr < nst; ++vr) {
+                    if (vt && e->defer) continue;
+                    if (tune_stg) e->stage(vt, vr);
+                    else e->stage(e->staging_fixed ? fixed_t : STG_CP, e->staging_fixed ? fixed_r : STG_CP);
+                    double t = 0.0;
+                    TRY(time_sequence(e, 5, &t));
+                    if (best.zchunk == 0 || t < best_ms) {
+                        best = tune_stg ? Tuned{c, vt, vr, ty} : Tuned{c, e->stg_tdgl, e->stg_refine, ty};
+                        best_ms = t;
+                    }
+                }
         }
     }
     e->stile_ty = best.tile_y;
