@@ -1701,9 +1701,10 @@ cmsl_status get_iters(Engine *e, int film, int n, int32_t *iters, int32_t *refin
 // PCG kernels (persistent FP32 solver: ms[2] per iteration, ms[3] the step
 // end; direct solve: ms[2] the solve, ms[3] the update pass, 0 under
 // deferred checks, whose TDGL kernel forms the check and is timed with every
-// depolarised film pending).  The refinement passes run in force mode, which
-// leaves the solver state as it is, so every repetition times the same kind
-// of pass.
+// depolarised film pending).  The kernels run in force mode, which leaves the
+// solver state as it is, so every repetition times the same kind of pass; the
+// TDGL step forms a sweep row and every launch's last block its film totals,
+// as in a step, without writing them.
 cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
 {
     if (!ms || reps < 1) return fail(CMSL_ERR_ARG, "bad arguments");
@@ -1716,10 +1717,10 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
     const Fields<double> F64 = e->fields<double>();
     const Fields<float> F32 = e->fields<float>();
     std::vector<double> e0(F, 0.0);
-    std::vector<int> rowm1(F, -1);
+    std::vector<int> row0(F, 0);        // a sweep row, as every step of the benchmark schedules forms one
     CK(cudaMemcpy2D(e->d_wave, sizeof(double) * e->wstride, e0.data(), sizeof(double), sizeof(double), F,
                     cudaMemcpyHostToDevice));
-    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, rowm1.data(), sizeof(int), sizeof(int), F,
+    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, row0.data(), sizeof(int), sizeof(int), F,
                     cudaMemcpyHostToDevice));
     CK(cudaMemset(&e->d_ctl->run_step, 0, sizeof(int)));
     cudaEvent_t a, b;
@@ -1815,10 +1816,10 @@ cmsl_status time_sequence(Engine *e, int reps, double *ms)
     d2.force_pass = 2;
     const Fields<float> F32 = e->fields<float>();
     std::vector<double> e0(F, 0.0);
-    std::vector<int> rowm1(F, -1);
+    std::vector<int> row0(F, 0);        // a sweep row, as every step of the benchmark schedules forms one
     CK(cudaMemcpy2D(e->d_wave, sizeof(double) * e->wstride, e0.data(), sizeof(double), sizeof(double), F,
                     cudaMemcpyHostToDevice));
-    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, rowm1.data(), sizeof(int), sizeof(int), F,
+    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, row0.data(), sizeof(int), sizeof(int), F,
                     cudaMemcpyHostToDevice));
     CK(cudaMemset(&e->d_ctl->run_step, 0, sizeof(int)));
     std::vector<SolveDev> S(F);

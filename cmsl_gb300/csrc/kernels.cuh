@@ -613,6 +613,8 @@ __device__ __forceinline__ void step_reopen(const Dev &d)
     d.ctl->redo = 1;
 }
 
+// Under kernel timing (d.force) the totals are formed as a step forms them
+// and nothing is written.
 template <bool DF>
 __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)[7], double (&sTot)[7])
 {
@@ -622,12 +624,12 @@ __device__ __forceinline__ void tdgl_finish(const Dev &d, int rs, double (*sRed)
         if (frow >= 0) {
             if (DF) film_total32<7>(d, ff, sRed, sTot);
             else film_total<7>(d, ff, sRed, sTot);
-            if (threadIdx.x == 0) row_write(d, fi, frow, sTot);
+            if (threadIdx.x == 0 && !d.force) row_write(d, fi, frow, sTot);
         }
-        if (threadIdx.x == 0) step_reset(d, fi);
+        if (threadIdx.x == 0 && !d.force) step_reset(d, fi);
     }
     if (threadIdx.x == 0) {
-        step_begin(d, rs);
+        if (!d.force) step_begin(d, rs);
         *d.counter = 0u;
     }
 }
@@ -805,7 +807,9 @@ __device__ __forceinline__ void step_end(const Dev &d)
 // solve's target.
 __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], double (&sTot)[3])
 {
-    if (d.force) {              // kernel timing: the state stays as it is
+    if (d.force) {              // kernel timing: the totals as a pass forms them; the state stays as it is
+        for (int fi = 0; fi < d.n_films; ++fi)
+            if (d.films[fi].dep_flag) film_total32<3>(d, d.films + fi, sRed, sTot);
         if (threadIdx.x == 0) *d.counter = 0u;
         return;
     }

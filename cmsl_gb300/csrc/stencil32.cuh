@@ -434,7 +434,10 @@ template <int NV>
 __device__ __forceinline__ void tdgl_finish_def(const Dev &d, int rs, double (*sRed)[NV], double (&sTot)[NV])
 {
     static_assert(NV == 8, "seven row sums and the check's r.r");
-    if (d.force) {              // kernel timing: the state stays as it is
+    if (d.force) {              // kernel timing: the totals as a step forms them; the state stays as it is
+        for (int fi = 0; fi < d.n_films; ++fi)
+            if (d.films[fi].dep_flag || d.rows[(long long)fi * d.wstride + rs] >= 0)
+                film_total32<NV>(d, d.films + fi, sRed, sTot);
         if (threadIdx.x == 0) *d.counter = 0u;
         return;
     }
