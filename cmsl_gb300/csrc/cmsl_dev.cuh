@@ -181,7 +181,6 @@ struct Dev {
     int wstride, rstride;
     int use_cond;
     int force;                  // run the PCG kernels whatever the flags (kernel timing)
-    int force_pass;             // under force: 0 the solver state's pass, 1 a step's first pass, 2 an update pass
     int step_end;               // a residual pass that leaves no film active also ends the step
     int defer;                  // films with defer_ok end a step on its direct solve (SolveDev::pending)
     unsigned int *arrive;       // grid-barrier counter of the persistent PCG (or null)

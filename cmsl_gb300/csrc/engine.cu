@@ -1522,6 +1522,7 @@ cmsl_status set_state(Engine *e, int film, const double *const P[6], const doubl
     if (!P) return fail(CMSL_ERR_ARG, "NULL argument");
     if (film < 0 || film >= e->n_films) return fail(CMSL_ERR_ARG, "film %d outside [0,%d)", film, e->n_films);
     CK(cudaDeviceSynchronize());
+    e->has_state = true;
     if (reset_clock) CK(cudaMemset(e->d_ctl, 0, sizeof(Ctl)));
     Ctl c;
     CK(cudaMemcpy(&c, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
@@ -1798,59 +1799,87 @@ cmsl_status time_kernels(Engine *e, int reps, void *stream, double *ms)
 
 cmsl_status autotune_items(Engine *e, int32_t *zchunk);
 
-// One FP32 step's stencil kernels launched back to back in force mode, as a
-// step runs them: the TDGL step, a step's first residual pass, the direct
-// inner solve and, unless the next TDGL step forms its check, the update
-// pass (the persistent PCG's launch does not depend on the tiles and is left
-// out).  Kernels that follow each other find part of their input in L2, so
-// the autotuner compares tiles on this sequence rather than on kernels timed
-// alone.  The solver state is restored afterwards; *ms is per sequence.
-cmsl_status time_sequence(Engine *e, int reps, double *ms)
+// The autotuner's trial steps (FP32): every buffer a step reads or writes is
+// copied aside before the trials and back before each, so that every
+// candidate tiling runs the same steps from the same state -- a sweep row a
+// step, field 0 -- and the films end the tuning as they began.  Films that
+// have no state yet (P = 0 gives b = 0 and no solve) get a fixed pseudo-random
+// P of amplitude 0.05 for the trials.
+struct StepSnapshot {
+    std::vector<std::pair<void *, size_t>> regions;
+    char *store = nullptr;
+    ~StepSnapshot() { if (store) cudaFree(store); }
+};
+
+static size_t snap_pad(size_t n) { return (n + 255) & ~(size_t)255; }
+
+cmsl_status snapshot_take(Engine *e, StepSnapshot &s)
 {
-    CK(cudaDeviceSynchronize());
+    const size_t cells = (size_t)e->ncells, F = (size_t)e->n_films;
+    for (int set = 0; set < 2; ++set) s.regions.push_back({e->d_P[set][0], 6 * e->esz * cells});
+    for (int b = 0; b < 5; ++b)
+        if (e->d_phi[b]) s.regions.push_back({e->d_phi[b], sizeof(double) * cells});
+    s.regions.push_back({e->d_x, e->esz * cells});
+    s.regions.push_back({e->d_r, e->esz * cells});
+    s.regions.push_back({e->d_solve, sizeof(SolveDev) * F});
+    s.regions.push_back({e->d_ctl, sizeof(Ctl)});
+    s.regions.push_back({e->d_rowbuf, sizeof(double) * 11 * (size_t)e->rstride * F});
+    s.regions.push_back({e->d_iters, sizeof(int) * (size_t)e->wstride * F});
+    s.regions.push_back({e->d_refine, sizeof(int) * (size_t)e->wstride * F});
+    size_t bytes = 0;
+    for (const auto &r : s.regions) bytes += snap_pad(r.second);
+    CK(cudaMalloc(&s.store, bytes));
+    size_t o = 0;
+    for (const auto &r : s.regions) {
+        CK(cudaMemcpy(s.store + o, r.first, r.second, cudaMemcpyDeviceToDevice));
+        o += snap_pad(r.second);
+    }
+    return CMSL_OK;
+}
+
+cmsl_status snapshot_put(const StepSnapshot &s)
+{
+    size_t o = 0;
+    for (const auto &r : s.regions) {
+        CK(cudaMemcpy(r.first, s.store + o, r.second, cudaMemcpyDeviceToDevice));
+        o += snap_pad(r.second);
+    }
+    return CMSL_OK;
+}
+
+// ms per step of W + K trial steps (the last K timed) from snapshot s.
+cmsl_status trial_steps(Engine *e, const StepSnapshot &s, bool synthetic, double *ms)
+{
+    constexpr int W = 4, K = 8;
+    TRY(snapshot_put(s));
+    if (synthetic) {
+        for (int set = 0; set < 2; ++set)
+            k_trial_P<<<XFER_GRID, XFER_NT>>>((float *)e->d_P[set][0], 6LL * e->ncells);
+        CK(cudaGetLastError());
+    }
     const size_t F = (size_t)e->n_films;
-    Dev d = e->dev(0);
-    d.force = 1;
-    Dev d1 = d, d2 = d;
-    d1.force_pass = 1;
-    d2.force_pass = 2;
-    const Fields<float> F32 = e->fields<float>();
-    std::vector<double> e0(F, 0.0);
-    std::vector<int> row0(F, 0);        // a sweep row, as every step of the benchmark schedules forms one
-    CK(cudaMemcpy2D(e->d_wave, sizeof(double) * e->wstride, e0.data(), sizeof(double), sizeof(double), F,
-                    cudaMemcpyHostToDevice));
-    CK(cudaMemcpy2D(e->d_rows, sizeof(int) * e->wstride, row0.data(), sizeof(int), sizeof(int), F,
-                    cudaMemcpyHostToDevice));
-    CK(cudaMemset(&e->d_ctl->run_step, 0, sizeof(int)));
-    std::vector<SolveDev> S(F);
-    CK(cudaMemcpy(S.data(), e->d_solve, sizeof(SolveDev) * F, cudaMemcpyDeviceToHost));
+    std::vector<double> Ez(F * (W + K), 0.0);
+    std::vector<int32_t> rows(F * (W + K), 0);
+    TRY(run(e, W, Ez.data(), rows.data(), nullptr));
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
-    for (int r = -1; r < reps; ++r) {
-        if (r == 0) CK(cudaEventRecord(a, nullptr));
-        TRY(launch_tdgl32(e, nullptr, d, F32));
-        TRY(launch_refine(e, nullptr, d1, F32));
-        if (e->spectral) TRY(spec_launch(e, nullptr, d, F32));
-        if (e->spectral && !e->defer) TRY(launch_refine(e, nullptr, d2, F32));
-        CK(cudaGetLastError());
-    }
+    CK(cudaEventRecord(a, nullptr));
+    TRY(run(e, K, Ez.data(), rows.data(), nullptr));
     CK(cudaEventRecord(b, nullptr));
     CK(cudaEventSynchronize(b));
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, a, b));
-    *ms = (double)t / reps;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    CK(cudaMemcpy(e->d_solve, S.data(), sizeof(SolveDev) * F, cudaMemcpyHostToDevice));
+    *ms = (double)t / K;
     return CMSL_OK;
 }
 
-// Tile-shape autotuner: times the stencil passes (FP32: one step's kernel
-// sequence, time_sequence; FP64: the TDGL step and the PCG kernels) for
-// z chunks 4, 8, 16, ... up to the thickest film, tile heights and stagings,
-// keeps the fastest, and remembers it for handles of the same film-shape
-// class.
+// Tile-shape autotuner: times trial steps (FP32, trial_steps) or the TDGL
+// step and the PCG kernels (FP64) for z chunks 4, 8, 16, ... up to the
+// thickest film, tile heights and stagings, keeps the fastest, and remembers
+// it for handles of the same film-shape class.
 cmsl_status autotune(Engine *e, int32_t *zchunk)
 {
     // the FP64 PCG kernels update the potential in place when timed: keep a copy
@@ -1880,11 +1909,15 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
     for (int c = ZCHUNK_MIN; c < maxnz; c *= 2) cands.push_back(c);
     cands.push_back(maxnz);
     // per tile height (FP32; 4, 8 and 16 rows unless CMSL_TILE_Y fixed one)
-    // and z chunk: every staging of the TDGL and of the residual passes where
-    // the tensor copies apply (8-row tiles of films with full tiles; the two
-    // kernels are independent, so each takes its fastest staging; a staging
-    // fixed by CMSL_STAGING is kept)
+    // and z chunk: every pair of stagings of the TDGL and the residual passes
+    // where the tensor copies apply (8-row tiles of films with full tiles; a
+    // staging fixed by CMSL_STAGING is kept)
     const bool fp32 = e->precision != CMSL_FP64;
+    std::unique_ptr<StepSnapshot> snap;
+    if (fp32) {
+        snap.reset(new StepSnapshot());
+        TRY(snapshot_take(e, *snap));
+    }
     std::vector<int> tys;
     if (!fp32 || e->tile_fixed) tys.push_back(e->stile_ty);
     else tys.assign(TILE_YS, TILE_YS + 3);
@@ -1916,7 +1949,7 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
                     if (tune_stg) e->stage(vt, vr);
                     else e->stage(e->staging_fixed ? fixed_t : STG_CP, e->staging_fixed ? fixed_r : STG_CP);
                     double t = 0.0;
-                    TRY(time_sequence(e, 5, &t));
+                    TRY(trial_steps(e, *snap, !e->has_state, &t));
                     if (best.zchunk == 0 || t < best_ms) {
                         best = tune_stg ? Tuned{c, vt, vr, ty} : Tuned{c, e->stg_tdgl, e->stg_refine, ty};
                         best_ms = t;
@@ -1924,6 +1957,7 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
                 }
         }
     }
+    if (snap) TRY(snapshot_put(*snap));
     e->stile_ty = best.tile_y;
     TRY(set_items(e, best.zchunk));
     if (fp32) e->stage(best.stg_tdgl, best.stg_refine);
@@ -2091,6 +2125,7 @@ cmsl_status cmsl_film_depol_device(cmsl_film *f, const double *Pmx, const double
     CK(cudaMemcpyAsync(&c, f->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&S, f->d_solve, sizeof(SolveDev), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    f->has_state = true;
     const double *src[3] = {Pmx, Pmy, Pmz};
     const int ps = f->pstride();
     for (int q = 0; q < 3; ++q) {

@@ -1104,6 +1104,19 @@ static __global__ void k_step_end(Dev d)
     step_end(d);
 }
 
+// A fixed pseudo-random P of amplitude 0.05 (FP32 pairs, n floats) for the
+// autotuner's trial steps on films that have no state yet.
+static __global__ void k_trial_P(float *P, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        uint32_t h = (uint32_t)i * 2654435761u;
+        h ^= h >> 15;
+        h *= 2246822519u;
+        h ^= h >> 13;
+        P[i] = 0.05f * ((float)(h & 0xffffu) / 32768.f - 1.f);
+    }
+}
+
 // After the last step of a run (one thread): every film whose last step
 // ended on its direct solve gets its check as an update pass.  That step is
 // reopened, so that the residual pass that ends it again leaves the counters

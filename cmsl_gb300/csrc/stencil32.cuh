@@ -657,10 +657,8 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_r
     rc.cf_h = f->cf_h;
     rc.cf_l = f->cf_l;
     const bool run = f->dep_flag != 0 && (d.force || S->outer_active);
-    // later pass: x = phi + dx; first: the warm start (kernel timing may fix the kind)
-    const int fk = d.force ? d.force_pass : 0;
-    const bool apply = fk ? fk == 2 : S->refine > 0;
-    const bool upd = UNI && apply && (fk ? true : S->upd != 0) && f->upd_ok;   // r <- r - A dx (after the direct solve, one eps)
+    const bool apply = S->refine > 0;                   // later pass: x = phi + dx; first: the warm start
+    const bool upd = UNI && apply && S->upd && f->upd_ok;   // r <- r - A dx (after the direct solve, one eps)
     const int cur = d.ctl->cur, fr = phi_free(S);
     const long long off = f->off, fs = d.ncells;
     const float2 *xh = phi2_sel(d, apply ? S->phi_cur : fr) + off;

@@ -61,9 +61,14 @@ def _close(a, b, tol):
     return max(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300) for x, y in zip(a, b)) <= tol
 
 
-@pytest.mark.parametrize("shape", [(64, 32, 13), (48, 36, 9), (96, 12, 7)])
-def test_deferred_checks_match_oracle_and_update_pass(gpu, shape, monkeypatch):
-    """Full and partial tiles (the direct solve takes Dirichlet films)."""
+@pytest.mark.parametrize("shape,staging", [((64, 32, 13), "00"), ((64, 32, 13), "11"), ((48, 36, 9), None),
+                                           ((96, 12, 7), None)])
+def test_deferred_checks_match_oracle_and_update_pass(gpu, shape, staging, monkeypatch):
+    """Full tiles with both stagings of the residual passes (the cp.async
+    ring, tensor copies; CMSL_STAGING -- the TDGL kernel that forms the check
+    has the ring) and partial tiles; the direct solve takes Dirichlet films."""
+    if staging:
+        monkeypatch.setenv("CMSL_STAGING", staging)
     f, P = _film(shape, seed=sum(shape))
     n = 24
     Ez = np.linspace(0.0, 0.35, n)
