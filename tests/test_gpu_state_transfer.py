@@ -82,6 +82,37 @@ def test_page_locked_outputs(gpu, precision):
             assert np.array_equal(pha, phb)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_page_locked_inputs(gpu, precision):
+    """set_state from page-locked P and phi gives the state and the run
+    that pageable inputs give, and page-locked outputs read it back
+    identically."""
+    f, P = random_film(36, 20, 10, seed=107, eps_0_nd=3.0, p_scale=0.2)
+    phi = np.random.default_rng(7).normal(0.0, 0.3, f.N)
+    kw = dict(precision=gpu.FP64 if precision == "fp64" else gpu.FP32_REFINED)
+    Ez = np.linspace(0.0, 0.2, 6)
+    P_in = [gpu.pinned_empty(f.N) for _ in range(6)]
+    for a, p in zip(P_in, P):
+        a[:] = p
+    phi_in = gpu.pinned_empty(f.N)
+    phi_in[:] = phi
+    res = []
+    for Pu, phu in ((P, phi), (P_in, phi_in)):
+        with gpu.Film.from_oracle_film(f, **kw) as g:
+            g.set_state(Pu, phu)
+            s0 = g.get_state()
+            g.run(Ez)
+            out = ([gpu.pinned_empty(f.N) for _ in range(6)], gpu.pinned_empty(f.N))
+            s1 = g.get_state(out=out)
+            res.append((s0, [np.array(a) for a in s1[0]], np.array(s1[1])))
+    for a, b in zip(res[0][0][0], res[1][0][0]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(res[0][0][1], res[1][0][1])
+    for a, b in zip(res[0][1], res[1][1]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(res[0][2], res[1][2])
+
+
 def test_bad_out_arrays(gpu):
     f, P = random_film(12, 12, 4, seed=105, eps_0_nd=3.0, p_scale=0.2)
     with gpu.Film.from_oracle_film(f) as g:
