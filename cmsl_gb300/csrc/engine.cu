@@ -477,15 +477,19 @@ cmsl_status build_graph(Engine *e)
         const Node rows[] = {
             {(void *)k_spec_x<true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
             {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
-            {(void *)k_spec_z, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
+            {(void *)k_spec_z<false>, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
             {(void *)k_spec_y, e->spec_grid[1], SPEC_NT, a_s, e->spec_smem[1]},
             {(void *)k_spec_x<false>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
         const Node cols[] = {
             {(void *)k_spec_x<true, true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]},
             {(void *)k_spec_yzy, e->spec_grid[3], SPEC_YZY_NT, a_s, e->spec_smem[3]},
             {(void *)k_spec_x<false, true>, e->spec_grid[0], SPEC_NT, a_x, e->spec_smem[0]}};
-        const Node *seq = e->spec_col ? cols : rows;
-        const int nseq = e->spec_col ? 3 : 5;
+        const Node clus[] = {
+            {(void *)k_spec_cxy, e->spec_grid[4], SPEC_CL_NT, a_x, e->spec_smem[4]},
+            {(void *)k_spec_z<true>, e->spec_grid[2], e->spec_zt, a_s, e->spec_smem[2]},
+            {(void *)k_spec_cyx, e->spec_grid[4], SPEC_CL_NT, a_x, e->spec_smem[4]}};
+        const Node *seq = e->spec_cl ? clus : e->spec_col ? cols : rows;
+        const int nseq = e->spec_cl || e->spec_col ? 3 : 5;
         const cudaGraphNode_t *prev = dep;
         for (int qi = 0; qi < nseq; ++qi) {
             const Node &q = seq[qi];
@@ -734,6 +738,13 @@ cmsl_status launch_tdgl32(Engine *e, cudaStream_t st, const Dev &d, const Fields
 cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<float> &F32)
 {
     const SpecDev &sp = e->spec;
+    if (e->spec_cl) {
+        k_spec_cxy<<<e->spec_grid[4], SPEC_CL_NT, e->spec_smem[4], st>>>(d, F32, sp);
+        k_spec_z<true><<<e->spec_grid[2], e->spec_zt, e->spec_smem[2], st>>>(d, sp);
+        k_spec_cyx<<<e->spec_grid[4], SPEC_CL_NT, e->spec_smem[4], st>>>(d, F32, sp);
+        CK(cudaGetLastError());
+        return CMSL_OK;
+    }
     if (e->spec_col) {
         k_spec_x<true, true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
         k_spec_yzy<<<e->spec_grid[3], SPEC_YZY_NT, e->spec_smem[3], st>>>(d, sp);
@@ -743,7 +754,7 @@ cmsl_status spec_launch(Engine *e, cudaStream_t st, const Dev &d, const Fields<f
     }
     k_spec_x<true><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
     k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
-    k_spec_z<<<e->spec_grid[2], e->spec_zt, e->spec_smem[2], st>>>(d, sp);
+    k_spec_z<false><<<e->spec_grid[2], e->spec_zt, e->spec_smem[2], st>>>(d, sp);
     k_spec_y<<<e->spec_grid[1], SPEC_NT, e->spec_smem[1], st>>>(d, sp);
     k_spec_x<false><<<e->spec_grid[0], SPEC_NT, e->spec_smem[0], st>>>(d, F32, sp);
     CK(cudaGetLastError());
@@ -1293,8 +1304,24 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         // per-film plans, tables and block ranges of the three passes
         const int zt = spec_zthreads(spec_mmax);
         std::vector<SpecFilm> sf((size_t)n);
-        std::vector<int> bxf, byf, bzf, bqf;
-        size_t smq = 0;
+        std::vector<int> bxf, byf, bzf, bqf, bcf;
+        size_t smq = 0, smc = 0;
+        int dev_o = 0, optin = 0;
+        CK(cudaGetDevice(&dev_o));
+        CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_o));
+        // the cluster transforms (CMSL_SPEC_CL=1, where every depolarised
+        // film takes them): a shorter solve at 64x64x16 and 128x128x16 (24.7
+        // against 32.7 us, 28.0 against 31.8) but no shorter a step there,
+        // and a longer solve at 256x256x32 (55.4 against 43.0 us, one block
+        // of 512 threads per SM on 120 SMs), so the row layout stays the
+        // default; the column layout by CMSL_SPEC_COLS=1 otherwise
+        const char *clv = getenv("CMSL_SPEC_CL");
+        bool cl_ok = clv && atoi(clv) != 0;
+        for (int fi = 0; fi < n; ++fi)
+            if (e->fh[fi].dep)
+                cl_ok = cl_ok && spec_cl_ok(spec_plan(e->fh[fi].nx), spec_plan(e->fh[fi].ny), e->fh[fi].nx,
+                                            e->fh[fi].ny, (size_t)optin);
+        e->spec_cl = cl_ok;
         long long ioff = 0;
         std::vector<float2> tw;
         std::vector<float> lam;
@@ -1315,6 +1342,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             SpecFilm &P = sf[fi];
             P.nx = h.nx; P.ny = h.ny; P.nz = h.nz; P.off = h.off;
             P.bx0 = (int)bxf.size(); P.by0 = (int)byf.size(); P.bz0 = (int)bzf.size(); P.bq0 = (int)bqf.size();
+            P.bc0 = (int)bcf.size();
             if (!h.dep) continue;                                    // no solve, no blocks
             P.M = h.nz - 2;
             P.Mp = (P.M + 1) / 2;
@@ -1332,11 +1360,16 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
             const long long gx = ((long long)P.Mp * h.ny + rbx - 1) / rbx;
             const long long gy = (long long)P.Mp * ((h.nx + cby - 1) / cby);
-            const long long gz = (spec_canon_count(h.nx, h.ny) + zt - 1) / zt;   // one thread per mode pair
+            // one thread per mode pair (column by column: the count with nx and ny swapped)
+            const long long gz = ((e->spec_cl ? spec_canon_count(h.ny, h.nx) : spec_canon_count(h.nx, h.ny)) + zt - 1) / zt;
             bxf.insert(bxf.end(), (size_t)gx, fi);
             byf.insert(byf.end(), (size_t)gy, fi);
             bzf.insert(bzf.end(), (size_t)gz, fi);
             bqf.insert(bqf.end(), (size_t)(h.nx / 2 + 1), fi);                  // mirror pairs of columns
+            if (e->spec_cl) {
+                bcf.insert(bcf.end(), (size_t)P.Mp * SPEC_CL, fi);               // a cluster per packed plane
+                smc = std::max(smc, spec_cl_bytes(h.nx, h.ny));
+            }
             smq = std::max(smq, spec_yzy_bytes(h.ny, P.Mp, P.M));
             smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * spec_x_pitch(h.nx, true)) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
@@ -1346,11 +1379,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         // 3-5 us less kernel time per solve, but no shorter a step: measured
         // equal at 256x256x32 and 1-2 us longer at 64x64x16 and 128x128x16)
         {
-            int dev = 0, optin = 0;
-            CK(cudaGetDevice(&dev));
-            CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
             const char *cl = getenv("CMSL_SPEC_COLS");
-            e->spec_col = smq <= (size_t)optin && cl && atoi(cl) != 0;
+            e->spec_col = e->spec_cl || (smq <= (size_t)optin && cl && atoi(cl) != 0);
         }
         // Thomas pivots of every film, mode and interior plane, in double:
         // dg = lam_x + lam_y + 2, inv_k = 1 / (dg - c'_{k-1}) with c'_k = -inv_k
@@ -1385,6 +1415,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         TRY(upload(byf.data(), sizeof(int) * byf.size(), &p)); sp.by_film = (const int *)p;
         TRY(upload(bzf.data(), sizeof(int) * bzf.size(), &p)); sp.bz_film = (const int *)p;
         TRY(upload(bqf.data(), sizeof(int) * bqf.size(), &p)); sp.bq_film = (const int *)p;
+        if (bcf.empty()) bcf.push_back(0);
+        TRY(upload(bcf.data(), sizeof(int) * bcf.size(), &p)); sp.bc_film = (const int *)p;
         TRY(upload(tw.data(), sizeof(float2) * tw.size(), &p)); sp.tw = (const float2 *)p;
         TRY(upload(lam.data(), sizeof(float) * lam.size(), &p)); sp.lam = (const float *)p;
         TRY(upload(piv.data(), sizeof(float) * piv.size(), &p)); sp.piv = (const float *)p;
@@ -1399,11 +1431,18 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         CK(cudaFuncSetAttribute(k_spec_x<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[0]));
         CK(cudaFuncSetAttribute(k_spec_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[1]));
-        CK(cudaFuncSetAttribute(k_spec_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[2]));
+        CK(cudaFuncSetAttribute(k_spec_z<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[2]));
+        CK(cudaFuncSetAttribute(k_spec_z<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->spec_smem[2]));
+        if (e->spec_cl) {
+            e->spec_grid[4] = (int)bcf.size();
+            e->spec_smem[4] = smc;
+            CK(cudaFuncSetAttribute(k_spec_cxy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+            CK(cudaFuncSetAttribute(k_spec_cyx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+        }
         {
             e->spec_grid[3] = (int)bqf.size();
             e->spec_smem[3] = smq;
-            if (e->spec_col) {
+            if (e->spec_col && !e->spec_cl) {
                 CK(cudaFuncSetAttribute(k_spec_x<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)e->spec_smem[0]));
                 CK(cudaFuncSetAttribute(k_spec_x<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -99,10 +99,11 @@ struct Engine {
     int refine_nt = 0, tdgl_nt = 0;     // threads per block
     bool spectral = false;      // FP32 inner solve by the direct spectral solve (one film, uniform eps)
     SpecDev spec{};
-    int spec_grid[4] = {0, 0, 0, 0};   // blocks of the x, y, z passes and of the column-pair pass
+    int spec_grid[5] = {0, 0, 0, 0, 0};   // blocks of the x, y, z passes, the column-pair pass, the cluster passes
     int spec_zt = 0;            // threads per block of the z solve
-    size_t spec_smem[4] = {0, 0, 0, 0};
+    size_t spec_smem[5] = {0, 0, 0, 0, 0};
     bool spec_col = false;      // column layout: x, fused y-z-y, x (three launches per solve)
+    bool spec_cl = false;       // column layout by cluster transforms: xy, z, yx (three launches per solve)
     bool persistent = false;
     // staging of the FP32 stencil passes: STG_CP the cp.async ring (any
     // film), STG_TMA tensor copies (every film's nx % 32 == 0, ny % 8 == 0).

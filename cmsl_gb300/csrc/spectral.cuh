@@ -35,6 +35,7 @@
 // (nx - kx, ny - ky), and the y transforms back, with contiguous column reads
 // and writes (k_spec_yzy).
 #pragma once
+#include <cooperative_groups.h>
 #include "kernels.cuh"
 
 namespace cmsl {
@@ -59,6 +60,7 @@ struct SpecFilm {
     float scale;                // h^2 / (eps nx ny)
     int bx0, by0, bz0;          // first block of the film in the x, y and z grids
     int bq0;                    // first block of the film in the column-pair grid (column layout)
+    int bc0;                    // first block of the film in the cluster grids (SPEC_CL blocks per packed plane)
     long long ioff;             // first pivot of the film in SpecDev::piv
 };
 
@@ -69,6 +71,7 @@ struct SpecDev {
     const float *lam;           // 2 - 2 cos(2 pi t / n) per film and axis
     const int *bx_film, *by_film, *bz_film;   // film of every block of the three grids
     const int *bq_film;         // film of every block of the column-pair grid (column layout)
+    const int *bc_film;         // film of every block of the cluster grids
     // Thomas pivots 1 / (dg - c'_{k-1}) of every interior plane k and mode,
     // [k][mode] per film (mode kx * ny + ky in the column layout, ky * nx + kx
     // in the row layout), computed on the host in double: the z solves run
@@ -504,6 +507,22 @@ __host__ __device__ inline long long spec_canon_count(int nx, int ny)
 {
     return (long long)((ny - 1) / 2) * nx + (long long)(nx / 2 + 1) * ((ny & 1) == 0 ? 2 : 1);
 }
+// The same set column by column (the column layout: consecutive threads take
+// consecutive y): columns x = 1 .. (nx-1)/2 in full, then column 0 and, for
+// even nx, column nx/2 with y = 0 .. ny/2.
+__device__ __forceinline__ bool spec_canon_mode_col(long long t, int nx, int ny, int &x, int &y)
+{
+    const long long full = (long long)((nx - 1) / 2) * ny;
+    if (t < full) {
+        x = 1 + (int)(t / ny);
+        y = (int)(t - (long long)(x - 1) * ny);
+        return true;
+    }
+    const int hy = ny / 2 + 1, t2 = (int)(t - full);
+    if (t2 < hy) { x = 0; y = t2; return true; }
+    if ((nx & 1) == 0 && t2 < 2 * hy) { x = nx / 2; y = t2 - hy; return true; }
+    return false;
+}
 
 // Thomas algorithm along z, one thread per canonical mode m (the mirror's
 // solution is the conjugate).  The thread's packed spectra at m and -m for
@@ -512,7 +531,9 @@ __host__ __device__ inline long long spec_canon_count(int nx, int ny)
 // the eliminated right-hand sides (d'_2j, d'_2j+1), and [M][blockDim] of
 // the mode's pivots (SpecDev::piv) staged with them.
 // Writes the conjugates of the packed scaled solutions, so that the next
-// forward transforms invert.
+// forward transforms invert.  COL: the spectra (and the pivots) in the column
+// layout [Mp][nx][ny] of the cluster transforms, modes taken column by column.
+template <bool COL = false>
 static __global__ void k_spec_z(Dev d, SpecDev sp)
 {
     extern __shared__ float2 sm2[];
@@ -522,10 +543,12 @@ static __global__ void k_spec_z(Dev d, SpecDev sp)
     const int M = P.M, Mp = P.Mp, T = blockDim.x, tx = threadIdx.x;
     float4 *dp = (float4 *)sm2;
     int x, y;
-    if (!spec_canon_mode((long long)(blockIdx.x - P.bz0) * T + tx, P.nx, P.ny, x, y)) return;
+    const long long t = (long long)(blockIdx.x - P.bz0) * T + tx;
+    if (!(COL ? spec_canon_mode_col(t, P.nx, P.ny, x, y) : spec_canon_mode(t, P.nx, P.ny, x, y))) return;
     const long long modes = (long long)P.nx * P.ny;
-    const long long m = (long long)y * P.nx + x;
-    const long long mm = (long long)(y == 0 ? 0 : P.ny - y) * P.nx + (x == 0 ? 0 : P.nx - x);
+    const int xm = x == 0 ? 0 : P.nx - x, ym = y == 0 ? 0 : P.ny - y;
+    const long long m = COL ? (long long)x * P.ny + y : (long long)y * P.nx + x;
+    const long long mm = COL ? (long long)xm * P.ny + ym : (long long)ym * P.nx + xm;
     float2 *Ca = sp.C + P.coff + m, *Cb = sp.C + P.coff + mm;
     float *pvs = (float *)(dp + (size_t)Mp * T) + tx;   // this thread's pivots, plane k at pvs[k * T]
     {
@@ -703,6 +726,136 @@ static __global__ void __launch_bounds__(SPEC_YZY_NT, 1) k_spec_yzy(Dev d, SpecD
         const float2 *res = fft_mixed<false>(R, R == A ? B : A, nseq, ay, 1, ny, tw);
         for (int t = threadIdx.x; t < nseq * ny; t += blockDim.x) gcol(t / ny)[t - (t / ny) * ny] = res[spec_pad(t)];
     }
+}
+
+// ------------------------------------------------- cluster transforms
+// The in-plane transforms of a packed plane in one thread-block cluster of
+// SPEC_CL blocks (films with power-of-two sides divisible by SPEC_CL whose
+// tiles fit one block's shared memory): block q of the cluster owns rows
+// y0 = q ny / SPEC_CL .. and columns x0 = q nx / SPEC_CL .. of the plane.
+// Forward (k_spec_cxy): x transforms of its rows into its tile T, a cluster
+// barrier, then y transforms of its columns whose first pass reads the other
+// blocks' tiles through distributed shared memory, written to the spectra
+// in the column layout [Mp][nx][ny].  Inverse (k_spec_cyx): y transforms of
+// its columns into T (column-major), a cluster barrier, x transforms of its
+// rows reading the tiles of the cluster, written to dx.  A solve is these
+// two launches around the column-layout z solve, with no pass over the
+// spectra between the x and the y transforms.  T's rows (columns) are
+// padded to an odd pitch in 8-byte words so that the strided reads of
+// another block's tile spread over the banks; a last cluster barrier keeps
+// every block resident until the others have read its tile.
+constexpr int SPEC_CL = 8;
+constexpr int SPEC_CL_NT = 512;
+
+__host__ __device__ inline int spec_cl_tile(int nx, int ny)     // float2 of T, A or B
+{
+    const int rows = ny / SPEC_CL, cols = nx / SPEC_CL;
+    const int t = rows * (nx + 1) > cols * (ny + 1) ? rows * (nx + 1) : cols * (ny + 1);
+    const int a = spec_pad(rows * nx) + 1;                      // = spec_pad(cols * ny) + 1
+    return t > a ? t : a;
+}
+__host__ __device__ inline size_t spec_cl_bytes(int nx, int ny)
+{
+    return sizeof(float2) * (3 * (size_t)spec_cl_tile(nx, ny) + nx + ny);
+}
+__host__ inline bool spec_cl_ok(const SpecAxis &ax, const SpecAxis &ay, int nx, int ny, size_t smem_max)
+{
+    return ax.lg >= 0 && ay.lg >= 0 && nx % SPEC_CL == 0 && ny % SPEC_CL == 0 && nx >= 32 && ny >= 32 &&
+           spec_cl_bytes(nx, ny) <= smem_max;
+}
+
+static __global__ void __cluster_dims__(SPEC_CL, 1, 1) __launch_bounds__(SPEC_CL_NT, 1)
+    k_spec_cxy(Dev d, Fields<float> F, SpecDev sp)
+{
+    namespace cgr = cooperative_groups;
+    extern __shared__ float2 sm2[];
+    const cgr::cluster_group cl = cgr::this_cluster();
+    const int f = __ldg(sp.bc_film + blockIdx.x);
+    if (!spec_run(d, f)) return;                     // the whole cluster: one film
+    const SpecFilm &P = sp.films[f];
+    const int nx = P.nx, ny = P.ny, M = P.M;
+    const int j = (blockIdx.x - P.bc0) / SPEC_CL, q = (int)cl.block_rank();
+    const int rows = ny / SPEC_CL, cols = nx / SPEC_CL, y0 = q * rows, x0 = q * cols;
+    const int tile = spec_cl_tile(nx, ny), pitch = nx + 1;
+    float2 *T = sm2, *A = T + tile, *B = A + tile, *twx = B + tile, *twy = twx + nx;
+    for (int t = threadIdx.x; t < nx; t += blockDim.x) twx[t] = __ldg(sp.tw + P.twx + t);
+    for (int t = threadIdx.x; t < ny; t += blockDim.x) twy[t] = __ldg(sp.tw + P.twy + t);
+    __syncthreads();
+    // x transforms of rows y0 + sq: interior z planes 2j+1 and 2j+2 of r as
+    // real and imaginary parts
+    const long long plane = (long long)nx * ny;
+    const float *rr = F.r + P.off;
+    auto ldr = [&](int sq, int e) -> float2 {
+        const long long o = (long long)(2 * j + 1) * plane + (long long)(y0 + sq) * nx + e;
+        return make_float2(rr[o], 2 * j + 1 < M ? rr[o + plane] : 0.f);
+    };
+    auto stT = [&](int sq, int e, float2 v) { T[sq * pitch + e] = v; };
+    fft_pow2<false>(A, B, rows, P.ax.lg, 1, nx, twx, ldr, stT);
+    cl.sync();
+    // y transforms of columns x0 + sq: element y sits in block y / rows, row y % rows
+    float2 *Cf = sp.C + P.coff;
+    auto ldT = [&](int sq, int e) -> float2 {
+        const int p = e / rows, r = e - p * rows;
+        return cl.map_shared_rank(T, p)[r * pitch + x0 + sq];
+    };
+    auto stC = [&](int sq, int e, float2 v) { Cf[((long long)j * nx + x0 + sq) * ny + e] = v; };
+    fft_pow2<false>(A, B, cols, P.ay.lg, 1, ny, twy, ldT, stC);
+    cl.sync();
+}
+
+static __global__ void __cluster_dims__(SPEC_CL, 1, 1) __launch_bounds__(SPEC_CL_NT, 1)
+    k_spec_cyx(Dev d, Fields<float> F, SpecDev sp)
+{
+    namespace cgr = cooperative_groups;
+    extern __shared__ float2 sm2[];
+    const cgr::cluster_group cl = cgr::this_cluster();
+    const int f = __ldg(sp.bc_film + blockIdx.x);
+    if (!spec_run(d, f)) {
+        spec_finish(d);
+        return;
+    }
+    const SpecFilm &P = sp.films[f];
+    const int nx = P.nx, ny = P.ny, M = P.M, Mp = P.Mp;
+    const int j = (blockIdx.x - P.bc0) / SPEC_CL, q = (int)cl.block_rank();
+    const int rows = ny / SPEC_CL, cols = nx / SPEC_CL, y0 = q * rows, x0 = q * cols;
+    const int tile = spec_cl_tile(nx, ny), pitch = ny + 1;
+    float2 *T = sm2, *A = T + tile, *B = A + tile, *twx = B + tile, *twy = twx + nx;
+    for (int t = threadIdx.x; t < nx; t += blockDim.x) twx[t] = __ldg(sp.tw + P.twx + t);
+    for (int t = threadIdx.x; t < ny; t += blockDim.x) twy[t] = __ldg(sp.tw + P.twy + t);
+    __syncthreads();
+    // y transforms of the conjugated solutions, columns x0 + sq, into T (column-major)
+    const float2 *Cf = sp.C + P.coff;
+    auto ldC = [&](int sq, int e) { return Cf[((long long)j * nx + x0 + sq) * ny + e]; };
+    auto stT = [&](int sq, int e, float2 v) { T[sq * pitch + e] = v; };
+    fft_pow2<false>(A, B, cols, P.ay.lg, 1, ny, twy, ldC, stT);
+    cl.sync();
+    // x transforms of rows y0 + sq (element x in block x / cols, column x % cols)
+    // into the correction: the transform of conj(W) is conj(x_2j + i x_2j+1),
+    // combined with the previous increment as k_spec_x
+    float *xx = F.x + P.off;
+    const long long plane = (long long)nx * ny;
+    const SolveDev *Sf = d.solve + f;
+    const float cw = d.force || Sf->cheb_w == 0.f ? 1.f : Sf->cheb_w;
+    const float cm = d.force ? 0.f : Sf->cheb_m;
+    auto ldT = [&](int sq, int e) -> float2 {
+        const int p = e / cols, c = e - p * cols;
+        return cl.map_shared_rank(T, p)[c * pitch + y0 + sq];
+    };
+    auto st = [&](int sq, int e, float2 v) {
+        const long long yx = (long long)(y0 + sq) * nx + e, o = (long long)(2 * j + 1) * plane + yx;
+        if (cm != 0.f) {
+            xx[o] = cw * v.x + cm * xx[o];
+            if (2 * j + 1 < M) xx[o + plane] = cw * -v.y + cm * xx[o + plane];
+        } else {
+            xx[o] = cw * v.x;
+            if (2 * j + 1 < M) xx[o + plane] = cw * -v.y;
+        }
+        if (j == 0) xx[yx] = 0.f;                                        // first Dirichlet plane
+        if (j == Mp - 1) xx[(long long)(M + 1) * plane + yx] = 0.f;      // last one
+    };
+    fft_pow2<false>(A, B, rows, P.ax.lg, 1, nx, twx, ldT, st);
+    cl.sync();
+    spec_finish(d);
 }
 
 }  // namespace cmsl

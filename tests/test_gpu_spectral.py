@@ -33,12 +33,17 @@ def _uniform(shape, seed, eps=30.0):
     return f, P
 
 
-@pytest.mark.parametrize("layout", ["columns", "rows"])
-@pytest.mark.parametrize("shape", [(32, 24, 8), (48, 36, 10), (64, 16, 5), (96, 12, 7), (8, 9, 3), (27, 32, 12)])
+@pytest.mark.parametrize("layout", ["columns", "rows", "clusters"])
+@pytest.mark.parametrize("shape", [(32, 24, 8), (48, 36, 10), (64, 16, 5), (96, 12, 7), (8, 9, 3), (27, 32, 12),
+                                   (64, 64, 10), (128, 32, 9), (32, 256, 6), (256, 64, 7)])
 def test_direct_solve_run_vs_oracle(gpu, shape, layout, monkeypatch):
-    """Both layouts of the spectra: rows (five passes, the default) and
-    columns (x transforms, one block per mirror pair of columns for y, z and
-    y, x transforms; CMSL_SPEC_COLS=1)."""
+    """The three forms of the solve: rows (five passes), columns (x
+    transforms, one block per mirror pair of columns for y, z and y, x
+    transforms; CMSL_SPEC_COLS=1) and clusters (the x and y transforms of a
+    packed plane in one block cluster, the z solve column by column;
+    CMSL_SPEC_CL=1 where every side is a power of two, a multiple of 8 and at
+    least 32 -- other films take the rows here)."""
+    monkeypatch.setenv("CMSL_SPEC_CL", "1" if layout == "clusters" else "0")
     monkeypatch.setenv("CMSL_SPEC_COLS", "1" if layout == "columns" else "0")
     f, P = _uniform(shape, seed=sum(shape))
     n = 16
