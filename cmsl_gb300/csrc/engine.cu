@@ -1357,7 +1357,21 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             P.scale = (float)(h.h * h.h / (eps * (double)h.nx * h.ny));
             tables(h.nx, &P.twx, &P.lamx);
             tables(h.ny, &P.twy, &P.lamy);
-            const int rbx = std::max(1, SPEC_ELEMS / h.nx), cby = std::max(1, SPEC_ELEMS / h.ny);
+            // rows (columns) per transform block: about two blocks per SM for
+            // the film's Mp ny rows (Mp nx columns), a power of two, at most
+            // SPEC_ELEMS values (8 rows of 256 at 256x256x32, 8 of 512 at
+            // 512x512x64, 1 of 64 at 64x64x16); CMSL_SPEC_RB fixes it
+            const char *rbe = getenv("CMSL_SPEC_RB");
+            auto per_block = [&](long long lines, int len) {
+                const int cap = std::max(1, SPEC_ELEMS / len);
+                int r = 1;
+                while (2LL * r * 2 * 152 <= lines && 2 * r <= cap) r *= 2;
+                if (rbe && atoi(rbe) > 0) r = std::min(cap, atoi(rbe));
+                return r;
+            };
+            const int rbx = per_block((long long)P.Mp * h.ny, h.nx), cby = per_block((long long)P.Mp * h.nx, h.ny);
+            P.rb = rbx;
+            P.cb = cby;
             const long long gx = ((long long)P.Mp * h.ny + rbx - 1) / rbx;
             const long long gy = (long long)P.Mp * ((h.nx + cby - 1) / cby);
             // one thread per mode pair (column by column: the count with nx and ny swapped)

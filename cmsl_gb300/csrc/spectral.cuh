@@ -41,7 +41,7 @@
 namespace cmsl {
 
 constexpr int SPEC_MAX_STAGES = 13;       // 2^12 = 4096
-constexpr int SPEC_ELEMS = 2048;          // complex values staged per block (6 blocks per SM)
+constexpr int SPEC_ELEMS = 4096;          // complex values staged per block at most
 constexpr int SPEC_NT = 256;
 
 struct SpecAxis {
@@ -61,6 +61,7 @@ struct SpecFilm {
     int bx0, by0, bz0;          // first block of the film in the x, y and z grids
     int bq0;                    // first block of the film in the column-pair grid (column layout)
     int bc0;                    // first block of the film in the cluster grids (SPEC_CL blocks per packed plane)
+    int rb, cb;                 // rows of an x-transform block, columns of a y-transform block
     long long ioff;             // first pivot of the film in SpecDev::piv
 };
 
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_x(Dev d, Fields<float> F, S
         return;
     }
     const SpecFilm &P = sp.films[f];
-    const int nx = P.nx, ny = P.ny, rows = P.Mp * ny, rb = max(1, SPEC_ELEMS / nx);
+    const int nx = P.nx, ny = P.ny, rows = P.Mp * ny, rb = P.rb;
     const int r0 = (blockIdx.x - P.bx0) * rb, nr = min(rb, rows - r0);
     const long long plane = (long long)nx * ny;
     const float *rr = F.r + P.off;
@@ -464,7 +465,7 @@ static __global__ void __launch_bounds__(SPEC_NT, 4) k_spec_y(Dev d, SpecDev sp)
     const int f = __ldg(sp.by_film + blockIdx.x);
     if (!spec_run(d, f)) return;
     const SpecFilm &P = sp.films[f];
-    const int nx = P.nx, ny = P.ny, cb = max(1, SPEC_ELEMS / ny);
+    const int nx = P.nx, ny = P.ny, cb = P.cb;
     const int groups = (nx + cb - 1) / cb;
     const int lb = blockIdx.x - P.by0;
     const int kk = lb / groups, x0 = (lb - kk * groups) * cb, nc = min(cb, nx - x0);
