@@ -178,3 +178,38 @@ def test_batch_with_deferred_and_ordinary_films(gpu, monkeypatch):
             _, rf = b.iters(i)
             assert _close(Pg, alone[i][0], 1e-6)
             assert (rf == alone[i][1]).all()
+
+
+def test_batch_where_some_checks_fail(gpu, monkeypatch):
+    """Two one-permittivity films in a batch, one with refine_tol 1e-11 (every
+    deferred check fails and reopens the step) and one with 1e-8 (its checks
+    pass; it stays pending through the reopened step and is checked again
+    when the step repeats): each film as it runs alone."""
+    fa, Pa = _film((48, 24, 9), seed=31)
+    fb, Pb = _film((64, 32, 7), seed=32)
+    n = 10
+    Ez = np.linspace(0.0, 0.3, n)
+    rows = np.arange(n, dtype=np.int32)
+    monkeypatch.setenv("CMSL_DEFER", "1")
+    base = dict(precision=gpu.FP32_REFINED, inner_tol=1e-5)
+    tols = (1e-11, 1e-8)
+    alone = []
+    for (f, P), tol in zip(((fa, Pa), (fb, Pb)), tols):
+        with gpu.Film.from_oracle_film(f, refine_tol=tol, **base) as g:
+            g.set_state(P)
+            g.run(Ez, rows)
+            alone.append((g.get_state(), g.iters()[1], g.rows()))
+    from cmsl_gb300.film import _oracle_kw
+    with gpu.Batch([{**_oracle_kw(f), **base, "refine_tol": tol} for f, tol in zip((fa, fb), tols)]) as b:
+        b.set_state(0, Pa)
+        b.set_state(1, Pb)
+        b.run(np.stack([Ez, Ez]), np.stack([rows, rows]))
+        for i in range(2):
+            (Pg, phig) = b.get_state(i)
+            _, rf = b.iters(i)
+            (Pw, phiw), rfw, rw = alone[i]
+            assert _close(Pg, Pw, 1e-6)
+            assert np.abs(phig - phiw).max() <= 1e-6 * np.abs(phiw).max()
+            assert (rf == rfw).all()
+            assert np.abs(b.rows(i)[:, :10] - rw[:, :10]).max() <= 1e-6
+        assert (b.iters(0)[1] >= 3).all() and (b.iters(1)[1] == 2).all()
