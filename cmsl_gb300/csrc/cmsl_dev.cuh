@@ -171,6 +171,7 @@ struct Dev {
     double *phi[5];
     double *partial;            // [n_items * NPART]
     unsigned int *counter;      // one ticket counter (reset by the last block)
+    unsigned int *fcount;       // [n_films] per-film ticket counters of the FP32 stencil passes (batches)
     SolveDev *solve;            // [n_films]
     Ctl *ctl;
     const double *wave;         // [n_films * wstride] applied field per run step

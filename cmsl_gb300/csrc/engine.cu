@@ -1240,6 +1240,7 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
     TRY(e->alloc((void **)&e->d_items, sizeof(int4) * e->items_cap));
     TRY(e->alloc((void **)&e->d_sitems, sizeof(int4) * e->sitems_cap));
     TRY(e->alloc((void **)&e->d_partial, sizeof(double) * NPART * std::max(e->items_cap, e->sitems_cap)));
+    TRY(e->alloc((void **)&e->d_fcount, sizeof(unsigned int) * n));
     {
         // tile height of the FP32 stencil passes: CMSL_TILE_Y (4, 8 or 16)
         // fixes it; else a tuned handle of the same shape class, else TY
@@ -1498,16 +1499,34 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         const char *nt = getenv("CMSL_NO_TMA");
         e->tma = !(nt && atoi(nt) != 0);
         for (int fi = 0; fi < n; ++fi) e->tma = e->tma && e->fh[fi].nx % TX == 0 && e->fh[fi].ny % TY == 0;
-        // the cp.async ring at every tile height, the tensor copies at TY rows
-        e->refine_cp[0] = uni ? (void *)k_refine32<true, R32_NS, 4> : (void *)k_refine32<false, R32_NS, 4>;
-        e->refine_cp[1] = uni ? (void *)k_refine32<true, R32_NS, 8> : (void *)k_refine32<false, R32_NS, 8>;
-        e->refine_cp[2] = uni ? (void *)k_refine32<true, R32_NS, 16> : (void *)k_refine32<false, R32_NS, 16>;
+        // the cp.async ring at every tile height, the tensor copies at TY
+        // rows; batches take the kernels that finish each film in its own
+        // last block
+        const bool fb = n > 1;
+        if (fb) {
+            e->refine_cp[0] = uni ? (void *)k_refine32<true, R32_NS, 4, true> : (void *)k_refine32<false, R32_NS, 4, true>;
+            e->refine_cp[1] = uni ? (void *)k_refine32<true, R32_NS, 8, true> : (void *)k_refine32<false, R32_NS, 8, true>;
+            e->refine_cp[2] = uni ? (void *)k_refine32<true, R32_NS, 16, true> : (void *)k_refine32<false, R32_NS, 16, true>;
+            e->tdgl_cp[0] = (void *)k_tdgl32<T32_NS, 4, false, true>;
+            e->tdgl_cp[1] = (void *)k_tdgl32<T32_NS, 8, false, true>;
+            e->tdgl_cp[2] = (void *)k_tdgl32<T32_NS, 16, false, true>;
+            e->tdgl_def[0] = (void *)k_tdgl32<T32_NS, 4, true, true>;
+            e->tdgl_def[1] = (void *)k_tdgl32<T32_NS, 8, true, true>;
+            e->tdgl_def[2] = (void *)k_tdgl32<T32_NS, 16, true, true>;
+        } else {
+            e->refine_cp[0] = uni ? (void *)k_refine32<true, R32_NS, 4> : (void *)k_refine32<false, R32_NS, 4>;
+            e->refine_cp[1] = uni ? (void *)k_refine32<true, R32_NS, 8> : (void *)k_refine32<false, R32_NS, 8>;
+            e->refine_cp[2] = uni ? (void *)k_refine32<true, R32_NS, 16> : (void *)k_refine32<false, R32_NS, 16>;
+            e->tdgl_cp[0] = (void *)k_tdgl32<T32_NS, 4>;
+            e->tdgl_cp[1] = (void *)k_tdgl32<T32_NS, 8>;
+            e->tdgl_cp[2] = (void *)k_tdgl32<T32_NS, 16>;
+            e->tdgl_def[0] = (void *)k_tdgl32<T32_NS, 4, true>;
+            e->tdgl_def[1] = (void *)k_tdgl32<T32_NS, 8, true>;
+            e->tdgl_def[2] = (void *)k_tdgl32<T32_NS, 16, true>;
+        }
         e->refine_cp_smem[0] = uni ? r32_smem<true, 4>() : r32_smem<false, 4>();
         e->refine_cp_smem[1] = uni ? r32_smem<true, 8>() : r32_smem<false, 8>();
         e->refine_cp_smem[2] = uni ? r32_smem<true, 16>() : r32_smem<false, 16>();
-        e->tdgl_cp[0] = (void *)k_tdgl32<T32_NS, 4>;
-        e->tdgl_cp[1] = (void *)k_tdgl32<T32_NS, 8>;
-        e->tdgl_cp[2] = (void *)k_tdgl32<T32_NS, 16>;
         e->tdgl_cp_smem[0] = t32_smem<4>();
         e->tdgl_cp_smem[1] = t32_smem<8>();
         e->tdgl_cp_smem[2] = t32_smem<16>();
@@ -1517,9 +1536,6 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         bool any_def = false;
         for (int fi = 0; fi < n; ++fi) any_def |= fds[fi].defer_ok != 0;
         e->defer = e->defer && any_def;
-        e->tdgl_def[0] = (void *)k_tdgl32<T32_NS, 4, true>;
-        e->tdgl_def[1] = (void *)k_tdgl32<T32_NS, 8, true>;
-        e->tdgl_def[2] = (void *)k_tdgl32<T32_NS, 16, true>;
         e->tdgl_def_smem[0] = t32_smem<4, true>();
         e->tdgl_def_smem[1] = t32_smem<8, true>();
         e->tdgl_def_smem[2] = t32_smem<16, true>();
@@ -1533,9 +1549,10 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         }
         if (e->tma) {
             TRY(make_maps(e));
-            e->refine_tma = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
+            if (fb) e->refine_tma = uni ? (void *)k_refine32t<true, RT_NS, true> : (void *)k_refine32t<false, RT_NS, true>;
+            else e->refine_tma = uni ? (void *)k_refine32t<true, RT_NS> : (void *)k_refine32t<false, RT_NS>;
             e->refine_tma_smem = uni ? rt_smem<true>() : rt_smem<false>();
-            e->tdgl_tma = (void *)k_tdgl32t<TT_NS>;
+            e->tdgl_tma = fb ? (void *)k_tdgl32t<TT_NS, true> : (void *)k_tdgl32t<TT_NS>;
             e->tdgl_tma_smem = TT_SMEM;
             CK(cudaFuncSetAttribute(e->refine_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)e->refine_tma_smem));

@@ -69,6 +69,7 @@ struct Engine {
     void *d_TR = nullptr;
     double *d_phi[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     double *d_partial = nullptr;
+    unsigned int *d_fcount = nullptr;   // per-film ticket counters (batches)
     unsigned int *d_counter = nullptr;
     SolveDev *d_solve = nullptr;
     Ctl *d_ctl = nullptr;
@@ -184,6 +185,7 @@ struct Engine {
         d.code = d_code; d.ncells = ncells;
         for (int q = 0; q < 5; ++q) d.phi[q] = d_phi[q];
         d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
+        d.fcount = d_fcount;
         d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
         d.iters_log = d_iters; d.refine_log = d_refine;
         d.wstride = wstride; d.rstride = rstride;

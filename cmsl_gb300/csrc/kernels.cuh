@@ -183,6 +183,49 @@ __device__ __forceinline__ bool ticket_last(unsigned int *counter)
     return s_last;
 }
 
+// Batches: true in every thread of the last block of film fi's stencil items
+// to arrive.  That block forms the film's totals
+// while the other films' blocks still run, instead of the grid's last block
+// forming every film's one after another.
+__device__ __forceinline__ bool film_ticket_last(const Dev &d, int fi)
+{
+    __shared__ bool s_flast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const FilmDev *f = d.films + fi;
+        const unsigned int n = (unsigned int)(f->sitem_end - f->sitem_begin);
+        const unsigned int t = atomicAdd(d.fcount + fi, 1u);
+        s_flast = t + 1u == n;
+        if (s_flast) d.fcount[fi] = 0u;          // every block of the film has arrived
+    }
+    __syncthreads();
+    if (s_flast) __threadfence();
+    return s_flast;
+}
+
+// The end of an FP32 stencil pass has a film part (film fi's totals and
+// state, every thread of one block) and a grid part (what depends on every
+// film).  FB false: the grid's last block runs every film's part and the grid
+// part.  FB true (kernels built for batches): each film's last block runs its
+// film part while other films' blocks still run, and the grid's last block
+// the grid part.  A compile-time choice: the single-film kernels keep their
+// register allocation.
+template <bool FB, class FilmFn, class GridFn>
+__device__ __forceinline__ void finish32(const Dev &d, FilmFn film, GridFn grid)
+{
+    if constexpr (FB) {
+        const int mine = d.sitems[blockIdx.x].x;
+        for (int fi = 0; fi < d.n_films; ++fi)      // the loop form keeps the stencil loop's registers
+            if (fi == mine && film_ticket_last(d, fi)) film(fi);
+        if (!ticket_last(d.counter)) return;
+    } else {
+        if (!ticket_last(d.counter)) return;
+        for (int fi = 0; fi < d.n_films; ++fi) film(fi);
+    }
+    grid();
+}
+
 // In the last block: sums the NV partials of film f's items (item order,
 // thread-strided then block tree).  Result valid in thread 0.
 template <int NV>
@@ -613,6 +656,26 @@ __device__ __forceinline__ void step_reopen(const Dev &d)
     d.ctl->redo = 1;
 }
 
+// The FP32 TDGL step's end (finish32): film fi's sweep row and the reset of
+// its solver state; then the step's conditions.  Under kernel timing
+// (d.force) the totals are formed as a step forms them and nothing is written.
+__device__ __forceinline__ void tdgl_film32(const Dev &d, int rs, int fi, double (*sRed)[7], double (&sTot)[7])
+{
+    const int frow = d.rows[(long long)fi * d.wstride + rs];
+    if (frow >= 0) {
+        film_total32<7>(d, d.films + fi, sRed, sTot);
+        if (threadIdx.x == 0 && !d.force) row_write(d, fi, frow, sTot);
+    }
+    if (threadIdx.x == 0 && !d.force) step_reset(d, fi);
+}
+__device__ __forceinline__ void tdgl_grid32(const Dev &d, int rs)
+{
+    if (threadIdx.x == 0) {
+        if (!d.force) step_begin(d, rs);
+        *d.counter = 0u;
+    }
+}
+
 // Under kernel timing (d.force) the totals are formed as a step forms them
 // and nothing is written.
 template <bool DF>
@@ -805,16 +868,14 @@ __device__ __forceinline__ void step_end(const Dev &d)
 // reduced r.r, b.b and r.D^-1.r, applies the refinement stop test
 // ||r|| <= refine_tol ||b||, rotates the buffers and sets the next inner
 // solve's target.
-__device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], double (&sTot)[3])
+// Film fi's part (finish32): its totals, the stop test and its next pass.
+__device__ __forceinline__ void refine_film(const Dev &d, int fi, double (*sRed)[3], double (&sTot)[3])
 {
     if (d.force) {              // kernel timing: the totals as a pass forms them; the state stays as it is
-        for (int fi = 0; fi < d.n_films; ++fi)
-            if (d.films[fi].dep_flag) film_total32<3>(d, d.films + fi, sRed, sTot);
-        if (threadIdx.x == 0) *d.counter = 0u;
+        if (d.films[fi].dep_flag) film_total32<3>(d, d.films + fi, sRed, sTot);
         return;
     }
-    int any_outer = 0, any_inner = 0;
-    for (int fi = 0; fi < d.n_films; ++fi) {
+    {
         const FilmDev *ff = d.films + fi;
         SolveDev *S = d.solve + fi;
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
@@ -888,10 +949,25 @@ __device__ __forceinline__ void refine_finish(const Dev &d, double (*sRed)[3], d
                     S->outer_active = 0;
                 }
             }
-            any_outer |= S->outer_active;
-            any_inner |= S->active;
         }
     }
+}
+
+// What depends on every film (finish32): the loop conditions, and the end of
+// the step when no film continues (d.step_end).
+__device__ __forceinline__ void refine_grid(const Dev &d)
+{
+    if (d.force) {
+        if (threadIdx.x == 0) *d.counter = 0u;
+        return;
+    }
+    // other blocks updated the films' slots (volatile: not from this block's L1)
+    int any_outer = 0, any_inner = 0;
+    if (threadIdx.x == 0)
+        for (int fi = 0; fi < d.n_films; ++fi) {
+            any_outer |= *(volatile const int *)&d.solve[fi].outer_active;
+            any_inner |= *(volatile const int *)&d.solve[fi].active;
+        }
     __shared__ int s_any;
     if (threadIdx.x == 0) {
         set_cond(d, d.h_outer, any_outer);

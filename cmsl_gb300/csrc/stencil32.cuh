@@ -240,7 +240,8 @@ template <int TYc, bool DEF = false> constexpr size_t t32_smem()
 }
 
 template <int NV>
-__device__ __forceinline__ void tdgl_finish_def(const Dev &d, int rs, double (*sRed)[NV], double (&sTot)[NV]);
+__device__ __forceinline__ void tdgl_def_film(const Dev &d, int rs, int fi, double (*sRed)[NV], double (&sTot)[NV]);
+__device__ __forceinline__ void tdgl_def_grid(const Dev &d, int rs);
 
 // TYc: the tile height (TX x TYc threads, one column each).
 // DEF: a film whose previous step ended on its direct solve (SolveDev::pending;
@@ -260,7 +261,7 @@ template <int TYc, bool DEF> constexpr int tdgl32_minb()
     return DEF && TYc < 16 ? TileShape<TYc>::MINB * 3 / 4 : TileShape<TYc>::MINB;
 }
 
-template <int NS, int TYc = TY, bool DEF = false>
+template <int NS, int TYc = TY, bool DEF = false, bool FB = false>
 __global__ void __launch_bounds__(TileShape<TYc>::NTt, tdgl32_minb<TYc, DEF>()) k_tdgl32(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
@@ -415,53 +416,62 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, tdgl32_minb<TYc, DEF>()) 
     cp_wait<0>();
 
     if (row >= 0 || pend) block_partial32<NV>(d, acc, sRed);
-    if (!ticket_last(d.counter)) return;
-    if constexpr (DEF) tdgl_finish_def<NV>(d, rs, sRed, sTot);
-    else tdgl_finish<true>(d, rs, sRed, sTot);
+    if constexpr (DEF)
+        finish32<FB>(d, [&](int fi) { tdgl_def_film<NV>(d, rs, fi, sRed, sTot); }, [&] { tdgl_def_grid(d, rs); });
+    else
+        finish32<FB>(d, [&](int fi) { tdgl_film32(d, rs, fi, sRed, sTot); }, [&] { tdgl_grid32(d, rs); });
 }
 
-// Last block of a TDGL step that may carry deferred checks: every pending
-// film's r.r of its check decides whether its previous step stands (the
-// update pass's test, ||r|| <= refine_tol ||b||).  If every check passes,
-// the checked potentials become current and the step begins as
-// tdgl_finish<true> begins it.  If one fails, the previous step is reopened:
-// the step counters and the P sets roll back, the failed films are set up
-// for the update pass that the step's next residual pass then is, the films
+// The end of a TDGL step that may carry deferred checks (finish32): every
+// pending film's r.r of its check decides whether its previous step stands
+// (the update pass's test, ||r|| <= refine_tol ||b||).  If every check
+// passes, the checked potentials become current and the step begins as
+// tdgl_grid32 begins it.  If one fails, the previous step is reopened: the
+// step counters and the P sets roll back, the failed films are set up for
+// the update pass that the step's next residual pass then is, the films
 // whose checks passed stay pending (the repeated step checks them again, to
 // the same result), and the step loop runs this step again after that pass
 // has ended the previous one.
+// Film fi's part: its sweep row and its check's r.r (S->rr64).
 template <int NV>
-__device__ __forceinline__ void tdgl_finish_def(const Dev &d, int rs, double (*sRed)[NV], double (&sTot)[NV])
+__device__ __forceinline__ void tdgl_def_film(const Dev &d, int rs, int fi, double (*sRed)[NV], double (&sTot)[NV])
 {
     static_assert(NV == 8, "seven row sums and the check's r.r");
+    const FilmDev *ff = d.films + fi;
+    SolveDev *S = d.solve + fi;
+    const int frow = d.rows[(long long)fi * d.wstride + rs];
     if (d.force) {              // kernel timing: the totals as a step forms them; the state stays as it is
-        for (int fi = 0; fi < d.n_films; ++fi)
-            if (d.films[fi].dep_flag || d.rows[(long long)fi * d.wstride + rs] >= 0)
-                film_total32<NV>(d, d.films + fi, sRed, sTot);
-        if (threadIdx.x == 0) *d.counter = 0u;
+        if (ff->dep_flag || frow >= 0) film_total32<NV>(d, ff, sRed, sTot);
         return;
     }
-    __shared__ int s_fail;
-    if (threadIdx.x == 0) s_fail = 0;
-    for (int fi = 0; fi < d.n_films; ++fi) {
-        const FilmDev *ff = d.films + fi;
-        SolveDev *S = d.solve + fi;
-        const int frow = d.rows[(long long)fi * d.wstride + rs];
-        const bool pend = ff->dep_flag != 0 && uniform_flag(&S->pending);
-        if (frow < 0 && !pend) continue;
-        film_total32<NV>(d, ff, sRed, sTot);
-        if (threadIdx.x == 0) {
-            if (frow >= 0) row_write(d, fi, frow, sTot);
-            if (pend) {
-                const double rr = sTot[NV - 1];
-                S->rr64 = rr;
-                if (!(rr <= ff->refine_tol2 * S->bb || rr == 0.0)) s_fail = 1;   // NaN fails too
-            }
-        }
+    const bool pend = ff->dep_flag != 0 && uniform_flag(&S->pending);
+    if (frow < 0 && !pend) return;
+    film_total32<NV>(d, ff, sRed, sTot);
+    if (threadIdx.x == 0) {
+        if (frow >= 0) row_write(d, fi, frow, sTot);
+        if (pend) S->rr64 = sTot[NV - 1];
     }
-    __syncthreads();
+}
+
+// A pending film's check passed (NaN fails); rr read past this block's L1.
+__device__ __forceinline__ bool def_check_ok(const Dev &d, int fi)
+{
+    const double rr = *(volatile const double *)&d.solve[fi].rr64;
+    return rr <= d.films[fi].refine_tol2 * d.solve[fi].bb || rr == 0.0;
+}
+
+// What depends on every film: resolve and begin, or reopen.
+__device__ __forceinline__ void tdgl_def_grid(const Dev &d, int rs)
+{
     if (threadIdx.x != 0) return;
-    if (!s_fail) {
+    if (d.force) {
+        *d.counter = 0u;
+        return;
+    }
+    bool fail = false;
+    for (int fi = 0; fi < d.n_films; ++fi)
+        if (d.films[fi].dep_flag && d.solve[fi].pending && !def_check_ok(d, fi)) fail = true;
+    if (!fail) {
         for (int fi = 0; fi < d.n_films; ++fi) {
             SolveDev *S = d.solve + fi;
             if (S->pending) {
@@ -478,9 +488,8 @@ __device__ __forceinline__ void tdgl_finish_def(const Dev &d, int rs, double (*s
         step_begin(d, rs);
     } else {
         for (int fi = 0; fi < d.n_films; ++fi) {
-            const FilmDev *ff = d.films + fi;
             SolveDev *S = d.solve + fi;
-            if (S->pending && !(S->rr64 <= ff->refine_tol2 * S->bb || S->rr64 == 0.0)) {
+            if (S->pending && !def_check_ok(d, fi)) {
                 S->pending = 0;
                 S->outer_active = 1;
                 S->active = 0;
@@ -630,7 +639,7 @@ template <bool UNI, int TYc = TY> constexpr size_t r32_smem()
     return sizeof(float) * R32_NS * R32Lay<UNI, TYc>::STAGE;
 }
 
-template <bool UNI, int NS, int TYc = TY>
+template <bool UNI, int NS, int TYc = TY, bool FB = false>
 __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_refine32(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
@@ -753,8 +762,7 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_r
     }
     cp_wait<0>();
     refine_partials(d, acc, sRed);
-    if (!ticket_last(d.counter)) return;
-    refine_finish(d, sRed, sTot);
+    finish32<FB>(d, [&](int fi) { refine_film(d, fi, sRed, sTot); }, [&] { refine_grid(d); });
 }
 
 }  // namespace cmsl

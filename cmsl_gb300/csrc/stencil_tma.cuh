@@ -144,7 +144,7 @@ constexpr int TT_PHI = 3 * REG2, TT_CODE = 4 * REG2, TT_STAGE = 4 * REG2 + BODY1
 constexpr size_t TT_SMEM = (size_t)TT_NS * TT_STAGE + 128;
 constexpr int TT_OPS = 3 * 5 + 5 + 1;
 
-template <int NS>
+template <int NS, bool FB = false>
 __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
@@ -256,8 +256,7 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
     }
 
     if (row >= 0) block_partial32<7>(d, acc, sRed);
-    if (!ticket_last(d.counter)) return;
-    tdgl_finish<true>(d, rs, sRed, sTot);
+    finish32<FB>(d, [&](int fi) { tdgl_film32(d, rs, fi, sRed, sTot); }, [&] { tdgl_grid32(d, rs); });
 }
 
 // ------------------------------------------------- double-float residual
@@ -274,7 +273,7 @@ template <bool UNI> __host__ __device__ constexpr int rt_stage() { return UNI ? 
 template <bool UNI> constexpr size_t rt_smem() { return (size_t)RT_NS * rt_stage<UNI>() + 128; }
 constexpr int RT_OPS = 5 + 5 + 5 + 1 + 5 + 1;
 
-template <bool UNI, int NS>
+template <bool UNI, int NS, bool FB = false>
 __global__ void __launch_bounds__(NT, 4) k_refine32t(Dev d, Fields<float> F)
 {
     static_assert(NS >= 4, "the ring holds planes k-1, k, k+1 and at least one in flight");
@@ -386,8 +385,7 @@ __global__ void __launch_bounds__(NT, 4) k_refine32t(Dev d, Fields<float> F)
         if (apply) nh[o] = make_float2(c.xc.h, c.xc.l);
     }
     refine_partials(d, acc, sRed);
-    if (!ticket_last(d.counter)) return;
-    refine_finish(d, sRed, sTot);
+    finish32<FB>(d, [&](int fi) { refine_film(d, fi, sRed, sTot); }, [&] { refine_grid(d); });
 }
 
 
