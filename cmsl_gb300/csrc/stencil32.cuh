@@ -252,7 +252,7 @@ __device__ __forceinline__ void tdgl_def_grid(const Dev &d, int rs);
 // potential's buffer (a warm start of at most quadratic order never reads
 // it), and forms the check the update pass would have formed: r <- r - A dx
 // in FP32 (r.r in the eighth partial sum).  The last block decides whether
-// the previous step stands (tdgl_finish_def).
+// the previous step stands (tdgl_def_film, tdgl_def_grid).
 // The check's values raise the registers a thread needs: the DEF kernels are
 // built for three quarters of the blocks per SM (80 registers at 32 x 8
 // tiles, where the 64 of four blocks spilled and ran 15 % slower).
