@@ -107,13 +107,19 @@ int film_zchunk(const Engine *e, int fi, int zc)
     return zc > 0 ? std::min(zc, nz) : pick_zchunk(e->xy_tiles, nz);
 }
 
+// A column of nz planes in chunks of at most c planes: ceil(nz / c) chunks
+// whose sizes differ by one at most (chunk i starts at i * nz / nchunks), so
+// that no short last chunk leaves blocks of the last wave idle.
+int z_chunks(int nz, int c) { return (nz + c - 1) / c; }
+int z_chunk_start(int nz, int nchunks, int i) { return (int)((long long)i * nz / nchunks); }
+
 size_t count_items(const Engine *e, int zc, int ty = TY)
 {
     size_t n = 0;
     for (int fi = 0; fi < e->n_films; ++fi) {
         const FilmHost &h = e->fh[fi];
         const int c = film_zchunk(e, fi, zc);
-        n += (size_t)((h.nx + TX - 1) / TX) * ((h.ny + ty - 1) / ty) * ((h.nz + c - 1) / c);
+        n += (size_t)((h.nx + TX - 1) / TX) * ((h.ny + ty - 1) / ty) * z_chunks(h.nz, c);
     }
     return n;
 }
@@ -132,13 +138,14 @@ cmsl_status set_items(Engine *e, int zc)
         v.clear();
         for (int fi = 0; fi < e->n_films; ++fi) {
             const FilmHost &h = e->fh[fi];
-            const int c = film_zchunk(e, fi, zc);
+            const int nc = z_chunks(h.nz, film_zchunk(e, fi, zc));
             FilmDev &fd = e->fdh[fi];
             (list ? fd.sitem_begin : fd.item_begin) = (int)v.size();
             for (int y0 = 0; y0 < h.ny; y0 += ty)
                 for (int x0 = 0; x0 < h.nx; x0 += TX)
-                    for (int z0 = 0; z0 < h.nz; z0 += c)
-                        v.push_back(make_int4(fi, x0, y0, z0 | (std::min(h.nz, z0 + c) << 16)));
+                    for (int i = 0; i < nc; ++i)
+                        v.push_back(make_int4(fi, x0, y0, z_chunk_start(h.nz, nc, i) |
+                                                              (z_chunk_start(h.nz, nc, i + 1) << 16)));
             (list ? fd.sitem_end : fd.item_end) = (int)v.size();
         }
     }
@@ -1975,9 +1982,13 @@ cmsl_status autotune_items(Engine *e, int32_t *zchunk)
 {
     int maxnz = 1;
     for (const FilmHost &h : e->fh) maxnz = std::max(maxnz, h.nz);
+    // every chunk count of the thickest film down to chunks of ZCHUNK_MIN
+    // planes (the wave count of the stencil passes is what differs)
     std::vector<int> cands;
-    for (int c = ZCHUNK_MIN; c < maxnz; c *= 2) cands.push_back(c);
-    cands.push_back(maxnz);
+    for (int nc = 1; nc == 1 || (maxnz + nc - 1) / nc >= ZCHUNK_MIN; ++nc) {
+        const int c = (maxnz + nc - 1) / nc;
+        if (cands.empty() || cands.back() != c) cands.push_back(c);
+    }
     // per tile height (FP32; 4, 8 and 16 rows unless CMSL_TILE_Y fixed one)
     // and z chunk: every pair of stagings of the TDGL and the residual passes
     // where the tensor copies apply (8-row tiles of films with full tiles; a

@@ -197,7 +197,8 @@ cmsl_status cmsl_film_time_kernels(cmsl_film *film, int reps, void *stream, doub
 cmsl_status cmsl_film_inner_solver(cmsl_film *film, int *solver);
 
 /* Tile-shape autotuner: times the stencil passes of this film for work-item z
- * chunks 4, 8, 16, ... up to nz on the device -- and, for CMSL_FP32_REFINED
+ * chunks ceil(nz / n), n = 1, 2, ... down to 4 planes (a column's chunks
+ * differ by one plane at most) on the device -- and, for CMSL_FP32_REFINED
  * films with full 32 x 8 tiles, both stagings of the TDGL and of the
  * residual passes (tensor copies or the cp.async ring) -- keeps the fastest
  * (the z chunk in *zchunk, may be NULL) and remembers it for films of the same
