@@ -106,6 +106,9 @@ struct SolveDev {               // per film, lives in device memory
     int phi_prev;               // previous step's potential (extrapolated warm start)
     int phi_prev2;              // the one before (quadratic extrapolation)
     int phi_prev3;              // and the one before that (cubic extrapolation)
+    int hist;                   // FP32_REFINED: valid potentials among phi_cur, phi_prev, ... (0: phi_cur is
+                                // the zero start of a state without a potential; at most 4); the warm
+                                // start extrapolates to order min(warm, hist - 1)
     int sticky;                 // first non-zero status seen since set_state
     double inner_tol2;          // inner target of the current refinement pass
     int inner_max;              // inner iteration cap of the current pass

@@ -1642,6 +1642,7 @@ cmsl_status set_state(Engine *e, int film, const double *const P[6], const doubl
     S0.phi_prev = e->precision == CMSL_FP64 ? 0 : 1;
     S0.phi_prev2 = e->precision == CMSL_FP64 ? 0 : 2;
     S0.phi_prev3 = e->precision == CMSL_FP64 ? 0 : 3;
+    S0.hist = phi ? 1 : 0;              // a state without a potential starts from zero
     CK(cudaMemcpy(e->d_solve + film, &S0, sizeof(SolveDev), cudaMemcpyHostToDevice));
     return CMSL_OK;
 }
@@ -2231,6 +2232,7 @@ cmsl_status cmsl_film_depol_device(cmsl_film *f, const double *Pmx, const double
     S.phi_prev = f->precision == CMSL_FP64 ? 0 : 1;
     S.phi_prev2 = f->precision == CMSL_FP64 ? 0 : 2;
     S.phi_prev3 = f->precision == CMSL_FP64 ? 0 : 3;
+    S.hist = 1;                         // the caller's potential
     S.outer_active = 1;
     CK(cudaMemcpyAsync(f->d_solve, &S, sizeof(SolveDev), cudaMemcpyHostToDevice, st));
     // the solve kernels read the new Pm from set cur^1: point it at set cur

@@ -891,6 +891,7 @@ __device__ __forceinline__ void refine_film(const Dev &d, int fi, double (*sRed)
                 S->phi_prev3 = q0;
                 S->phi_prev2 = p0;
                 S->phi_prev = c0;
+                S->hist = min(S->hist + 1, 4);   // this step's potential joins the history
                 (void)r0;                    // phi_{n-3} is no longer needed: it becomes the free buffer
             }
             S->phi_cur = fr;                 // this pass wrote the free buffer

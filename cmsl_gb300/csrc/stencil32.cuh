@@ -49,6 +49,14 @@ __device__ __forceinline__ df extrap_phi(int warm, df a, df q, df u, df v)
     return a;
 }
 
+// The extrapolation order a film's next warm start can take: its warm start
+// order, lowered while fewer potentials than it needs are valid (after a
+// state upload; a state without a potential starts from zero).
+__device__ __forceinline__ int warm_order(const FilmDev *f, const SolveDev *S)
+{
+    return min(f->warm, max(S->hist - 1, 0));
+}
+
 // Difference of two double-float potentials rounded to FP32, for E: the hi
 // difference of neighbouring values is exact when they lie within a factor
 // of two of each other (Sterbenz) and one FP32 rounding off otherwise; the
@@ -282,11 +290,11 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, tdgl32_minb<TYc, DEF>()) 
     const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
     const int row = d.rows[(long long)it.x * d.wstride + rs];
     // film constants in registers (the stores below might alias the film table)
-    const int dep = f->dep_flag, nz = g.nz, warm = f->warm;
+    const SolveDev *S = d.solve + it.x;
+    const int dep = f->dep_flag, nz = g.nz, warm = warm_order(f, S);
     const bool neu = f->zbc != 0;
     const float inv_2hf = f->inv_2hf;
     const long long off = f->off, lo = d.ncells, fs = d.ncells;
-    const SolveDev *S = d.solve + it.x;
     const bool pend = DEF && dep && (d.force || S->pending != 0);
     const float2 *ph = phi2_sel(d, S->phi_cur) + off;
     const float2 *qh = phi2_sel(d, S->phi_prev) + off;
@@ -520,9 +528,10 @@ static __global__ void __launch_bounds__(NT) k_extrap(Dev d)
     const float2 *uh = phi2_sel(d, S->phi_prev2) + off;
     const float2 *vh = phi2_sel(d, S->phi_prev3) + off;
     float2 *nh = phi2_sel(d, phi_free(S)) + off;
+    const int warm = warm_order(f, S);
     for (int k = z0; k < z1; ++k) {
         const long long o = g.own_pl + (long long)k * g.plane;
-        const df w = extrap_phi(f->warm, ld_df(ph + o), ld_df(qh + o), ld_df(uh + o), ld_df(vh + o));
+        const df w = extrap_phi(warm, ld_df(ph + o), ld_df(qh + o), ld_df(uh + o), ld_df(vh + o));
         nh[o] = make_float2(w.h, w.l);
     }
 }

@@ -162,11 +162,11 @@ __global__ void __launch_bounds__(NT, 4) k_tdgl32t(Dev d, Fields<float> F)
     const int cur = d.ctl->cur, rs = d.ctl->run_step;
     const float mEz = (float)(-d.wave[(long long)it.x * d.wstride + rs]);   // dfdPmz_app, kernels_evol.cu:210
     const int row = d.rows[(long long)it.x * d.wstride + rs];
-    const int dep = f->dep_flag, warm = f->warm;
+    const SolveDev *S = d.solve + it.x;
+    const int dep = f->dep_flag, warm = warm_order(f, S);
     const bool neu = f->zbc != 0;
     const float inv_2hf = f->inv_2hf;
     const long long off = f->off, fs = d.ncells, plane = (long long)nx * ny;
-    const SolveDev *S = d.solve + it.x;
     const int pcur = S->phi_cur;
     const float2 *qh = phi2_sel(d, S->phi_prev) + off;
     const float2 *uh = phi2_sel(d, S->phi_prev2) + off;
