@@ -652,6 +652,64 @@ __global__ void k_phi_out(const float2 *__restrict__ src, double *__restrict__ d
         dst[i] = (double)v.x + (double)v.y;
     }
 }
+
+// The whole state of one FP32 film in one launch each way, the P set and
+// the potential buffer picked on the device (Ctl::cur, SolveDev::phi_cur):
+// no host round trip for them and no launch per field.  The link to the
+// host's memory is the bound (measured ~205 GB/s in, ~190 GB/s out with
+// either one launch per field or one for all; one launch saves the launches
+// and host synchronisations between them).
+struct StateIn {
+    const double *P[6];         // the caller's fields (device-readable)
+    const double *phi;          // the caller's potential, or null (zero)
+    float2 *pair[2][3];         // the film's (P[2j], P[2j+1]) pairs of both sets
+    float2 *phi0;               // the film's slice of potential buffer 0
+    float *x;                   // the film's slice of the correction
+    const Ctl *ctl;
+    long long n;
+};
+__global__ void k_state_in(StateIn s)
+{
+    float2 *const *pr = s.pair[s.ctl->cur];     // the set the next step reads
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += (long long)gridDim.x * blockDim.x) {
+        double v[6];
+        #pragma unroll
+        for (int q = 0; q < 6; ++q) v[q] = s.P[q][i];
+        const double p = s.phi ? s.phi[i] : 0.0;
+        #pragma unroll
+        for (int j = 0; j < 3; ++j) pr[j][i] = make_float2((float)v[2 * j], (float)v[2 * j + 1]);
+        const float h = (float)p;
+        s.phi0[i] = make_float2(h, (float)(p - (double)h));
+        s.x[i] = 0.f;
+    }
+}
+struct StateOut {
+    double *P[6];               // page-locked outputs (device addresses), null where not wanted
+    double *phi;
+    const float2 *pair[2][3];
+    const float2 *phib[5];      // the film's slice of every potential buffer
+    const Ctl *ctl;
+    const SolveDev *S;
+    long long n;
+};
+__global__ void k_state_out(StateOut s)
+{
+    const float2 *const *pr = s.pair[s.ctl->cur];
+    const float2 *ph = s.phi ? s.phib[s.S->phi_cur] : nullptr;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += (long long)gridDim.x * blockDim.x) {
+        float2 v[3];
+        #pragma unroll
+        for (int j = 0; j < 3; ++j)
+            if (s.P[2 * j] || s.P[2 * j + 1]) v[j] = pr[j][i];
+        const float2 w = ph ? ph[i] : make_float2(0.f, 0.f);
+        #pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            if (s.P[2 * j]) s.P[2 * j][i] = (double)v[j].x;
+            if (s.P[2 * j + 1]) s.P[2 * j + 1][i] = (double)v[j].y;
+        }
+        if (ph) s.phi[i] = (double)w.x + (double)w.y;
+    }
+}
 // Per-cell codes of one film on the device (the set-up of main.cu:13-52 and
 // init_conf.cu:68-106 reduced to one word per cell): grain id | material
 // << 24 | interface << 26, the interface flag of build_interface_flag unless
@@ -1598,9 +1656,36 @@ cmsl_status set_state(Engine *e, int film, const double *const P[6], const doubl
 {
     if (!P) return fail(CMSL_ERR_ARG, "NULL argument");
     if (film < 0 || film >= e->n_films) return fail(CMSL_ERR_ARG, "film %d outside [0,%d)", film, e->n_films);
+    for (int q = 0; q < 6; ++q)
+        if (!P[q]) return fail(CMSL_ERR_ARG, "P[%d] is NULL", q);
     CK(cudaDeviceSynchronize());
     e->has_state = true;
     if (reset_clock) CK(cudaMemset(e->d_ctl, 0, sizeof(Ctl)));
+    const FilmHost &hf = e->fh[film];
+    if (e->precision != CMSL_FP64 && e->host_direct) {
+        // one launch: P into set cur, phi (or zero) into buffer 0, x = 0.
+        // The other potential buffers are not read before they hold this
+        // run's potentials (SolveDev::hist starts at 1, or 0 without phi).
+        StateIn s{};
+        for (int q = 0; q < 6; ++q) s.P[q] = P[q];
+        s.phi = phi;
+        for (int set = 0; set < 2; ++set)
+            for (int j = 0; j < 3; ++j) s.pair[set][j] = (float2 *)e->d_P[set][2 * j] + hf.off;
+        s.phi0 = (float2 *)e->d_phi[0] + hf.off;
+        s.x = (float *)e->d_x + hf.off;
+        s.ctl = e->d_ctl;
+        s.n = hf.N;
+        k_state_in<<<XFER_GRID, XFER_NT>>>(s);
+        CK(cudaGetLastError());
+        SolveDev S0{};
+        S0.phi_prev = 1;
+        S0.phi_prev2 = 2;
+        S0.phi_prev3 = 3;
+        S0.hist = phi ? 1 : 0;
+        CK(cudaMemcpyAsync(e->d_solve + film, &S0, sizeof(SolveDev), cudaMemcpyHostToDevice, 0));
+        CK(cudaDeviceSynchronize());
+        return CMSL_OK;
+    }
     Ctl c;
     CK(cudaMemcpy(&c, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     if (e->precision == CMSL_FP64) TRY(put_fields<double>(e, film, c.cur, P));
@@ -1651,6 +1736,27 @@ cmsl_status get_state(Engine *e, int film, double *const P[6], double *phi)
 {
     if (film < 0 || film >= e->n_films) return fail(CMSL_ERR_ARG, "film %d outside [0,%d)", film, e->n_films);
     CK(cudaDeviceSynchronize());
+    if (e->precision != CMSL_FP64) {
+        // every wanted output page-locked: one launch
+        StateOut s{};
+        bool all = true;
+        for (int q = 0; q < 6 && P; ++q)
+            if (P[q]) all = all && (s.P[q] = locked_dst(P[q])) != nullptr;
+        if (phi) all = all && (s.phi = locked_dst(phi)) != nullptr;
+        if (all) {
+            const FilmHost &hf = e->fh[film];
+            for (int set = 0; set < 2; ++set)
+                for (int j = 0; j < 3; ++j) s.pair[set][j] = (const float2 *)e->d_P[set][2 * j] + hf.off;
+            for (int b = 0; b < 5; ++b) s.phib[b] = (const float2 *)e->d_phi[b] + hf.off;
+            s.ctl = e->d_ctl;
+            s.S = e->d_solve + film;
+            s.n = hf.N;
+            k_state_out<<<XFER_GRID, XFER_NT>>>(s);
+            CK(cudaGetLastError());
+            CK(cudaDeviceSynchronize());
+            return CMSL_OK;
+        }
+    }
     Ctl c;
     SolveDev S;
     CK(cudaMemcpy(&c, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));

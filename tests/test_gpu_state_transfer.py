@@ -23,9 +23,13 @@ def gpu():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_state_round_trip_and_run(gpu, precision, monkeypatch):
+@pytest.mark.parametrize("with_phi", [True, False])
+def test_state_round_trip_and_run(gpu, precision, with_phi, monkeypatch):
+    """With a potential and without one (zero start): the GPU conversion
+    (one launch for the whole FP32 state each way) and the host-side one give
+    the same state and identical runs."""
     f, P = random_film(36, 20, 10, seed=101, eps_0_nd=3.0, p_scale=0.2)
-    phi = np.random.default_rng(5).normal(0.0, 0.3, f.N)
+    phi = np.random.default_rng(5).normal(0.0, 0.3, f.N) if with_phi else None
     kw = dict(precision=gpu.FP64 if precision == "fp64" else gpu.FP32_REFINED)
     Ez = np.linspace(0.0, 0.2, 6)
     out = []
@@ -37,7 +41,9 @@ def test_state_round_trip_and_run(gpu, precision, monkeypatch):
             for a, b in zip(Pg, P):
                 want = b if precision == "fp64" else np.asarray(b, np.float32).astype(np.float64)
                 assert np.array_equal(a, want)
-            if precision == "fp64":
+            if phi is None:
+                assert not phig.any()
+            elif precision == "fp64":
                 assert np.array_equal(phig, phi)
             else:
                 assert np.abs(phig - phi).max() <= 1e-14 * np.abs(phi).max()
