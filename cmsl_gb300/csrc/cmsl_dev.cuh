@@ -116,6 +116,8 @@ struct SolveDev {               // per film, lives in device memory
                                 // forming b - A phi in double-float
     double cheb_rho;            // Chebyshev recurrence of the preconditioned refinement (rho_k)
     float cheb_w, cheb_m;       // the next direct solve's increment: dx <- w M^-1 r + m dx
+    int row_pend;               // Dev::row_off: the sweep row (+1; 0 none) whose item partials the
+                                // TDGL step left for the next residual pass to total and write
     int pending;                // the step ended on its direct solve: the potential is phi_cur (the
                                 // warm start) + dx, its check r <- r - A dx still to come (next TDGL)
 };
@@ -169,12 +171,19 @@ struct Dev {
     int n_films, n_items;
     const int4 *sitems;         // items of the FP32 stencil passes (tile height of the autotuner's choice)
     int n_sitems;
+    int row_off;                // single films with deferred checks: block 0 of the step's first
+                                // residual pass totals and writes the TDGL step's sweep row
+                                // (SolveDev::row_pend) while the other blocks run their items.
+                                // (Kept in the padding after n_sitems: a Dev above 256 bytes
+                                // measured 1-2 us more per graph step.)
     const uint32_t *code;
     long long ncells;           // cells of all films (stride of the FP32 P pairs)
     double *phi[5];
     double *partial;            // [n_items * NPART]
-    unsigned int *counter;      // one ticket counter (reset by the last block)
-    unsigned int *fcount;       // [n_films] per-film ticket counters of the FP32 stencil passes (batches)
+    double *rpartial;           // [n_items * NPART] the FP32 residual passes' partial sums (apart from
+                                // the TDGL's, which the step's first residual pass may still total)
+    unsigned int *counter;      // [4 + n_films] the grid's ticket counter (reset by the last block);
+                                // from 4 on the per-film ones of the FP32 stencil passes (batches)
     SolveDev *solve;            // [n_films]
     Ctl *ctl;
     const double *wave;         // [n_films * wstride] applied field per run step

@@ -68,9 +68,9 @@ struct Engine {
     uint32_t *d_code = nullptr;
     void *d_TR = nullptr;
     double *d_phi[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    double *d_partial = nullptr;
-    unsigned int *d_fcount = nullptr;   // per-film ticket counters (batches)
-    unsigned int *d_counter = nullptr;
+    double *d_partial = nullptr;        // the TDGL's item partials, then the residual passes'
+    size_t part_cap = 0;                // items of each half
+    unsigned int *d_counter = nullptr;  // [4 + n_films] (Dev::counter)
     SolveDev *d_solve = nullptr;
     Ctl *d_ctl = nullptr;
     void *d_P[2][6] = {};
@@ -185,7 +185,11 @@ struct Engine {
         d.code = d_code; d.ncells = ncells;
         for (int q = 0; q < 5; ++q) d.phi[q] = d_phi[q];
         d.partial = d_partial; d.counter = d_counter; d.solve = d_solve; d.ctl = d_ctl;
-        d.fcount = d_fcount;
+        d.rpartial = d_partial + (size_t)NPART * part_cap;
+        // the residual pass's block 0 hides the row total only where the
+        // pass has more blocks than one wave (152 SMs, 32 / TY' resident
+        // blocks each); otherwise the total stays at the TDGL step's end
+        d.row_off = defer && n_films == 1 && (long long)sitems.size() > 152LL * 32 / stile_ty ? 1 : 0;
         d.wave = d_wave; d.rows = d_rows; d.rowbuf = d_rowbuf;
         d.iters_log = d_iters; d.refine_log = d_refine;
         d.wstride = wstride; d.rstride = rstride;

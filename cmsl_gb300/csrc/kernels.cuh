@@ -195,9 +195,10 @@ __device__ __forceinline__ bool film_ticket_last(const Dev &d, int fi)
         __threadfence();
         const FilmDev *f = d.films + fi;
         const unsigned int n = (unsigned int)(f->sitem_end - f->sitem_begin);
-        const unsigned int t = atomicAdd(d.fcount + fi, 1u);
+        unsigned int *fc = d.counter + 4 + fi;
+        const unsigned int t = atomicAdd(fc, 1u);
         s_flast = t + 1u == n;
-        if (s_flast) d.fcount[fi] = 0u;          // every block of the film has arrived
+        if (s_flast) *fc = 0u;                   // every block of the film has arrived
     }
     __syncthreads();
     if (s_flast) __threadfence();
@@ -247,7 +248,7 @@ __device__ __forceinline__ void film_total(const Dev &d, const FilmDev *f, doubl
 // so that neither the blocks' epilogues nor the last block's film totals
 // queue on the FP64 pipe.  The summation order is fixed (deterministic).
 template <int NV>
-__device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], double (*sm)[NV])
+__device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], double (*sm)[NV], double *part = nullptr)
 {
     static_assert(NV <= 32, "one lane per value");
     float *ws = (float *)&sm[0][0];               // [warps][NV] warp sums
@@ -262,7 +263,7 @@ __device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], do
         const int nw = (int)(blockDim.x >> 5);
         df s{0.f, 0.f};
         for (int q = 0; q < nw; ++q) s = df_add_f(s, ws[q * NV + threadIdx.x]);
-        *(float2 *)(d.partial + (long long)blockIdx.x * NPART + threadIdx.x) = make_float2(s.h, s.l);
+        *(float2 *)((part ? part : d.partial) + (long long)blockIdx.x * NPART + threadIdx.x) = make_float2(s.h, s.l);
     }
     __syncthreads();
 }
@@ -272,11 +273,13 @@ __device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], do
 // warp tree, then warps in order), valid in thread 0.  The last block runs
 // alone at the end of its grid, so the sum is laid out for latency: every
 // load of a round is issued before its sums, and the values' warp trees
-// interleave.
-template <int NV>
+// interleave.  OFF: the first slot; part: the partials (default the TDGL's).
+template <int NV, int OFF = 0>
 __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, double (*sm)[NV],
-                                             double (&out)[NV])
+                                             double (&out)[NV], const double *part = nullptr)
 {
+    static_assert(OFF + NV <= NPART, "slots of an item");
+    const double *pp = part ? part : d.partial;
     static_assert(NV <= 32 && sizeof(float2) == sizeof(double), "one lane and one slot per value");
     __shared__ double s_tot[NV];
     float2 *ws = (float2 *)&sm[0][0];             // [warps][NV] warp totals
@@ -284,14 +287,14 @@ __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, dou
     #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = df{0.f, 0.f};
     const int b1 = f->sitem_end, stride = (int)blockDim.x;
-    auto part = [&](int it, int i) { return __ldcg((const float2 *)(d.partial + (long long)it * NPART + i)); };
+    auto ld = [&](int it, int i) { return __ldcg((const float2 *)(pp + (long long)it * NPART + OFF + i)); };
     int it = f->sitem_begin + (int)threadIdx.x;
     for (; it + stride < b1; it += 2 * stride) {
         float2 p[NV], q[NV];
         #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            p[i] = part(it, i);
-            q[i] = part(it + stride, i);
+            p[i] = ld(it, i);
+            q[i] = ld(it + stride, i);
         }
         #pragma unroll
         for (int i = 0; i < NV; ++i) v[i] = df_add_acc(v[i], df_add_acc(df{p[i].x, p[i].y}, df{q[i].x, q[i].y}));
@@ -299,7 +302,7 @@ __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, dou
     if (it < b1) {
         #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            const float2 p = part(it, i);
+            const float2 p = ld(it, i);
             v[i] = df_add_acc(v[i], df{p.x, p.y});
         }
     }
@@ -872,14 +875,14 @@ __device__ __forceinline__ void step_end(const Dev &d)
 __device__ __forceinline__ void refine_film(const Dev &d, int fi, double (*sRed)[3], double (&sTot)[3])
 {
     if (d.force) {              // kernel timing: the totals as a pass forms them; the state stays as it is
-        if (d.films[fi].dep_flag) film_total32<3>(d, d.films + fi, sRed, sTot);
+        if (d.films[fi].dep_flag) film_total32<3>(d, d.films + fi, sRed, sTot, d.rpartial);
         return;
     }
     {
         const FilmDev *ff = d.films + fi;
         SolveDev *S = d.solve + fi;
         const bool was = ff->dep_flag != 0 && uniform_flag(&S->outer_active);
-        if (was) film_total32<3>(d, ff, sRed, sTot);
+        if (was) film_total32<3>(d, ff, sRed, sTot, d.rpartial);
         if (threadIdx.x == 0 && was) {
             // an update pass (r <- r - A dx) leaves b.b as the last full pass formed it
             const bool was_upd = ff->upd_ok && S->upd && S->refine > 0;

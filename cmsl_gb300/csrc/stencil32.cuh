@@ -440,7 +440,10 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, tdgl32_minb<TYc, DEF>()) 
 // whose checks passed stay pending (the repeated step checks them again, to
 // the same result), and the step loop runs this step again after that pass
 // has ended the previous one.
-// Film fi's part: its sweep row and its check's r.r (S->rr64).
+// Film fi's part: its sweep row and its check's r.r (S->rr64).  Under
+// Dev::row_off the row is left to the step's first residual pass
+// (row_from_tdgl): only the check's r.r is totalled here, one value instead
+// of eight at the end of the grid.
 template <int NV>
 __device__ __forceinline__ void tdgl_def_film(const Dev &d, int rs, int fi, double (*sRed)[NV], double (&sTot)[NV])
 {
@@ -448,6 +451,13 @@ __device__ __forceinline__ void tdgl_def_film(const Dev &d, int rs, int fi, doub
     const FilmDev *ff = d.films + fi;
     SolveDev *S = d.solve + fi;
     const int frow = d.rows[(long long)fi * d.wstride + rs];
+    if (d.row_off) {
+        if (!ff->dep_flag || !(d.force || uniform_flag(&S->pending))) return;
+        double rr[1];
+        film_total32<1, NV - 1>(d, ff, (double (*)[1])sRed, rr);
+        if (threadIdx.x == 0 && !d.force) S->rr64 = rr[0];
+        return;
+    }
     if (d.force) {              // kernel timing: the totals as a step forms them; the state stays as it is
         if (ff->dep_flag || frow >= 0) film_total32<NV>(d, ff, sRed, sTot);
         return;
@@ -492,6 +502,10 @@ __device__ __forceinline__ void tdgl_def_grid(const Dev &d, int rs)
                 S->pending = 0;
             }
             step_reset(d, fi);
+            if (d.row_off) {    // the step's first residual pass totals and writes the row
+                const int frow = d.rows[(long long)fi * d.wstride + rs];
+                S->row_pend = frow >= 0 ? frow + 1 : 0;
+            }
         }
         step_begin(d, rs);
     } else {
@@ -631,7 +645,26 @@ __device__ __forceinline__ void refine_cell(const RConst &rc, int k, bool ident,
 
 __device__ __forceinline__ void refine_partials(const Dev &d, float (&acc)[3], double (*sRed)[3])
 {
-    block_partial32<3>(d, acc, sRed);
+    block_partial32<3>(d, acc, sRed, d.rpartial);
+}
+
+// Dev::row_off (a single film with deferred checks): block 0 of the step's
+// first residual pass totals the sweep row from the TDGL step's item
+// partials (slots 0-6, which the residual passes leave alone) and writes it,
+// while the other blocks run their items; the TDGL step's last block formed
+// only the check's r.r.  Under kernel timing the total is formed and nothing
+// written.  Every thread of block 0.
+__device__ __forceinline__ void row_from_tdgl(const Dev &d, double (*sRow)[7])
+{
+    SolveDev *S = d.solve;
+    const int rp = d.force ? 1 : S->row_pend;
+    if (rp <= 0) return;
+    double t[7];
+    film_total32<7>(d, d.films, sRow, t);
+    if (threadIdx.x == 0 && !d.force) {
+        row_write(d, 0, rp - 1, t);
+        S->row_pend = 0;
+    }
 }
 
 // Stage layout (floats): x = phi (+ dx) as one (hi, lo) float2 plane, dx,
@@ -658,6 +691,10 @@ __global__ void __launch_bounds__(TileShape<TYc>::NTt, TileShape<TYc>::MINB) k_r
     float *ring = (float *)smem_r32;
     __shared__ double sRed[NT / 32][3];
     __shared__ double sTot[3];
+    if (!FB && d.row_off && blockIdx.x == 0) {
+        __shared__ double sRow[NT / 32][7];
+        row_from_tdgl(d, sRow);
+    }
     const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const SolveDev *S = d.solve + it.x;

@@ -283,6 +283,10 @@ __global__ void __launch_bounds__(NT, 4) k_refine32t(Dev d, Fields<float> F)
     __shared__ TmaOp ops[RT_OPS];
     __shared__ double sRed[NT / 32][3];
     __shared__ double sTot[3];
+    if (!FB && d.row_off && blockIdx.x == 0) {
+        __shared__ double sRow[NT / 32][7];
+        row_from_tdgl(d, sRow);
+    }
     const int4 it = d.sitems[blockIdx.x];
     const FilmDev *f = d.films + it.x;
     const SolveDev *S = d.solve + it.x;
