@@ -214,3 +214,31 @@ def test_batch_where_some_checks_fail(gpu, monkeypatch):
             assert np.abs(b.rows(i)[:, :10] - rw[:, :10]).max() <= 1e-6
         # every step of the first film reopened; the second settles to its two passes after the cold start
         assert (b.iters(0)[1] >= 3).all() and b.iters(1)[1][-1] == 2
+
+
+@pytest.mark.parametrize("tol", [1e-8, 1e-11])
+def test_rows_totalled_by_the_residual_pass(gpu, tol, monkeypatch):
+    """A film whose residual pass has more blocks than one wave (256 x 128 x
+    24 in 4-plane chunks: 768 items of 32 x 8 columns) has its sweep rows
+    totalled by block 0 of each step's first residual pass, the TDGL step's
+    last block forming only the check's r.r.  Its rows match the oracle's
+    and the update-pass schedule's (rows formed in the TDGL step), with the
+    checks passing and (refine_tol 1e-11) failing, the reopened steps' rows
+    formed again when they repeat."""
+    monkeypatch.setenv("CMSL_ZCHUNK", "4")
+    f, P = _film((256, 128, 24), seed=41)
+    n = 8
+    Ez = np.linspace(0.0, 0.3, n)
+    rows = np.arange(n, dtype=np.int32)
+    Pw, _, phiw, statw, _, rc = oracle.load().run(f, P, np.zeros(f.N), Ez, rows)
+    assert rc == 0
+    Pd, phid, rd, itd, rfd = _run(gpu, f, P, Ez, rows, monkeypatch, defer=True, refine_tol=tol)
+    Pu, phiu, ru, itu, rfu = _run(gpu, f, P, Ez, rows, monkeypatch, defer=False, refine_tol=tol)
+    assert (rfd == rfu).all()
+    if tol < 1e-10:
+        assert (rfd >= 3).all()
+    for rg in (rd, ru):
+        assert np.abs(rg[:, :10] - statw[:, :10]).max() <= 1e-5
+    assert np.abs(rd[:, :11] - ru[:, :11]).max() <= 1e-6
+    assert np.array_equal(rd[:, 10], np.arange(1, n + 1))       # the step count column
+    assert _close(Pd, Pw, 2e-5) and _close(Pd, Pu, 1e-6)
