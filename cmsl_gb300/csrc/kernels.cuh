@@ -269,7 +269,7 @@ __device__ __forceinline__ void block_partial32(const Dev &d, float (&v)[NV], do
 }
 
 // In the last block: film f's totals of the block_partial32 pairs of its
-// stencil items (Dev::sitems; item order: thread-strided two items a round,
+// stencil items (Dev::sitems; item order: thread-strided U items a round,
 // warp tree, then warps in order), valid in thread 0.  The last block runs
 // alone at the end of its grid, so the sum is laid out for latency: every
 // load of a round is issued before its sums, and the values' warp trees
@@ -288,23 +288,21 @@ __device__ __forceinline__ void film_total32(const Dev &d, const FilmDev *f, dou
     for (int i = 0; i < NV; ++i) v[i] = df{0.f, 0.f};
     const int b1 = f->sitem_end, stride = (int)blockDim.x;
     auto ld = [&](int it, int i) { return __ldcg((const float2 *)(pp + (long long)it * NPART + OFF + i)); };
-    int it = f->sitem_begin + (int)threadIdx.x;
-    for (; it + stride < b1; it += 2 * stride) {
-        float2 p[NV], q[NV];
+    // U items a round, all their loads issued before the sums (about 16
+    // values in flight per thread: one round for a 1536-item film's single
+    // value instead of six)
+    constexpr int U = 16 / NV > 8 ? 8 : (16 / NV < 2 ? 2 : 16 / NV);
+    for (int it = f->sitem_begin + (int)threadIdx.x; it < b1; it += U * stride) {
+        float2 p[U][NV];
         #pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            p[i] = ld(it, i);
-            q[i] = ld(it + stride, i);
-        }
+        for (int u = 0; u < U; ++u)
+            #pragma unroll
+            for (int i = 0; i < NV; ++i)
+                p[u][i] = it + u * stride < b1 ? ld(it + u * stride, i) : make_float2(0.f, 0.f);
         #pragma unroll
-        for (int i = 0; i < NV; ++i) v[i] = df_add_acc(v[i], df_add_acc(df{p[i].x, p[i].y}, df{q[i].x, q[i].y}));
-    }
-    if (it < b1) {
-        #pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            const float2 p = ld(it, i);
-            v[i] = df_add_acc(v[i], df{p.x, p.y});
-        }
+        for (int u = 0; u < U; ++u)
+            #pragma unroll
+            for (int i = 0; i < NV; ++i) v[i] = df_add_acc(v[i], df{p[u][i].x, p[u][i].y});
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     #pragma unroll
