@@ -1379,8 +1379,8 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
         // film takes them): a shorter solve at 64x64x16 and 128x128x16 (24.7
         // against 32.7 us, 28.0 against 31.8) but no shorter a step there,
         // and a longer solve at 256x256x32 (55.4 against 43.0 us, one block
-        // of 512 threads per SM on 120 SMs), so the row layout stays the
-        // default; the column layout by CMSL_SPEC_COLS=1 otherwise
+        // of 512 threads per SM on 120 SMs), so it stays opt-in (64x64x16
+        // steps: 59.3 us against 55.8 for the column layout)
         const char *clv = getenv("CMSL_SPEC_CL");
         bool cl_ok = clv && atoi(clv) != 0;
         for (int fi = 0; fi < n; ++fi)
@@ -1454,13 +1454,18 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             smx = std::max(smx, sizeof(float2) * (2 * (spec_pad(rbx * spec_x_pitch(h.nx, true)) + 1) + h.nx));   // two tiles + twiddles
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }
-        // the row layout; CMSL_SPEC_COLS=1 selects the column layout for films
-        // whose column pairs fit one block (three launches instead of five,
-        // 3-5 us less kernel time per solve, but no shorter a step: measured
-        // equal at 256x256x32 and 1-2 us longer at 64x64x16 and 128x128x16)
+        // the column layout (three launches per solve instead of five) where
+        // the column pairs fit one block and every film has at most 64 x 64
+        // columns: there the shorter solve shortens the step (64x64x16: 55.8
+        // against 61.7 us per step), while at 256x256x32 the row layout's
+        // step is shorter (151.0 against 152.8 us).  CMSL_SPEC_COLS=1 / 0
+        // selects either where the column pairs fit.
         {
+            bool small = true;
+            for (int fi = 0; fi < n; ++fi) small = small && (long long)e->fh[fi].nx * e->fh[fi].ny <= 64 * 64;
             const char *cl = getenv("CMSL_SPEC_COLS");
-            e->spec_col = e->spec_cl || (smq <= (size_t)optin && cl && atoi(cl) != 0);
+            const bool want = cl && *cl ? atoi(cl) != 0 : small;
+            e->spec_col = e->spec_cl || (smq <= (size_t)optin && want);
         }
         // Thomas pivots of every film, mode and interior plane, in double:
         // dg = lam_x + lam_y + 2, inv_k = 1 / (dg - c'_{k-1}) with c'_k = -inv_k
