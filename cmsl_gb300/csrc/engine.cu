@@ -1455,14 +1455,14 @@ cmsl_status engine_create(Engine *e, const cmsl_film_desc *descs, int n)
             smy = std::max(smy, sizeof(float2) * (2 * cby * h.ny + h.ny));
         }
         // the column layout (three launches per solve instead of five) where
-        // the column pairs fit one block and every film has at most 64 x 64
-        // columns: there the shorter solve shortens the step (64x64x16: 55.8
-        // against 61.7 us per step), while at 256x256x32 the row layout's
-        // step is shorter (151.0 against 152.8 us).  CMSL_SPEC_COLS=1 / 0
-        // selects either where the column pairs fit.
+        // the column pairs fit one block and every film has at most 128 x 128
+        // columns: there the shorter solve shortens the step (64x64x16: 55.6
+        // against 60.3 us per step, 128x128x16: 62.2 against 66.3), while at
+        // 256x256x32 the row layout's step is shorter (151.0 against 152.8
+        // us).  CMSL_SPEC_COLS=1 / 0 selects either where the column pairs fit.
         {
             bool small = true;
-            for (int fi = 0; fi < n; ++fi) small = small && (long long)e->fh[fi].nx * e->fh[fi].ny <= 64 * 64;
+            for (int fi = 0; fi < n; ++fi) small = small && (long long)e->fh[fi].nx * e->fh[fi].ny <= 128 * 128;
             const char *cl = getenv("CMSL_SPEC_COLS");
             const bool want = cl && *cl ? atoi(cl) != 0 : small;
             e->spec_col = e->spec_cl || (smq <= (size_t)optin && want);
